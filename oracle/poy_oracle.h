@@ -1,0 +1,53 @@
+/*
+ * ORACLE / TEST INFRASTRUCTURE ONLY: C restatement of POY's direct-
+ * optimization pairwise alignment path (poy_oracle.c). Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline arm may load it.
+ */
+#ifndef POY_ORACLE_H
+#define POY_ORACLE_H 1
+#include <stdint.h>
+
+void *orc_cm_new(const int *tcm, int alph, int gap_open);
+void orc_cm_free(void *cm);
+int orc_cm_tables(void *cm, int *cost, uint8_t *median, int *worst, int *tail,
+                  int *prepend, int *info);
+void *orc_ws_new(void);
+void orc_ws_free(void *ws);
+void orc_set_check(int on);
+const char *orc_last_error(void);
+
+int orc_simple_2(void *cm, void *ws, const uint8_t *s1, int l1,
+                 const uint8_t *s2, int l2, int deltawh, int *cost);
+int orc_backtrace_2d(void *cm, void *ws, const uint8_t *s1, int l1,
+                     const uint8_t *s2, int l2, int swap, uint8_t *r1,
+                     uint8_t *r2, int cap, int *len);
+int orc_cost_linear(void *cm, void *ws, const uint8_t *a, int la,
+                    const uint8_t *b, int lb, int deltaw, int *cost);
+int orc_cost_affine(void *cm, void *ws, const uint8_t *a, int la,
+                    const uint8_t *b, int lb, int *cost);
+int orc_median_linear(void *cm, void *ws, const uint8_t *a, int la,
+                      const uint8_t *b, int lb, int *cost, uint8_t *ea,
+                      uint8_t *eb, int *elen, uint8_t *anc, int *anclen,
+                      uint8_t *mwg, int *mwglen, int *maxcost);
+int orc_median_affine(void *cm, void *ws, const uint8_t *a, int la,
+                      const uint8_t *b, int lb, int *cost, uint8_t *med,
+                      int *medlen, uint8_t *ea, uint8_t *eb, int *elen,
+                      uint8_t *mwg, int *mwglen, int *maxcost);
+
+/* Batched DOS.median over many pairs, OpenMP across pairs. Pair k reads
+ * a = seqs[offa[k] .. +lena[k]), b likewise; writes results into slot k of a
+ * flat output with capacity cap[k] = lena[k] + lenb[k] + 2 at out_off[k].
+ * Per-pair status lands in status[k] (0 ok). Returns the number of failures. */
+int orc_median_batch(void *cm, int affine, int npairs, const uint8_t *seqs,
+                     const int64_t *offa, const int *lena, const int64_t *offb,
+                     const int *lenb, const int64_t *out_off, int *cost,
+                     int *maxcost, int *alen, int *mlen, int *wlen, uint8_t *ea,
+                     uint8_t *eb, uint8_t *med, uint8_t *mwg, int *status,
+                     int nthreads);
+
+/* Band schedule statistics of one linear / affine alignment (internal order
+ * already applied): number of doubling iterations and cells filled. */
+int orc_schedule(void *cm, int affine, const uint8_t *a, int la,
+                 const uint8_t *b, int lb, int *iters, int64_t *cells);
+
+#endif
