@@ -1,0 +1,185 @@
+/*
+ * poyalgn -- GB300 (sm_103a) direct-optimization pairwise alignment.
+ *
+ * C ABI of libpoyalgn.so. Plain pointers and sizes only; no CUDA or Python
+ * types cross this boundary (streams are passed as void *).
+ *
+ * Sequences are POY bitset sequences: one byte per position, A=1 C=2 G=4
+ * T=8 gap=16 (ambiguities are unions), position 0 holding the leading gap
+ * (POY src/data.ml:618). Aligned outputs are written back to front so that
+ * each sequence ENDS at the last byte of its buffer, as POY's seq_prepend
+ * leaves a `struct seq` (src/seq.c:155-161); lengths are returned.
+ *
+ * Per-call entry points replace POY's OCaml externals one for one and keep
+ * their argument meaning (paths relative to the POY 5.1.1 source tree). Like
+ * POY's process-wide Matrix.default workspace, a context holds the fill of
+ * the last simple_2 call for a following backtrace_2d; a context is not
+ * reentrant. Batched entry points have no POY counterpart: they run many
+ * SeqCS.DOS.median computations (src/seqCS.ml:985-1084) in one launch
+ * sequence.
+ *
+ * Return values: 0 on success, a negative POYALGN_E* code otherwise;
+ * poyalgn_last_error() describes the last failure of the calling thread.
+ */
+#ifndef POYALGN_H
+#define POYALGN_H 1
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define POYALGN_EINVAL -1       /* bad argument (POY would failwith or assert) */
+#define POYALGN_ENOMEM -2       /* device or host allocation failed */
+#define POYALGN_ECUDA -3        /* CUDA runtime error */
+#define POYALGN_EUNSUPPORTED -4 /* input outside what the GPU path handles */
+#define POYALGN_EPAIR -5        /* one or more pairs of a batch failed (see status) */
+
+/* Per-pair status codes written by the batched entry points. */
+#define POYALGN_PAIR_OK 0
+#define POYALGN_PAIR_CAPACITY -2   /* output capacity exceeded */
+#define POYALGN_PAIR_ZERO_MEDIAN -3 /* "median should not be 0" (src/algn.c:3619) */
+#define POYALGN_PAIR_EMPTY -4      /* empty sequence / empty median (POY UB) */
+#define POYALGN_PAIR_TOO_WIDE -5   /* band wider than the largest pipeline */
+#define POYALGN_PAIR_TOO_LONG -6   /* sequence longer than 65535 */
+
+typedef struct poyalgn_ctx poyalgn_ctx;
+typedef struct poyalgn_cm poyalgn_cm;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Bind a context to CUDA device `device`. No POY counterpart. */
+int poyalgn_init(int device, poyalgn_ctx **out);
+void poyalgn_free(poyalgn_ctx *ctx);
+const char *poyalgn_last_error(void);
+/* Library version string, e.g. "poyalgn 0.1 sm_103a". */
+const char *poyalgn_version(void);
+
+/* ---- cost matrices -------------------------------------------------------- */
+
+/*
+ * Build the tables of a bitset alphabet from an alph x alph transformation
+ * cost matrix (row-major, gap last) and a gap-opening cost (0 = linear).
+ * Replaces Cost_matrix.Two_D.of_list / fill_cost_matrix
+ * (src/cost_matrix.ml:1140-1189, 1300-1312) followed, when gap_open > 0, by
+ * set_cost_model (Affine gap_open) (src/cost_matrix.ml:1003-1017). alph <= 5.
+ */
+int poyalgn_cm_build(poyalgn_ctx *ctx, const int32_t *tcm, int alph,
+                     int gap_open, poyalgn_cm **out);
+
+/*
+ * Adopt tables POY already built: the arrays of `struct cm` (src/cm.h:33-76;
+ * each 2 << (2*lcm) entries, index (a << lcm) + b). This is the conversion
+ * the drop-in stub library performs on cm_CAML_create's block
+ * (src/cm.c:2452-2469) before the first alignment.
+ */
+int poyalgn_cm_adopt(poyalgn_ctx *ctx, int lcm, int gap, int a_sz,
+                     int combinations, int cost_model, int gap_open,
+                     const int32_t *cost, const uint8_t *median,
+                     const int32_t *worst, const int32_t *tail,
+                     const int32_t *prepend, poyalgn_cm **out);
+
+/* Copy the tables out (same layout as above). info = {lcm, gap, a_sz,
+ * combinations, cost_model, gap_open, min_non0_cost}. Returns #entries. */
+int poyalgn_cm_tables(const poyalgn_cm *cm, int32_t *cost, uint8_t *median,
+                      int32_t *worst, int32_t *tail, int32_t *prepend,
+                      int32_t *info);
+void poyalgn_cm_free(poyalgn_cm *cm);
+
+/* ---- per-call drop-in entry points ---------------------------------------- */
+
+/*
+ * algn_CAML_simple_2 (src/algn.c:3133-3158): cost of aligning s1 (the
+ * shorter, l1 <= l2) with s2 under a linear cost matrix, band doubling seeded
+ * with deltawh (algn_nw, src/algn.c:2954-2975). The fill stays in the
+ * context for poyalgn_backtrace_2d.
+ */
+int poyalgn_simple_2(poyalgn_ctx *ctx, const poyalgn_cm *cm, const uint8_t *s1,
+                     int l1, const uint8_t *s2, int l2, int deltawh,
+                     int32_t *cost);
+
+/*
+ * algn_CAML_backtrace_2d (src/algn.c:3423-3440): aligned s1p/s2p (capacity
+ * cap each, results end at cap-1) from the fill of the last simple_2 call on
+ * the same s1/s2. swap = 1 prefers insertions over deletions on ties.
+ */
+int poyalgn_backtrace_2d(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                         const uint8_t *s1, int l1, const uint8_t *s2, int l2,
+                         uint8_t *s1p, uint8_t *s2p, int cap, int32_t *len,
+                         int swap);
+
+/* algn_CAML_align_2d (src/algn.c:3502-3512): simple_2 then backtrace_2d. */
+int poyalgn_align_2d(poyalgn_ctx *ctx, const poyalgn_cm *cm, const uint8_t *s1,
+                     int l1, const uint8_t *s2, int l2, uint8_t *s1p,
+                     uint8_t *s2p, int cap, int32_t *len, int deltawh,
+                     int swap, int32_t *cost);
+
+/*
+ * algn_CAML_align_affine_3 (src/algn.c:2358-2447): affine alignment of si
+ * (the shorter, li <= lj, else POYALGN_EINVAL like "pass the shorter one as
+ * first") with sj; writes resi, resj, median and medianwg (capacity cap
+ * each; lens = {len resi/resj, len median, len medianwg}) and the cost.
+ */
+int poyalgn_align_affine_3(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                           const uint8_t *si, int li, const uint8_t *sj, int lj,
+                           uint8_t *resi, uint8_t *resj, uint8_t *median,
+                           uint8_t *medianwg, int cap, int32_t *lens,
+                           int swaped, int32_t *cost);
+
+/*
+ * algn_CAML_ancestor_2 (src/algn.c:3741-3752) and
+ * seq_CAML_median_2_with_gaps (src/seq.c:287-298) and algn_CAML_worst_2
+ * (src/algn.c:3107-3118) on an aligned pair of length len: ancestor (cap
+ * >= len + 1, ends at cap-1), with-gap median (len), worst cost.
+ */
+int poyalgn_aligned_medians(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                            const uint8_t *a, const uint8_t *b, int len,
+                            uint8_t *ancestor, int cap, int32_t *anc_len,
+                            uint8_t *median_wg, int32_t *worst);
+
+/* ---- batched SeqCS.DOS.median ---------------------------------------------- */
+
+/*
+ * Median of every pair k (a = seqs[offa[k]..+lena[k]), b likewise) under the
+ * cost model of `cm` (linear or affine), exactly as DOS.median computes it
+ * with Algn_Normal. Pair k writes its aligned a/b (ea, eb), its median
+ * (ancestor_2 for linear, the backtrace median for affine; med) and its
+ * median with gaps (mwg) into [out_off[k], out_off[k] + cap_k) of each
+ * output buffer, cap_k = lena[k] + lenb[k] + 2, each ending at the last byte.
+ * cost/maxcost/alen/mlen/wlen/status are per pair.
+ *
+ * poyalgn_median_batch takes host pointers (copies in and out inside the
+ * call); poyalgn_median_batch_device takes device pointers and a cudaStream_t
+ * (as void *) and only enqueues work; max_pair_len bounds lena + lenb and
+ * out_bytes bounds out_off[k] + cap_k (the size of each output buffer).
+ * passes (optional) receives the band iterations run per pair.
+ */
+int poyalgn_median_batch(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
+                         const uint8_t *seqs, const int64_t *offa,
+                         const int32_t *lena, const int64_t *offb,
+                         const int32_t *lenb, const int64_t *out_off,
+                         int32_t *cost, int32_t *maxcost, int32_t *alen,
+                         int32_t *mlen, int32_t *wlen, int32_t *status,
+                         uint8_t *ea, uint8_t *eb, uint8_t *med, uint8_t *mwg,
+                         int32_t *passes);
+
+int poyalgn_median_batch_device(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                                int npairs, int max_pair_len,
+                                int64_t out_bytes, const uint8_t *seqs,
+                                const int64_t *offa,
+                                const int32_t *lena, const int64_t *offb,
+                                const int32_t *lenb, const int64_t *out_off,
+                                int32_t *cost, int32_t *maxcost, int32_t *alen,
+                                int32_t *mlen, int32_t *wlen, int32_t *status,
+                                uint8_t *ea, uint8_t *eb, uint8_t *med,
+                                uint8_t *mwg, int32_t *passes, void *stream);
+
+/* Number of kernel launches the last batch enqueued (for accounting). */
+int poyalgn_last_launches(const poyalgn_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* POYALGN_H */

@@ -1,0 +1,14 @@
+"""GB300-native direct-optimization pairwise alignment (POY's algn.c path).
+
+The compute path is the CUDA library ``libpoyalgn.so`` built from
+``poy5_gb300/csrc`` (see :mod:`poy5_gb300.build`); this package is its
+host-side interface.
+"""
+from .align import (Align, BatchResult, Context, CostMatrix, DOSMedian, PackedPairs,
+                    PoyAlgnError, count_gaps, deltaw_calc, dos_median, encode,
+                    median_batch, pack_pairs)
+
+__all__ = ["Align", "BatchResult", "Context", "CostMatrix", "DOSMedian", "PackedPairs",
+           "PoyAlgnError", "count_gaps", "deltaw_calc", "dos_median", "encode",
+           "median_batch", "pack_pairs"]
+__version__ = "0.1.0"

@@ -1,0 +1,83 @@
+"""ctypes binding of libpoyalgn.so (the C ABI in include/poyalgn.h).
+
+The library is the only compute path: importing this module on a machine
+without the built library, or calling into it without a CUDA device, raises.
+There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpoyalgn.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "poyalgn.h")
+
+_P = C.c_void_p
+_I = C.c_int
+_I64 = C.c_int64
+
+# POYALGN_* return codes
+EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, EPAIR = -1, -2, -3, -4, -5
+PAIR_STATUS = {0: "ok", -2: "output capacity exceeded", -3: "median should not be 0",
+               -4: "empty sequence or empty median", -5: "band wider than the largest pipeline",
+               -6: "sequence longer than 65535", 1: "not processed"}
+
+
+class PoyAlgnError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"poyalgn error {code}: {msg}")
+        self.code = code
+
+
+_SIGS = {
+    "poyalgn_init": (_I, [_I, C.POINTER(_P)]),
+    "poyalgn_free": (None, [_P]),
+    "poyalgn_last_error": (C.c_char_p, []),
+    "poyalgn_version": (C.c_char_p, []),
+    "poyalgn_cm_build": (_I, [_P, _P, _I, _I, C.POINTER(_P)]),
+    "poyalgn_cm_adopt": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, C.POINTER(_P)]),
+    "poyalgn_cm_tables": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "poyalgn_cm_free": (None, [_P]),
+    "poyalgn_simple_2": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
+    "poyalgn_backtrace_2d": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _I, _P, _I]),
+    "poyalgn_align_2d": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _I, _P, _I, _I, _P]),
+    "poyalgn_align_affine_3": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _I, _P, _I, _P]),
+    "poyalgn_aligned_medians": (_I, [_P, _P, _P, _P, _I, _P, _I, _P, _P, _P]),
+    "poyalgn_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
+    "poyalgn_median_batch_device": (_I, [_P, _P, _I, _I, _I64] + [_P] * 18),
+    "poyalgn_last_launches": (_I, [_P]),
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/poyalgn.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(poyalgn_[a-z0-9_]+)\s*\(", text)))
+
+
+def load() -> C.CDLL:
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FileNotFoundError(
+            f"{LIB_PATH} is missing: build it with `python -m poy5_gb300.build` "
+            "(the CUDA library is the only compute path)")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc != 0:
+        msg = load().poyalgn_last_error().decode(errors="replace")
+        raise PoyAlgnError(rc, msg)

@@ -1,0 +1,611 @@
+// C ABI of libpoyalgn.so (include/poyalgn.h): contexts, cost matrices, the
+// batched DOS.median driver and the per-call stubs that replace POY's
+// algn_CAML_* externals.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "../../include/poyalgn.h"
+#include "pa_kernels.h"
+#include "pa_tables.h"
+
+using namespace pa;
+
+namespace {
+
+thread_local char g_err[512];
+
+int set_err(int code, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CU(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return set_err(POYALGN_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                           __FILE__, __LINE__);                                         \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+int reserve(DevBuf& b, size_t bytes)
+{
+    if (bytes <= b.n && b.p) return 0;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(POYALGN_ENOMEM, "cudaMalloc of %zu bytes failed", want);
+    }
+    b.n = want;
+    return 0;
+}
+
+template <class T>
+T* as(DevBuf& b) { return reinterpret_cast<T*>(b.p); }
+
+}  // namespace
+
+struct poyalgn_cm {
+    HostCM h;
+    Tables t;
+    Tables* d = nullptr;
+};
+
+struct poyalgn_ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    int bps[2][NCLASS] = {{0}};
+    // host-pointer batches: staging of inputs and outputs
+    DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
+    // per-batch scratch
+    DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
+    DevBuf dwh, swp;
+    int last_launches = 0;
+    // per-call stub state: the fill of the last simple_2 / align_affine_3
+    bool call_valid = false;
+    int call_affine = 0, call_l1 = 0, call_l2 = 0;
+    const poyalgn_cm* call_cm = nullptr;
+    std::vector<uint8_t> call_s1, call_s2;
+    long long call_strides[NCLASS] = {0};
+};
+
+namespace {
+
+int ensure_device(poyalgn_ctx* c)
+{
+    CU(cudaSetDevice(c->device));
+    return 0;
+}
+
+// Enqueue one batch on `st`. All pointers are device pointers. `out_total`
+// bounds out_off[k] + cap_k (sizes the affine row-0 scratch).
+int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
+              int maxmn, long long out_total, const uint8_t* seqs,
+              const long long* offa, const int* lena, const long long* offb,
+              const int* lenb, const long long* out_off, int* cost, int* maxcost,
+              int* alen, int* mlen, int* wlen, int* status, uint8_t* ea,
+              uint8_t* eb, uint8_t* med, uint8_t* mwg, int* passes,
+              const int* dwh, const int* swp, int do_traceback, cudaStream_t st)
+{
+    int rc;
+    if (npairs <= 0) return 0;
+    if ((rc = reserve(c->pfull, (size_t)npairs * 4))) return rc;
+    if ((rc = reserve(c->eh0, (size_t)npairs * 4))) return rc;
+    if ((rc = reserve(c->lastcls, (size_t)npairs * 4))) return rc;
+    if ((rc = reserve(c->slabcta, (size_t)npairs * 4))) return rc;
+    if (!passes) {
+        if ((rc = reserve(c->passes, (size_t)npairs * 4))) return rc;
+        passes = as<int>(c->passes);
+    }
+    if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
+    if ((rc = reserve(c->qitems, (size_t)NCLASS * npairs * sizeof(int2)))) return rc;
+    if ((rc = reserve(c->qctr, 2 * NCLASS * sizeof(int)))) return rc;
+    if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
+
+    // persistent grid per class, bounded by a slab budget
+    size_t free_b = 0, total_b = 0;
+    CU(cudaMemGetInfo(&free_b, &total_b));
+    const long long budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
+    int grid[NCLASS];
+    long long strides[NCLASS];
+    long long arena = 0;
+    for (int k = 0; k < NCLASS; k++) {
+        const int pipes = class_pipes_per_cta(affine, k);
+        strides[k] = class_slab_bytes(affine, k, maxmn);
+        long long g = (long long)c->nsm * std::max(1, c->bps[affine][k]);
+        g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
+        g = std::min<long long>(g, std::max<long long>(1, budget / (strides[k] * pipes)));
+        grid[k] = (int)std::max<long long>(1, g);
+        arena = std::max(arena, (long long)grid[k] * pipes * strides[k]);
+    }
+    if ((rc = reserve(c->slab, (size_t)arena))) return rc;
+    CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
+    memcpy(c->call_strides, strides, sizeof(strides));
+    CU(cudaMemsetAsync(c->qctr.p, 0, 2 * NCLASS * sizeof(int), st));
+
+    BatchArgs A;
+    memset(&A, 0, sizeof(A));
+    A.seqs = seqs;
+    A.offa = offa;
+    A.lena = lena;
+    A.offb = offb;
+    A.lenb = lenb;
+    A.npairs = npairs;
+    A.affine = affine;
+    A.do_traceback = do_traceback;
+    A.tables = cm->d;
+    A.pfull = as<int>(c->pfull);
+    A.shadow = as<int>(c->shadow);
+    A.shadowEH0 = as<int>(c->eh0);
+    A.qitems = as<int2>(c->qitems);
+    A.qcount = as<int>(c->qctr);
+    A.qhead = as<int>(c->qctr) + NCLASS;
+    A.qcap = npairs;
+    A.slab = as<uint8_t>(c->slab);
+    A.out_off = out_off;
+    A.cost = cost;
+    A.maxcost = maxcost;
+    A.alen = alen;
+    A.mlen = mlen;
+    A.wlen = wlen;
+    A.status = status;
+    A.passes = passes;
+    A.lastcls = as<int>(c->lastcls);
+    A.slab_cta = as<int>(c->slabcta);
+    A.deltawh_override = dwh;
+    A.swap_override = swp;
+    A.ea = ea;
+    A.eb = eb;
+    A.med = med;
+    A.mwg = mwg;
+
+    int launches = 0;
+    launch_prep(A, st);
+    launches++;
+    for (int k = 0; k < NCLASS; k++) {
+        A.slab_stride = strides[k];
+        launch_class(A, k, grid[k], st);
+        launches++;
+    }
+    CU(cudaGetLastError());
+    c->last_launches = launches;
+    return 0;
+}
+
+int upload_cm(poyalgn_cm* m)
+{
+    kernel_tables(m->h, &m->t);
+    CU(cudaMalloc(&m->d, sizeof(Tables)));
+    CU(cudaMemcpy(m->d, &m->t, sizeof(Tables), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+// Stage a one-pair batch (a then b) into the context's buffers.
+int stage_pair(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int lb)
+{
+    int rc;
+    const int cap = la + lb + 2;
+    if ((rc = reserve(c->seqs, (size_t)la + lb))) return rc;
+    if ((rc = reserve(c->offa, 4 * sizeof(long long)))) return rc;
+    if ((rc = reserve(c->lena, 4 * sizeof(int)))) return rc;
+    if ((rc = reserve(c->ints, 16 * sizeof(int)))) return rc;
+    if ((rc = reserve(c->bytes, (size_t)4 * cap))) return rc;
+    if ((rc = reserve(c->dwh, sizeof(int)))) return rc;
+    if ((rc = reserve(c->swp, sizeof(int)))) return rc;
+    CU(cudaMemcpyAsync(as<uint8_t>(c->seqs), a, la, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(as<uint8_t>(c->seqs) + la, b, lb, cudaMemcpyHostToDevice, c->stream));
+    long long offs[3] = {0, la, 0};
+    int lens[2] = {la, lb};
+    CU(cudaMemcpyAsync(c->offa.p, offs, sizeof(offs), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->lena.p, lens, sizeof(lens), cudaMemcpyHostToDevice, c->stream));
+    return 0;
+}
+
+// Run the fill of the staged pair, keeping the final fill in the slab.
+int fill_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
+              const int* dwh_host, int32_t* cost)
+{
+    int rc;
+    const long long* offa = as<long long>(c->offa);
+    const int* lena = as<int>(c->lena);
+    int* ints = as<int>(c->ints);
+    uint8_t* bytes = as<uint8_t>(c->bytes);
+    const int cap = la + lb + 2;
+    const int* dwh = nullptr;
+    if (dwh_host) {
+        CU(cudaMemcpyAsync(c->dwh.p, dwh_host, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        dwh = as<int>(c->dwh);
+    }
+    // offa[2] = 0 is the output offset of the single pair
+    if ((rc = run_batch(c, cm, affine, 1, la + lb, cap, as<uint8_t>(c->seqs), offa, lena,
+                        offa + 1, lena + 1, offa + 2, ints + 0, ints + 1, ints + 2,
+                        ints + 3, ints + 4, ints + 5, bytes, bytes + cap,
+                        bytes + 2 * cap, bytes + 3 * cap, ints + 6, dwh, nullptr, 0,
+                        c->stream)))
+        return rc;
+    int h[7];
+    CU(cudaMemcpyAsync(h, ints, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (h[5] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[5]);
+    *cost = h[0];
+    return 0;
+}
+
+// Trace back the staged pair's kept fill with tie preference `swap`.
+int trace_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
+               int swap, int* res)
+{
+    const long long* offa = as<long long>(c->offa);
+    const int* lena = as<int>(c->lena);
+    int* ints = as<int>(c->ints);
+    uint8_t* bytes = as<uint8_t>(c->bytes);
+    const int cap = la + lb + 2;
+    CU(cudaMemcpyAsync(c->swp.p, &swap, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    BatchArgs A;
+    memset(&A, 0, sizeof(A));
+    A.seqs = as<uint8_t>(c->seqs);
+    A.offa = offa;
+    A.lena = lena;
+    A.offb = offa + 1;
+    A.lenb = lena + 1;
+    A.out_off = offa + 2;
+    A.npairs = 1;
+    A.affine = affine;
+    A.tables = cm->d;
+    A.slab = as<uint8_t>(c->slab);
+    A.cost = ints + 0;
+    A.maxcost = ints + 1;
+    A.alen = ints + 2;
+    A.mlen = ints + 3;
+    A.wlen = ints + 4;
+    A.status = ints + 5;
+    A.lastcls = as<int>(c->lastcls);
+    A.slab_cta = as<int>(c->slabcta);
+    A.swap_override = as<int>(c->swp);
+    A.ea = bytes;
+    A.eb = bytes + cap;
+    A.med = bytes + 2 * cap;
+    A.mwg = bytes + 3 * cap;
+    launch_traceback(A, as<long long>(c->strides), c->stream);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(res, ints, 6 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (res[5] != 0) return set_err(POYALGN_EINVAL, "traceback failed (status %d)", res[5]);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* poyalgn_last_error(void) { return g_err; }
+
+const char* poyalgn_version(void) { return "poyalgn 0.1 sm_103a"; }
+
+int poyalgn_init(int device, poyalgn_ctx** out)
+{
+    if (!out) return set_err(POYALGN_EINVAL, "null output");
+    *out = nullptr;
+    int n = 0;
+    CU(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return set_err(POYALGN_EINVAL, "no CUDA device %d", device);
+    poyalgn_ctx* c = new (std::nothrow) poyalgn_ctx;
+    if (!c) return set_err(POYALGN_ENOMEM, "context allocation");
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return set_err(POYALGN_ECUDA, "device setup: %s", cudaGetErrorString(e));
+    }
+    for (int a = 0; a < 2; a++)
+        for (int k = 0; k < NCLASS; k++) c->bps[a][k] = class_blocks_per_sm(a, k);
+    *out = c;
+    return 0;
+}
+
+void poyalgn_free(poyalgn_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    DevBuf* bufs[] = {&c->seqs, &c->offa, &c->lena, &c->offb, &c->lenb, &c->outoff,
+                      &c->ints, &c->bytes, &c->pfull, &c->eh0, &c->lastcls, &c->slabcta,
+                      &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
+                      &c->dwh, &c->swp};
+    for (DevBuf* b : bufs)
+        if (b->p) cudaFree(b->p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int poyalgn_cm_build(poyalgn_ctx* ctx, const int32_t* tcm, int alph, int gap_open,
+                     poyalgn_cm** out)
+{
+    if (!ctx || !tcm || !out) return set_err(POYALGN_EINVAL, "null argument");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    poyalgn_cm* m = new (std::nothrow) poyalgn_cm;
+    if (!m) return set_err(POYALGN_ENOMEM, "cost matrix allocation");
+    rc = build_cm(&m->h, tcm, alph, gap_open);
+    if (rc) {
+        delete m;
+        return set_err(rc == -1 ? POYALGN_EUNSUPPORTED : POYALGN_EINVAL,
+                       "cost matrix rejected (alph %d, gap_open %d)", alph, gap_open);
+    }
+    if ((rc = upload_cm(m))) {
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return 0;
+}
+
+int poyalgn_cm_adopt(poyalgn_ctx* ctx, int lcm, int gap, int a_sz, int combinations,
+                     int cost_model, int gap_open, const int32_t* cost,
+                     const uint8_t* median, const int32_t* worst, const int32_t* tail,
+                     const int32_t* prepend, poyalgn_cm** out)
+{
+    if (!ctx || !cost || !median || !worst || !tail || !prepend || !out)
+        return set_err(POYALGN_EINVAL, "null argument");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    poyalgn_cm* m = new (std::nothrow) poyalgn_cm;
+    if (!m) return set_err(POYALGN_ENOMEM, "cost matrix allocation");
+    if (adopt_cm(&m->h, lcm, gap, a_sz, combinations, cost_model, gap_open, cost, median,
+                 worst, tail, prepend)) {
+        delete m;
+        return set_err(POYALGN_EUNSUPPORTED, "only bitset alphabets with lcm <= 5");
+    }
+    if ((rc = upload_cm(m))) {
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return 0;
+}
+
+int poyalgn_cm_tables(const poyalgn_cm* m, int32_t* cost, uint8_t* median, int32_t* worst,
+                      int32_t* tail, int32_t* prepend, int32_t* info)
+{
+    if (!m) return set_err(POYALGN_EINVAL, "null cost matrix");
+    const int n = 2 * (1 << m->h.lcm) * (1 << m->h.lcm);
+    if (cost) memcpy(cost, m->h.cost, (size_t)n * 4);
+    if (worst) memcpy(worst, m->h.worst, (size_t)n * 4);
+    if (tail) memcpy(tail, m->h.tail, (size_t)n * 4);
+    if (prepend) memcpy(prepend, m->h.prepend, (size_t)n * 4);
+    if (median) memcpy(median, m->h.median, (size_t)n);
+    if (info) {
+        info[0] = m->h.lcm;
+        info[1] = m->h.gap;
+        info[2] = m->h.a_sz;
+        info[3] = m->h.combinations;
+        info[4] = m->h.cost_model;
+        info[5] = m->h.gap_open;
+        info[6] = m->h.mnz;
+    }
+    return n;
+}
+
+void poyalgn_cm_free(poyalgn_cm* m)
+{
+    if (!m) return;
+    if (m->d) cudaFree(m->d);
+    delete m;
+}
+
+int poyalgn_simple_2(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, int l1,
+                     const uint8_t* s2, int l2, int deltawh, int32_t* cost)
+{
+    if (!ctx || !cm || !s1 || !s2 || !cost) return set_err(POYALGN_EINVAL, "null argument");
+    if (l1 < 1 || l2 < 1) return set_err(POYALGN_EINVAL, "empty sequence");
+    if (l1 > l2) return set_err(POYALGN_EINVAL, "pass the shorter sequence first");
+    int rc;
+    ctx->call_valid = false;
+    if ((rc = ensure_device(ctx))) return rc;
+    if ((rc = stage_pair(ctx, s1, l1, s2, l2))) return rc;
+    if ((rc = fill_pair(ctx, cm, 0, l1, l2, &deltawh, cost))) return rc;
+    ctx->call_valid = true;
+    ctx->call_affine = 0;
+    ctx->call_cm = cm;
+    ctx->call_l1 = l1;
+    ctx->call_l2 = l2;
+    ctx->call_s1.assign(s1, s1 + l1);
+    ctx->call_s2.assign(s2, s2 + l2);
+    return 0;
+}
+
+int poyalgn_backtrace_2d(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, int l1,
+                         const uint8_t* s2, int l2, uint8_t* s1p, uint8_t* s2p, int cap,
+                         int32_t* len, int swap)
+{
+    if (!ctx || !cm || !s1 || !s2 || !s1p || !s2p || !len)
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (!ctx->call_valid || ctx->call_affine || ctx->call_l1 != l1 || ctx->call_l2 != l2 ||
+        memcmp(ctx->call_s1.data(), s1, l1) || memcmp(ctx->call_s2.data(), s2, l2))
+        return set_err(POYALGN_EINVAL, "backtrace_2d needs the fill of simple_2 on the same pair");
+    int rc, res[6];
+    if ((rc = ensure_device(ctx))) return rc;
+    if ((rc = trace_pair(ctx, cm, 0, l1, l2, swap ? 1 : 0, res))) return rc;
+    const int L = res[2], pcap = l1 + l2 + 2;
+    if (L > cap) return set_err(POYALGN_EINVAL, "capacity %d < aligned length %d", cap, L);
+    uint8_t* bytes = as<uint8_t>(ctx->bytes);
+    const uint8_t* ea = bytes + (pcap - L);
+    const uint8_t* eb = bytes + pcap + (pcap - L);
+    // the traceback writes caller order; with swap the first sequence is y
+    CU(cudaMemcpy(s1p + cap - L, swap ? eb : ea, L, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(s2p + cap - L, swap ? ea : eb, L, cudaMemcpyDeviceToHost));
+    *len = L;
+    return 0;
+}
+
+int poyalgn_align_2d(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, int l1,
+                     const uint8_t* s2, int l2, uint8_t* s1p, uint8_t* s2p, int cap,
+                     int32_t* len, int deltawh, int swap, int32_t* cost)
+{
+    int rc = poyalgn_simple_2(ctx, cm, s1, l1, s2, l2, deltawh, cost);
+    if (rc) return rc;
+    return poyalgn_backtrace_2d(ctx, cm, s1, l1, s2, l2, s1p, s2p, cap, len, swap);
+}
+
+int poyalgn_align_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* si, int li,
+                           const uint8_t* sj, int lj, uint8_t* resi, uint8_t* resj,
+                           uint8_t* median, uint8_t* medianwg, int cap, int32_t* lens,
+                           int swaped, int32_t* cost)
+{
+    if (!ctx || !cm || !si || !sj || !resi || !resj || !median || !medianwg || !lens || !cost)
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (lj < li) return set_err(POYALGN_EINVAL, "pass the shorter one as first");
+    if (li < 1 || (li == 1 && lj == 1)) return set_err(POYALGN_EINVAL, "empty sequences");
+    int rc, res[6];
+    ctx->call_valid = false;
+    if ((rc = ensure_device(ctx))) return rc;
+    if ((rc = stage_pair(ctx, si, li, sj, lj))) return rc;
+    if ((rc = fill_pair(ctx, cm, 1, li, lj, nullptr, cost))) return rc;
+    if ((rc = trace_pair(ctx, cm, 1, li, lj, swaped ? 1 : 0, res))) return rc;
+    const int L = res[2], ML = res[3], WL = res[4], pcap = li + lj + 2;
+    if (L > cap || ML > cap || WL > cap) return set_err(POYALGN_EINVAL, "capacity %d too small", cap);
+    uint8_t* bytes = as<uint8_t>(ctx->bytes);
+    const uint8_t* ea = bytes + (pcap - L);
+    const uint8_t* eb = bytes + pcap + (pcap - L);
+    CU(cudaMemcpy(resi + cap - L, swaped ? eb : ea, L, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(resj + cap - L, swaped ? ea : eb, L, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(median + cap - ML, bytes + 2 * pcap + (pcap - ML), ML, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(medianwg + cap - WL, bytes + 3 * pcap + (pcap - WL), WL, cudaMemcpyDeviceToHost));
+    lens[0] = L;
+    lens[1] = ML;
+    lens[2] = WL;
+    return 0;
+}
+
+int poyalgn_aligned_medians(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* a,
+                            const uint8_t* b, int len, uint8_t* ancestor, int cap,
+                            int32_t* anc_len, uint8_t* median_wg, int32_t* worst)
+{
+    if (!ctx || !cm || !a || !b || !ancestor || !anc_len || !median_wg || !worst)
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (len < 1) return set_err(POYALGN_EINVAL, "empty alignment");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    if ((rc = reserve(ctx->seqs, (size_t)2 * len))) return rc;
+    if ((rc = reserve(ctx->bytes, (size_t)2 * len + 2))) return rc;
+    if ((rc = reserve(ctx->ints, 16 * sizeof(int)))) return rc;
+    uint8_t* d = as<uint8_t>(ctx->seqs);
+    uint8_t* o = as<uint8_t>(ctx->bytes);
+    CU(cudaMemcpyAsync(d, a, len, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d + len, b, len, cudaMemcpyHostToDevice, ctx->stream));
+    launch_aligned_medians(cm->d, d, d + len, len, o, o + len + 1, as<int>(ctx->ints), ctx->stream);
+    CU(cudaGetLastError());
+    int h[3];
+    CU(cudaMemcpyAsync(h, ctx->ints.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (h[2] != 0) return set_err(POYALGN_EINVAL, "median should not be 0");
+    if (h[0] > cap) return set_err(POYALGN_EINVAL, "ancestor capacity %d < %d", cap, h[0]);
+    CU(cudaMemcpy(ancestor + cap - h[0], o, h[0], cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(median_wg, o + len + 1, len, cudaMemcpyDeviceToHost));
+    *anc_len = h[0];
+    *worst = h[1];
+    return 0;
+}
+
+int poyalgn_median_batch_device(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
+                                int max_pair_len, int64_t out_bytes, const uint8_t* seqs,
+                                const int64_t* offa, const int32_t* lena, const int64_t* offb,
+                                const int32_t* lenb, const int64_t* out_off, int32_t* cost,
+                                int32_t* maxcost, int32_t* alen, int32_t* mlen, int32_t* wlen,
+                                int32_t* status, uint8_t* ea, uint8_t* eb, uint8_t* med,
+                                uint8_t* mwg, int32_t* passes, void* stream)
+{
+    if (!ctx || !cm) return set_err(POYALGN_EINVAL, "null argument");
+    if (npairs < 0 || max_pair_len < 2 || out_bytes < 1) return set_err(POYALGN_EINVAL, "bad batch shape");
+    if (npairs == 0) return 0;
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    return run_batch(ctx, cm, cm->h.cost_model == 1, npairs, max_pair_len, out_bytes, seqs,
+                     reinterpret_cast<const long long*>(offa), lena,
+                     reinterpret_cast<const long long*>(offb), lenb,
+                     reinterpret_cast<const long long*>(out_off), cost, maxcost, alen, mlen,
+                     wlen, status, ea, eb, med, mwg, passes, nullptr, nullptr, 1,
+                     (cudaStream_t)stream);
+}
+
+int poyalgn_median_batch(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
+                         const uint8_t* seqs, const int64_t* offa, const int32_t* lena,
+                         const int64_t* offb, const int32_t* lenb, const int64_t* out_off,
+                         int32_t* cost, int32_t* maxcost, int32_t* alen, int32_t* mlen,
+                         int32_t* wlen, int32_t* status, uint8_t* ea, uint8_t* eb,
+                         uint8_t* med, uint8_t* mwg, int32_t* passes)
+{
+    if (!ctx || !cm || (npairs > 0 && (!seqs || !offa || !lena || !offb || !lenb || !out_off ||
+                                       !cost || !maxcost || !alen || !mlen || !wlen || !status ||
+                                       !ea || !eb || !med || !mwg)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (npairs <= 0) return 0;
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    long long seq_bytes = 0, out_total = 0;
+    int maxmn = 2;
+    for (int k = 0; k < npairs; k++) {
+        if (lena[k] < 1 || lenb[k] < 1) return set_err(POYALGN_EINVAL, "pair %d: empty sequence", k);
+        seq_bytes = std::max<long long>(seq_bytes, std::max(offa[k] + lena[k], offb[k] + lenb[k]));
+        out_total = std::max<long long>(out_total, out_off[k] + lena[k] + lenb[k] + 2);
+        maxmn = std::max(maxmn, lena[k] + lenb[k]);
+    }
+    const size_t ni = (size_t)npairs;
+    if ((rc = reserve(ctx->seqs, (size_t)seq_bytes))) return rc;
+    if ((rc = reserve(ctx->offa, ni * 8))) return rc;
+    if ((rc = reserve(ctx->offb, ni * 8))) return rc;
+    if ((rc = reserve(ctx->lena, ni * 4))) return rc;
+    if ((rc = reserve(ctx->lenb, ni * 4))) return rc;
+    if ((rc = reserve(ctx->outoff, ni * 8))) return rc;
+    if ((rc = reserve(ctx->ints, ni * 4 * 7))) return rc;
+    if ((rc = reserve(ctx->bytes, (size_t)out_total * 4))) return rc;
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(ctx->seqs.p, seqs, (size_t)seq_bytes, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->offa.p, offa, ni * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->offb.p, offb, ni * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->lena.p, lena, ni * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->lenb.p, lenb, ni * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->outoff.p, out_off, ni * 8, cudaMemcpyHostToDevice, st));
+    int* I = as<int>(ctx->ints);
+    uint8_t* B = as<uint8_t>(ctx->bytes);
+    const size_t ot = (size_t)out_total;
+    if ((rc = run_batch(ctx, cm, cm->h.cost_model == 1, npairs, maxmn, out_total,
+                        as<uint8_t>(ctx->seqs), as<long long>(ctx->offa), as<int>(ctx->lena),
+                        as<long long>(ctx->offb), as<int>(ctx->lenb), as<long long>(ctx->outoff),
+                        I, I + ni, I + 2 * ni, I + 3 * ni, I + 4 * ni, I + 5 * ni, B, B + ot,
+                        B + 2 * ot, B + 3 * ot, I + 6 * ni, nullptr, nullptr, 1, st)))
+        return rc;
+    int32_t* outs[7] = {cost, maxcost, alen, mlen, wlen, status, passes};
+    for (int j = 0; j < 7; j++)
+        if (outs[j]) CU(cudaMemcpyAsync(outs[j], I + j * ni, ni * 4, cudaMemcpyDeviceToHost, st));
+    uint8_t* bo[4] = {ea, eb, med, mwg};
+    for (int j = 0; j < 4; j++)
+        CU(cudaMemcpyAsync(bo[j], B + j * ot, ot, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    for (int k = 0; k < npairs; k++)
+        if (status[k] != 0) return set_err(POYALGN_EPAIR, "pair %d failed with status %d", k, status[k]);
+    return 0;
+}
+
+int poyalgn_last_launches(const poyalgn_ctx* ctx) { return ctx ? ctx->last_launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,853 @@
+// Core of the GB300 direct-optimization aligner: cell rules, band schedule,
+// lane-pipeline step functions and tracebacks.
+//
+// Everything in this header is plain arithmetic on registers and pointers so
+// that the same code is compiled into the CUDA kernels (pa_kernels.cu) and,
+// for testing only, into a host build that replays the lane pipeline one lane
+// at a time (pa_emul.cpp).
+//
+// Fill layout ("lane pipeline"): a pipeline of P lanes (one CTA of P/32
+// warps) aligns one pair. Lane g owns blocks of R consecutive rows; block b of
+// the pair (rows 1 + bR .. bR + R) belongs to lane b mod P. All lanes step
+// through anti-diagonals T = i + j together; at step T a lane computes cell
+// (i, T - i) of each of its R rows that lies inside the band. Row q of a block
+// reads its up/diagonal neighbours from row q-1 of the same lane (registers)
+// and the top row reads them from the bottom row of lane g-1, which arrive by
+// a rotating warp shuffle (shared memory across warp boundaries). Because the
+// band shifts one column per row, a block of R rows is live for W + 2R - 2
+// steps; the (P, R) pair is chosen so that the next block of the same lane
+// (P*R rows further down) cannot start before the current one has drained
+// (see band_fits).
+//
+// Direction codes are stored per step: dm[T * P*R + g*R + q], so every step of
+// a warp is one contiguous store.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define PA_HD __host__ __device__ __forceinline__
+#else
+#define PA_HD static inline
+#endif
+
+namespace pa {
+
+constexpr int HIGH = 1000000;   // POY's "infinite" cost, src/algn.c:37
+constexpr int NSTATE = 32;      // table rows: states < 1 << lcm, lcm <= 5
+constexpr int CSW_STRIDE = 64;  // swizzled cost row: two copies of a row
+
+// linear direction bits (src/matrices.h:22-27)
+enum : int { L_ALIGN = 1, L_INSERT = 2, L_DELETE = 4 };
+
+// affine direction flags (src/algn.c:1185-1199)
+enum : int {
+    A2A = 1, A2V = 2, A2H = 4, A2D = 8,
+    BEG_B = 16, END_B = 32, BEG_V = 64, END_V = 128, BEG_H = 256, END_H = 512,
+    DO_A = 1024, DO_V = 2048, DO_H = 4096, H_EQ_V = 8192, DO_D = 16384
+};
+constexpr int TMPGAP = 16;   // affine code hard-wires the DNA gap bit
+constexpr int NTMPGAP = 15;
+
+// Cost-matrix tables as the kernels see them (copied into shared memory).
+// Costs are stored twice per row at a per-row rotation so that a warp whose
+// lanes look up different (row, column) pairs of the DNA singletons hits 16
+// different banks: cost(a, b) = csw[rowoff[a] + b].
+struct Tables {
+    int csw[NSTATE * CSW_STRIDE];
+    int rowoff[NSTATE];
+    int worst[NSTATE * NSTATE];
+    int tail[NSTATE];
+    int prepend[NSTATE];
+    uint8_t median[NSTATE * NSTATE];
+    int gap, lcm, go, mnz, comb, model, a_sz, pad;
+};
+
+PA_HD int tcost(const Tables& t, int a, int b) { return t.csw[t.rowoff[a] + b]; }
+PA_HD int tmin(int a, int b) { return a < b ? a : b; }
+PA_HD int tmax(int a, int b) { return a > b ? a : b; }
+
+// per-halfword unsigned max of two packed u16 pairs
+PA_HD uint32_t vmax2(uint32_t a, uint32_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __vmaxu2(a, b);
+#else
+    uint32_t lo = tmax((int)(a & 0xFFFF), (int)(b & 0xFFFF));
+    uint32_t hi = tmax((int)(a >> 16), (int)(b >> 16));
+    return lo | (hi << 16);
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Pipeline shapes. A "class" is a (K warps, R rows per lane) shape; a pair
+// moves up the ladder as its band doubles. Linear and affine use different
+// ladders because affine lanes hold more state per row.
+
+constexpr int NCLASS = 8;
+// Top shapes are bounded by registers: a 512-thread CTA leaves 128 registers
+// per thread, enough for 8 linear rows or 4 affine rows per lane.
+PA_HD int class_K(int affine, int c)
+{
+    const int lk[NCLASS] = {1, 1, 1, 1, 2, 4, 8, 16};
+    const int ak[NCLASS] = {1, 1, 1, 2, 4, 8, 16, 16};
+    return affine ? ak[c] : lk[c];
+}
+PA_HD int class_R(int affine, int c)
+{
+    const int lr[NCLASS] = {1, 2, 4, 8, 8, 8, 8, 8};
+    const int ar[NCLASS] = {1, 2, 4, 4, 4, 4, 4, 4};
+    return affine ? ar[c] : lr[c];
+}
+
+// A (P, R) pipeline processes a band of unclipped width wu over n columns
+// without two blocks of one lane overlapping in time when either bound holds
+// (next block start >= current block end + 2).
+PA_HD bool band_fits(int P, int R, long long wu, int n)
+{
+    long long pr = (long long)(P - 1) * R;
+    return (wu <= 2 * pr + 1) || (pr >= n);
+}
+
+// Smallest class for a band; -1 if none. wu < 0 means "full plane".
+PA_HD int pick_class(int affine, long long wu, int n)
+{
+    for (int c = 0; c < NCLASS; c++) {
+        int P = 32 * class_K(affine, c);
+        if (band_fits(P, class_R(affine, c), wu < 0 ? (1LL << 40) : wu, n)) return c;
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Linear band (algn_newkk_test, src/algn.c:1063-1114; full plane :927-973)
+
+struct LinBand {
+    int m, n, D;    // rows (len of shorter incl. leading gap), cols, n - m
+    int newk;       // band half-width (clipped to m - 1)
+    int first;      // cells of row 0 that are filled
+    int full;       // algn_fill_plane semantics
+};
+
+PA_HD LinBand lin_band(int m, int n, int full, int p)
+{
+    LinBand b;
+    b.m = m;
+    b.n = n;
+    b.D = n - m;
+    b.full = full;
+    if (full) {
+        b.newk = m - 1;
+        b.first = n;
+    } else {
+        b.newk = p >= m ? m - 1 : p;
+        int f = n - m + 1 + p;
+        b.first = f > n ? n : f;
+    }
+    return b;
+}
+PA_HD int lin_hasL(const LinBand& b, int i) { return !b.full && (i - b.newk) > 0; }
+PA_HD int lin_hasR(const LinBand& b, int i) { return !b.full && (i + b.D + b.newk) <= (b.n - 1); }
+PA_HD int lin_s(const LinBand& b, int i) { return lin_hasL(b, i) ? i - b.newk : 0; }
+PA_HD int lin_e(const LinBand& b, int i) { return lin_hasR(b, i) ? i + b.D + b.newk : b.n - 1; }
+// unclipped width used to pick the pipeline class
+PA_HD long long lin_wu(const LinBand& b) { return b.full ? -1 : (long long)b.D + 2LL * b.newk + 1; }
+
+// Affine band (algn_newkk_test_aff, src/algn.c:2185-2306). Rows i = 1..m-1,
+// columns 0..n-1 (the reference's leni = m-1, lenj = n-1).
+struct AffBand {
+    int m, n, D;
+    int newk;       // clipped to leni - 1 = m - 2
+};
+PA_HD AffBand aff_band(int m, int n, int p)
+{
+    AffBand b;
+    b.m = m;
+    b.n = n;
+    b.D = n - m;
+    int lenX = m - 1;
+    b.newk = p >= lenX ? lenX - 1 : p;
+    return b;
+}
+PA_HD int aff_s(const AffBand& b, int i) { return (i - b.newk) > 0 ? i - b.newk : 0; }
+PA_HD int aff_e(const AffBand& b, int i) { return tmin(b.n - 1, i + b.D + b.newk); }
+PA_HD long long aff_wu(const AffBand& b) { return (long long)b.D + 2LL * b.newk + 1; }
+
+// HAS_GAP_OPENING with gapstart <= 1 (src/algn.c:1236-1253)
+PA_HD int gap_opening(int idx, int prev, int curr, int gap, int go)
+{
+    if (idx == 1 && (gap & curr)) return 0;
+    if (idx > 1 && !(gap & prev) && (gap & curr)) return 0;
+    return go;
+}
+
+// Slab addressing shared by the fills and the tracebacks.
+PA_HD long long dm_index(int P, int R, int i, int j)
+{
+    int b = (i - 1) / R;
+    int g = b % P;
+    int q = (i - 1) - b * R;
+    return (long long)(i + j) * (P * R) + g * R + q;
+}
+
+// ---------------------------------------------------------------------------
+// Linear lane state and step
+
+template <int R>
+struct LinLane {
+    int V[R], Vp[R];        // cost at steps T-1, T-2 of each row
+    uint32_t N[R], Np[R];   // forward gap counts (#ins | #del << 16)
+    int J[R], G[R];         // column symbol s2[j] and its insert cost
+    int rb[R], dc[R];       // cost-row offset and delete cost of the row symbol
+    int ic[R];
+    int itop;               // first row of the current block
+    int nstart;             // step at which the lane moves to its next block
+    int sV, sVp;            // neighbour bottom row at T-1 / T-2
+    uint32_t sN, sNp;
+    int gV, gVp;            // row-0 generator (lane 0, first block)
+};
+
+PA_HD int block_start_step_lin(const LinBand& b, int itop)
+{
+    return itop <= b.m - 1 ? itop + lin_s(b, itop) : 0x7fffffff;
+}
+
+template <int R>
+PA_HD void lin_enter_block(LinLane<R>& L, const LinBand& b, const Tables& t,
+                           const uint8_t* s1, int itop, int P)
+{
+    L.itop = itop;
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        int i = itop + q;
+        int c = i <= b.m - 1 ? s1[i] : 0;
+        L.ic[q] = c;
+        L.rb[q] = t.rowoff[c];
+        L.dc[q] = t.csw[t.rowoff[c] + t.gap];
+    }
+    L.nstart = block_start_step_lin(b, itop + P * R);
+}
+
+template <int R>
+PA_HD void lin_lane_init(LinLane<R>& L, const LinBand& b, const Tables& t,
+                         const uint8_t* s1, int g, int P)
+{
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        L.V[q] = L.Vp[q] = 0;
+        L.N[q] = L.Np[q] = 0;
+        L.J[q] = 0;
+        L.G[q] = 0;
+    }
+    L.sV = L.sVp = L.gV = L.gVp = 0;
+    L.sN = L.sNp = 0;
+    lin_enter_block(L, b, t, s1, 1 + g * R, P);
+}
+
+// One anti-diagonal step of one lane. recvV/recvN: bottom row of lane g-1
+// after step T-1. dcode[q] receives the direction code of row q (0 when the
+// row has no cell in the band at this step).
+template <int R>
+PA_HD void lin_step(LinLane<R>& L, const LinBand& b, const Tables& t,
+                    const uint8_t* s1, const uint8_t* s2, int P, int T,
+                    int recvV, uint32_t recvN, int (&dcode)[R])
+{
+    L.sVp = L.sV;
+    L.sNp = L.sN;
+    L.sV = recvV;
+    L.sN = recvN;
+    const bool moved = (T >= L.nstart);
+    if (moved) lin_enter_block(L, b, t, s1, L.itop + P * R, P);
+    const bool gen = (L.itop == 1);
+    if (gen) {  // row 0 at column T-1: prefix sums of the prepend costs
+        int j0 = T - 1;
+        L.gVp = L.gV;
+        if (j0 == 0) L.gV = 0;
+        else if (j0 < b.first) L.gV += t.prepend[s2[j0]];
+    }
+    if (moved) {  // a new block: every row needs its own column
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            int j = T - L.itop - q;
+            int c = (j >= 0 && j < b.n) ? s2[j] : 0;
+            L.J[q] = c;
+            L.G[q] = tcost(t, t.gap, c);
+        }
+    } else {  // row q takes row q-1's column of the previous step
+#pragma unroll
+        for (int q = R - 1; q > 0; q--) {
+            L.J[q] = L.J[q - 1];
+            L.G[q] = L.G[q - 1];
+        }
+        int j = T - L.itop;
+        int c = (j >= 0 && j < b.n) ? s2[j] : 0;
+        L.J[0] = c;
+        L.G[0] = tcost(t, t.gap, c);
+    }
+#pragma unroll
+    for (int q = R - 1; q >= 0; q--) {
+        const int i = L.itop + q;
+        const int j = T - i;
+        int upV, dgV;
+        uint32_t upN, dgN;
+        if (q > 0) {
+            upV = L.V[q - 1]; upN = L.N[q - 1];
+            dgV = L.Vp[q - 1]; dgN = L.Np[q - 1];
+        } else if (gen) {
+            upV = L.gV; upN = (uint32_t)(T - 1);
+            dgV = L.gVp; dgN = (uint32_t)(T - 2);
+        } else {
+            upV = L.sV; upN = L.sN;
+            dgV = L.sVp; dgN = L.sNp;
+        }
+        const int lfV = L.V[q];
+        const uint32_t lfN = L.N[q];
+        L.Vp[q] = L.V[q];
+        L.Np[q] = L.N[q];
+        dcode[q] = 0;
+        if (i <= b.m - 1) {
+            const int hasL = lin_hasL(b, i), hasR = lin_hasR(b, i);
+            const int s = hasL ? i - b.newk : 0;
+            const int e = hasR ? i + b.D + b.newk : b.n - 1;
+            if (j >= s && j <= e) {
+                int v, d;
+                const int ic = L.ic[q];
+                if (j == 0) {
+                    v = upV + (b.full ? L.dc[q] : t.tail[ic]);
+                    d = L_DELETE;
+                } else {
+                    const int aln = dgV + t.csw[L.rb[q] + L.J[q]];
+                    if (hasL && j == s) {
+                        if (hasR && e == s) {
+                            v = aln;
+                            d = L_ALIGN;
+                        } else {
+                            const int del = upV + L.dc[q];
+                            if (del < aln) { v = del; d = L_DELETE; }
+                            else if (aln < del) { v = aln; d = L_ALIGN; }
+                            else { v = del; d = L_ALIGN | L_DELETE; }
+                        }
+                    } else if (hasR && j == e) {
+                        const int ins = lfV + L.G[q];
+                        if (ins < aln) { v = ins; d = L_INSERT; }
+                        else if (aln < ins) { v = aln; d = L_ALIGN; }
+                        else { v = aln; d = L_ALIGN | L_INSERT; }
+                    } else {
+                        const int del = upV + L.dc[q];
+                        const int ins = lfV + L.G[q];
+                        v = tmin(tmin(aln, ins), del);
+                        d = (aln == v ? L_ALIGN : 0) | (ins == v ? L_INSERT : 0) |
+                            (del == v ? L_DELETE : 0);
+                    }
+                }
+                if (!hasR && j == b.n - 1 && j > 0) {  // last column: tail delete
+                    const int cst = t.tail[ic] + upV;
+                    if (cst < v) { v = cst; d = L_DELETE; }
+                    else if (cst == v) d |= L_DELETE;
+                }
+                // forward gap count along the path backtrace_2d_gaps follows
+                const uint32_t cn = (d & L_ALIGN) ? dgN : (d & L_INSERT) ? lfN + 1u : upN + 0x10000u;
+                L.V[q] = v;
+                L.N[q] = cn;
+                dcode[q] = d;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Affine lane state and step (algn_newkk_fill_a_row_aff, src/algn.c:2112-2180,
+// cells :1220-1492, ASSIGN_MINIMUM :1935-1981, gap numbers :126-176)
+
+struct AffCell {
+    int EH, EV, EB, CB;
+    uint32_t GM;  // gap numbers: gm1 | gm2 << 16
+};
+
+template <int R>
+struct AffLane {
+    AffCell V[R], Vp[R];
+    int J[R], Jm[R];                 // sj[j], sj[j-1] for the row's column
+    int sgext[R], sgop[R], svext[R]; // per-row constants
+    int srb[R];                      // cost row of (row symbol & 15)
+    int icf[R];                      // bit0: ic has gap, bit1: ip has gap, bit2: ic == ic & 15
+    int itop, nstart;
+    AffCell s, sp;                   // neighbour bottom row at T-1 / T-2
+    AffCell g, gp;                   // row-0 generator (lane 0, first block)
+    int gCB;                         // running CB of row 0
+};
+
+PA_HD int block_start_step_aff(const AffBand& b, int itop)
+{
+    return itop <= b.m - 1 ? itop + aff_s(b, itop) : 0x7fffffff;
+}
+
+template <int R>
+PA_HD void aff_enter_block(AffLane<R>& L, const AffBand& b, const Tables& t,
+                           const uint8_t* si, int itop, int P)
+{
+    L.itop = itop;
+    const int gap = t.gap, go = t.go;
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        int i = itop + q;
+        int ic = 0, ip = 0;
+        if (i <= b.m - 1) {
+            ic = si[i];
+            ip = si[i - 1];
+        }
+        int sg = tcost(t, ic, gap);
+        int so = gap_opening(i, ip, ic, gap, go);
+        L.sgext[q] = sg;
+        L.sgop[q] = so;
+        L.svext[q] = ((i > 1) && ((ip & gap) && !(ic & gap))) ? so + sg : sg;
+        L.srb[q] = t.rowoff[NTMPGAP & ic];
+        L.icf[q] = ((ic & TMPGAP) ? 1 : 0) | ((ip & TMPGAP) ? 2 : 0) | ((ic == (NTMPGAP & ic)) ? 4 : 0);
+    }
+    L.nstart = block_start_step_aff(b, itop + P * R);
+}
+
+template <int R>
+PA_HD void aff_lane_init(AffLane<R>& L, const AffBand& b, const Tables& t,
+                         const uint8_t* si, int g, int P)
+{
+    const AffCell z = {0, 0, 0, 0, 0u};
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        L.V[q] = z;
+        L.Vp[q] = z;
+        L.J[q] = 0;
+        L.Jm[q] = 0;
+    }
+    L.s = L.sp = L.g = L.gp = z;
+    L.gCB = 0;
+    aff_enter_block(L, b, t, si, 1 + g * R, P);
+}
+
+// shadow: EB of row 0 left in the base buffer by earlier doubling iterations
+// (read at column j), and EH of row 0 column 0. The caller passes the state
+// of the pair and receives the writes of this step through `shw_*`.
+template <int R>
+PA_HD void aff_step(AffLane<R>& L, const AffBand& b, const Tables& t,
+                    const uint8_t* si, const uint8_t* sj, int P, int T,
+                    const AffCell& recv, const int* shadowEB, int shadowEH0,
+                    int* shadowEB_out, int (&dcode)[R])
+{
+    L.sp = L.s;
+    L.s = recv;
+    const bool moved = (T >= L.nstart);
+    if (moved) aff_enter_block(L, b, t, si, L.itop + P * R, P);
+    const int gap = t.gap, go = t.go;
+    const bool gen = (L.itop == 1);
+    if (gen) {  // row 0 at column T-1 (algn_newkk_test_aff init block)
+        int j0 = T - 1;
+        L.gp = L.g;
+        if (j0 <= b.n - 1) {
+            AffCell c;
+            if (j0 == 0) {
+                L.gCB = 0;
+                c.EH = shadowEH0;
+            } else {
+                int cj = sj[j0], cm1 = sj[j0 - 1];
+                int gr = t.prepend[cj];
+                int gop = gap_opening(j0, cm1, cj, gap, go);
+                int shx = ((cm1 & gap) && !(cj & gap)) ? gop + gr : gr;
+                L.gCB += shx;
+                c.EH = L.gCB;
+            }
+            c.CB = L.gCB;
+            c.EV = HIGH;
+            c.EB = shadowEB[j0];
+            c.GM = (uint32_t)j0;
+            L.g = c;
+        }
+    }
+    if (moved) {
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            int j = T - L.itop - q;
+            L.J[q] = (j >= 0 && j < b.n) ? sj[j] : 0;
+            L.Jm[q] = (j >= 1 && j - 1 < b.n) ? sj[j - 1] : 0;
+        }
+    } else {
+#pragma unroll
+        for (int q = R - 1; q > 0; q--) {
+            L.J[q] = L.J[q - 1];
+            L.Jm[q] = L.Jm[q - 1];
+        }
+        int j = T - L.itop;
+        L.Jm[0] = L.J[0];
+        L.J[0] = (j >= 0 && j < b.n) ? sj[j] : 0;
+    }
+    const int lenj = b.n - 1, leni = b.m - 1;
+#pragma unroll
+    for (int q = R - 1; q >= 0; q--) {
+        const int i = L.itop + q;
+        const int j = T - i;
+        AffCell up, dg;
+        if (q > 0) { up = L.V[q - 1]; dg = L.Vp[q - 1]; }
+        else if (gen) { up = L.g; dg = L.gp; }
+        else { up = L.s; dg = L.sp; }
+        const AffCell lf = L.V[q];
+        L.Vp[q] = L.V[q];
+        dcode[q] = 0;
+        if (i <= leni) {
+            const int s = aff_s(b, i), e = aff_e(b, i);
+            if (j >= s && j <= e) {
+                const int right = (j == i + b.D + b.newk);
+                const int left = (j == s);
+                const int jc = L.J[q];
+                const int jm = L.Jm[q];           // sj[j-1]
+                const int jp = left ? jc : jm;    // fill_a_row_aff's jp quirk
+                const int jgr = t.prepend[jc];
+                const int jgop = j >= 1 ? gap_opening(j, jm, jc, gap, go) : 0;
+                const int shx = (j == 1) ? jgr : (((jm & gap) && !(jc & gap)) ? jgop + jgr : jgr);
+                const int f = L.icf[q];
+                int dir = 0;
+                AffCell c;
+                if (!left) {
+                    int ext = lf.EH + shx, open = lf.CB + jgop + jgr;
+                    if (ext < open) { dir |= BEG_H; c.EH = ext; }
+                    else { dir |= END_H; c.EH = open; }
+                } else {
+                    c.EH = HIGH;
+                }
+                if (!right) {
+                    int ext = up.EV + L.svext[q], open = up.CB + L.sgop[q] + L.sgext[q];
+                    if (ext < open) { dir |= BEG_V; c.EV = ext; }
+                    else { dir |= END_V; c.EV = open; }
+                } else {
+                    c.EV = HIGH;
+                }
+                if (j > 0) {
+                    const int flag = (f & 1) && (TMPGAP & jc);
+                    const int flag2 = !(f & 2) && !(TMPGAP & jp);
+                    const int diag = flag ? 0 : HIGH;
+                    const int odiag = flag ? (flag2 ? 0 : 2 * go) : HIGH;
+                    int ext = dg.EB + diag, open = dg.CB + odiag;
+                    if (ext < open) { dir |= BEG_B; c.EB = ext; }
+                    else { dir |= END_B; c.EB = open; }
+                    const int dgc = t.csw[L.srb[q] + (NTMPGAP & jc)];
+                    const int sgop = L.sgop[q];
+                    const int xgo = (jgop < sgop) ? sgop : jgop;
+                    const int algn = dg.CB + dgc;
+                    const int fv = dg.EV + dgc + ((f & 4) ? 0 : jgop);
+                    const int fh = dg.EH + dgc + ((jc == (NTMPGAP & jc)) ? 0 : sgop);
+                    const int fd = dg.EB + dgc + xgo;
+                    int v = algn, mask = A2A;
+                    if (v >= fv) { if (v > fv) { v = fv; mask = A2V; } else mask |= A2V; }
+                    if (v >= fh) { if (v > fh) { v = fh; mask = A2H; } else mask |= A2H; }
+                    if (v >= fd) { if (v > fd) { v = fd; mask = A2D; } else mask |= A2D; }
+                    c.CB = v;
+                    dir |= mask;
+                } else {
+                    c.CB = HIGH;
+                    c.EB = HIGH;
+                }
+                int fmin = c.EH, mask = DO_H;
+                if (fmin >= c.EV) { if (fmin > c.EV) { fmin = c.EV; mask = DO_V; } else mask |= DO_V; }
+                if (fmin >= c.EB) { if (fmin > c.EB) { fmin = c.EB; mask = DO_D; } else mask |= DO_D; }
+                if (fmin >= c.CB) { if (fmin > c.CB) { fmin = c.CB; mask = DO_A; } else mask |= DO_A; }
+                if (fmin == c.EH && c.EH == c.EV) mask |= H_EQ_V;
+                dir |= mask;
+                uint32_t gm = 0;
+                if (dir & (DO_A | DO_D)) gm = dg.GM;
+                if (dir & DO_H) gm = vmax2(gm, lf.GM + 1u);
+                if (dir & DO_V) gm = vmax2(gm, up.GM + 0x10000u);
+                c.GM = gm;
+                L.V[q] = c;
+                // EB left in row 0's buffer: the last even row >= 2 covering j
+                if (shadowEB_out && (i & 1) == 0 && i >= 2 && i == (tmin(leni, j + b.newk) & ~1))
+                    shadowEB_out[j] = c.EB;
+                dcode[q] = dir;
+                (void)fmin;
+                (void)lenj;
+            }
+        }
+    }
+}
+
+// Final cost of the affine corner cell from its four states.
+PA_HD int aff_final(const AffCell& c) { return tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB)); }
+PA_HD int aff_gapnum(const AffCell& c) { return tmax((int)(c.GM & 0xFFFF), (int)(c.GM >> 16)); }
+
+// ---------------------------------------------------------------------------
+// Per-pair planning: the OCaml facade's argument order and plane choice, and
+// the band-doubling schedule.
+
+// count_gaps / seq_CAML_count (src/sequence.ml:854-865, src/seq.c:644-669)
+PA_HD int count_gap_states(const uint8_t* s, int len, int gap)
+{
+    int n = 0;
+    for (int i = 0; i < len; i++) n += (s[i] >= gap && (s[i] & gap)) ? 1 : 0;
+    return n;
+}
+
+struct PairPlan {
+    int swaped;  // caller's first sequence is the longer one
+    int m, n;    // internal order: m = shorter length, n = longer
+    int full;    // linear: algn_fill_plane instead of band doubling
+    int T0;      // initial band parameter T
+};
+
+// Sequence.Align.cost_2 (src/sequence.ml:868-925, deltaw = None) feeding
+// algn_nw_limit / algn_fill_plane_2 (src/algn.c:2954-2964, 1134-1177).
+// int_of_float (0.1 * len) equals len / 10 for every int length, and the
+// single-precision 1.5 test is exact for lengths below 2^24.
+PA_HD PairPlan plan_linear(const Tables& t, int gaps_a, int la, int gaps_b, int lb)
+{
+    PairPlan p;
+    p.swaped = la <= lb ? 0 : 1;
+    p.m = p.swaped ? lb : la;
+    p.n = p.swaped ? la : lb;
+    const int gaps = tmax(gaps_a, gaps_b);
+    const int lower = p.m / 10;
+    const int dw = (p.m - p.n) < lower ? lower / 2 : 2;
+    const int deltawh = gaps + dw;
+    int height = (p.m - p.n) + 50 + deltawh;
+    if (height > p.m) height = p.m;
+    if (2LL * p.m >= 3LL * p.n) p.full = 1;
+    else if (2 * height < p.m) p.full = 0;
+    else p.full = (8 >= p.m - height) ? 1 : 0;
+    p.T0 = (p.n - p.m + 1) * t.mnz;
+    return p;
+}
+
+// algn_nw called directly with s1 = a, s2 = b and the caller's deltawh
+// (the algn_CAML_simple_2 external): no reordering.
+PA_HD PairPlan plan_linear_deltawh(const Tables& t, int la, int lb, int deltawh)
+{
+    PairPlan p;
+    p.swaped = 0;
+    p.m = la;
+    p.n = lb;
+    int height = (p.m - p.n) + 50 + deltawh;
+    if (height > p.m) height = p.m;
+    if (2LL * p.m >= 3LL * p.n) p.full = 1;
+    else if (2 * height < p.m) p.full = 0;
+    else p.full = (8 >= p.m - height) ? 1 : 0;
+    p.T0 = (p.n - p.m + 1) * t.mnz;
+    return p;
+}
+
+// Sequence.Align.align_affine_3 (src/sequence.ml:633-649) + iniT of
+// algn_fill_plane_3_aff (src/algn.c:2340-2354).
+PA_HD PairPlan plan_affine(const Tables& t, int la, int lb)
+{
+    PairPlan p;
+    p.swaped = la <= lb ? 0 : 1;
+    p.m = p.swaped ? lb : la;
+    p.n = p.swaped ? la : lb;
+    p.full = 0;
+    p.T0 = (p.n - p.m + 1) * t.mnz;
+    return p;
+}
+
+PA_HD int band_p(int T, int m, int n) { return (T - (n - m)) / 2; }
+
+// algn_newkk_increaseT stop rule (src/algn.c:1118-1130)
+PA_HD bool lin_done(int T, int m, int n, int gapnum)
+{
+    const int p = band_p(T, m, n);
+    const int newp = (2 * T - (n - m)) / 2;
+    return (gapnum + 1) < p || newp - n + 1 >= 0;
+}
+
+// algn_newkk_increaseT_aff stop rule (src/algn.c:2310-2336); lenj = n - 1
+PA_HD bool aff_done(int T, int m, int n, int gapnum)
+{
+    const int p = band_p(T, m, n);
+    const int newp = (2 * T - (n - m)) / 2;
+    return gapnum < p || newp - (n - 1) + 1 >= 0;
+}
+
+// ---------------------------------------------------------------------------
+// Tracebacks and medians. Outputs are written back to front so that each
+// sequence ends at index cap-1 of its buffer, as seq_prepend leaves them.
+
+struct PairOut {
+    uint8_t *ea, *eb, *med, *mwg;
+    int cap;
+};
+struct PairRes {
+    int alen, mlen, wlen, maxcost, status;
+};
+
+PA_HD int lin_dm(const uint8_t* dm, int P, int R, int i, int j)
+{
+    if (i == 0) return j == 0 ? L_ALIGN : L_INSERT;
+    return dm[dm_index(P, R, i, j)];
+}
+
+// backtrace_2d + algn_ancestor_2 + seq_get_median_2d_with_gaps + algn_worst_2
+// (src/algn.c:3277-3327, 3602-3626, 3002-3105; src/seq.c:241-252), linear
+// model. x = shorter (rows), y = longer; `swaped` = the caller passed y first.
+PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
+                            const uint8_t* x, int m, const uint8_t* y, int n,
+                            int swaped, const PairOut& o)
+{
+    PairRes r = {0, 0, 0, 0, 0};
+    const int gap = t.gap, lcm = t.lcm;
+    int i = m - 1, j = n - 1;
+    int k = o.cap, ka = o.cap;
+    int worst = 0, nga = 0, ngb = 0, wfirst = 0;
+    int a = 0, bsym = 0;
+    while (i >= 0) {
+        if (k <= 0) { r.status = -2; return r; }
+        int d = lin_dm(dm, P, R, i, j);
+        int xs, ys;
+        if (d & L_ALIGN) {
+            xs = x[i--];
+            ys = y[j--];
+        } else {
+            int ins = swaped ? (d & L_INSERT) != 0 : !(d & L_DELETE);
+            if (ins) { xs = gap; ys = y[j--]; }
+            else { xs = x[i--]; ys = gap; }
+        }
+        a = swaped ? ys : xs;
+        bsym = swaped ? xs : ys;
+        k--;
+        o.ea[k] = (uint8_t)a;
+        o.eb[k] = (uint8_t)bsym;
+        int med = t.median[(a << lcm) + bsym];
+        if (med == 0) { r.status = -3; return r; }
+        o.mwg[k] = (uint8_t)med;
+        if (med != gap) o.med[--ka] = (uint8_t)med;
+        wfirst = t.worst[(a << lcm) + bsym];
+        worst += wfirst;
+        nga |= (a != gap);
+        ngb |= (bsym != gap);
+    }
+    // the first aligned column is skipped when both carry the gap bit
+    if ((gap & a) && (gap & bsym)) worst -= wfirst;
+    o.med[--ka] = (uint8_t)gap;  // ancestor keeps a leading gap
+    r.alen = o.cap - k;
+    r.wlen = r.alen;
+    r.mlen = o.cap - ka;
+    r.maxcost = (nga && ngb) ? worst : 0;
+    return r;
+}
+
+PA_HD int aff_dm(const uint16_t* dm, int P, int R, int i, int j)
+{
+    return dm[dm_index(P, R, i, j)];
+}
+
+// algn_calculate_from_2_aligned on the worst table, bitset alphabet
+PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int L)
+{
+    const int gap = t.gap, go = t.go;
+    int i = ((gap & x[0]) && (gap & y[0])) ? 1 : 0, res = 0, st = 0;
+    for (; i < L; i++) {
+        int a = x[i], b = y[i];
+        if (st == 0) {
+            if ((a & gap) && !(b & gap)) { res += go; st = 1; }
+            else if ((b & gap) && !(a & gap)) { res += go; st = 2; }
+        } else if (st == 1) {
+            if (!(a & gap)) {
+                if ((b & gap) && !(a & gap)) { res += go; st = 2; }
+                else st = 0;
+            }
+        } else {
+            if (!(b & gap)) {
+                if (a & gap) { res += go; st = 1; }
+                else st = 0;
+            }
+        }
+        res += t.worst[(a << t.lcm) + b];
+    }
+    return res;
+}
+
+// backtrace_aff (src/algn.c:1714-1819) in internal order (x shorter), then
+// the caller-order aligned pair and max_cost_2 on it.
+PA_HD PairRes aff_traceback(const uint16_t* dm, int P, int R, const Tables& t,
+                            const uint8_t* x, int m, const uint8_t* y, int n,
+                            int swaped, const PairOut& o)
+{
+    PairRes r = {0, 0, 0, 0, 0};
+    uint8_t* ri = swaped ? o.eb : o.ea;  // aligned x in caller order slot
+    uint8_t* rj = swaped ? o.ea : o.eb;
+    int i = m - 1, j = n - 1;
+    int km = o.cap, kw = o.cap, kr = o.cap;
+    int mode = 0;  // 0 todo, 1 vertical, 2 horizontal, 3 diagonal, 4 align
+    int ic = x[i], jc = y[j];
+    const int lcm = t.lcm;
+#define PA_PUT(buf, k, v) do { if ((k) <= 0) { r.status = -2; return r; } (buf)[--(k)] = (uint8_t)(v); } while (0)
+#define PA_PUTR(a, b) do { if (kr <= 0) { r.status = -2; return r; } kr--; ri[kr] = (uint8_t)(a); rj[kr] = (uint8_t)(b); } while (0)
+    while (i != 0 && j != 0) {
+        const int d = aff_dm(dm, P, R, i, j);
+        if (mode == 0) {
+            int fv = d & DO_V, fh = d & DO_H, fd = d & DO_D;
+            if (!swaped) mode = fv ? 1 : fh ? 2 : fd ? 3 : 4;
+            else mode = fh ? 2 : fv ? 1 : fd ? 3 : 4;
+        } else if (mode == 1) {
+            if ((d & END_V) || (d & H_EQ_V)) mode = 0;
+            if (!(ic & TMPGAP)) { PA_PUT(o.med, km, ic | TMPGAP); PA_PUT(o.mwg, kw, ic | TMPGAP); }
+            else PA_PUT(o.mwg, kw, TMPGAP);
+            PA_PUTR(ic, TMPGAP);
+            i--;
+            ic = x[i];
+        } else if (mode == 2) {
+            if ((d & END_H) || (d & H_EQ_V)) mode = 0;
+            if (!(jc & TMPGAP)) { PA_PUT(o.med, km, jc | TMPGAP); PA_PUT(o.mwg, kw, jc | TMPGAP); }
+            else PA_PUT(o.mwg, kw, TMPGAP);
+            PA_PUTR(TMPGAP, jc);
+            j--;
+            jc = y[j];
+        } else if (mode == 3) {
+            if (d & END_B) mode = 0;
+            PA_PUTR(ic, jc);
+            PA_PUT(o.mwg, kw, TMPGAP);
+            i--;
+            j--;
+            jc = y[j];
+            ic = x[i];
+        } else {
+            int fd = d & A2D, fv = d & A2V, fh = d & A2H;
+            if (!swaped) mode = fv ? 1 : fh ? 2 : fd ? 3 : 4;
+            else mode = fh ? 2 : fv ? 1 : fd ? 3 : 4;
+            int pm = t.median[((ic & NTMPGAP) << lcm) + (jc & NTMPGAP)];
+            PA_PUT(o.med, km, pm);
+            PA_PUT(o.mwg, kw, pm);
+            PA_PUTR(ic, jc);
+            i--;
+            j--;
+            jc = y[j];
+            ic = x[i];
+        }
+    }
+    while (i != 0) {
+        if (!(ic & TMPGAP)) { PA_PUT(o.med, km, ic | TMPGAP); PA_PUT(o.mwg, kw, ic | TMPGAP); }
+        else PA_PUT(o.mwg, kw, TMPGAP);
+        PA_PUTR(ic, TMPGAP);
+        i--;
+        ic = x[i];
+    }
+    while (j != 0) {
+        if (!(jc & TMPGAP)) { PA_PUT(o.med, km, jc | TMPGAP); PA_PUT(o.mwg, kw, jc | TMPGAP); }
+        else PA_PUT(o.mwg, kw, TMPGAP);
+        PA_PUTR(TMPGAP, jc);
+        j--;
+        jc = y[j];
+    }
+    PA_PUTR(TMPGAP, TMPGAP);
+    PA_PUT(o.mwg, kw, TMPGAP);
+    if (km == o.cap) { r.status = -4; return r; }  // empty median: undefined in POY
+    if (TMPGAP != o.med[km]) PA_PUT(o.med, km, TMPGAP);
+#undef PA_PUT
+#undef PA_PUTR
+    r.alen = o.cap - kr;
+    r.mlen = o.cap - km;
+    r.wlen = o.cap - kw;
+    const uint8_t* ea = o.ea + kr;
+    const uint8_t* eb = o.eb + kr;
+    int nga = 0, ngb = 0;
+    for (int k = 0; k < r.alen; k++) {
+        nga |= ea[k] != t.gap;
+        ngb |= eb[k] != t.gap;
+    }
+    r.maxcost = (nga && ngb) ? worst_aligned(t, ea, eb, r.alen) : 0;
+    return r;
+}
+
+}  // namespace pa

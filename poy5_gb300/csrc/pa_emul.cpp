@@ -1,0 +1,226 @@
+// TEST-ONLY host replay of the GPU lane pipeline.
+//
+// Builds into libpa_emul.so, which only tests/ load. It runs the exact step
+// functions of pa_core.cuh that the kernels run, lane by lane, with the
+// rotating neighbour exchange done through an array, so the kernel algorithm
+// can be checked against the oracle on a machine without a GPU. The product
+// library never links this file.
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "pa_core.cuh"
+#include "pa_tables.h"
+
+using namespace pa;
+
+namespace {
+
+template <int R>
+void lin_pass(const LinBand& b, int P, const Tables& t, const uint8_t* x,
+              const uint8_t* y, uint8_t* dm, int* cost, int* gapnum)
+{
+    std::vector<LinLane<R>> L(P);
+    for (int g = 0; g < P; g++) lin_lane_init(L[g], b, t, x, g, P);
+    std::vector<int> sv(P);
+    std::vector<uint32_t> sn(P);
+    const int Tlast = (b.m - 1) + (b.n - 1);
+    for (int T = 1; T <= Tlast; T++) {
+        for (int g = 0; g < P; g++) {
+            sv[g] = L[g].V[R - 1];
+            sn[g] = L[g].N[R - 1];
+        }
+        for (int g = 0; g < P; g++) {
+            int src = (g + P - 1) % P;
+            int dc[R];
+            lin_step<R>(L[g], b, t, x, y, P, T, sv[src], sn[src], dc);
+            for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint8_t)dc[q];
+        }
+    }
+    const int i = b.m - 1;
+    const int blk = (i - 1) / R, g = blk % P, q = (i - 1) - blk * R;
+    *cost = L[g].V[q];
+    const uint32_t N = L[g].N[q];
+    *gapnum = tmax((int)(N & 0xFFFF), (int)(N >> 16));
+}
+
+template <int R>
+void aff_pass(const AffBand& b, int P, const Tables& t, const uint8_t* x,
+              const uint8_t* y, uint16_t* dm, int* shadowEB, int shadowEH0,
+              int* cost, int* gapnum)
+{
+    std::vector<AffLane<R>> L(P);
+    for (int g = 0; g < P; g++) aff_lane_init(L[g], b, t, x, g, P);
+    std::vector<AffCell> sv(P);
+    const int Tlast = (b.m - 1) + (b.n - 1);
+    for (int T = 1; T <= Tlast; T++) {
+        for (int g = 0; g < P; g++) sv[g] = L[g].V[R - 1];
+        for (int g = 0; g < P; g++) {
+            int src = (g + P - 1) % P;
+            int dc[R];
+            aff_step<R>(L[g], b, t, x, y, P, T, sv[src], shadowEB, shadowEH0,
+                        shadowEB, dc);
+            for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint16_t)dc[q];
+        }
+    }
+    const int i = b.m - 1;
+    const int blk = (i - 1) / R, g = blk % P, q = (i - 1) - blk * R;
+    *cost = aff_final(L[g].V[q]);
+    *gapnum = aff_gapnum(L[g].V[q]);
+}
+
+struct Emul {
+    HostCM cm;
+    Tables t;
+};
+
+int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb,
+               int* cost, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
+               int cap, int* res, int* passes, int* last_class)
+{
+    const Tables& t = E.t;
+    PairPlan pl = plan_linear(t, count_gap_states(a, la, t.gap), la,
+                              count_gap_states(b, lb, t.gap), lb);
+    const uint8_t* x = pl.swaped ? b : a;
+    const uint8_t* y = pl.swaped ? a : b;
+    const int m = pl.m, n = pl.n;
+    std::vector<uint8_t> dm;
+    int P = 32, R = 1, T = pl.T0, g = 0;
+    *passes = 0;
+    *last_class = -1;
+    for (;;) {
+        LinBand bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
+        int c = pick_class(0, lin_wu(bd), n);
+        if (c < 0) return -5;
+        P = 32 * class_K(0, c);
+        R = class_R(0, c);
+        *last_class = c;
+        dm.assign((size_t)(m + n + 1) * P * R, 0);
+        (*passes)++;
+        if (m == 1) {  // no rows: row 0 is the whole alignment
+            int s = 0;
+            for (int j = 1; j < n; j++) s += t.prepend[y[j]];
+            *cost = s;
+            g = n - 1;
+        } else {
+            switch (R) {
+                case 1: lin_pass<1>(bd, P, t, x, y, dm.data(), cost, &g); break;
+                case 2: lin_pass<2>(bd, P, t, x, y, dm.data(), cost, &g); break;
+                case 4: lin_pass<4>(bd, P, t, x, y, dm.data(), cost, &g); break;
+                default: lin_pass<8>(bd, P, t, x, y, dm.data(), cost, &g); break;
+            }
+        }
+        if (pl.full || lin_done(T, m, n, g)) break;
+        T *= 2;
+    }
+    PairOut o = {ea, eb, med, mwg, cap};
+    PairRes r = lin_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    res[0] = r.alen;
+    res[1] = r.mlen;
+    res[2] = r.wlen;
+    res[3] = r.maxcost;
+    return r.status;
+}
+
+int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb,
+               int* cost, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
+               int cap, int* res, int* passes, int* last_class)
+{
+    const Tables& t = E.t;
+    PairPlan pl = plan_affine(t, la, lb);
+    const uint8_t* x = pl.swaped ? b : a;
+    const uint8_t* y = pl.swaped ? a : b;
+    const int m = pl.m, n = pl.n;
+    if (m == 1 && n == 1) return -4;
+    std::vector<uint16_t> dm;
+    std::vector<int> shadow(n, HIGH);
+    int shadowEH0 = t.go;
+    int P = 32, R = 1, T = pl.T0, g = 0;
+    *passes = 0;
+    *last_class = -1;
+    for (;;) {
+        AffBand bd = aff_band(m, n, band_p(T, m, n));
+        int c = pick_class(1, aff_wu(bd), n);
+        if (c < 0) return -5;
+        P = 32 * class_K(1, c);
+        R = class_R(1, c);
+        *last_class = c;
+        dm.assign((size_t)(m + n + 1) * P * R, 0);
+        (*passes)++;
+        if (m == 1) {  // leni = 0: the initial row is the whole alignment
+            int s = t.go;
+            for (int j = 1; j < n; j++) s += t.prepend[y[j]];
+            *cost = s;
+            g = 0xFFFF;
+        } else {
+            switch (R) {
+                case 1: aff_pass<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                case 2: aff_pass<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                default: aff_pass<4>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+            }
+            if (tmin(m - 1, bd.newk) >= 2) shadowEH0 = HIGH;
+        }
+        if (aff_done(T, m, n, g)) break;
+        T *= 2;
+    }
+    PairOut o = {ea, eb, med, mwg, cap};
+    PairRes r = aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    res[0] = r.alen;
+    res[1] = r.mlen;
+    res[2] = r.wlen;
+    res[3] = r.maxcost;
+    return r.status;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* pa_emul_new(const int* tcm, int alph, int gap_open)
+{
+    Emul* e = new Emul;
+    if (build_cm(&e->cm, tcm, alph, gap_open)) {
+        delete e;
+        return nullptr;
+    }
+    kernel_tables(e->cm, &e->t);
+    return e;
+}
+
+void pa_emul_free(void* e) { delete (Emul*)e; }
+
+// Copies out the product's host tables for comparison with the oracle.
+int pa_emul_tables(void* h, int* cost, uint8_t* median, int* worst, int* tail,
+                   int* prepend, int* info)
+{
+    const HostCM& cm = ((Emul*)h)->cm;
+    const int n = 2 * (1 << cm.lcm) * (1 << cm.lcm);
+    memcpy(cost, cm.cost, (size_t)n * sizeof(int));
+    memcpy(worst, cm.worst, (size_t)n * sizeof(int));
+    memcpy(tail, cm.tail, (size_t)n * sizeof(int));
+    memcpy(prepend, cm.prepend, (size_t)n * sizeof(int));
+    memcpy(median, cm.median, (size_t)n);
+    info[0] = cm.lcm;
+    info[1] = cm.gap;
+    info[2] = cm.a_sz;
+    info[3] = cm.combinations;
+    info[4] = cm.cost_model;
+    info[5] = cm.gap_open;
+    return n;
+}
+
+// DOS.median of one pair through the replayed pipeline. Outputs end at
+// index cap-1 of each buffer; res = {alen, mlen, wlen, maxcost}.
+int pa_emul_median(void* h, int affine, const uint8_t* a, int la,
+                   const uint8_t* b, int lb, int* cost, uint8_t* ea,
+                   uint8_t* eb, uint8_t* med, uint8_t* mwg, int cap, int* res,
+                   int* passes, int* last_class)
+{
+    const Emul& E = *(Emul*)h;
+    if (affine)
+        return run_affine(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
+    return run_linear(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// Launch interface between the C-ABI layer and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pa_core.cuh"
+
+namespace pa {
+
+// Everything a batch launch needs, all device pointers.
+struct BatchArgs {
+    const uint8_t* seqs;       // concatenated input sequences
+    const long long* offa;     // pair k: a = seqs[offa[k] .. + lena[k])
+    const int* lena;
+    const long long* offb;
+    const int* lenb;
+    int npairs;
+    int affine;
+    int do_traceback;          // 0: keep the last fill in the slab (per-call stubs)
+    const Tables* tables;
+    int* pfull;                // linear plane choice per pair
+    int* shadow;               // affine: row-0 EB left by earlier iterations (n per pair)
+    int* shadowEH0;            // affine: row-0 EH at column 0
+    int2* qitems;              // NCLASS queues of (pair, T) with capacity qcap
+    int* qcount;
+    int* qhead;
+    int qcap;
+    uint8_t* slab;             // per-CTA direction slabs, reused class after class
+    long long slab_stride;     // bytes per CTA for the class being launched
+    const long long* out_off;  // pair k writes its outputs at out_off[k]
+    int* cost;
+    int* maxcost;
+    int* alen;
+    int* mlen;
+    int* wlen;
+    int* status;               // 1 pending, 0 done, < 0 error
+    int* passes;               // band iterations run
+    int* lastcls;              // class of the final iteration
+    int* slab_cta;             // pipeline whose slab holds the final fill
+    const int* deltawh_override;  // per-call linear stub: caller's deltawh, no reordering
+    const int* swap_override;     // per-call stubs: caller's tie preference
+    uint8_t* ea;
+    uint8_t* eb;
+    uint8_t* med;
+    uint8_t* mwg;
+};
+
+// Persistent CTAs per SM a class kernel can keep resident.
+int class_blocks_per_sm(int affine, int cls);
+// Bytes of direction slab one CTA of a class needs for pairs up to maxmn = m + n.
+long long class_slab_bytes(int affine, int cls, int maxmn);
+
+void launch_prep(const BatchArgs& a, cudaStream_t s);
+void launch_class(const BatchArgs& a, int cls, int grid, cudaStream_t s);
+// Traceback + medians of pairs whose fill was left in the slab (per-call
+// path); d_strides[c] = slab bytes per pipeline of class c.
+void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
+// Pipelines per CTA of a class launch.
+int class_pipes_per_cta(int affine, int cls);
+// Column-wise medians of already aligned pairs (ancestor_2 / with-gaps / worst).
+void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
+                            int len, uint8_t* anc, uint8_t* mwg, int* out3,
+                            cudaStream_t s);
+
+}  // namespace pa

@@ -1,0 +1,115 @@
+"""The kernels' lane-pipeline algorithm, replayed on the host (no GPU).
+
+libpa_emul.so compiles the same step and traceback functions the CUDA
+kernels run (poy5_gb300/csrc/pa_core.cuh) plus the library's own cost-table
+builder, and replays P pipeline lanes one at a time. These tests pin that
+algorithm to the reference (golden fixtures) and to the oracle, so a GPU run
+only has to confirm the CUDA mechanics.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import golden_lib
+from cases import AFF_TCM, STD_TCM, edge_pairs, random_pairs
+from conftest import build_emulator
+
+_P = C.c_void_p
+
+
+@pytest.fixture(scope="module")
+def emul():
+    lib = C.CDLL(build_emulator())
+    lib.pa_emul_new.restype = _P
+    lib.pa_emul_new.argtypes = [_P, C.c_int, C.c_int]
+    lib.pa_emul_free.argtypes = [_P]
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P)
+
+
+class Emu:
+    def __init__(self, lib, tcm, go):
+        self.lib = lib
+        flat = np.ascontiguousarray(np.asarray(tcm, np.int32).reshape(-1))
+        self.h = _P(lib.pa_emul_new(_ptr(flat), int(np.asarray(tcm).shape[0]), go))
+        assert self.h
+        self.affine = go > 0
+
+    def tables(self):
+        n = 8192
+        cost, worst, tail, prep = (np.zeros(n, np.int32) for _ in range(4))
+        med = np.zeros(n, np.uint8)
+        info = np.zeros(6, np.int32)
+        k = self.lib.pa_emul_tables(self.h, _ptr(cost), _ptr(med), _ptr(worst), _ptr(tail),
+                                    _ptr(prep), _ptr(info))
+        return dict(cost=cost[:k], median=med[:k], worst=worst[:k], tail=tail[:k],
+                    prepend=prep[:k])
+
+    def median(self, a, b):
+        a = np.ascontiguousarray(a, np.uint8)
+        b = np.ascontiguousarray(b, np.uint8)
+        cap = len(a) + len(b) + 2
+        bufs = [np.zeros(cap, np.uint8) for _ in range(4)]
+        res = np.zeros(4, np.int32)
+        cost, ps, lc = C.c_int(), C.c_int(), C.c_int()
+        rc = self.lib.pa_emul_median(self.h, int(self.affine), _ptr(a), len(a), _ptr(b), len(b),
+                                     C.byref(cost), *(_ptr(x) for x in bufs), cap, _ptr(res),
+                                     C.byref(ps), C.byref(lc))
+        assert rc == 0, rc
+        al, ml, wl, mx = (int(x) for x in res)
+        return (cost.value, bufs[0][cap - al:], bufs[1][cap - al:], bufs[2][cap - ml:],
+                bufs[3][cap - wl:], mx, lc.value)
+
+    def __del__(self):
+        self.lib.pa_emul_free(self.h)
+
+
+@pytest.mark.parametrize("name", golden_lib.NAMES)
+def test_pipeline_matches_golden(emul, name):
+    g = golden_lib.load(name)
+    e = Emu(emul, g.tcm, g.gap_open)
+    t = e.tables()
+    for key, want in g.tables.items():
+        assert np.array_equal(t[key], want), key
+    for k, (a, b) in enumerate(g.pairs):
+        cost, ea, eb, med, mwg, mx, _ = e.median(a, b)
+        bad = golden_lib.mismatches(g, k, cost, ea, eb, med, mwg, mx)
+        assert not bad, (name, k, bad)
+
+
+@pytest.mark.parametrize("affine", [False, True])
+def test_pipeline_matches_oracle_random(emul, oracle, affine):
+    rng = np.random.default_rng(314 + affine)
+    tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
+    e = Emu(emul, tcm, go)
+    cm = oracle.cm(tcm=tcm, gap_open=go)
+    classes = set()
+    for a, b in edge_pairs() + random_pairs(rng, 300, maxlen=700):
+        cost, ea, eb, med, mwg, mx, cls = e.median(a, b)
+        r = oracle.median(cm, a, b, affine)
+        classes.add(cls)
+        assert (cost, mx) == (r.cost, r.maxcost)
+        assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb)
+        assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
+    assert len(classes) >= 4  # single-warp and multi-warp pipelines exercised
+
+
+def test_pipeline_random_tables(emul, oracle):
+    rng = np.random.default_rng(8)
+    for t in range(12):
+        M = rng.integers(1, 5, (5, 5))
+        M = np.triu(M) + np.triu(M, 1).T
+        if t % 2:
+            np.fill_diagonal(M, 0)
+        go = 2 if t % 3 == 0 else 0
+        e = Emu(emul, M, go)
+        cm = oracle.cm(tcm=M.tolist(), gap_open=go)
+        for a, b in random_pairs(rng, 10, maxlen=200):
+            cost, ea, eb, med, mwg, mx, _ = e.median(a, b)
+            r = oracle.median(cm, a, b, go > 0)
+            assert (cost, mx) == (r.cost, r.maxcost)
+            assert np.array_equal(med, r.median) and np.array_equal(ea, r.ea)
