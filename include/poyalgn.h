@@ -43,6 +43,8 @@ extern "C" {
 #define POYALGN_PAIR_EMPTY -4      /* empty sequence / empty median (POY UB) */
 #define POYALGN_PAIR_TOO_WIDE -5   /* band wider than the largest pipeline */
 #define POYALGN_PAIR_TOO_LONG -6   /* sequence longer than 65535 */
+#define POYALGN_PAIR_BAD_STATE -7  /* a state outside the cost matrix's alphabet */
+#define POYALGN_PAIR_NO_CONVERGE -8 /* band doubling did not stop (e.g. all costs 0) */
 
 typedef struct poyalgn_ctx poyalgn_ctx;
 typedef struct poyalgn_cm poyalgn_cm;

@@ -22,7 +22,8 @@ _I64 = C.c_int64
 EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, EPAIR = -1, -2, -3, -4, -5
 PAIR_STATUS = {0: "ok", -2: "output capacity exceeded", -3: "median should not be 0",
                -4: "empty sequence or empty median", -5: "band wider than the largest pipeline",
-               -6: "sequence longer than 65535", 1: "not processed"}
+               -6: "sequence longer than 65535", -7: "state outside the alphabet",
+               -8: "band doubling did not stop", 1: "not processed"}
 
 
 class PoyAlgnError(RuntimeError):

@@ -24,6 +24,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int NARROW_WARPS = 4;  // pipelines per CTA for K = 1 classes
+constexpr int MAX_PASSES = 40;   // band doublings before a pair is failed
 
 __device__ __forceinline__ void load_tables(Tables& st, const Tables* g)
 {
@@ -216,12 +217,16 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
         const int m = swaped ? lb : la, n = swaped ? la : lb;
         const int full = A.pfull[k];
         int cost = 0;
+        int npass = A.passes[k];  // passes run by smaller classes (earlier launches)
         bool done = false, moved = false;
         while (!done) {
             const LinBand b = lin_band(m, n, full, full ? 0 : band_p(T, m, n));
             const int c = pick_class(0, lin_wu(b), n);
-            if (c > cls) {
-                if (p.g == 0) push_item(A, c, k, T);
+            if (c > cls || c < 0 || npass >= MAX_PASSES) {
+                if (p.g == 0) {
+                    if (c > cls && npass < MAX_PASSES) push_item(A, c, k, T);
+                    else A.status[k] = c < 0 ? -5 : -8;
+                }
                 moved = true;
                 break;
             }
@@ -237,7 +242,8 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
                 gapnum = res[1];
                 pipe_sync(p);
             }
-            if (p.g == 0) A.passes[k] += 1;
+            npass++;
+            if (p.g == 0) A.passes[k] = npass;
             done = full || lin_done(T, m, n, gapnum);
             if (!done) T *= 2;
         }
@@ -329,12 +335,16 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
         const int m = swaped ? lb : la, n = swaped ? la : lb;
         int* shadow = A.shadow + A.out_off[k];
         int cost = 0;
+        int npass = A.passes[k];  // passes run by smaller classes (earlier launches)
         bool done = false, moved = false;
         while (!done) {
             const AffBand b = aff_band(m, n, band_p(T, m, n));
             const int c = pick_class(1, aff_wu(b), n);
-            if (c > cls) {
-                if (p.g == 0) push_item(A, c, k, T);
+            if (c > cls || c < 0 || npass >= MAX_PASSES) {
+                if (p.g == 0) {
+                    if (c > cls && npass < MAX_PASSES) push_item(A, c, k, T);
+                    else A.status[k] = c < 0 ? -5 : -8;
+                }
                 moved = true;
                 break;
             }
@@ -352,7 +362,8 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
                 if (p.g == 0 && tmin(m - 1, b.newk) >= 2) A.shadowEH0[k] = HIGH;
                 pipe_sync(p);
             }
-            if (p.g == 0) A.passes[k] += 1;
+            npass++;
+            if (p.g == 0) A.passes[k] = npass;
             done = aff_done(T, m, n, gapnum);
             if (!done) T *= 2;
             pipe_sync(p);
@@ -386,6 +397,12 @@ __global__ void prep_kernel(BatchArgs A)
     const int la = A.lena[k], lb = A.lenb[k];
     const uint8_t* a = A.seqs + A.offa[k];
     const uint8_t* b = A.seqs + A.offb[k];
+    // every state must index the 1 << lcm tables
+    int bad = 0;
+    const int ns = 1 << t.lcm;
+    for (int i = lane; i < la; i += 32) bad |= (a[i] >= ns);
+    for (int i = lane; i < lb; i += 32) bad |= (b[i] >= ns);
+    bad = __any_sync(FULL, bad);
     PairPlan pl;
     if (A.affine) {
         pl = plan_affine(t, la, lb);
@@ -410,6 +427,10 @@ __global__ void prep_kernel(BatchArgs A)
     A.lastcls[k] = -1;
     if (la < 1 || lb < 1 || (A.affine && la == 1 && lb == 1)) {
         A.status[k] = -4;
+        return;
+    }
+    if (bad) {
+        A.status[k] = -7;
         return;
     }
     if (pl.n > 65535) {  // gap counts travel as packed 16-bit halves
