@@ -1,0 +1,422 @@
+#!/usr/bin/env python
+"""Benchmark: batched SeqCS.DOS.median on one GB300 (and N replicas).
+
+Default workload: 65,536 affine pairs (lognormal lengths, median 800,
+clipped 50-4,000; second sequence 10% substitutions + 2% indels; gap opening
+3, extension 1, substitution 1). A "step" is one full batch: every pair's
+band-doubling fill, traceback, median and worst cost.
+
+  value  GCUPS over matrix cells (sum of len(a)*len(b)), inputs resident in
+         HBM, timed with CUDA events on the launch stream
+  e2e    the same through poyalgn_median_batch with pinned host buffers
+         (host->device inputs and device->host outputs inside the timing)
+
+`--impl reference` times the reference path's CPU implementation (the
+reference algn.c build when it loads on this host, else the oracle's C
+restatement) on all host cores over bounded samples.
+Multi-GPU (torchrun): each rank aligns its own batch (weak scaling), no
+collective on the data path; value = all ranks' cells / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("GCUPS & alignments/s batched+served vs plain per-pair kernel, 1 GB300, "
+          "bit-exact; p50/p99")
+OPS_PER_CELL = {"affine": 51, "linear": 8}   # int32 ops per DP cell
+DM_BYTES = {"affine": 2, "linear": 1}        # direction bytes written per cell
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", choices=["affine_pairs", "plain_pairs"],
+                    default="affine_pairs")
+    ap.add_argument("--pairs", type=int, default=0, help="override the pair count")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU work of the host baseline sample")
+    return ap.parse_args(argv)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def make_workload(name: str, n_pairs: int, rank: int):
+    from poy5_gb300 import workloads as wl
+    if name == "affine_pairs":
+        return wl.affine_pairs(n_pairs or 65536, seed=wl.SEED_BASE + 2 + 1000 * rank)
+    return wl.plain_pairs(n_pairs or 4096, seed=wl.SEED_BASE + 1 + 1000 * rank)
+
+
+def cells_full(w) -> int:
+    return int(sum(len(a) * len(b) for a, b in w.pairs))
+
+
+def host_oracle():
+    """The CPU implementation of the path on this host: the reference algn.c
+    build when it loads here (x86 with the POY sources), else the port."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    if oracle_lib.available("ref"):
+        try:
+            return oracle_lib.Oracle("ref"), "reference"
+        except OSError:
+            pass
+    return oracle_lib.Oracle("port"), "port"
+
+
+def cpu_rate(w, target_s: float, threads: int, single_thread_ref: bool = True):
+    """Cells/s and pairs/s of the host CPU implementation on a bounded
+    sample of `w` (pairs taken in order until ~target_s of work)."""
+    orc, kind = host_oracle()
+    cm = orc.cm(subs=w.subs, indel=w.indel, gap_open=w.gap_open)
+    pairs = w.pairs
+    if kind == "reference":
+        # the reference harness is single-threaded per process workspace
+        threads = 1
+        t0 = time.perf_counter()
+        n = 0
+        cells = 0
+        while n < len(pairs) and time.perf_counter() - t0 < target_s:
+            a, b = pairs[n]
+            orc.median(cm, a, b, w.affine)
+            cells += len(a) * len(b)
+            n += 1
+        dt = time.perf_counter() - t0
+    else:
+        probe = pairs[:64]
+        t0 = time.perf_counter()
+        orc.median_batch(cm, [a for a, _ in probe], [b for _, b in probe], w.affine, threads)
+        per_pair = (time.perf_counter() - t0) / len(probe)
+        n = int(min(len(pairs), max(64, target_s / max(per_pair, 1e-7))))
+        sample = pairs[:n]
+        t0 = time.perf_counter()
+        orc.median_batch(cm, [a for a, _ in sample], [b for _, b in sample], w.affine, threads)
+        dt = time.perf_counter() - t0
+        cells = sum(len(a) * len(b) for a, b in sample)
+    return {"cells_per_s": cells / dt, "pairs_per_s": n / dt, "pairs": n,
+            "seconds": dt, "threads": threads, "kind": kind}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def run_gpu(args):
+    import ctypes as C
+
+    import torch
+
+    import poy5_gb300 as pg
+    from poy5_gb300 import _lib, schedule
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = make_workload(args.workload, args.pairs, rank)
+    model = "affine" if w.affine else "linear"
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    lib = _lib.load()
+    pk = pg.pack_pairs(w.pairs)
+    n = pk.npairs
+    dev = torch.device("cuda", local)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_in = [t(pk.seqs), t(pk.offa), t(pk.lena), t(pk.offb), t(pk.lenb), t(pk.out_off)]
+    d_int = [torch.zeros(n, dtype=torch.int32, device=dev) for _ in range(7)]
+    d_out = [torch.zeros(pk.out_bytes, dtype=torch.uint8, device=dev) for _ in range(4)]
+    P = lambda x: C.c_void_p(x.data_ptr())
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        rc = lib.poyalgn_median_batch_device(
+            ctx.handle, cm.handle, n, pk.max_pair_len, pk.out_bytes,
+            *(P(x) for x in d_in), *(P(x) for x in d_int[:6]), *(P(x) for x in d_out),
+            P(d_int[6]), C.c_void_p(stream.cuda_stream))
+        _lib.check(rc)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    status = d_int[5].cpu().numpy()
+    if not np.all(status == 0):
+        raise RuntimeError(f"{int((status != 0).sum())} pairs failed: {np.unique(status)}")
+    passes = d_int[6].cpu().numpy()
+    launches_per_step = ctx.last_launches()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    # per-launch timing over a second set of steps (same work, events per launch)
+    ctx.profile_begin(args.steps)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize(dev)
+    prof = ctx.profile_end()
+    clk = clocks.stop()
+
+    # end to end through the host-pointer entry point, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        h_in = [pin(pk.seqs), pin(pk.offa), pin(pk.lena), pin(pk.offb), pin(pk.lenb),
+                pin(pk.out_off)]
+        h_int = [torch.zeros(n, dtype=torch.int32).pin_memory() for _ in range(7)]
+        h_out = [torch.zeros(pk.out_bytes, dtype=torch.uint8).pin_memory() for _ in range(4)]
+
+        def e2e_step():
+            rc = lib.poyalgn_median_batch(ctx.handle, cm.handle, n, *(P(x) for x in h_in),
+                                          *(P(x) for x in h_int[:6]), *(P(x) for x in h_out),
+                                          P(h_int[6]))
+            _lib.check(rc)
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        barrier()
+        h2d = int(pk.seqs.nbytes + pk.offa.nbytes * 3 + pk.lena.nbytes * 2)
+        d2h = int(7 * 4 * n + 4 * pk.out_bytes)
+        e2e = {"seconds": e2e_s, "h2d": h2d, "d2h": d2h}
+
+    cells = cells_full(w)
+    full = None
+    if not w.affine:
+        gaps = lambda s: int(np.count_nonzero((s >= 16) & ((s & 16) != 0)))
+        full = schedule.linear_full_plane(pk.lena, pk.lenb, [gaps(a) for a, _ in w.pairs],
+                                          [gaps(b) for _, b in w.pairs])
+    mnz = cm.tables()["min_non0_cost"]
+    computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, w.affine, full).sum())
+    return dict(w=w, model=model, n=n, ms=ms, cells=cells, computed=computed, prof=prof,
+                clocks=clk, e2e=e2e, launches=launches_per_step, passes=passes,
+                world=world, rank=rank, pk=pk)
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def gpu_line(args, r) -> dict:
+    world = r["world"]
+    ms = reduce_max(r["ms"], world)
+    cells = reduce_sum(r["cells"], world)
+    pairs = reduce_sum(r["n"], world)
+    computed = reduce_sum(r["computed"], world)
+    gcups = cells / (ms * 1e-3) / 1e9
+    model = r["model"]
+    prof = r["prof"]
+    nb = max(prof["batches"], 1)
+    cls_ms = {k: v / nb for k, v in prof.items() if k.startswith("class")}
+    fill_ms = sum(cls_ms.values())
+    dom = max(cls_ms, key=cls_ms.get)
+    peaks = measured_peaks()
+    # HBM view of the class kernels: direction codes written per filled cell,
+    # sequences read, outputs written (algorithmic bytes)
+    pk = r["pk"]
+    alg_bytes = (r["computed"] * DM_BYTES[model] + int(pk.seqs.nbytes) + 4 * int(pk.out_bytes))
+    gbs = alg_bytes / (fill_ms * 1e-3) / 1e9
+    hbm_peak = peaks.get("hbm_gbs")
+    clk = r["clocks"]
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    nsm = 152
+    try:
+        import torch
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    int_peak = nsm * 128 * sm_mhz * 1e6 / 1e12  # Tops: 128 int32 lanes per SM
+    int_ach = r["computed"] * OPS_PER_CELL[model] / (fill_ms * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": round(gcups, 3), "unit": "GCUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+        "config": {"workload": r["w"].name, "pairs_per_gpu": r["n"],
+                   "cost_model": (f"affine open {r['w'].gap_open} ext {r['w'].indel} "
+                                  f"subs {r['w'].subs}" if r["w"].affine else
+                                  f"linear subs {r['w'].subs} indel {r['w'].indel}"),
+                   "cells_per_gpu": r["cells"], "cells_computed_per_gpu": r["computed"],
+                   "parallelism": f"replicas{world}",
+                   "l2": "inputs+outputs+direction slabs > 129 MB L2 (no flush needed)"},
+        "alignments_per_s": round(pairs / (ms * 1e-3), 1),
+        "gcups_computed_cells": round(computed / (ms * 1e-3) / 1e9, 3),
+        "gpu_launches": r["launches"] * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "class kernels (fill+traceback), dominant "
+                     + dom, "achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(gbs / hbm_peak, 4) if hbm_peak else None,
+                     "traffic": None, "peak_source": "measured" if hbm_peak else None},
+        "roofline_int32": {"bound": "int32 ALU", "ops_per_cell": OPS_PER_CELL[model],
+                           "achieved": round(int_ach, 2), "peak": round(int_peak, 2),
+                           "unit": "Tops", "frac": round(int_ach / int_peak, 4),
+                           "peak_source": "nominal 128 int32 lanes/SM x sampled SM clock"},
+        "launch_ms": {k: round(v / nb, 3) for k, v in prof.items() if k != "batches"},
+        "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"),
+                   "reasons": clk.get("reasons")},
+        "passes_mean": round(float(np.mean(r["passes"])), 3),
+    }
+    if r["e2e"]:
+        e = r["e2e"]
+        e_s = reduce_max(e["seconds"], world)
+        line["e2e"] = {"value": round(cells / e_s / 1e9, 3), "unit": "GCUPS",
+                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
+                       "alignments_per_s": round(pairs / e_s, 1)}
+    return line
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        w = make_workload(args.workload, args.pairs, 0)
+        threads = os.cpu_count() or 1
+        per = max(args.cpu_seconds / max(args.steps, 1), 1.0)
+        for _ in range(args.warmup):
+            cpu_rate(w, min(per, 1.0), threads)
+        rates = [cpu_rate(w, per, threads) for _ in range(args.steps)]
+        cps = float(np.median([x["cells_per_s"] for x in rates]))
+        aps = float(np.median([x["pairs_per_s"] for x in rates]))
+        kind = rates[0]["kind"]
+        v = round(cps / 1e9, 4)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "GCUPS",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(1e3 * float(np.median([x["seconds"] for x in rates])), 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int32", "data": "synthetic (seeded)",
+                "config": {"workload": w.name, "pairs_per_step": rates[0]["pairs"]},
+                "alignments_per_s": round(aps, 2),
+                "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": rates[0]["threads"],
+                                 "kind": kind,
+                                 "sample": f"first {rates[0]['pairs']} pairs of {w.name} per step"},
+                "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    r = run_gpu(args)
+    line = gpu_line(args, r)
+    if rank == 0:
+        cpu = cpu_rate(r["w"], args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = {
+            "value": round(cpu["cells_per_s"] / 1e9, 4), "unit": "GCUPS",
+            "cores": cpu["threads"], "kind": cpu["kind"],
+            "sample": f"first {cpu['pairs']} pairs of {r['w'].name} ({cpu['seconds']:.1f} s)",
+            "alignments_per_s": round(cpu["pairs_per_s"], 2)}
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -180,6 +180,17 @@ int poyalgn_median_batch_device(poyalgn_ctx *ctx, const poyalgn_cm *cm,
 /* Number of kernel launches the last batch enqueued (for accounting). */
 int poyalgn_last_launches(const poyalgn_ctx *ctx);
 
+/*
+ * Launch timing (no POY counterpart). After poyalgn_profile_begin, each of
+ * the next max_batches batches records CUDA events on its own stream around
+ * its prep launch and each pipeline-class launch. poyalgn_profile_end waits
+ * for them and writes, per launch slot (prep, class 0 .. class N-1, N =
+ * poyalgn_num_classes()), the summed milliseconds into ms[N + 1].
+ */
+int poyalgn_profile_begin(poyalgn_ctx *ctx, int max_batches);
+int poyalgn_profile_end(poyalgn_ctx *ctx, float *ms, int *batches);
+int poyalgn_num_classes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,22 @@ class Context:
     def last_launches(self) -> int:
         return _lib.load().poyalgn_last_launches(self._h)
 
+    def profile_begin(self, max_batches: int):
+        """Record per-launch CUDA events for the next `max_batches` batches."""
+        check(_lib.load().poyalgn_profile_begin(self._h, int(max_batches)))
+
+    def profile_end(self) -> dict:
+        """Summed ms per launch slot: {'prep': t, 'class0': t, ...}."""
+        lib = _lib.load()
+        n = lib.poyalgn_num_classes()
+        ms = np.zeros(n + 1, np.float32)
+        nb = C.c_int()
+        check(lib.poyalgn_profile_end(self._h, _ptr(ms), C.byref(nb)))
+        out = {"prep": float(ms[0]), "batches": nb.value}
+        for k in range(n):
+            out[f"class{k}"] = float(ms[k + 1])
+        return out
+
 
 class CostMatrix:
     """Device-resident cost tables of a bitset alphabet (POY ``struct cm``)."""

@@ -79,6 +79,10 @@ struct poyalgn_ctx {
     DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
     DevBuf dwh, swp;
     int last_launches = 0;
+    // optional per-launch timing: one event before the prep launch and one
+    // after each launch of a batch, for up to prof_cap batches
+    std::vector<cudaEvent_t> prof_ev;
+    int prof_cap = 0, prof_used = 0;
     // per-call stub state: the fill of the last simple_2 / align_affine_3
     bool call_valid = false;
     int call_affine = 0, call_l1 = 0, call_l2 = 0;
@@ -178,12 +182,20 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.mwg = mwg;
 
     int launches = 0;
+    cudaEvent_t* ev = nullptr;
+    if (c->prof_used < c->prof_cap) {
+        ev = &c->prof_ev[(size_t)c->prof_used * (NCLASS + 2)];
+        c->prof_used++;
+        CU(cudaEventRecord(ev[0], st));
+    }
     launch_prep(A, st);
     launches++;
+    if (ev) CU(cudaEventRecord(ev[1], st));
     for (int k = 0; k < NCLASS; k++) {
         A.slab_stride = strides[k];
         launch_class(A, k, grid[k], st);
         launches++;
+        if (ev) CU(cudaEventRecord(ev[k + 2], st));
     }
     CU(cudaGetLastError());
     c->last_launches = launches;
@@ -333,6 +345,7 @@ void poyalgn_free(poyalgn_ctx* c)
                       &c->dwh, &c->swp};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -607,5 +620,42 @@ int poyalgn_median_batch(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
 }
 
 int poyalgn_last_launches(const poyalgn_ctx* ctx) { return ctx ? ctx->last_launches : 0; }
+
+int poyalgn_profile_begin(poyalgn_ctx* ctx, int max_batches)
+{
+    if (!ctx || max_batches < 0) return set_err(POYALGN_EINVAL, "bad argument");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+    ctx->prof_ev.assign((size_t)max_batches * (NCLASS + 2), nullptr);
+    for (auto& e : ctx->prof_ev) CU(cudaEventCreate(&e));
+    ctx->prof_cap = max_batches;
+    ctx->prof_used = 0;
+    return 0;
+}
+
+int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
+{
+    if (!ctx || !ms || !batches) return set_err(POYALGN_EINVAL, "bad argument");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    for (int k = 0; k < NCLASS + 1; k++) ms[k] = 0.f;
+    for (int b = 0; b < ctx->prof_used; b++) {
+        cudaEvent_t* ev = &ctx->prof_ev[(size_t)b * (NCLASS + 2)];
+        CU(cudaEventSynchronize(ev[NCLASS + 1]));
+        for (int k = 0; k < NCLASS + 1; k++) {
+            float t = 0.f;
+            CU(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            ms[k] += t;
+        }
+    }
+    *batches = ctx->prof_used;
+    for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+    ctx->prof_ev.clear();
+    ctx->prof_cap = ctx->prof_used = 0;
+    return 0;
+}
+
+int poyalgn_num_classes(void) { return NCLASS; }
 
 }  // extern "C"

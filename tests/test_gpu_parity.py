@@ -41,9 +41,16 @@ def test_batch_matches_oracle_random(ctx, oracle, affine):
     ocm = oracle.cm(tcm=tcm, gap_open=go)
     pairs = edge_pairs() + random_pairs(rng, 600, maxlen=900)
     res = pg.median_batch(ctx, cm, pairs)
-    assert np.all(res.status == 0)
     for k, (a, b) in enumerate(pairs):
-        d, r = res.pair(k), oracle.median(ocm, a, b, affine)
+        try:
+            r = oracle.median(ocm, a, b, affine)
+        except Exception as e:
+            # an empty affine median is undefined in POY (it reads median[0]
+            # of an empty sequence); both sides must refuse the pair
+            assert "empty" in str(e) and res.status[k] == -4, (k, res.status[k], e)
+            continue
+        assert res.status[k] == 0, (k, res.status[k])
+        d = res.pair(k)
         assert (d.cost, d.maxcost) == (r.cost, r.maxcost), k
         assert np.array_equal(d.aligned_a, r.ea) and np.array_equal(d.aligned_b, r.eb), k
         assert np.array_equal(d.median, r.median), k

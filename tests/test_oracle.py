@@ -102,3 +102,26 @@ def test_oracle_stubs_match_reference():
         assert port.cost_affine(ap, a, b) == ref.cost_affine(ar, a, b)
         for dw in (-1, 8):
             assert port.cost_linear(cp, a, b, dw) == ref.cost_linear(cr, a, b, dw)
+
+
+def test_schedule_cells_match_oracle(oracle):
+    """Host schedule arithmetic (used for GCUPS) vs the oracle's own count."""
+    from poy5_gb300 import schedule
+    rng = np.random.default_rng(3)
+    for affine in (False, True):
+        tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
+        cm = oracle.cm(tcm=tcm, gap_open=go)
+        pairs = random_pairs(rng, 150, maxlen=600)
+        la = np.array([len(a) for a, _ in pairs])
+        lb = np.array([len(b) for _, b in pairs])
+        its, want = zip(*[oracle.schedule(cm, a, b, affine) for a, b in pairs])
+        full = None
+        if not affine:
+            g = lambda s: int(np.count_nonzero((s >= 16) & ((s & 16) != 0)))
+            full = schedule.linear_full_plane(la, lb, [g(a) for a, _ in pairs],
+                                              [g(b) for _, b in pairs])
+            # the oracle reports 0 iterations for a full plane
+            assert all((i == 0) == f for i, f in zip(its, full))
+        got = schedule.cells_computed(la, lb, np.array(its), 1, affine, full)
+        ok = [a > 1 or affine is False for a in np.minimum(la, lb)]
+        assert np.array_equal(got[ok], np.array(want)[ok])
