@@ -72,7 +72,7 @@ struct poyalgn_ctx {
     int device = 0;
     int nsm = 0;
     cudaStream_t stream = nullptr;
-    int bps[2][NCLASS] = {{0}};
+    int bps[2][NCLASS][2] = {};
     // host-pointer batches: staging of inputs and outputs
     DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
     // per-batch scratch
@@ -120,30 +120,32 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         passes = as<int>(c->passes);
     }
     if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
-    if ((rc = reserve(c->qitems, (size_t)NCLASS * npairs * sizeof(int2)))) return rc;
-    if ((rc = reserve(c->qctr, 2 * NCLASS * sizeof(int)))) return rc;
+    if ((rc = reserve(c->qitems, (size_t)NQUEUE * npairs * sizeof(int2)))) return rc;
+    if ((rc = reserve(c->qctr, 2 * NQUEUE * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
 
     // persistent grid per class, bounded by a slab budget
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     const long long budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
-    int grid[NCLASS];
+    int grid[NCLASS][2];
     long long strides[NCLASS];
     long long arena = 0;
     for (int k = 0; k < NCLASS; k++) {
         const int pipes = class_pipes_per_cta(affine, k);
         strides[k] = class_slab_bytes(affine, k, maxmn);
-        long long g = (long long)c->nsm * std::max(1, c->bps[affine][k]);
-        g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
-        g = std::min<long long>(g, std::max<long long>(1, budget / (strides[k] * pipes)));
-        grid[k] = (int)std::max<long long>(1, g);
-        arena = std::max(arena, (long long)grid[k] * pipes * strides[k]);
+        for (int v = 0; v < 2; v++) {
+            long long g = (long long)c->nsm * std::max(1, c->bps[affine][k][v]);
+            g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
+            g = std::min<long long>(g, std::max<long long>(1, budget / (strides[k] * pipes)));
+            grid[k][v] = (int)std::max<long long>(1, g);
+            arena = std::max(arena, (long long)grid[k][v] * pipes * strides[k]);
+        }
     }
     if ((rc = reserve(c->slab, (size_t)arena))) return rc;
     CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
     memcpy(c->call_strides, strides, sizeof(strides));
-    CU(cudaMemsetAsync(c->qctr.p, 0, 2 * NCLASS * sizeof(int), st));
+    CU(cudaMemsetAsync(c->qctr.p, 0, 2 * NQUEUE * sizeof(int), st));
 
     BatchArgs A;
     memset(&A, 0, sizeof(A));
@@ -161,7 +163,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.shadowEH0 = as<int>(c->eh0);
     A.qitems = as<int2>(c->qitems);
     A.qcount = as<int>(c->qctr);
-    A.qhead = as<int>(c->qctr) + NCLASS;
+    A.qhead = as<int>(c->qctr) + NQUEUE;
     A.qcap = npairs;
     A.slab = as<uint8_t>(c->slab);
     A.out_off = out_off;
@@ -193,8 +195,10 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if (ev) CU(cudaEventRecord(ev[1], st));
     for (int k = 0; k < NCLASS; k++) {
         A.slab_stride = strides[k];
-        launch_class(A, k, grid[k], st);
-        launches++;
+        for (int v = 0; v < (affine ? 2 : 1); v++) {
+            launch_class(A, k, v, grid[k][v], st);
+            launches++;
+        }
         if (ev) CU(cudaEventRecord(ev[k + 2], st));
     }
     CU(cudaGetLastError());
@@ -330,7 +334,8 @@ int poyalgn_init(int device, poyalgn_ctx** out)
         return set_err(POYALGN_ECUDA, "device setup: %s", cudaGetErrorString(e));
     }
     for (int a = 0; a < 2; a++)
-        for (int k = 0; k < NCLASS; k++) c->bps[a][k] = class_blocks_per_sm(a, k);
+        for (int k = 0; k < NCLASS; k++)
+            for (int v = 0; v < 2; v++) c->bps[a][k][v] = class_blocks_per_sm(a, k, v);
     *out = c;
     return 0;
 }

@@ -566,6 +566,183 @@ PA_HD void aff_step(AffLane<R>& L, const AffBand& b, const Tables& t,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Affine fast path for gap-free pairs: no state past position 0 of either
+// sequence carries the gap bit (the usual DNA input). Under that condition
+// the gap-dependent terms of the cell rules are exact constants:
+// HAS_GAP_OPENING returns go for every row and column, sj_horizontal_extension
+// is the prepend cost, si_vertical_extension the gap cost of the row symbol,
+// FILL_CLOSE_BLOCK_DIAGONAL adds no opening to the vertical/horizontal
+// predecessors and go to the diagonal one, and FILL_EXTEND_BLOCK_DIAGONAL
+// adds HIGH to both of its candidates. Results are identical to aff_step;
+// only the per-cell work is smaller.
+
+template <int R>
+struct AffFastLane {
+    AffCell V[R], Vp[R];
+    int J[R], JG[R];      // sj[j] and prepend[sj[j]] of the row's column
+    int sgext[R];         // gap cost of the row symbol
+    int srb[R];           // cost row of the row symbol
+    int itop, nstart;
+    AffCell s, sp;
+    AffCell g, gp;
+    int gCB;
+};
+
+template <int R>
+PA_HD void aff_fast_enter_block(AffFastLane<R>& L, const AffBand& b, const Tables& t,
+                                const uint8_t* si, int itop, int P)
+{
+    L.itop = itop;
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        const int i = itop + q;
+        const int ic = i <= b.m - 1 ? si[i] : 0;
+        L.sgext[q] = tcost(t, ic, t.gap);
+        L.srb[q] = t.rowoff[NTMPGAP & ic];
+    }
+    L.nstart = block_start_step_aff(b, itop + P * R);
+}
+
+template <int R>
+PA_HD void aff_fast_lane_init(AffFastLane<R>& L, const AffBand& b, const Tables& t,
+                              const uint8_t* si, int g, int P)
+{
+    const AffCell z = {0, 0, 0, 0, 0u};
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        L.V[q] = z;
+        L.Vp[q] = z;
+        L.J[q] = 0;
+        L.JG[q] = 0;
+    }
+    L.s = L.sp = L.g = L.gp = z;
+    L.gCB = 0;
+    aff_fast_enter_block(L, b, t, si, 1 + g * R, P);
+}
+
+template <int R>
+PA_HD void aff_fast_step(AffFastLane<R>& L, const AffBand& b, const Tables& t,
+                         const uint8_t* si, const uint8_t* sj, int P, int T,
+                         const AffCell& recv, int* shadowEB, int shadowEH0,
+                         int (&dcode)[R])
+{
+    L.sp = L.s;
+    L.s = recv;
+    const bool moved = (T >= L.nstart);
+    if (moved) aff_fast_enter_block(L, b, t, si, L.itop + P * R, P);
+    const int go = t.go;
+    const bool gen = (L.itop == 1);
+    if (gen) {  // row 0 at column T-1
+        const int j0 = T - 1;
+        L.gp = L.g;
+        if (j0 <= b.n - 1) {
+            AffCell c;
+            if (j0 == 0) {
+                L.gCB = 0;
+                c.EH = shadowEH0;
+            } else {
+                // sj_horizontal_extension before its j = 1 override: the
+                // leading gap followed by a base opens a gap at column 1
+                const int cj = sj[j0];
+                const int gr = t.prepend[cj];
+                L.gCB += (j0 == 1 && (sj[0] & t.gap)) ? go + gr : gr;
+                c.EH = L.gCB;
+            }
+            c.CB = L.gCB;
+            c.EV = HIGH;
+            c.EB = shadowEB[j0];
+            c.GM = (uint32_t)j0;
+            L.g = c;
+        }
+    }
+    if (moved) {
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            const int j = T - L.itop - q;
+            const int c = (j >= 0 && j < b.n) ? sj[j] : 0;
+            L.J[q] = c;
+            L.JG[q] = t.prepend[c];
+        }
+    } else {
+#pragma unroll
+        for (int q = R - 1; q > 0; q--) {
+            L.J[q] = L.J[q - 1];
+            L.JG[q] = L.JG[q - 1];
+        }
+        const int j = T - L.itop;
+        const int c = (j >= 0 && j < b.n) ? sj[j] : 0;
+        L.J[0] = c;
+        L.JG[0] = t.prepend[c];
+    }
+    const int leni = b.m - 1;
+    const int kr = b.D + b.newk;  // right border: j == i + kr
+#pragma unroll
+    for (int q = R - 1; q >= 0; q--) {
+        const int i = L.itop + q;
+        const int j = T - i;
+        AffCell up, dg;
+        if (q > 0) { up = L.V[q - 1]; dg = L.Vp[q - 1]; }
+        else if (gen) { up = L.g; dg = L.gp; }
+        else { up = L.s; dg = L.sp; }
+        const AffCell lf = L.V[q];
+        L.Vp[q] = L.V[q];
+        const int s = tmax(0, i - b.newk);
+        const int e = tmin(b.n - 1, i + kr);
+        dcode[q] = 0;
+        if (i <= leni && j >= s && j <= e) {
+            const int jgr = L.JG[q];
+            int dir;
+            AffCell c;
+            // extend horizontal (left border: HIGH, no flag)
+            {
+                const int ext = lf.EH + jgr, open = lf.CB + go + jgr;
+                const bool left = (j == s);
+                c.EH = left ? HIGH : tmin(ext, open);
+                dir = left ? 0 : (ext < open ? BEG_H : END_H);
+            }
+            // extend vertical (right border: HIGH, no flag)
+            {
+                const int sg = L.sgext[q];
+                const int ext = up.EV + sg, open = up.CB + go + sg;
+                const bool right = (j == i + kr);
+                c.EV = right ? HIGH : tmin(ext, open);
+                dir |= right ? 0 : (ext < open ? BEG_V : END_V);
+            }
+            if (j > 0) {
+                const int ext = dg.EB + HIGH, open = dg.CB + HIGH;
+                c.EB = tmin(ext, open);
+                dir |= ext < open ? BEG_B : END_B;
+                const int dgc = t.csw[L.srb[q] + (NTMPGAP & L.J[q])];
+                const int algn = dg.CB + dgc, fv = dg.EV + dgc, fh = dg.EH + dgc;
+                const int fd = dg.EB + dgc + go;
+                int v = algn, mask = A2A;
+                if (v >= fv) { if (v > fv) { v = fv; mask = A2V; } else mask |= A2V; }
+                if (v >= fh) { if (v > fh) { v = fh; mask = A2H; } else mask |= A2H; }
+                if (v >= fd) { if (v > fd) { v = fd; mask = A2D; } else mask |= A2D; }
+                c.CB = v;
+                dir |= mask;
+            } else {
+                c.CB = HIGH;
+                c.EB = HIGH;
+            }
+            int f = c.EH, mask = DO_H;
+            if (f >= c.EV) { if (f > c.EV) { f = c.EV; mask = DO_V; } else mask |= DO_V; }
+            if (f >= c.EB) { if (f > c.EB) { f = c.EB; mask = DO_D; } else mask |= DO_D; }
+            if (f >= c.CB) { if (f > c.CB) { f = c.CB; mask = DO_A; } else mask |= DO_A; }
+            if (f == c.EH && c.EH == c.EV) mask |= H_EQ_V;
+            dir |= mask;
+            uint32_t gm = (dir & (DO_A | DO_D)) ? dg.GM : 0u;
+            if (dir & DO_H) gm = vmax2(gm, lf.GM + 1u);
+            if (dir & DO_V) gm = vmax2(gm, up.GM + 0x10000u);
+            c.GM = gm;
+            L.V[q] = c;
+            if ((i & 1) == 0 && i >= 2 && i == (tmin(leni, j + b.newk) & ~1)) shadowEB[j] = c.EB;
+            dcode[q] = dir;
+        }
+    }
+}
+
 // Final cost of the affine corner cell from its four states.
 PA_HD int aff_final(const AffCell& c) { return tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB)); }
 PA_HD int aff_gapnum(const AffCell& c) { return tmax((int)(c.GM & 0xFFFF), (int)(c.GM >> 16)); }

@@ -70,6 +70,30 @@ void aff_pass(const AffBand& b, int P, const Tables& t, const uint8_t* x,
     *gapnum = aff_gapnum(L[g].V[q]);
 }
 
+template <int R>
+void aff_pass_fast(const AffBand& b, int P, const Tables& t, const uint8_t* x,
+              const uint8_t* y, uint16_t* dm, int* shadowEB, int shadowEH0,
+              int* cost, int* gapnum)
+{
+    std::vector<AffFastLane<R>> L(P);
+    for (int g = 0; g < P; g++) aff_fast_lane_init(L[g], b, t, x, g, P);
+    std::vector<AffCell> sv(P);
+    const int Tlast = (b.m - 1) + (b.n - 1);
+    for (int T = 1; T <= Tlast; T++) {
+        for (int g = 0; g < P; g++) sv[g] = L[g].V[R - 1];
+        for (int g = 0; g < P; g++) {
+            int src = (g + P - 1) % P;
+            int dc[R];
+            aff_fast_step<R>(L[g], b, t, x, y, P, T, sv[src], shadowEB, shadowEH0, dc);
+            for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint16_t)dc[q];
+        }
+    }
+    const int i = b.m - 1;
+    const int blk = (i - 1) / R, g = blk % P, q = (i - 1) - blk * R;
+    *cost = aff_final(L[g].V[q]);
+    *gapnum = aff_gapnum(L[g].V[q]);
+}
+
 struct Emul {
     HostCM cm;
     Tables t;
@@ -135,6 +159,9 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     if (m == 1 && n == 1) return -4;
     std::vector<uint16_t> dm;
     std::vector<int> shadow(n, HIGH);
+    bool gapfree = t.gap == TMPGAP;
+    for (int i = 1; i < la; i++) gapfree = gapfree && !(a[i] & TMPGAP);
+    for (int i = 1; i < lb; i++) gapfree = gapfree && !(b[i] & TMPGAP);
     int shadowEH0 = t.go;
     int P = 32, R = 1, T = pl.T0, g = 0;
     *passes = 0;
@@ -154,10 +181,18 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
             *cost = s;
             g = 0xFFFF;
         } else {
-            switch (R) {
-                case 1: aff_pass<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
-                case 2: aff_pass<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
-                default: aff_pass<4>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+            if (gapfree) {
+                switch (R) {
+                    case 1: aff_pass_fast<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                    case 2: aff_pass_fast<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                    default: aff_pass_fast<4>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                }
+            } else {
+                switch (R) {
+                    case 1: aff_pass<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                    case 2: aff_pass<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                    default: aff_pass<4>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                }
             }
             if (tmin(m - 1, bd.newk) >= 2) shadowEH0 = HIGH;
         }

@@ -99,25 +99,26 @@ __device__ __forceinline__ void pipe_sync(const Pipe& p)
 }
 
 // Pop the next work item of class `cls` for this pipeline (-1 when empty).
-__device__ __forceinline__ int pop_item(const BatchArgs& A, int cls, const Pipe& p, int* sh)
+// Queue q = 2 * class + variant (variant 1: affine gap-free fast path).
+__device__ __forceinline__ int pop_item(const BatchArgs& A, int q, const Pipe& p, int* sh)
 {
     int it = 0;
     if (p.K == 1) {
-        if (p.lane == 0) it = atomicAdd(&A.qhead[cls], 1);
+        if (p.lane == 0) it = atomicAdd(&A.qhead[q], 1);
         it = __shfl_sync(FULL, it, 0);
     } else {
         __syncthreads();
-        if (threadIdx.x == 0) *sh = atomicAdd(&A.qhead[cls], 1);
+        if (threadIdx.x == 0) *sh = atomicAdd(&A.qhead[q], 1);
         __syncthreads();
         it = *sh;
     }
-    return it < A.qcount[cls] ? it : -1;
+    return it < A.qcount[q] ? it : -1;
 }
 
-__device__ __forceinline__ void push_item(const BatchArgs& A, int cls, int pair, int T)
+__device__ __forceinline__ void push_item(const BatchArgs& A, int q, int pair, int T)
 {
-    int slot = atomicAdd(&A.qcount[cls], 1);
-    A.qitems[cls * A.qcap + slot] = make_int2(pair, T);
+    int slot = atomicAdd(&A.qcount[q], 1);
+    A.qitems[q * A.qcap + slot] = make_int2(pair, T);
 }
 
 __device__ __forceinline__ PairOut pair_out(const BatchArgs& A, int k)
@@ -193,6 +194,7 @@ __device__ void lin_fill(const LinBand& b, const Tables& st, const uint8_t* x,
 template <int R>
 __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
 {
+    constexpr int VARIANT = 0;
     __shared__ Tables st;
     __shared__ int xv[2][32];
     __shared__ uint32_t xn[2][32];
@@ -205,9 +207,9 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
     int* res = sres[K == 1 ? (threadIdx.x >> 5) : 0];
     uint8_t* dm = A.slab + (long long)p.slot * A.slab_stride;
     for (;;) {
-        const int it = pop_item(A, cls, p, &sitem);
+        const int it = pop_item(A, 2 * cls, p, &sitem);
         if (it < 0) break;
-        const int2 w = A.qitems[cls * A.qcap + it];
+        const int2 w = A.qitems[2 * cls * A.qcap + it];
         const int k = w.x;
         int T = w.y;
         const int la = A.lena[k], lb = A.lenb[k];
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
             const int c = pick_class(0, lin_wu(b), n);
             if (c > cls || c < 0 || npass >= MAX_PASSES) {
                 if (p.g == 0) {
-                    if (c > cls && npass < MAX_PASSES) push_item(A, c, k, T);
+                    if (c > cls && npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, k, T);
                     else A.status[k] = c < 0 ? -5 : -8;
                 }
                 moved = true;
@@ -310,8 +312,51 @@ __device__ void aff_fill(const AffBand& b, const Tables& st, const uint8_t* x,
 }
 
 template <int R>
+__device__ void aff_fill_fast(const AffBand& b, const Tables& st, const uint8_t* x,
+                         const uint8_t* y, uint16_t* dm, int* shadow, int shadowEH0,
+                         const Pipe& p, AffCell (*xc)[32], int* res)
+{
+    AffFastLane<R> L;
+    aff_fast_lane_init(L, b, st, x, p.g, p.P);
+    const int Tlast = (b.m - 1) + (b.n - 1);
+    const int src = (p.lane + 31) & 31;
+    for (int T = 1; T <= Tlast; T++) {
+        const AffCell sv = L.V[R - 1];
+        AffCell rc;
+        rc.EH = __shfl_sync(FULL, sv.EH, src);
+        rc.EV = __shfl_sync(FULL, sv.EV, src);
+        rc.EB = __shfl_sync(FULL, sv.EB, src);
+        rc.CB = __shfl_sync(FULL, sv.CB, src);
+        rc.GM = __shfl_sync(FULL, sv.GM, src);
+        if (p.K > 1) {
+            if (p.lane == 31) xc[T & 1][p.warp] = sv;
+            __syncthreads();
+            if (p.lane == 0) rc = xc[T & 1][(p.warp + p.K - 1) % p.K];
+        }
+        int dc[R];
+        aff_fast_step<R>(L, b, st, x, y, p.P, T, rc, shadow, shadowEH0, dc);
+        store_u16<R>(dm + (long long)T * (p.P * R) + p.g * R, dc);
+        // order this step's shadow writes after the generator's read of the
+        // same column one step earlier
+        if (p.K == 1) __syncwarp();
+    }
+    const int i = b.m - 1;
+    const int blk = (i - 1) / R, g = blk % p.P, q = (i - 1) - blk * R;
+    if (p.g == g) {
+        AffCell c = L.V[0];
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (r == q) c = L.V[r];
+        res[0] = aff_final(c);
+        res[1] = aff_gapnum(c);
+    }
+    pipe_sync(p);
+}
+
+template <int R, bool FAST>
 __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
 {
+    constexpr int VARIANT = FAST ? 1 : 0;
     __shared__ Tables st;
     __shared__ AffCell xc[2][32];
     __shared__ int sres[NARROW_WARPS][2];
@@ -323,9 +368,9 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
     int* res = sres[K == 1 ? (threadIdx.x >> 5) : 0];
     uint16_t* dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
     for (;;) {
-        const int it = pop_item(A, cls, p, &sitem);
+        const int it = pop_item(A, 2 * cls + VARIANT, p, &sitem);
         if (it < 0) break;
-        const int2 w = A.qitems[cls * A.qcap + it];
+        const int2 w = A.qitems[(2 * cls + VARIANT) * A.qcap + it];
         const int k = w.x;
         int T = w.y;
         const int la = A.lena[k], lb = A.lenb[k];
@@ -342,7 +387,7 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
             const int c = pick_class(1, aff_wu(b), n);
             if (c > cls || c < 0 || npass >= MAX_PASSES) {
                 if (p.g == 0) {
-                    if (c > cls && npass < MAX_PASSES) push_item(A, c, k, T);
+                    if (c > cls && npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, k, T);
                     else A.status[k] = c < 0 ? -5 : -8;
                 }
                 moved = true;
@@ -356,7 +401,8 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
                 gapnum = 0xFFFF;
             } else {
                 const int eh0 = A.shadowEH0[k];
-                aff_fill<R>(b, st, x, y, dm, shadow, eh0, p, xc, res);
+                if constexpr (FAST) aff_fill_fast<R>(b, st, x, y, dm, shadow, eh0, p, xc, res);
+                else aff_fill<R>(b, st, x, y, dm, shadow, eh0, p, xc, res);
                 cost = res[0];
                 gapnum = res[1];
                 if (p.g == 0 && tmin(m - 1, b.newk) >= 2) A.shadowEH0[k] = HIGH;
@@ -403,12 +449,20 @@ __global__ void prep_kernel(BatchArgs A)
     for (int i = lane; i < la; i += 32) bad |= (a[i] >= ns);
     for (int i = lane; i < lb; i += 32) bad |= (b[i] >= ns);
     bad = __any_sync(FULL, bad);
+    // gap bit anywhere past the leading position -> generic affine cells
+    int gapped = 0;
+    for (int i = 1 + lane; i < la; i += 32) gapped |= (a[i] & TMPGAP);
+    for (int i = 1 + lane; i < lb; i += 32) gapped |= (b[i] & TMPGAP);
+    gapped = __any_sync(FULL, gapped);
     PairPlan pl;
     if (A.affine) {
         pl = plan_affine(t, la, lb);
         int* shadow = A.shadow + A.out_off[k];
         for (int j = lane; j < pl.n; j += 32) shadow[j] = HIGH;
-        if (lane == 0) A.shadowEH0[k] = t.go;
+        if (lane == 0) {
+            A.shadowEH0[k] = t.go;
+            A.pfull[k] = (!gapped && t.gap == TMPGAP) ? 2 : 0;
+        }
     } else {
         int ga = 0, gb = 0;
         for (int i = lane; i < la; i += 32) ga += (a[i] >= t.gap && (a[i] & t.gap)) ? 1 : 0;
@@ -444,7 +498,7 @@ __global__ void prep_kernel(BatchArgs A)
         A.status[k] = -5;
         return;
     }
-    push_item(A, c, k, pl.T0);
+    push_item(A, 2 * c + ((A.affine && (A.pfull[k] & 2)) ? 1 : 0), k, pl.T0);
 }
 
 // Traceback of fills kept in their slabs (per-call stub path); one thread
@@ -532,16 +586,16 @@ __global__ void aligned_medians_kernel(const Tables* tg, const uint8_t* x, const
 
 }  // namespace
 
-int class_blocks_per_sm(int affine, int cls)
+int class_blocks_per_sm(int affine, int cls, int variant)
 {
     const int K = class_K(affine, cls), R = class_R(affine, cls);
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     int n = 0;
     if (affine) {
         switch (R) {
-            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, aff_class_kernel<1>, threads, 0); break;
-            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, aff_class_kernel<2>, threads, 0); break;
-            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, aff_class_kernel<4>, threads, 0); break;
+            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<1, true> : aff_class_kernel<1, false>, threads, 0); break;
+            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<2, true> : aff_class_kernel<2, false>, threads, 0); break;
+            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<4, true> : aff_class_kernel<4, false>, threads, 0); break;
         }
     } else {
         switch (R) {
@@ -570,15 +624,24 @@ void launch_prep(const BatchArgs& a, cudaStream_t s)
     prep_kernel<<<blocks, threads, 0, s>>>(a);
 }
 
-void launch_class(const BatchArgs& a, int cls, int grid, cudaStream_t s)
+void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream_t s)
 {
     const int K = class_K(a.affine, cls), R = class_R(a.affine, cls);
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     if (a.affine) {
         switch (R) {
-            case 1: aff_class_kernel<1><<<grid, threads, 0, s>>>(a, cls); break;
-            case 2: aff_class_kernel<2><<<grid, threads, 0, s>>>(a, cls); break;
-            default: aff_class_kernel<4><<<grid, threads, 0, s>>>(a, cls); break;
+            case 1:
+                if (variant) aff_class_kernel<1, true><<<grid, threads, 0, s>>>(a, cls);
+                else aff_class_kernel<1, false><<<grid, threads, 0, s>>>(a, cls);
+                break;
+            case 2:
+                if (variant) aff_class_kernel<2, true><<<grid, threads, 0, s>>>(a, cls);
+                else aff_class_kernel<2, false><<<grid, threads, 0, s>>>(a, cls);
+                break;
+            default:
+                if (variant) aff_class_kernel<4, true><<<grid, threads, 0, s>>>(a, cls);
+                else aff_class_kernel<4, false><<<grid, threads, 0, s>>>(a, cls);
+                break;
         }
     } else {
         switch (R) {

@@ -21,7 +21,7 @@ struct BatchArgs {
     int* pfull;                // linear plane choice per pair
     int* shadow;               // affine: row-0 EB left by earlier iterations (n per pair)
     int* shadowEH0;            // affine: row-0 EH at column 0
-    int2* qitems;              // NCLASS queues of (pair, T) with capacity qcap
+    int2* qitems;              // NQUEUE queues of (pair, T) with capacity qcap
     int* qcount;
     int* qhead;
     int qcap;
@@ -45,13 +45,15 @@ struct BatchArgs {
     uint8_t* mwg;
 };
 
+// Work queues: 2 per class (variant 1 = affine gap-free fast path).
+constexpr int NQUEUE = 2 * NCLASS;
 // Persistent CTAs per SM a class kernel can keep resident.
-int class_blocks_per_sm(int affine, int cls);
+int class_blocks_per_sm(int affine, int cls, int variant);
 // Bytes of direction slab one CTA of a class needs for pairs up to maxmn = m + n.
 long long class_slab_bytes(int affine, int cls, int maxmn);
 
 void launch_prep(const BatchArgs& a, cudaStream_t s);
-void launch_class(const BatchArgs& a, int cls, int grid, cudaStream_t s);
+void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream_t s);
 // Traceback + medians of pairs whose fill was left in the slab (per-call
 // path); d_strides[c] = slab bytes per pipeline of class c.
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
