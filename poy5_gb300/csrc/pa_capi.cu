@@ -77,7 +77,7 @@ struct poyalgn_ctx {
     DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
     // per-batch scratch
     DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
-    DevBuf dwh, swp;
+    DevBuf dwh, swp, order, order_scratch;
     int last_launches = 0;
     // optional per-launch timing: one event before the prep launch and one
     // after each launch of a batch, for up to prof_cap batches
@@ -182,6 +182,13 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.eb = eb;
     A.med = med;
     A.mwg = mwg;
+
+    // longest pairs enter the queues first so the persistent grid drains evenly
+    if ((rc = reserve(c->order, (size_t)npairs * 4))) return rc;
+    if ((rc = reserve(c->order_scratch, order_scratch_bytes(npairs)))) return rc;
+    if (launch_order(lena, lenb, npairs, as<int>(c->order), c->order_scratch.p, st) != 0)
+        return set_err(POYALGN_ECUDA, "ordering pairs failed");
+    A.order = as<int>(c->order);
 
     int launches = 0;
     cudaEvent_t* ev = nullptr;
@@ -347,7 +354,7 @@ void poyalgn_free(poyalgn_ctx* c)
     DevBuf* bufs[] = {&c->seqs, &c->offa, &c->lena, &c->offb, &c->lenb, &c->outoff,
                       &c->ints, &c->bytes, &c->pfull, &c->eh0, &c->lastcls, &c->slabcta,
                       &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
-                      &c->dwh, &c->swp};
+                      &c->dwh, &c->swp, &c->order, &c->order_scratch};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);

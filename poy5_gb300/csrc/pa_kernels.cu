@@ -16,6 +16,8 @@
 // shared-memory tables are shared.
 #include <cuda_runtime.h>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "pa_kernels.h"
 
 namespace pa {
@@ -436,9 +438,10 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
 
 __global__ void prep_kernel(BatchArgs A)
 {
-    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int wk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (k >= A.npairs) return;
+    if (wk >= A.npairs) return;
+    const int k = A.order ? A.order[wk] : wk;
     const Tables& t = *A.tables;
     const int la = A.lena[k], lb = A.lenb[k];
     const uint8_t* a = A.seqs + A.offa[k];
@@ -615,6 +618,39 @@ long long class_slab_bytes(int affine, int cls, int maxmn)
     return (b + 255) & ~255LL;
 }
 
+__global__ void order_keys_kernel(const int* lena, const int* lenb, int n, unsigned* key,
+                                  int* idx);
+
+static size_t sort_temp_bytes(int n)
+{
+    size_t tb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned*)nullptr, (unsigned*)nullptr,
+                                    (const int*)nullptr, (int*)nullptr, n);
+    return tb;
+}
+
+size_t order_scratch_bytes(int npairs)
+{
+    const size_t a = ((size_t)npairs * 4 + 255) & ~(size_t)255;
+    return 3 * a + sort_temp_bytes(npairs) + 256;
+}
+
+int launch_order(const int* lena, const int* lenb, int npairs, int* order, void* scratch,
+                 cudaStream_t s)
+{
+    if (npairs <= 0) return 0;
+    const size_t a = ((size_t)npairs * 4 + 255) & ~(size_t)255;
+    char* p = static_cast<char*>(scratch);
+    unsigned* key_in = reinterpret_cast<unsigned*>(p);
+    unsigned* key_out = reinterpret_cast<unsigned*>(p + a);
+    int* idx_in = reinterpret_cast<int*>(p + 2 * a);
+    void* temp = p + 3 * a;
+    size_t tb = sort_temp_bytes(npairs);
+    order_keys_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(lena, lenb, npairs, key_in, idx_in);
+    return (int)cub::DeviceRadixSort::SortPairs(temp, tb, key_in, key_out, idx_in, order,
+                                                npairs, 0, 32, s);
+}
+
 void launch_prep(const BatchArgs& a, cudaStream_t s)
 {
     if (a.npairs <= 0) return;
@@ -658,6 +694,16 @@ void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream
     if (a.npairs <= 0) return;
     const int threads = 128;
     traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a, d_strides);
+}
+
+__global__ void order_keys_kernel(const int* lena, const int* lenb, int n, unsigned* key,
+                                  int* idx)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned long long w = (unsigned long long)lena[k] * (unsigned long long)lenb[k];
+    key[k] = ~(unsigned)(w > 0xffffffffull ? 0xffffffffull : w);  // descending work
+    idx[k] = k;
 }
 
 int class_pipes_per_cta(int affine, int cls) { return class_K(affine, cls) == 1 ? NARROW_WARPS : 1; }

@@ -39,6 +39,7 @@ struct BatchArgs {
     int* slab_cta;             // pipeline whose slab holds the final fill
     const int* deltawh_override;  // per-call linear stub: caller's deltawh, no reordering
     const int* swap_override;     // per-call stubs: caller's tie preference
+    const int* order;             // prep visits pairs in this order (longest first)
     uint8_t* ea;
     uint8_t* eb;
     uint8_t* med;
@@ -53,6 +54,11 @@ int class_blocks_per_sm(int affine, int cls, int variant);
 long long class_slab_bytes(int affine, int cls, int maxmn);
 
 void launch_prep(const BatchArgs& a, cudaStream_t s);
+// Longest-first order of the pairs (by len(a) * len(b)) into `order`.
+// `scratch` must hold order_scratch_bytes(npairs) bytes.
+size_t order_scratch_bytes(int npairs);
+int launch_order(const int* lena, const int* lenb, int npairs, int* order, void* scratch,
+                 cudaStream_t s);
 void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream_t s);
 // Traceback + medians of pairs whose fill was left in the slab (per-call
 // path); d_strides[c] = slab bytes per pipeline of class c.
