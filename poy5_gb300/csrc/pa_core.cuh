@@ -83,20 +83,27 @@ PA_HD uint32_t vmax2(uint32_t a, uint32_t b)
 // moves up the ladder as its band doubles. Linear and affine use different
 // ladders because affine lanes hold more state per row.
 
-constexpr int NCLASS = 8;
-// Top shapes are bounded by registers: a 512-thread CTA leaves 128 registers
-// per thread, enough for 8 linear rows or 4 affine rows per lane.
-PA_HD int class_K(int affine, int c)
+constexpr int NCLASS = 10;
+// Pipeline of P lanes with R rows per lane. P < 32: 32/P pipelines share a
+// warp (one pair each, shuffles of width P); P >= 32: P/32 warps of one CTA.
+// Wider shapes are bounded by registers: a 512-thread CTA leaves 128
+// registers per thread, enough for 8 linear or 4 affine rows per lane.
+PA_HD int class_P(int affine, int c)
 {
-    const int lk[NCLASS] = {1, 1, 1, 1, 2, 4, 8, 16};
-    const int ak[NCLASS] = {1, 1, 1, 2, 4, 8, 16, 16};
-    return affine ? ak[c] : lk[c];
+    const int lp[NCLASS] = {4, 8, 16, 32, 32, 32, 64, 128, 256, 512};
+    const int ap[NCLASS] = {4, 8, 16, 32, 32, 64, 128, 256, 512, 512};
+    return affine ? ap[c] : lp[c];
 }
 PA_HD int class_R(int affine, int c)
 {
-    const int lr[NCLASS] = {1, 2, 4, 8, 8, 8, 8, 8};
-    const int ar[NCLASS] = {1, 2, 4, 4, 4, 4, 4, 4};
+    const int lr[NCLASS] = {2, 2, 2, 2, 4, 8, 8, 8, 8, 8};
+    const int ar[NCLASS] = {2, 2, 2, 2, 4, 4, 4, 4, 4, 4};
     return affine ? ar[c] : lr[c];
+}
+PA_HD int class_K(int affine, int c)
+{
+    const int P = class_P(affine, c);
+    return P >= 32 ? P / 32 : 1;
 }
 
 // A (P, R) pipeline processes a band of unclipped width wu over n columns
@@ -112,7 +119,7 @@ PA_HD bool band_fits(int P, int R, long long wu, int n)
 PA_HD int pick_class(int affine, long long wu, int n)
 {
     for (int c = 0; c < NCLASS; c++) {
-        int P = 32 * class_K(affine, c);
+        int P = class_P(affine, c);
         if (band_fits(P, class_R(affine, c), wu < 0 ? (1LL << 40) : wu, n)) return c;
     }
     return -1;

@@ -117,7 +117,7 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
         LinBand bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
         int c = pick_class(0, lin_wu(bd), n);
         if (c < 0) return -5;
-        P = 32 * class_K(0, c);
+        P = class_P(0, c);
         R = class_R(0, c);
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);
@@ -170,7 +170,7 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
         AffBand bd = aff_band(m, n, band_p(T, m, n));
         int c = pick_class(1, aff_wu(bd), n);
         if (c < 0) return -5;
-        P = 32 * class_K(1, c);
+        P = class_P(1, c);
         R = class_R(1, c);
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);

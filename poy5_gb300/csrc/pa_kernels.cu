@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <type_traits>
 
 #include "pa_kernels.h"
 
@@ -68,26 +69,32 @@ __device__ __forceinline__ void store_u16(uint16_t* p, const int (&d)[R])
     }
 }
 
-// Pipeline geometry of the calling thread.
+// Pipeline geometry of the calling thread. P < 32: 32/P pipelines share a
+// warp, each aligning its own pair (shuffles of width P); P >= 32: one
+// pipeline per warp (K = 1) or per CTA of K = P/32 warps.
 struct Pipe {
-    int K, P;       // warps and lanes per pipeline
-    int g;          // lane index within the pipeline
-    int lane, warp; // warp lane and warp index within the pipeline
-    int slot;       // pipeline index within the grid (selects the slab)
+    int P, K, G;     // lanes per pipeline, warps per pipeline, pipelines per warp
+    int gl;          // lane index within the pipeline
+    int grp;         // pipeline index within the warp (P < 32)
+    int lane, warp;  // warp lane; warp index within a multi-warp pipeline
+    int slot;        // pipeline index in the grid (selects the slab)
 };
 
-__device__ __forceinline__ Pipe make_pipe(int K)
+__device__ __forceinline__ Pipe make_pipe(int P)
 {
     Pipe p;
-    p.K = K;
-    p.P = 32 * K;
+    p.P = P;
+    p.K = P >= 32 ? P / 32 : 1;
+    p.G = P < 32 ? 32 / P : 1;
     p.lane = threadIdx.x & 31;
-    if (K == 1) {
-        p.g = p.lane;
+    if (p.K == 1) {
+        p.gl = p.lane & (P - 1);
+        p.grp = p.lane / P;
         p.warp = 0;
-        p.slot = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        p.slot = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * p.G + p.grp;
     } else {
-        p.g = threadIdx.x;
+        p.gl = threadIdx.x;
+        p.grp = 0;
         p.warp = threadIdx.x >> 5;
         p.slot = blockIdx.x;
     }
@@ -100,13 +107,41 @@ __device__ __forceinline__ void pipe_sync(const Pipe& p)
     else __syncthreads();
 }
 
-// Pop the next work item of class `cls` for this pipeline (-1 when empty).
+// True if any pipeline of the warp (or the CTA's one pipeline) is live.
+__device__ __forceinline__ bool any_live(const Pipe& p, bool live)
+{
+    return p.K == 1 ? __any_sync(FULL, live) : live;
+}
+
+// Warp-wide max (pipelines of a warp run their steps in lockstep).
+__device__ __forceinline__ int group_max(const Pipe& p, int v)
+{
+    return p.K == 1 ? __reduce_max_sync(FULL, v) : v;
+}
+
+// Rotate a value from lane g-1 of the pipeline (lane P-1 for lane 0).
+template <class V>
+__device__ __forceinline__ V rot_prev(const Pipe& p, V v)
+{
+    if (p.P < 32) return __shfl_sync(FULL, v, (p.gl + p.P - 1) & (p.P - 1), p.P);
+    return __shfl_sync(FULL, v, (p.lane + 31) & 31);
+}
+
+// Value held by pipeline lane `src` (K = 1 pipelines only).
+template <class V>
+__device__ __forceinline__ V from_lane(const Pipe& p, V v, int src)
+{
+    return __shfl_sync(FULL, v, src, p.P < 32 ? p.P : 32);
+}
+
 // Queue q = 2 * class + variant (variant 1: affine gap-free fast path).
-__device__ __forceinline__ int pop_item(const BatchArgs& A, int q, const Pipe& p, int* sh)
+// A warp of small pipelines takes G consecutive items at once; returns the
+// first index, or -1 when the queue is drained.
+__device__ __forceinline__ int pop_items(const BatchArgs& A, int q, const Pipe& p, int* sh)
 {
     int it = 0;
     if (p.K == 1) {
-        if (p.lane == 0) it = atomicAdd(&A.qhead[q], 1);
+        if (p.lane == 0) it = atomicAdd(&A.qhead[q], p.G);
         it = __shfl_sync(FULL, it, 0);
     } else {
         __syncthreads();
@@ -145,23 +180,67 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& A, int k, int cost,
     A.status[k] = r.status;
 }
 
+// Work item of one pipeline: the pair in internal order and its band state.
+struct Item {
+    int k, T, m, n, swaped, full, npass;
+    const uint8_t* x;
+    const uint8_t* y;
+};
+
+__device__ __forceinline__ Item load_item(const BatchArgs& A, int q, int it)
+{
+    Item w;
+    const int2 e = A.qitems[q * A.qcap + it];
+    w.k = e.x;
+    w.T = e.y;
+    const int la = A.lena[w.k], lb = A.lenb[w.k];
+    w.swaped = la <= lb ? 0 : 1;
+    w.x = A.seqs + (w.swaped ? A.offb[w.k] : A.offa[w.k]);
+    w.y = A.seqs + (w.swaped ? A.offa[w.k] : A.offb[w.k]);
+    w.m = w.swaped ? lb : la;
+    w.n = w.swaped ? la : lb;
+    w.full = A.pfull[w.k] & 1;
+    w.npass = A.passes[w.k];  // passes run by smaller classes (earlier launches)
+    return w;
+}
+
+__device__ __forceinline__ Item empty_item(const BatchArgs& A)
+{
+    Item w;
+    w.k = 0;
+    w.T = 1;
+    w.m = 1;
+    w.n = 1;
+    w.swaped = 0;
+    w.full = 0;
+    w.npass = 0;
+    w.x = A.seqs;
+    w.y = A.seqs;
+    return w;
+}
+
 // ---------------------------------------------------------------------------
 // linear
 
+// One band iteration of every active pipeline of the warp/CTA, in lockstep
+// over Tmax anti-diagonal steps; returns the corner cost and gap count of
+// the calling lane's pipeline.
 template <int R>
 __device__ void lin_fill(const LinBand& b, const Tables& st, const uint8_t* x,
-                         const uint8_t* y, uint8_t* dm, const Pipe& p,
-                         int (*xv)[32], uint32_t (*xn)[32], int* res)
+                         const uint8_t* y, uint8_t* dm, const Pipe& p, bool active,
+                         int Tmax, int (*xv)[32], uint32_t (*xn)[32], int* sres,
+                         int& cost, int& gapnum)
 {
     LinLane<R> L;
-    lin_lane_init(L, b, st, x, p.g, p.P);
-    const int Tlast = (b.m - 1) + (b.n - 1);
-    const int src = (p.lane + 31) & 31;
-    for (int T = 1; T <= Tlast; T++) {
+    L.V[R - 1] = 0;
+    L.N[R - 1] = 0;
+    if (active) lin_lane_init(L, b, st, x, p.gl, p.P);
+    const int Tlast = active ? (b.m - 1) + (b.n - 1) : 0;
+    for (int T = 1; T <= Tmax; T++) {
         const int sv = L.V[R - 1];
         const uint32_t sn = L.N[R - 1];
-        int rv = __shfl_sync(FULL, sv, src);
-        uint32_t rn = __shfl_sync(FULL, sn, src);
+        int rv = rot_prev(p, sv);
+        uint32_t rn = rot_prev(p, sn);
         if (p.K > 1) {
             if (p.lane == 31) {
                 xv[T & 1][p.warp] = sv;
@@ -174,23 +253,38 @@ __device__ void lin_fill(const LinBand& b, const Tables& st, const uint8_t* x,
                 rn = xn[T & 1][w];
             }
         }
-        int dc[R];
-        lin_step<R>(L, b, st, x, y, p.P, T, rv, rn, dc);
-        store_u8<R>(dm + (long long)T * (p.P * R) + p.g * R, dc);
+        if (active && T <= Tlast) {
+            int dc[R];
+            lin_step<R>(L, b, st, x, y, p.P, T, rv, rn, dc);
+            store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+        }
     }
-    // the lane that owns the corner row reports cost and gap count
-    const int i = b.m - 1;
-    const int blk = (i - 1) / R, g = blk % p.P, q = (i - 1) - blk * R;
-    if (p.g == g) {
-        int v = 0;
-        uint32_t nn = 0;
+    // the lane owning the corner row reports cost and gap count
+    const int i = active ? b.m - 1 : 1;
+    const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
+    int v = 0;
+    uint32_t nn = 0;
 #pragma unroll
-        for (int r = 0; r < R; r++)
-            if (r == q) { v = L.V[r]; nn = L.N[r]; }
-        res[0] = v;
-        res[1] = tmax((int)(nn & 0xFFFF), (int)(nn >> 16));
+    for (int r = 0; r < R; r++)
+        if (r == oq) {
+            v = L.V[r];
+            nn = L.N[r];
+        }
+    if (p.K == 1) {
+        v = from_lane(p, v, og);
+        nn = from_lane(p, nn, og);
+    } else {
+        if (p.gl == og) {
+            sres[0] = v;
+            sres[1] = (int)nn;
+        }
+        __syncthreads();
+        v = sres[0];
+        nn = (uint32_t)sres[1];
+        __syncthreads();
     }
-    pipe_sync(p);
+    cost = v;
+    gapnum = tmax((int)(nn & 0xFFFF), (int)(nn >> 16));
 }
 
 template <int R>
@@ -200,68 +294,67 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
     __shared__ Tables st;
     __shared__ int xv[2][32];
     __shared__ uint32_t xn[2][32];
-    __shared__ int sres[NARROW_WARPS][2];
+    __shared__ int sres[2];
     __shared__ int sitem;
     load_tables(st, A.tables);
     __syncthreads();
-    const int K = class_K(0, cls);
-    const Pipe p = make_pipe(K);
-    int* res = sres[K == 1 ? (threadIdx.x >> 5) : 0];
+    const Pipe p = make_pipe(class_P(0, cls));
+    const int q = 2 * cls + VARIANT;
     uint8_t* dm = A.slab + (long long)p.slot * A.slab_stride;
     for (;;) {
-        const int it = pop_item(A, 2 * cls, p, &sitem);
-        if (it < 0) break;
-        const int2 w = A.qitems[2 * cls * A.qcap + it];
-        const int k = w.x;
-        int T = w.y;
-        const int la = A.lena[k], lb = A.lenb[k];
-        const int swaped = la <= lb ? 0 : 1;
-        const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
-        const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
-        const int m = swaped ? lb : la, n = swaped ? la : lb;
-        const int full = A.pfull[k];
+        const int base = pop_items(A, q, p, &sitem);
+        if (base < 0) break;
+        const int it = base + p.grp;
+        bool live = it < A.qcount[q];
+        Item w = live ? load_item(A, q, it) : empty_item(A);
+        bool finished = false;
         int cost = 0;
-        int npass = A.passes[k];  // passes run by smaller classes (earlier launches)
-        bool done = false, moved = false;
-        while (!done) {
-            const LinBand b = lin_band(m, n, full, full ? 0 : band_p(T, m, n));
-            const int c = pick_class(0, lin_wu(b), n);
-            if (c > cls || c < 0 || npass >= MAX_PASSES) {
-                if (p.g == 0) {
-                    if (c > cls && npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, k, T);
-                    else A.status[k] = c < 0 ? -5 : -8;
+        for (;;) {
+            const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
+            if (live) {
+                const int c = pick_class(0, lin_wu(b), w.n);
+                if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
+                    if (p.gl == 0) {
+                        if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
+                        else A.status[w.k] = c < 0 ? -5 : -8;
+                    }
+                    live = false;
                 }
-                moved = true;
-                break;
             }
-            int gapnum;
-            if (m == 1) {
-                int s = 0;
-                for (int j = 1; j < n; j++) s += st.prepend[y[j]];
-                cost = s;
-                gapnum = n - 1;
-            } else {
-                lin_fill<R>(b, st, x, y, dm, p, xv, xn, res);
-                cost = res[0];
-                gapnum = res[1];
-                pipe_sync(p);
+            if (!any_live(p, live)) break;
+            const bool act = live && w.m > 1;
+            const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
+            int fc = 0, fg = 0;
+            if (Tmax > 0) lin_fill<R>(b, st, w.x, w.y, dm, p, act, Tmax, xv, xn, sres, fc, fg);
+            if (live) {
+                int gapnum = fg;
+                cost = fc;
+                if (w.m == 1) {  // no rows: row 0 is the whole alignment
+                    int s = 0;
+                    for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
+                    cost = s;
+                    gapnum = w.n - 1;
+                }
+                w.npass++;
+                if (p.gl == 0) A.passes[w.k] = w.npass;
+                if (w.full || lin_done(w.T, w.m, w.n, gapnum)) {
+                    live = false;
+                    finished = true;
+                } else {
+                    w.T *= 2;
+                }
             }
-            npass++;
-            if (p.g == 0) A.passes[k] = npass;
-            done = full || lin_done(T, m, n, gapnum);
-            if (!done) T *= 2;
         }
-        if (moved) continue;
-        if (p.g == 0) {
-            A.lastcls[k] = cls;
-            A.slab_cta[k] = p.slot;
+        if (finished && p.gl == 0) {
+            A.lastcls[w.k] = cls;
+            A.slab_cta[w.k] = p.slot;
             if (A.do_traceback) {
-                __threadfence_block();
-                const PairRes r = lin_traceback(dm, p.P, R, st, x, m, y, n, swaped, pair_out(A, k));
-                finish_pair(A, k, cost, r);
+                const PairRes r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
+                                                pair_out(A, w.k));
+                finish_pair(A, w.k, cost, r);
             } else {
-                A.cost[k] = cost;
-                A.status[k] = 0;
+                A.cost[w.k] = cost;
+                A.status[w.k] = 0;
             }
         }
         pipe_sync(p);
@@ -271,88 +364,65 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
 // ---------------------------------------------------------------------------
 // affine
 
-template <int R>
+template <int R, bool FAST>
 __device__ void aff_fill(const AffBand& b, const Tables& st, const uint8_t* x,
                          const uint8_t* y, uint16_t* dm, int* shadow, int shadowEH0,
-                         const Pipe& p, AffCell (*xc)[32], int* res)
+                         const Pipe& p, bool active, int Tmax, AffCell (*xc)[32],
+                         int* sres, int& cost, int& gapnum)
 {
-    AffLane<R> L;
-    aff_lane_init(L, b, st, x, p.g, p.P);
-    const int Tlast = (b.m - 1) + (b.n - 1);
-    const int src = (p.lane + 31) & 31;
-    for (int T = 1; T <= Tlast; T++) {
+    using Lane = typename std::conditional<FAST, AffFastLane<R>, AffLane<R>>::type;
+    Lane L;
+    L.V[R - 1] = AffCell{0, 0, 0, 0, 0u};
+    if (active) {
+        if constexpr (FAST) aff_fast_lane_init(L, b, st, x, p.gl, p.P);
+        else aff_lane_init(L, b, st, x, p.gl, p.P);
+    }
+    const int Tlast = active ? (b.m - 1) + (b.n - 1) : 0;
+    for (int T = 1; T <= Tmax; T++) {
         const AffCell sv = L.V[R - 1];
         AffCell rc;
-        rc.EH = __shfl_sync(FULL, sv.EH, src);
-        rc.EV = __shfl_sync(FULL, sv.EV, src);
-        rc.EB = __shfl_sync(FULL, sv.EB, src);
-        rc.CB = __shfl_sync(FULL, sv.CB, src);
-        rc.GM = __shfl_sync(FULL, sv.GM, src);
+        rc.EH = rot_prev(p, sv.EH);
+        rc.EV = rot_prev(p, sv.EV);
+        rc.EB = rot_prev(p, sv.EB);
+        rc.CB = rot_prev(p, sv.CB);
+        rc.GM = rot_prev(p, sv.GM);
         if (p.K > 1) {
             if (p.lane == 31) xc[T & 1][p.warp] = sv;
             __syncthreads();
             if (p.lane == 0) rc = xc[T & 1][(p.warp + p.K - 1) % p.K];
         }
-        int dc[R];
-        aff_step<R>(L, b, st, x, y, p.P, T, rc, shadow, shadowEH0, shadow, dc);
-        store_u16<R>(dm + (long long)T * (p.P * R) + p.g * R, dc);
-        // order this step's shadow writes after the generator's read of the
-        // same column one step earlier
-        if (p.K == 1) __syncwarp();
-    }
-    const int i = b.m - 1;
-    const int blk = (i - 1) / R, g = blk % p.P, q = (i - 1) - blk * R;
-    if (p.g == g) {
-        AffCell c = L.V[0];
-#pragma unroll
-        for (int r = 0; r < R; r++)
-            if (r == q) c = L.V[r];
-        res[0] = aff_final(c);
-        res[1] = aff_gapnum(c);
-    }
-    pipe_sync(p);
-}
-
-template <int R>
-__device__ void aff_fill_fast(const AffBand& b, const Tables& st, const uint8_t* x,
-                         const uint8_t* y, uint16_t* dm, int* shadow, int shadowEH0,
-                         const Pipe& p, AffCell (*xc)[32], int* res)
-{
-    AffFastLane<R> L;
-    aff_fast_lane_init(L, b, st, x, p.g, p.P);
-    const int Tlast = (b.m - 1) + (b.n - 1);
-    const int src = (p.lane + 31) & 31;
-    for (int T = 1; T <= Tlast; T++) {
-        const AffCell sv = L.V[R - 1];
-        AffCell rc;
-        rc.EH = __shfl_sync(FULL, sv.EH, src);
-        rc.EV = __shfl_sync(FULL, sv.EV, src);
-        rc.EB = __shfl_sync(FULL, sv.EB, src);
-        rc.CB = __shfl_sync(FULL, sv.CB, src);
-        rc.GM = __shfl_sync(FULL, sv.GM, src);
-        if (p.K > 1) {
-            if (p.lane == 31) xc[T & 1][p.warp] = sv;
-            __syncthreads();
-            if (p.lane == 0) rc = xc[T & 1][(p.warp + p.K - 1) % p.K];
+        if (active && T <= Tlast) {
+            int dc[R];
+            if constexpr (FAST) aff_fast_step<R>(L, b, st, x, y, p.P, T, rc, shadow, shadowEH0, dc);
+            else aff_step<R>(L, b, st, x, y, p.P, T, rc, shadow, shadowEH0, shadow, dc);
+            store_u16<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
         }
-        int dc[R];
-        aff_fast_step<R>(L, b, st, x, y, p.P, T, rc, shadow, shadowEH0, dc);
-        store_u16<R>(dm + (long long)T * (p.P * R) + p.g * R, dc);
-        // order this step's shadow writes after the generator's read of the
-        // same column one step earlier
+        // order this step's shadow writes after the row-0 reads of one step
+        // earlier (multi-warp pipelines are ordered by the exchange barrier)
         if (p.K == 1) __syncwarp();
     }
-    const int i = b.m - 1;
-    const int blk = (i - 1) / R, g = blk % p.P, q = (i - 1) - blk * R;
-    if (p.g == g) {
-        AffCell c = L.V[0];
+    const int i = active ? b.m - 1 : 1;
+    const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
+    AffCell c = L.V[0];
 #pragma unroll
-        for (int r = 0; r < R; r++)
-            if (r == q) c = L.V[r];
-        res[0] = aff_final(c);
-        res[1] = aff_gapnum(c);
+    for (int r = 0; r < R; r++)
+        if (r == oq) c = L.V[r];
+    int f = aff_final(c), g = aff_gapnum(c);
+    if (p.K == 1) {
+        f = from_lane(p, f, og);
+        g = from_lane(p, g, og);
+    } else {
+        if (p.gl == og) {
+            sres[0] = f;
+            sres[1] = g;
+        }
+        __syncthreads();
+        f = sres[0];
+        g = sres[1];
+        __syncthreads();
     }
-    pipe_sync(p);
+    cost = f;
+    gapnum = g;
 }
 
 template <int R, bool FAST>
@@ -361,72 +431,73 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
     constexpr int VARIANT = FAST ? 1 : 0;
     __shared__ Tables st;
     __shared__ AffCell xc[2][32];
-    __shared__ int sres[NARROW_WARPS][2];
+    __shared__ int sres[2];
     __shared__ int sitem;
     load_tables(st, A.tables);
     __syncthreads();
-    const int K = class_K(1, cls);
-    const Pipe p = make_pipe(K);
-    int* res = sres[K == 1 ? (threadIdx.x >> 5) : 0];
+    const Pipe p = make_pipe(class_P(1, cls));
+    const int q = 2 * cls + VARIANT;
     uint16_t* dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
     for (;;) {
-        const int it = pop_item(A, 2 * cls + VARIANT, p, &sitem);
-        if (it < 0) break;
-        const int2 w = A.qitems[(2 * cls + VARIANT) * A.qcap + it];
-        const int k = w.x;
-        int T = w.y;
-        const int la = A.lena[k], lb = A.lenb[k];
-        const int swaped = la <= lb ? 0 : 1;
-        const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
-        const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
-        const int m = swaped ? lb : la, n = swaped ? la : lb;
-        int* shadow = A.shadow + A.out_off[k];
+        const int base = pop_items(A, q, p, &sitem);
+        if (base < 0) break;
+        const int it = base + p.grp;
+        bool live = it < A.qcount[q];
+        Item w = live ? load_item(A, q, it) : empty_item(A);
+        int* shadow = A.shadow + (live ? A.out_off[w.k] : 0);
+        bool finished = false;
         int cost = 0;
-        int npass = A.passes[k];  // passes run by smaller classes (earlier launches)
-        bool done = false, moved = false;
-        while (!done) {
-            const AffBand b = aff_band(m, n, band_p(T, m, n));
-            const int c = pick_class(1, aff_wu(b), n);
-            if (c > cls || c < 0 || npass >= MAX_PASSES) {
-                if (p.g == 0) {
-                    if (c > cls && npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, k, T);
-                    else A.status[k] = c < 0 ? -5 : -8;
+        for (;;) {
+            const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
+            if (live) {
+                const int c = pick_class(1, aff_wu(b), w.n);
+                if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
+                    if (p.gl == 0) {
+                        if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
+                        else A.status[w.k] = c < 0 ? -5 : -8;
+                    }
+                    live = false;
                 }
-                moved = true;
-                break;
             }
-            int gapnum;
-            if (m == 1) {
-                int s = st.go;
-                for (int j = 1; j < n; j++) s += st.prepend[y[j]];
-                cost = s;
-                gapnum = 0xFFFF;
-            } else {
-                const int eh0 = A.shadowEH0[k];
-                if constexpr (FAST) aff_fill_fast<R>(b, st, x, y, dm, shadow, eh0, p, xc, res);
-                else aff_fill<R>(b, st, x, y, dm, shadow, eh0, p, xc, res);
-                cost = res[0];
-                gapnum = res[1];
-                if (p.g == 0 && tmin(m - 1, b.newk) >= 2) A.shadowEH0[k] = HIGH;
-                pipe_sync(p);
+            if (!any_live(p, live)) break;
+            const bool act = live && w.m > 1;
+            const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
+            const int eh0 = live ? A.shadowEH0[w.k] : 0;
+            int fc = 0, fg = 0;
+            if (Tmax > 0)
+                aff_fill<R, FAST>(b, st, w.x, w.y, dm, shadow, eh0, p, act, Tmax, xc, sres, fc, fg);
+            if (live) {
+                int gapnum = fg;
+                cost = fc;
+                if (w.m == 1) {  // leni = 0: the initial row is the whole alignment
+                    int s = st.go;
+                    for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
+                    cost = s;
+                    gapnum = 0xFFFF;
+                } else if (p.gl == 0 && tmin(w.m - 1, b.newk) >= 2) {
+                    A.shadowEH0[w.k] = HIGH;
+                }
+                w.npass++;
+                if (p.gl == 0) A.passes[w.k] = w.npass;
+                if (aff_done(w.T, w.m, w.n, gapnum)) {
+                    live = false;
+                    finished = true;
+                } else {
+                    w.T *= 2;
+                }
             }
-            npass++;
-            if (p.g == 0) A.passes[k] = npass;
-            done = aff_done(T, m, n, gapnum);
-            if (!done) T *= 2;
             pipe_sync(p);
         }
-        if (moved) continue;
-        if (p.g == 0) {
-            A.lastcls[k] = cls;
-            A.slab_cta[k] = p.slot;
+        if (finished && p.gl == 0) {
+            A.lastcls[w.k] = cls;
+            A.slab_cta[w.k] = p.slot;
             if (A.do_traceback) {
-                __threadfence_block();
-                const PairRes r = aff_traceback(dm, p.P, R, st, x, m, y, n, swaped, pair_out(A, k));
-                finish_pair(A, k, cost, r);
+                const PairRes r = aff_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
+                                                pair_out(A, w.k));
+                finish_pair(A, w.k, cost, r);
             } else {
-                A.cost[k] = cost;
-                A.status[k] = 0;
+                A.cost[w.k] = cost;
+                A.status[w.k] = 0;
             }
         }
         pipe_sync(p);
@@ -518,7 +589,7 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
     const int m = swaped ? lb : la, n = swaped ? la : lb;
     const int tie = A.swap_override ? A.swap_override[k] : swaped;
     const int cls = A.lastcls[k];
-    const int P = 32 * class_K(A.affine, cls), R = class_R(A.affine, cls);
+    const int P = class_P(A.affine, cls), R = class_R(A.affine, cls);
     const uint8_t* base = A.slab + (long long)A.slab_cta[k] * strides[cls];
     PairRes r;
     if (A.affine) r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, tie, pair_out(A, k));
@@ -596,13 +667,11 @@ int class_blocks_per_sm(int affine, int cls, int variant)
     int n = 0;
     if (affine) {
         switch (R) {
-            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<1, true> : aff_class_kernel<1, false>, threads, 0); break;
             case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<2, true> : aff_class_kernel<2, false>, threads, 0); break;
             default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<4, true> : aff_class_kernel<4, false>, threads, 0); break;
         }
     } else {
         switch (R) {
-            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<1>, threads, 0); break;
             case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<2>, threads, 0); break;
             case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<4>, threads, 0); break;
             default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<8>, threads, 0); break;
@@ -613,7 +682,7 @@ int class_blocks_per_sm(int affine, int cls, int variant)
 
 long long class_slab_bytes(int affine, int cls, int maxmn)
 {
-    const long long PR = 32LL * class_K(affine, cls) * class_R(affine, cls);
+    const long long PR = (long long)class_P(affine, cls) * class_R(affine, cls);
     long long b = (long long)(maxmn + 1) * PR * (affine ? 2 : 1);
     return (b + 255) & ~255LL;
 }
@@ -666,10 +735,6 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     if (a.affine) {
         switch (R) {
-            case 1:
-                if (variant) aff_class_kernel<1, true><<<grid, threads, 0, s>>>(a, cls);
-                else aff_class_kernel<1, false><<<grid, threads, 0, s>>>(a, cls);
-                break;
             case 2:
                 if (variant) aff_class_kernel<2, true><<<grid, threads, 0, s>>>(a, cls);
                 else aff_class_kernel<2, false><<<grid, threads, 0, s>>>(a, cls);
@@ -681,7 +746,6 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
         }
     } else {
         switch (R) {
-            case 1: lin_class_kernel<1><<<grid, threads, 0, s>>>(a, cls); break;
             case 2: lin_class_kernel<2><<<grid, threads, 0, s>>>(a, cls); break;
             case 4: lin_class_kernel<4><<<grid, threads, 0, s>>>(a, cls); break;
             default: lin_class_kernel<8><<<grid, threads, 0, s>>>(a, cls); break;
@@ -706,7 +770,11 @@ __global__ void order_keys_kernel(const int* lena, const int* lenb, int n, unsig
     idx[k] = k;
 }
 
-int class_pipes_per_cta(int affine, int cls) { return class_K(affine, cls) == 1 ? NARROW_WARPS : 1; }
+int class_pipes_per_cta(int affine, int cls)
+{
+    const int P = class_P(affine, cls);
+    return P >= 64 ? 1 : NARROW_WARPS * (P < 32 ? 32 / P : 1);
+}
 
 void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
                             int len, uint8_t* anc, uint8_t* mwg, int* out3,
