@@ -272,6 +272,9 @@ def run_gpu(args):
         d2h = int(7 * 4 * n + 4 * pk.out_bytes)
         e2e = {"seconds": e2e_s, "h2d": h2d, "d2h": d2h}
 
+    # the plain per-call path: one drop-in stub call per pair (sample)
+    plain = plain_per_call(ctx, cm, w, seconds=3.0)
+
     cells = cells_full(w)
     full = None
     if not w.affine:
@@ -282,27 +285,44 @@ def run_gpu(args):
     computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, w.affine, full).sum())
     return dict(w=w, model=model, n=n, ms=ms, cells=cells, computed=computed, prof=prof,
                 clocks=clk, e2e=e2e, launches=launches_per_step, passes=passes,
-                world=world, rank=rank, pk=pk)
+                world=world, rank=rank, pk=pk, plain=plain)
+
+
+def plain_per_call(ctx, cm, w, seconds: float = 3.0) -> dict:
+    """One per-call drop-in invocation per pair (what POY's OCaml would do
+    through the stub library): algn_CAML_align_affine_3, or simple_2 +
+    backtrace_2d for the linear model; host buffers in and out."""
+    import poy5_gb300 as pg
+    al = pg.Align(ctx)
+    t0 = time.perf_counter()
+    n = cells = 0
+    while n < len(w.pairs) and time.perf_counter() - t0 < seconds:
+        a, b = w.pairs[n]
+        al.align_2(a, b, cm)
+        cells += len(a) * len(b)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"gcups": cells / dt / 1e9, "alignments_per_s": n / dt, "pairs": n}
+
+
+def _reduce(x: float, world: int, op: str) -> float:
+    """All-reduce one scalar across ranks (NCCL on GPUs, gloo on CPU)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
 
 
 def reduce_max(x: float, world: int) -> float:
-    if world <= 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return _reduce(x, world, "max")
 
 
 def reduce_sum(x: float, world: int) -> float:
-    if world <= 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, world, "sum")
 
 
 def gpu_line(args, r) -> dict:
@@ -362,6 +382,10 @@ def gpu_line(args, r) -> dict:
         "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"),
                    "reasons": clk.get("reasons")},
         "passes_mean": round(float(np.mean(r["passes"])), 3),
+        "plain_per_call": {"value": round(r["plain"]["gcups"], 3), "unit": "GCUPS",
+                           "alignments_per_s": round(r["plain"]["alignments_per_s"], 1),
+                           "sample": f"first {r['plain']['pairs']} pairs, one stub call each"},
+        "batched_over_plain": round(gcups / max(r["plain"]["gcups"], 1e-9), 1),
     }
     if r["e2e"]:
         e = r["e2e"]

@@ -750,6 +750,188 @@ PA_HD void aff_fast_step(AffFastLane<R>& L, const AffBand& b, const Tables& t,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Affine fast path, register-lean form (gap-free pairs whose costs stay far
+// below HIGH). Identical results to aff_step:
+//  * every "keep the smaller, OR the flag on ties" chain of ASSIGN_MINIMUM
+//    and FILL_CLOSE_BLOCK_DIAGONAL leaves exactly the flags of the candidates
+//    equal to the final minimum, so the flags are equality tests against it;
+//  * row 0's stale EB (left by earlier doubling iterations) only meets
+//    CB0 + HIGH and CB + cost + go comparisons that it can never win or tie
+//    when every EB is >= HIGH > CB0, so HIGH stands in for it and nothing
+//    has to be written back;
+//  * cell states ping-pong between two register sets (V0/V1, R0/R1, G0/G1)
+//    and the caller alternates their roles on even and odd steps, so no
+//    state is copied between steps.
+
+template <int R>
+struct AffLean {
+    AffCell V0[R], V1[R];   // row states of two consecutive steps
+    AffCell R0, R1;         // neighbour's bottom row, two consecutive steps
+    AffCell G0, G1;         // row 0 (lane 0 of the first block)
+    int J[R], JG[R];        // column symbol and its prepend cost, per row
+    int Ts[R], Te[R], Tr[R];// first / last / right-border step of each row
+    int sg[R], sgo[R];      // gap cost of the row symbol (and + go)
+    int srb[R];             // cost row of the row symbol
+    int itop, nstart, gCB;
+};
+
+template <int R>
+PA_HD void aff_lean_enter(AffLean<R>& L, const AffBand& b, const Tables& t,
+                          const uint8_t* si, int itop, int P)
+{
+    L.itop = itop;
+    const int kr = b.D + b.newk;
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        const int i = itop + q;
+        const bool real = i <= b.m - 1;
+        const int ic = real ? si[i] : 0;
+        const int sgv = tcost(t, ic, t.gap);
+        L.sg[q] = sgv;
+        L.sgo[q] = sgv + t.go;
+        L.srb[q] = t.rowoff[ic];
+        L.Ts[q] = real ? i + tmax(0, i - b.newk) : 0x7fffffff;
+        L.Te[q] = real ? i + tmin(b.n - 1, i + kr) : -1;
+        L.Tr[q] = 2 * i + kr;
+    }
+    L.nstart = block_start_step_aff(b, itop + P * R);
+}
+
+template <int R>
+PA_HD void aff_lean_init(AffLean<R>& L, const AffBand& b, const Tables& t,
+                         const uint8_t* si, int g, int P)
+{
+    const AffCell z = {0, 0, 0, 0, 0u};
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+        L.V0[q] = z;
+        L.V1[q] = z;
+        L.J[q] = 0;
+        L.JG[q] = 0;
+    }
+    L.R0 = L.R1 = L.G0 = L.G1 = z;
+    L.gCB = 0;
+    aff_lean_enter(L, b, t, si, 1 + g * R, P);
+}
+
+// The affine fast path needs every row-0 cost far below HIGH.
+PA_HD bool aff_lean_ok(const Tables& t, int n)
+{
+    int mp = 0;
+    for (int a = 0; a < NSTATE; a++) mp = tmax(mp, t.prepend[a]);
+    return (long long)n * (mp + t.go + 1) + t.go < HIGH / 4;
+}
+
+// One anti-diagonal step. VC/RC/GC hold step T-1 (up, left), VP/RP/GP hold
+// step T-2 (diagonal); the step's results overwrite VP/RP/GP, which the
+// caller then passes as VC/RC/GC of the next step.
+template <int R>
+PA_HD void aff_lean_step(AffLean<R>& L, AffCell (&VC)[R], AffCell (&VP)[R],
+                         AffCell& RC, AffCell& RP, AffCell& GC, AffCell& GP,
+                         const AffBand& b, const Tables& t, const uint8_t* si,
+                         const uint8_t* sj, int P, int T, const AffCell& recv,
+                         int shadowEH0, int (&dcode)[R])
+{
+    RP = recv;  // neighbour bottom row at T-1 becomes this step's "up"
+    const bool moved = (T >= L.nstart);
+    if (moved) aff_lean_enter(L, b, t, si, L.itop + P * R, P);
+    const int go = t.go;
+    const bool gen = (L.itop == 1);
+    if (gen) {  // row 0 at column T-1
+        const int j0 = T - 1;
+        if (j0 <= b.n - 1) {
+            AffCell c;
+            if (j0 == 0) {
+                L.gCB = 0;
+                c.EH = shadowEH0;
+            } else {
+                const int gr = t.prepend[sj[j0]];
+                L.gCB += (j0 == 1 && (sj[0] & t.gap)) ? go + gr : gr;
+                c.EH = L.gCB;
+            }
+            c.CB = L.gCB;
+            c.EV = HIGH;
+            c.EB = HIGH;
+            c.GM = (uint32_t)j0;
+            GP = c;
+        }
+    }
+    if (moved) {
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            const int j = T - L.itop - q;
+            const int c = (j >= 0 && j < b.n) ? sj[j] : 0;
+            L.J[q] = c;
+            L.JG[q] = t.prepend[c];
+        }
+    } else {
+#pragma unroll
+        for (int q = R - 1; q > 0; q--) {
+            L.J[q] = L.J[q - 1];
+            L.JG[q] = L.JG[q - 1];
+        }
+        const int j = T - L.itop;
+        const int c = (j >= 0 && j < b.n) ? sj[j] : 0;
+        L.J[0] = c;
+        L.JG[0] = t.prepend[c];
+    }
+    // the "up" neighbours of row 0 are this step's received / generated
+    // values (already in RP / GP); the diagonals are last step's (RC / GC)
+#pragma unroll
+    for (int q = R - 1; q >= 0; q--) {
+        const AffCell up = q > 0 ? VC[q - 1] : (gen ? GP : RP);
+        const AffCell dg = q > 0 ? VP[q - 1] : (gen ? GC : RC);
+        const AffCell& lf = VC[q];
+        dcode[q] = 0;
+        if (T >= L.Ts[q] && T <= L.Te[q]) {
+            const int j = T - (L.itop + q);
+            const int jgr = L.JG[q];
+            AffCell c;
+            int dir;
+            {
+                const int ext = lf.EH + jgr, open = lf.CB + go + jgr;
+                const bool left = (T == L.Ts[q]);
+                c.EH = left ? HIGH : tmin(ext, open);
+                dir = left ? 0 : (ext < open ? BEG_H : END_H);
+            }
+            {
+                const int ext = up.EV + L.sg[q], open = up.CB + L.sgo[q];
+                const bool right = (T == L.Tr[q]);
+                c.EV = right ? HIGH : tmin(ext, open);
+                dir |= right ? 0 : (ext < open ? BEG_V : END_V);
+            }
+            if (j > 0) {
+                const int ext = dg.EB + HIGH, open = dg.CB + HIGH;
+                c.EB = tmin(ext, open);
+                dir |= ext < open ? BEG_B : END_B;
+                const int dgc = t.csw[L.srb[q] + L.J[q]];
+                const int a0 = dg.CB + dgc, a1 = dg.EV + dgc, a2 = dg.EH + dgc;
+                const int a3 = dg.EB + dgc + go;
+                const int v = tmin(tmin(a0, a1), tmin(a2, a3));
+                c.CB = v;
+                dir |= (a0 == v ? A2A : 0) | (a1 == v ? A2V : 0) | (a2 == v ? A2H : 0) |
+                       (a3 == v ? A2D : 0);
+            } else {
+                c.CB = HIGH;
+                c.EB = HIGH;
+            }
+            const int f = tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB));
+            const bool hh = c.EH == f, vv = c.EV == f;
+            dir |= (hh ? DO_H : 0) | (vv ? DO_V : 0) | (c.EB == f ? DO_D : 0) |
+                   (c.CB == f ? DO_A : 0) | ((hh && vv) ? H_EQ_V : 0);
+            uint32_t gm = (dir & (DO_A | DO_D)) ? dg.GM : 0u;
+            if (hh) gm = vmax2(gm, lf.GM + 1u);
+            if (vv) gm = vmax2(gm, up.GM + 0x10000u);
+            c.GM = gm;
+            VP[q] = c;
+            dcode[q] = dir;
+        } else {
+            VP[q] = VC[q];  // keep the row's last state (read as diag/left)
+        }
+    }
+}
+
 // Final cost of the affine corner cell from its four states.
 PA_HD int aff_final(const AffCell& c) { return tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB)); }
 PA_HD int aff_gapnum(const AffCell& c) { return tmax((int)(c.GM & 0xFFFF), (int)(c.GM >> 16)); }

@@ -94,6 +94,37 @@ void aff_pass_fast(const AffBand& b, int P, const Tables& t, const uint8_t* x,
     *gapnum = aff_gapnum(L[g].V[q]);
 }
 
+template <int R>
+void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
+                   const uint8_t* y, uint16_t* dm, int shadowEH0, int* cost, int* gapnum)
+{
+    std::vector<AffLean<R>> L(P);
+    for (int g = 0; g < P; g++) aff_lean_init(L[g], b, t, x, g, P);
+    std::vector<AffCell> sv(P);
+    const int Tlast = (b.m - 1) + (b.n - 1);
+    for (int T = 1; T <= Tlast; T++) {
+        const bool odd = T & 1;
+        for (int g = 0; g < P; g++) sv[g] = odd ? L[g].V0[R - 1] : L[g].V1[R - 1];
+        for (int g = 0; g < P; g++) {
+            const int src = (g + P - 1) % P;
+            int dc[R];
+            AffLean<R>& l = L[g];
+            if (odd)
+                aff_lean_step<R>(l, l.V0, l.V1, l.R0, l.R1, l.G0, l.G1, b, t, x, y, P, T, sv[src],
+                                 shadowEH0, dc);
+            else
+                aff_lean_step<R>(l, l.V1, l.V0, l.R1, l.R0, l.G1, l.G0, b, t, x, y, P, T, sv[src],
+                                 shadowEH0, dc);
+            for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint16_t)dc[q];
+        }
+    }
+    const int i = b.m - 1;
+    const int blk = (i - 1) / R, g = blk % P, q = (i - 1) - blk * R;
+    const AffCell c = (Tlast & 1) ? L[g].V1[q] : L[g].V0[q];
+    *cost = aff_final(c);
+    *gapnum = aff_gapnum(c);
+}
+
 struct Emul {
     HostCM cm;
     Tables t;
@@ -181,7 +212,13 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
             *cost = s;
             g = 0xFFFF;
         } else {
-            if (gapfree) {
+            if (gapfree && aff_lean_ok(t, n)) {
+                switch (R) {
+                    case 1: aff_pass_lean<1>(bd, P, t, x, y, dm.data(), shadowEH0, cost, &g); break;
+                    case 2: aff_pass_lean<2>(bd, P, t, x, y, dm.data(), shadowEH0, cost, &g); break;
+                    default: aff_pass_lean<4>(bd, P, t, x, y, dm.data(), shadowEH0, cost, &g); break;
+                }
+            } else if (gapfree) {
                 switch (R) {
                     case 1: aff_pass_fast<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                     case 2: aff_pass_fast<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;

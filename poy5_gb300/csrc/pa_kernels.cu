@@ -425,6 +425,79 @@ __device__ void aff_fill(const AffBand& b, const Tables& st, const uint8_t* x,
     gapnum = g;
 }
 
+
+// Lean affine fill (gap-free pairs within aff_lean_ok): the step loop is
+// unrolled by two so the two register sets of AffLean swap roles statically.
+template <int R>
+__device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t* x,
+                              const uint8_t* y, uint16_t* dm, int shadowEH0, const Pipe& p,
+                              bool active, int Tmax, AffCell (*xc)[32], int* sres, int& cost,
+                              int& gapnum)
+{
+    AffLean<R> L;
+    L.V0[R - 1] = AffCell{0, 0, 0, 0, 0u};
+    L.V1[R - 1] = AffCell{0, 0, 0, 0, 0u};
+    if (active) aff_lean_init(L, b, st, x, p.gl, p.P);
+    const int Tlast = active ? (b.m - 1) + (b.n - 1) : 0;
+    auto exchange = [&](const AffCell& sv, int T) {
+        AffCell rc;
+        rc.EH = rot_prev(p, sv.EH);
+        rc.EV = rot_prev(p, sv.EV);
+        rc.EB = rot_prev(p, sv.EB);
+        rc.CB = rot_prev(p, sv.CB);
+        rc.GM = rot_prev(p, sv.GM);
+        if (p.K > 1) {
+            if (p.lane == 31) xc[T & 1][p.warp] = sv;
+            __syncthreads();
+            if (p.lane == 0) rc = xc[T & 1][(p.warp + p.K - 1) % p.K];
+        }
+        return rc;
+    };
+    for (int T = 1; T <= Tmax; T += 2) {
+        {
+            const AffCell rc = exchange(L.V0[R - 1], T);
+            if (active && T <= Tlast) {
+                int dc[R];
+                aff_lean_step<R>(L, L.V0, L.V1, L.R0, L.R1, L.G0, L.G1, b, st, x, y, p.P, T,
+                                 rc, shadowEH0, dc);
+                store_u16<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+            }
+        }
+        if (T + 1 <= Tmax) {
+            const AffCell rc = exchange(L.V1[R - 1], T + 1);
+            if (active && T + 1 <= Tlast) {
+                int dc[R];
+                aff_lean_step<R>(L, L.V1, L.V0, L.R1, L.R0, L.G1, L.G0, b, st, x, y, p.P,
+                                 T + 1, rc, shadowEH0, dc);
+                store_u16<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
+            }
+        }
+    }
+    const int i = active ? b.m - 1 : 1;
+    const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
+    AffCell c = L.V0[0];
+    const bool odd = (Tlast & 1) != 0;  // odd last step wrote V1
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (r == oq) c = odd ? L.V1[r] : L.V0[r];
+    int f = aff_final(c), g = aff_gapnum(c);
+    if (p.K == 1) {
+        f = from_lane(p, f, og);
+        g = from_lane(p, g, og);
+    } else {
+        if (p.gl == og) {
+            sres[0] = f;
+            sres[1] = g;
+        }
+        __syncthreads();
+        f = sres[0];
+        g = sres[1];
+        __syncthreads();
+    }
+    cost = f;
+    gapnum = g;
+}
+
 template <int R, bool FAST>
 __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
 {
@@ -464,8 +537,13 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
             const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
             const int eh0 = live ? A.shadowEH0[w.k] : 0;
             int fc = 0, fg = 0;
-            if (Tmax > 0)
-                aff_fill<R, FAST>(b, st, w.x, w.y, dm, shadow, eh0, p, act, Tmax, xc, sres, fc, fg);
+            if (Tmax > 0) {
+                if constexpr (FAST)
+                    aff_fill_lean<R>(b, st, w.x, w.y, dm, eh0, p, act, Tmax, xc, sres, fc, fg);
+                else
+                    aff_fill<R, false>(b, st, w.x, w.y, dm, shadow, eh0, p, act, Tmax, xc, sres,
+                                       fc, fg);
+            }
             if (live) {
                 int gapnum = fg;
                 cost = fc;
@@ -535,7 +613,7 @@ __global__ void prep_kernel(BatchArgs A)
         for (int j = lane; j < pl.n; j += 32) shadow[j] = HIGH;
         if (lane == 0) {
             A.shadowEH0[k] = t.go;
-            A.pfull[k] = (!gapped && t.gap == TMPGAP) ? 2 : 0;
+            A.pfull[k] = (!gapped && t.gap == TMPGAP && aff_lean_ok(t, tmax(la, lb))) ? 2 : 0;
         }
     } else {
         int ga = 0, gb = 0;
