@@ -177,6 +177,52 @@ int poyalgn_median_batch_device(poyalgn_ctx *ctx, const poyalgn_cm *cm,
                                 uint8_t *ea, uint8_t *eb, uint8_t *med,
                                 uint8_t *mwg, int32_t *passes, void *stream);
 
+/*
+ * poyalgn_median_batch_device without any memory allocation. No counterpart
+ * in the reference: it is for callers that must not allocate device memory
+ * during the call (a serving loop with a fixed memory budget, code that runs
+ * while an allocator is locked) but can accept a bounded batch.
+ *
+ * Arguments and results are those of poyalgn_median_batch_device, without
+ * the context; the work runs on the current CUDA device, which must be the
+ * device `cm` was built on. All scratch (work queues, direction slabs,
+ * per-pair state, the pair ordering) lives in one fixed region of
+ * POYALGN_NOALLOC_SCRATCH_BYTES of static device memory per device, which
+ * exists from the moment the library's device code is loaded on that device.
+ * Limits: npairs <= POYALGN_NOALLOC_MAX_PAIRS, max_pair_len (lena + lenb) <=
+ * POYALGN_NOALLOC_MAX_PAIR_LEN, out_bytes <= POYALGN_NOALLOC_MAX_OUT_BYTES;
+ * larger requests fail with POYALGN_EINVAL and a message naming the limit.
+ * Fewer CTAs may run than in poyalgn_median_batch_device (the direction
+ * slabs share the fixed region); results are identical.
+ *
+ * The first call on a device does one-time setup (looks up the region's
+ * address, queries the SM count and kernel occupancy); make one call per
+ * device before capturing a stream that uses this function. Each call
+ * clears the queue counters at the start of the region on `stream` before
+ * its first kernel; nothing else needs to start at zero, and the caller's
+ * output buffers need no clearing.
+ *
+ * The region is shared by every call on the same device: two calls whose
+ * work overlaps in time (different streams, or several host threads) race
+ * on it and give wrong results. Serialise calls per device, e.g. by issuing
+ * them all on one stream.
+ */
+#define POYALGN_NOALLOC_SCRATCH_BYTES (64u << 20)
+#define POYALGN_NOALLOC_MAX_PAIRS 16384
+#define POYALGN_NOALLOC_MAX_PAIR_LEN 4096
+#define POYALGN_NOALLOC_MAX_OUT_BYTES (4 << 20)
+
+int poyalgn_median_batch_device_noalloc(const poyalgn_cm *cm, int npairs,
+                                        int max_pair_len, int64_t out_bytes,
+                                        const uint8_t *seqs, const int64_t *offa,
+                                        const int32_t *lena, const int64_t *offb,
+                                        const int32_t *lenb, const int64_t *out_off,
+                                        int32_t *cost, int32_t *maxcost,
+                                        int32_t *alen, int32_t *mlen, int32_t *wlen,
+                                        int32_t *status, uint8_t *ea, uint8_t *eb,
+                                        uint8_t *med, uint8_t *mwg, int32_t *passes,
+                                        void *stream);
+
 /* Number of kernel launches the last batch enqueued (for accounting). */
 int poyalgn_last_launches(const poyalgn_ctx *ctx);
 

@@ -48,6 +48,7 @@ _SIGS = {
     "poyalgn_aligned_medians": (_I, [_P, _P, _P, _P, _I, _P, _I, _P, _P, _P]),
     "poyalgn_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
     "poyalgn_median_batch_device": (_I, [_P, _P, _I, _I, _I64] + [_P] * 18),
+    "poyalgn_median_batch_device_noalloc": (_I, [_P, _I, _I, _I64] + [_P] * 18),
     "poyalgn_last_launches": (_I, [_P]),
     "poyalgn_profile_begin": (_I, [_P, _I]),
     "poyalgn_profile_end": (_I, [_P, _P, _P]),

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -671,3 +672,187 @@ int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
 int poyalgn_num_classes(void) { return NCLASS; }
 
 }  // extern "C"
+
+// ---- poyalgn_median_batch_device_noalloc ----------------------------------
+//
+// The same launch sequence as run_batch (ordering, prep, one persistent
+// launch per class and variant), with every scratch buffer carved out of one
+// static device array instead of cudaMalloc'd context buffers.
+
+namespace {
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[POYALGN_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoAllocDevices = 64;
+
+struct NoAllocDevice {
+    bool ready = false;
+    unsigned char* base = nullptr;
+    int nsm = 0;
+    int bps[2][NCLASS][2] = {};
+};
+
+NoAllocDevice g_noalloc[kNoAllocDevices];
+std::mutex g_noalloc_mu;
+
+// One-time setup for `dev` (the current device): the region's address, the
+// SM count and the per-class occupancy that sizes the persistent grids.
+int noalloc_device(int dev, const NoAllocDevice** out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice& d = g_noalloc[dev];
+    if (!d.ready) {
+        void* p = nullptr;
+        CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        CU(cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, dev));
+        for (int a = 0; a < 2; a++)
+            for (int k = 0; k < NCLASS; k++)
+                for (int v = 0; v < 2; v++) d.bps[a][k][v] = class_blocks_per_sm(a, k, v);
+        CU(cudaGetLastError());
+        d.base = static_cast<unsigned char*>(p);
+        d.ready = true;
+    }
+    *out = &d;
+    return 0;
+}
+
+// Bump carving of the region in 256-byte aligned pieces.
+struct Carve {
+    unsigned char* base;
+    size_t used, cap;
+    void* take(size_t bytes)
+    {
+        const size_t a = (std::max<size_t>(bytes, 1) + 255) & ~(size_t)255;
+        if (used + a > cap) return nullptr;
+        void* r = base + used;
+        used += a;
+        return r;
+    }
+};
+
+}  // namespace
+
+extern "C" int poyalgn_median_batch_device_noalloc(
+    const poyalgn_cm* cm, int npairs, int max_pair_len, int64_t out_bytes, const uint8_t* seqs,
+    const int64_t* offa, const int32_t* lena, const int64_t* offb, const int32_t* lenb,
+    const int64_t* out_off, int32_t* cost, int32_t* maxcost, int32_t* alen, int32_t* mlen,
+    int32_t* wlen, int32_t* status, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
+    int32_t* passes, void* stream)
+{
+    if (!cm || (npairs > 0 && (!seqs || !offa || !lena || !offb || !lenb || !out_off || !cost ||
+                               !maxcost || !alen || !mlen || !wlen || !status || !ea || !eb ||
+                               !med || !mwg)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (npairs < 0 || max_pair_len < 2 || out_bytes < 1) return set_err(POYALGN_EINVAL, "bad batch shape");
+    if (npairs > POYALGN_NOALLOC_MAX_PAIRS)
+        return set_err(POYALGN_EINVAL, "npairs %d exceeds POYALGN_NOALLOC_MAX_PAIRS (%d)", npairs,
+                       POYALGN_NOALLOC_MAX_PAIRS);
+    if (max_pair_len > POYALGN_NOALLOC_MAX_PAIR_LEN)
+        return set_err(POYALGN_EINVAL, "max_pair_len %d exceeds POYALGN_NOALLOC_MAX_PAIR_LEN (%d)",
+                       max_pair_len, POYALGN_NOALLOC_MAX_PAIR_LEN);
+    if (out_bytes > POYALGN_NOALLOC_MAX_OUT_BYTES)
+        return set_err(POYALGN_EINVAL, "out_bytes %lld exceeds POYALGN_NOALLOC_MAX_OUT_BYTES (%d)",
+                       (long long)out_bytes, POYALGN_NOALLOC_MAX_OUT_BYTES);
+    if (npairs == 0) return 0;
+
+    int dev = -1;
+    CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocDevices)
+        return set_err(POYALGN_EUNSUPPORTED, "device ordinal %d beyond %d", dev, kNoAllocDevices - 1);
+    cudaPointerAttributes pa;
+    CU(cudaPointerGetAttributes(&pa, cm->d));
+    if (pa.device != dev)
+        return set_err(POYALGN_EINVAL, "cost matrix lives on device %d, current device is %d",
+                       pa.device, dev);
+    const NoAllocDevice* d = nullptr;
+    int rc;
+    if ((rc = noalloc_device(dev, &d))) return rc;
+
+    const int affine = cm->h.cost_model == 1;
+    const size_t ni = (size_t)npairs;
+    Carve cv{d->base, 0, (size_t)POYALGN_NOALLOC_SCRATCH_BYTES};
+    int* qctr = static_cast<int*>(cv.take(2 * NQUEUE * sizeof(int)));
+    int* pfull = static_cast<int*>(cv.take(ni * 4));
+    int* eh0 = static_cast<int*>(cv.take(ni * 4));
+    int* lastcls = static_cast<int*>(cv.take(ni * 4));
+    int* slabcta = static_cast<int*>(cv.take(ni * 4));
+    int* pass_buf = static_cast<int*>(cv.take(ni * 4));
+    int* order = static_cast<int*>(cv.take(ni * 4));
+    void* order_scratch = cv.take(order_scratch_bytes(npairs));
+    int2* qitems = static_cast<int2*>(cv.take((size_t)NQUEUE * ni * sizeof(int2)));
+    int* shadow = static_cast<int*>(cv.take((size_t)(affine ? out_bytes : 1) * 4));
+    if (!qctr || !pfull || !eh0 || !lastcls || !slabcta || !pass_buf || !order ||
+        !order_scratch || !qitems || !shadow)
+        return set_err(POYALGN_EINVAL, "batch state does not fit POYALGN_NOALLOC_SCRATCH_BYTES");
+    // the direction slabs take what is left, at least one CTA per class
+    const long long budget = (long long)(cv.cap - cv.used);
+    int grid[NCLASS][2];
+    long long strides[NCLASS];
+    long long arena = 0;
+    for (int k = 0; k < NCLASS; k++) {
+        const int pipes = class_pipes_per_cta(affine, k);
+        strides[k] = class_slab_bytes(affine, k, max_pair_len);
+        if (strides[k] * pipes > budget)
+            return set_err(POYALGN_EINVAL,
+                           "max_pair_len %d leaves no room for class %d in POYALGN_NOALLOC_SCRATCH_BYTES",
+                           max_pair_len, k);
+        for (int v = 0; v < 2; v++) {
+            long long g = (long long)d->nsm * std::max(1, d->bps[affine][k][v]);
+            g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
+            g = std::min<long long>(g, budget / (strides[k] * pipes));
+            grid[k][v] = (int)std::max<long long>(1, g);
+            arena = std::max(arena, (long long)grid[k][v] * pipes * strides[k]);
+        }
+    }
+    uint8_t* slab = static_cast<uint8_t*>(cv.take((size_t)arena));
+    if (!slab) return set_err(POYALGN_EINVAL, "direction slabs do not fit POYALGN_NOALLOC_SCRATCH_BYTES");
+
+    cudaStream_t st = (cudaStream_t)stream;
+    CU(cudaMemsetAsync(qctr, 0, 2 * NQUEUE * sizeof(int), st));
+
+    BatchArgs A;
+    memset(&A, 0, sizeof(A));
+    A.seqs = seqs;
+    A.offa = reinterpret_cast<const long long*>(offa);
+    A.lena = lena;
+    A.offb = reinterpret_cast<const long long*>(offb);
+    A.lenb = lenb;
+    A.npairs = npairs;
+    A.affine = affine;
+    A.do_traceback = 1;
+    A.tables = cm->d;
+    A.pfull = pfull;
+    A.shadow = shadow;
+    A.shadowEH0 = eh0;
+    A.qitems = qitems;
+    A.qcount = qctr;
+    A.qhead = qctr + NQUEUE;
+    A.qcap = npairs;
+    A.slab = slab;
+    A.out_off = reinterpret_cast<const long long*>(out_off);
+    A.cost = cost;
+    A.maxcost = maxcost;
+    A.alen = alen;
+    A.mlen = mlen;
+    A.wlen = wlen;
+    A.status = status;
+    A.passes = passes ? passes : pass_buf;
+    A.lastcls = lastcls;
+    A.slab_cta = slabcta;
+    A.deltawh_override = nullptr;
+    A.swap_override = nullptr;
+    A.ea = ea;
+    A.eb = eb;
+    A.med = med;
+    A.mwg = mwg;
+    if (launch_order(lena, lenb, npairs, order, order_scratch, st) != 0)
+        return set_err(POYALGN_ECUDA, "ordering pairs failed");
+    A.order = order;
+    launch_prep(A, st);
+    for (int k = 0; k < NCLASS; k++) {
+        A.slab_stride = strides[k];
+        for (int v = 0; v < (affine ? 2 : 1); v++) launch_class(A, k, v, grid[k][v], st);
+    }
+    CU(cudaGetLastError());
+    return 0;
+}
