@@ -50,6 +50,10 @@ def parse_args(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the host baseline sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the downpass and serving measurements")
+    ap.add_argument("--serve-seconds", type=float, default=1.0,
+                    help="arrival window of each serving rate")
     return ap.parse_args(argv)
 
 
@@ -305,6 +309,96 @@ def plain_per_call(ctx, cm, w, seconds: float = 3.0) -> dict:
     return {"gcups": cells / dt / 1e9, "alignments_per_s": n / dt, "pairs": n}
 
 
+def run_downpass(local: int, reps: int = 5) -> dict:
+    """Downpass of the 256-taxon Yule tree over device-resident leaves, one
+    batch per tree level; its CPU counterpart is the host implementation run
+    level by level on all host cores."""
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    t = wl.yule_tree()
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, t.subs, t.indel, t.gap_open)
+    store = pg.Store(ctx, 64 << 20)
+    leaves = [store.add(s) for s in t.leaves]
+    n0 = len(store)
+    for _ in range(2):
+        pg.downpass(store, cm, leaves, t.left, t.right)
+        store.truncate(n0)
+    t0 = time.perf_counter()
+    for k in range(reps):
+        res = pg.downpass(store, cm, leaves, t.left, t.right)
+        if k < reps - 1:
+            store.truncate(n0)
+    dt = (time.perf_counter() - t0) / reps
+    nl = len(t.leaves)
+    length = lambda ch: (len(t.leaves[ch]) if ch < nl else
+                         len(store.read(int(res.internal_node[ch - nl]))))
+    cells = sum(length(a) * length(b) for a, b in zip(t.left, t.right))
+    # host implementation, level by level (nodes of a level run in parallel)
+    host_oracle()  # puts the oracle's loader on the path
+    import oracle_lib
+    orc, kind = oracle_lib.Oracle("port"), "port"
+    ocm = orc.cm(subs=t.subs, indel=t.indel)
+    levels = pg.tree_levels(nl, t.left, t.right)
+    seqs = list(t.leaves) + [None] * len(t.left)
+    tot = 0
+    c0 = time.perf_counter()
+    for lv in range(1, int(levels.max()) + 1):
+        ks = np.flatnonzero(levels == lv)
+        out = orc.median_batch(ocm, [seqs[t.left[k]] for k in ks], [seqs[t.right[k]] for k in ks],
+                               False)
+        for j, k in enumerate(ks):
+            o = int(out["out_off"][j])
+            seqs[nl + k] = out["med"][o:o + out["mlen"][j]]
+        tot += int(out["cost"].sum())
+    cpu_s = time.perf_counter() - c0
+    store.close()
+    return {"workload": t.name, "internal_nodes": len(t.left), "levels": res.levels,
+            "ms": round(dt * 1e3, 3), "total_cost": res.total_cost,
+            "gcups": round(cells / dt / 1e9, 3), "medians_per_s": round(len(t.left) / dt, 1),
+            "cpu_baseline": {"ms": round(cpu_s * 1e3, 1), "kind": kind,
+                             "cores": os.cpu_count() or 1, "total_cost": tot},
+            "total_cost_matches_cpu": tot == res.total_cost}
+
+
+def run_serving(local: int, seconds: float = 1.0) -> dict:
+    """Open-loop Poisson replay against the continuous-batching server: each
+    request has U{1..64} pairs of a resident pool (lognormal lengths, median
+    1,000, clipped 100-5,000, ~30% divergence), affine 3/1/1."""
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    w = wl.serving_pairs(n_pairs=4096)
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    store = pg.Store(ctx, 64 << 20)
+    na = np.array([store.add(a) for a, _ in w.pairs], np.int32)
+    nb = np.array([store.add(b) for _, b in w.pairs], np.int32)
+    pair_cells = np.array([len(a) * len(b) for a, b in w.pairs], np.int64)
+    cfg = dict(nslots=3, max_batch_pairs=2048, max_waiting_pairs=16384)
+    srv = pg.Server(store, cm, hbm_budget=24 << 30, **cfg)
+    rng = np.random.default_rng(wl.SEED_BASE + 4)
+    srv.replay(pg.poisson_trace(rng, 2000.0, 200, na, nb))  # warm-up
+    points = []
+    for rate in (1000, 5000, 20000, 50000, 100000, 200000):
+        nreq = int(min(rate * seconds, 40000))
+        tr = pg.poisson_trace(rng, float(rate), nreq, na, nb)
+        res = srv.replay(tr)
+        ok = res.served()
+        lat = res.latency_s[ok] * 1e3
+        pair_ok = np.repeat(ok, tr.npairs)
+        cells = int(pair_cells[tr.node_a[pair_ok]].sum())
+        points.append({"rate_req_s": rate, "requests": nreq, "refused": int((~ok).sum()),
+                       "p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
+                       "p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
+                       "alignments_per_s": round(int(pair_ok.sum()) / res.wall_s, 1),
+                       "gcups": round(cells / res.wall_s / 1e9, 3)})
+    st = srv.stats()
+    srv.close()
+    store.close()
+    return {"workload": "serving_requests_poisson_1-64pairs_lognormal1000", **cfg,
+            "batches": st["batches"], "points": points}
+
+
 def _reduce(x: float, world: int, op: str) -> float:
     """All-reduce one scalar across ranks (NCCL on GPUs, gloo on CPU)."""
     if world <= 1:
@@ -435,6 +529,9 @@ def main(argv=None):
             "cores": cpu["threads"], "kind": cpu["kind"],
             "sample": f"first {cpu['pairs']} pairs of {r['w'].name} ({cpu['seconds']:.1f} s)",
             "alignments_per_s": round(cpu["pairs_per_s"], 2)}
+        if world == 1 and not args.no_extras:
+            line["downpass"] = run_downpass(local)
+            line["serving"] = run_serving(local, args.serve_seconds)
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -223,6 +223,130 @@ int poyalgn_median_batch_device_noalloc(const poyalgn_cm *cm, int npairs,
                                         uint8_t *med, uint8_t *mwg, int32_t *passes,
                                         void *stream);
 
+/* ---- device-resident sequences and the tree downpass ------------------------ */
+
+/*
+ * A store keeps node sequences (leaves and computed medians) in one device
+ * arena of fixed capacity, so that a downpass or a stream of scoring
+ * requests aligns them without copying sequences across the host boundary
+ * again. Node ids are dense, in order of addition. No counterpart in the
+ * reference, where each OCaml node holds its own `struct seq`; the batches
+ * compute exactly SeqCS.DOS.median (src/seqCS.ml:985-1084) per pair.
+ *
+ * A store belongs to one context and uses its stream; calls on one store
+ * must not run concurrently.
+ */
+typedef struct poyalgn_store poyalgn_store;
+
+int poyalgn_store_create(poyalgn_ctx *ctx, int64_t capacity_bytes,
+                         poyalgn_store **out);
+void poyalgn_store_free(poyalgn_store *s);
+
+/* Copy one sequence (leading gap included, len >= 1) to the device. */
+int poyalgn_store_add(poyalgn_store *s, const uint8_t *seq, int len,
+                      int32_t *node);
+int poyalgn_store_count(const poyalgn_store *s);
+int poyalgn_store_length(const poyalgn_store *s, int node);
+/* Copy node's sequence to host memory (cap >= its length). */
+int poyalgn_store_read(poyalgn_store *s, int node, uint8_t *out, int cap);
+/* Forget every node >= nodes and the arena space after the last kept one. */
+int poyalgn_store_truncate(poyalgn_store *s, int nodes);
+
+/*
+ * DOS.median of the resident pairs (node_a[k], node_b[k]) under `cm`. With
+ * keep != 0 each median becomes a new node (median_node[k]); otherwise the
+ * medians are discarded (cost-only use). cost, maxcost and status are per
+ * pair (maxcost and median_node may be NULL). Returns POYALGN_EPAIR if any
+ * pair failed (its status says why); other pairs' results are valid.
+ */
+int poyalgn_store_median_batch(poyalgn_store *s, const poyalgn_cm *cm,
+                               int npairs, const int32_t *node_a,
+                               const int32_t *node_b, int keep,
+                               int32_t *median_node, int32_t *cost,
+                               int32_t *maxcost, int32_t *status);
+
+/*
+ * Downpass of a rooted binary tree over resident leaves, one batched launch
+ * sequence per tree level (AllDirChar.internal_downpass,
+ * src/allDirChar.ml:1366, with Node.median reducing to DOS.median for one
+ * dynamic character). Internal node k (0 <= k < ninternal) has children
+ * left[k] and right[k], encoded as leaf index (< nleaves, stored as node
+ * leaf_node[index]) or nleaves + internal index; children come before their
+ * parent. Writes each internal node's store id and median cost, and the
+ * total tree cost (the sum).
+ */
+int poyalgn_downpass(poyalgn_store *s, const poyalgn_cm *cm, int nleaves,
+                     const int32_t *leaf_node, int ninternal,
+                     const int32_t *left, const int32_t *right,
+                     int32_t *internal_node, int32_t *internal_cost,
+                     int64_t *total_cost, int32_t *levels);
+
+/* ---- serving: continuous batching of scoring requests ------------------------ */
+
+/*
+ * A server takes requests of DOS.median pairs over resident store nodes (the
+ * SPR/TBR join and downpass scoring that POY issues one call at a time) and
+ * batches them continuously. No counterpart in the reference.
+ *
+ * A scheduler thread keeps nslots batches in flight, each on its own CUDA
+ * stream with its own preallocated buffers, so the work of requests that
+ * arrive while others run overlaps on the device. Whenever a slot frees it
+ * forms the next batch from the oldest waiting requests, up to
+ * max_batch_pairs pairs and the slot's share of the device-memory budget.
+ * Memory is reserved once, at creation: hbm_budget bytes (0: half of the free
+ * device memory) split across the slots. A request whose pairs cannot fit
+ * one slot is refused at submission (POYALGN_EINVAL), and a submission that
+ * would make more than max_waiting_pairs pairs wait is refused with
+ * POYALGN_EBUSY (admission control; nothing is queued).
+ *
+ * Nodes are those the store holds when the server is created (later
+ * additions are not visible to it); the store must outlive the server, and
+ * its arena must not be truncated below them meanwhile. Results are
+ * identical to poyalgn_store_median_batch for the same pairs, whatever the
+ * batch a request lands in.
+ */
+#define POYALGN_EBUSY -6 /* server admission refused: too many waiting pairs */
+
+typedef struct poyalgn_server poyalgn_server;
+
+int poyalgn_server_create(poyalgn_store *store, const poyalgn_cm *cm,
+                          int nslots, int max_batch_pairs,
+                          int max_waiting_pairs, int64_t hbm_budget,
+                          poyalgn_server **out);
+void poyalgn_server_free(poyalgn_server *s);
+
+/* Queue a request of npairs pairs (node ids); non-blocking. */
+int poyalgn_server_submit(poyalgn_server *s, int npairs, const int32_t *node_a,
+                          const int32_t *node_b, int64_t *ticket);
+
+/*
+ * Wait up to timeout_ms (< 0: no limit; POYALGN_EBUSY on timeout) for a
+ * ticket, then release it. Per pair: cost, status and the median's length;
+ * the medians themselves are concatenated into medians (NULL to skip;
+ * POYALGN_EINVAL if med_cap is too small). latency_s: submission to
+ * completion of the batch that carried the request.
+ */
+int poyalgn_server_wait(poyalgn_server *s, int64_t ticket, int timeout_ms,
+                        int32_t *cost, int32_t *status, int32_t *med_len,
+                        uint8_t *medians, int64_t med_cap, double *latency_s);
+
+/*
+ * Open-loop replay of a request trace (a load generator): request r is
+ * submitted at arrival_s[r] seconds after the call starts (arrival_s
+ * ascending) with the next req_npairs[r] pairs of node_a/node_b. Per pair it
+ * writes cost and status (status 1: request refused by admission control);
+ * per request the latency from its scheduled arrival to completion
+ * (latency_s, -1 if refused). wall_s: first arrival to last completion.
+ */
+int poyalgn_server_replay(poyalgn_server *s, int nreq, const double *arrival_s,
+                          const int32_t *req_npairs, const int32_t *node_a,
+                          const int32_t *node_b, int32_t *cost,
+                          int32_t *status, double *latency_s, double *wall_s);
+
+/* Counters since creation: batches launched, pairs completed, requests refused. */
+int poyalgn_server_stats(const poyalgn_server *s, int64_t *batches,
+                         int64_t *pairs, int64_t *refused);
+
 /* Number of kernel launches the last batch enqueued (for accounting). */
 int poyalgn_last_launches(const poyalgn_ctx *ctx);
 

@@ -19,7 +19,7 @@ _I = C.c_int
 _I64 = C.c_int64
 
 # POYALGN_* return codes
-EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, EPAIR = -1, -2, -3, -4, -5
+EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, EPAIR, EBUSY = -1, -2, -3, -4, -5, -6
 PAIR_STATUS = {0: "ok", -2: "output capacity exceeded", -3: "median should not be 0",
                -4: "empty sequence or empty median", -5: "band wider than the largest pipeline",
                -6: "sequence longer than 65535", -7: "state outside the alphabet",
@@ -49,6 +49,21 @@ _SIGS = {
     "poyalgn_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
     "poyalgn_median_batch_device": (_I, [_P, _P, _I, _I, _I64] + [_P] * 18),
     "poyalgn_median_batch_device_noalloc": (_I, [_P, _I, _I, _I64] + [_P] * 18),
+    "poyalgn_store_create": (_I, [_P, _I64, C.POINTER(_P)]),
+    "poyalgn_store_free": (None, [_P]),
+    "poyalgn_store_add": (_I, [_P, _P, _I, _P]),
+    "poyalgn_store_count": (_I, [_P]),
+    "poyalgn_store_length": (_I, [_P, _I]),
+    "poyalgn_store_read": (_I, [_P, _I, _P, _I]),
+    "poyalgn_store_truncate": (_I, [_P, _I]),
+    "poyalgn_store_median_batch": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P]),
+    "poyalgn_downpass": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
+    "poyalgn_server_create": (_I, [_P, _P, _I, _I, _I, _I64, C.POINTER(_P)]),
+    "poyalgn_server_free": (None, [_P]),
+    "poyalgn_server_submit": (_I, [_P, _I, _P, _P, _P]),
+    "poyalgn_server_wait": (_I, [_P, _I64, _I, _P, _P, _P, _P, _I64, _P]),
+    "poyalgn_server_replay": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "poyalgn_server_stats": (_I, [_P, _P, _P, _P]),
     "poyalgn_last_launches": (_I, [_P]),
     "poyalgn_profile_begin": (_I, [_P, _I]),
     "poyalgn_profile_end": (_I, [_P, _P, _P]),

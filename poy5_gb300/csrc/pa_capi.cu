@@ -11,15 +11,17 @@
 #include <new>
 #include <vector>
 
-#include "../../include/poyalgn.h"
-#include "pa_kernels.h"
-#include "pa_tables.h"
+#include "pa_runtime.h"
 
 using namespace pa;
 
 namespace {
 
 thread_local char g_err[512];
+
+}  // namespace
+
+namespace pa {
 
 int set_err(int code, const char* fmt, ...)
 {
@@ -29,19 +31,6 @@ int set_err(int code, const char* fmt, ...)
     va_end(ap);
     return code;
 }
-
-#define CU(call)                                                                        \
-    do {                                                                                \
-        cudaError_t e_ = (call);                                                        \
-        if (e_ != cudaSuccess)                                                          \
-            return set_err(POYALGN_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                           __FILE__, __LINE__);                                         \
-    } while (0)
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t n = 0;
-};
 
 int reserve(DevBuf& b, size_t bytes)
 {
@@ -58,41 +47,12 @@ int reserve(DevBuf& b, size_t bytes)
     return 0;
 }
 
-template <class T>
-T* as(DevBuf& b) { return reinterpret_cast<T*>(b.p); }
-
-}  // namespace
-
-struct poyalgn_cm {
-    HostCM h;
-    Tables t;
-    Tables* d = nullptr;
-};
-
-struct poyalgn_ctx {
-    int device = 0;
-    int nsm = 0;
-    cudaStream_t stream = nullptr;
-    int bps[2][NCLASS][2] = {};
-    // host-pointer batches: staging of inputs and outputs
-    DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
-    // per-batch scratch
-    DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
-    DevBuf dwh, swp, order, order_scratch;
-    int last_launches = 0;
-    // optional per-launch timing: one event before the prep launch and one
-    // after each launch of a batch, for up to prof_cap batches
-    std::vector<cudaEvent_t> prof_ev;
-    int prof_cap = 0, prof_used = 0;
-    // per-call stub state: the fill of the last simple_2 / align_affine_3
-    bool call_valid = false;
-    int call_affine = 0, call_l1 = 0, call_l2 = 0;
-    const poyalgn_cm* call_cm = nullptr;
-    std::vector<uint8_t> call_s1, call_s2;
-    long long call_strides[NCLASS] = {0};
-};
-
-namespace {
+void release(DevBuf& b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+}
 
 int ensure_device(poyalgn_ctx* c)
 {
@@ -128,7 +88,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     // persistent grid per class, bounded by a slab budget
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
-    const long long budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
+    long long budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
+    if (c->slab_budget > 0) budget = std::min(budget, c->slab_budget);
     int grid[NCLASS][2];
     long long strides[NCLASS];
     long long arena = 0;
@@ -213,6 +174,27 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     c->last_launches = launches;
     return 0;
 }
+
+int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
+               long long slab_bytes)
+{
+    int rc;
+    const size_t n = (size_t)std::max(max_pairs, 1);
+    DevBuf* per_pair[] = {&c->pfull, &c->eh0, &c->lastcls, &c->slabcta, &c->passes, &c->order};
+    for (DevBuf* b : per_pair)
+        if ((rc = reserve(*b, n * 4))) return rc;
+    if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
+    if ((rc = reserve(c->qitems, (size_t)NQUEUE * n * sizeof(int2)))) return rc;
+    if ((rc = reserve(c->qctr, 2 * NQUEUE * sizeof(int)))) return rc;
+    if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
+    if ((rc = reserve(c->order_scratch, order_scratch_bytes((int)n)))) return rc;
+    if ((rc = reserve(c->slab, (size_t)slab_bytes))) return rc;
+    return 0;
+}
+
+}  // namespace pa
+
+namespace {
 
 int upload_cm(poyalgn_cm* m)
 {

@@ -26,8 +26,10 @@
 
 #if defined(__CUDACC__)
 #define PA_HD __host__ __device__ __forceinline__
+#define PA_HDM __host__ __device__ __forceinline__
 #else
 #define PA_HD static inline
+#define PA_HDM inline
 #endif
 
 namespace pa {
@@ -752,23 +754,65 @@ PA_HD void aff_fast_step(AffFastLane<R>& L, const AffBand& b, const Tables& t,
 
 // ---------------------------------------------------------------------------
 // Affine fast path, register-lean form (gap-free pairs whose costs stay far
-// below HIGH). Identical results to aff_step:
+// below HIGH, see aff_lean_ok). Identical results to aff_step:
 //  * every "keep the smaller, OR the flag on ties" chain of ASSIGN_MINIMUM
 //    and FILL_CLOSE_BLOCK_DIAGONAL leaves exactly the flags of the candidates
 //    equal to the final minimum, so the flags are equality tests against it;
-//  * row 0's stale EB (left by earlier doubling iterations) only meets
-//    CB0 + HIGH and CB + cost + go comparisons that it can never win or tie
-//    when every EB is >= HIGH > CB0, so HIGH stands in for it and nothing
-//    has to be written back;
+//  * with no gap states the block-diagonal state only ever takes
+//    min(EB, CB) + HIGH of its diagonal neighbour, so EB >= HIGH, while every
+//    in-band cell (and row 0 and column 0) has EH, EV or CB below HIGH / 4:
+//    EB never attains a minimum, DO_D and A2D are never set, and the
+//    traceback never enters the block-diagonal mode. The lean cell drops EB
+//    and stores only the direction bits the traceback then reads, one byte
+//    per cell (LEAN_*);
 //  * cell states ping-pong between two register sets (V0/V1, R0/R1, G0/G1)
 //    and the caller alternates their roles on even and odd steps, so no
 //    state is copied between steps.
 
+struct LeanCell {
+    int EH, EV, CB;
+    uint32_t GM;  // gap numbers: gm1 | gm2 << 16
+};
+
+// direction byte of the lean path
+enum : int {
+    LEAN_A2V = 1, LEAN_A2H = 2, LEAN_END_V = 4, LEAN_END_H = 8,
+    LEAN_DO_V = 16, LEAN_DO_H = 32, LEAN_H_EQ_V = 64
+};
+
+// the flags of a lean direction byte in the aff_step encoding
+PA_HD int lean_flags(int b)
+{
+    return ((b & LEAN_A2V) ? A2V : 0) | ((b & LEAN_A2H) ? A2H : 0) |
+           ((b & LEAN_END_V) ? END_V : 0) | ((b & LEAN_END_H) ? END_H : 0) |
+           ((b & LEAN_DO_V) ? DO_V : 0) | ((b & LEAN_DO_H) ? DO_H : 0) |
+           ((b & LEAN_H_EQ_V) ? H_EQ_V : 0);
+}
+
+// min(a, b) and *le = (a <= b); min of three (DPX instructions on sm_90+)
+PA_HD int bmin_le(int a, int b, bool* le)
+{
+#if defined(__CUDA_ARCH__)
+    return __vibmin_s32(a, b, le);
+#else
+    *le = a <= b;
+    return a <= b ? a : b;
+#endif
+}
+PA_HD int min3(int a, int b, int c)
+{
+#if defined(__CUDA_ARCH__)
+    return __vimin3_s32(a, b, c);
+#else
+    return tmin(tmin(a, b), c);
+#endif
+}
+
 template <int R>
 struct AffLean {
-    AffCell V0[R], V1[R];   // row states of two consecutive steps
-    AffCell R0, R1;         // neighbour's bottom row, two consecutive steps
-    AffCell G0, G1;         // row 0 (lane 0 of the first block)
+    LeanCell V0[R], V1[R];  // row states of two consecutive steps
+    LeanCell R0, R1;        // neighbour's bottom row, two consecutive steps
+    LeanCell G0, G1;        // row 0 (lane 0 of the first block)
     int J[R], JG[R];        // column symbol and its prepend cost, per row
     int Ts[R], Te[R], Tr[R];// first / last / right-border step of each row
     int sg[R], sgo[R];      // gap cost of the row symbol (and + go)
@@ -802,7 +846,7 @@ template <int R>
 PA_HD void aff_lean_init(AffLean<R>& L, const AffBand& b, const Tables& t,
                          const uint8_t* si, int g, int P)
 {
-    const AffCell z = {0, 0, 0, 0, 0u};
+    const LeanCell z = {0, 0, 0, 0u};
 #pragma unroll
     for (int q = 0; q < R; q++) {
         L.V0[q] = z;
@@ -815,22 +859,30 @@ PA_HD void aff_lean_init(AffLean<R>& L, const AffBand& b, const Tables& t,
     aff_lean_enter(L, b, t, si, 1 + g * R, P);
 }
 
-// The affine fast path needs every row-0 cost far below HIGH.
+// The lean path needs every in-band cell to keep a state below HIGH / 4: a
+// monotone path of at most n steps, each costing at most the largest
+// substitution, insertion or deletion cost among gap-free states plus a gap
+// opening, bounds the smallest state of every cell.
 PA_HD bool aff_lean_ok(const Tables& t, int n)
 {
-    int mp = 0;
-    for (int a = 0; a < NSTATE; a++) mp = tmax(mp, t.prepend[a]);
-    return (long long)n * (mp + t.go + 1) + t.go < HIGH / 4;
+    int mc = 0;
+    for (int a = 0; a < 16; a++) {
+        mc = tmax(mc, t.prepend[a]);
+        mc = tmax(mc, tcost(t, a, t.gap));
+        for (int c = 0; c < 16; c++) mc = tmax(mc, tcost(t, a, c));
+    }
+    if (t.go < 0 || mc < 0) return false;
+    return (long long)n * (mc + t.go + 1) + t.go < HIGH / 4;
 }
 
 // One anti-diagonal step. VC/RC/GC hold step T-1 (up, left), VP/RP/GP hold
 // step T-2 (diagonal); the step's results overwrite VP/RP/GP, which the
 // caller then passes as VC/RC/GC of the next step.
 template <int R>
-PA_HD void aff_lean_step(AffLean<R>& L, AffCell (&VC)[R], AffCell (&VP)[R],
-                         AffCell& RC, AffCell& RP, AffCell& GC, AffCell& GP,
+PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
+                         LeanCell& RC, LeanCell& RP, LeanCell& GC, LeanCell& GP,
                          const AffBand& b, const Tables& t, const uint8_t* si,
-                         const uint8_t* sj, int P, int T, const AffCell& recv,
+                         const uint8_t* sj, int P, int T, const LeanCell& recv,
                          int shadowEH0, int (&dcode)[R])
 {
     RP = recv;  // neighbour bottom row at T-1 becomes this step's "up"
@@ -841,7 +893,7 @@ PA_HD void aff_lean_step(AffLean<R>& L, AffCell (&VC)[R], AffCell (&VP)[R],
     if (gen) {  // row 0 at column T-1
         const int j0 = T - 1;
         if (j0 <= b.n - 1) {
-            AffCell c;
+            LeanCell c;
             if (j0 == 0) {
                 L.gCB = 0;
                 c.EH = shadowEH0;
@@ -852,7 +904,6 @@ PA_HD void aff_lean_step(AffLean<R>& L, AffCell (&VC)[R], AffCell (&VP)[R],
             }
             c.CB = L.gCB;
             c.EV = HIGH;
-            c.EB = HIGH;
             c.GM = (uint32_t)j0;
             GP = c;
         }
@@ -880,57 +931,49 @@ PA_HD void aff_lean_step(AffLean<R>& L, AffCell (&VC)[R], AffCell (&VP)[R],
     // values (already in RP / GP); the diagonals are last step's (RC / GC)
 #pragma unroll
     for (int q = R - 1; q >= 0; q--) {
-        const AffCell up = q > 0 ? VC[q - 1] : (gen ? GP : RP);
-        const AffCell dg = q > 0 ? VP[q - 1] : (gen ? GC : RC);
-        const AffCell& lf = VC[q];
+        const LeanCell up = q > 0 ? VC[q - 1] : (gen ? GP : RP);
+        const LeanCell dg = q > 0 ? VP[q - 1] : (gen ? GC : RC);
+        const LeanCell& lf = VC[q];
         dcode[q] = 0;
         if (T >= L.Ts[q] && T <= L.Te[q]) {
             const int j = T - (L.itop + q);
             const int jgr = L.JG[q];
-            AffCell c;
-            int dir;
-            {
-                const int ext = lf.EH + jgr, open = lf.CB + go + jgr;
-                const bool left = (T == L.Ts[q]);
-                c.EH = left ? HIGH : tmin(ext, open);
-                dir = left ? 0 : (ext < open ? BEG_H : END_H);
-            }
-            {
-                const int ext = up.EV + L.sg[q], open = up.CB + L.sgo[q];
-                const bool right = (T == L.Tr[q]);
-                c.EV = right ? HIGH : tmin(ext, open);
-                dir |= right ? 0 : (ext < open ? BEG_V : END_V);
-            }
+            LeanCell c;
+            bool endh, endv;
+            // EH: extend (left EH) vs open (left CB); END_H when open <= extend
+            const int eh = bmin_le(lf.CB + go + jgr, lf.EH + jgr, &endh);
+            const bool left = (T == L.Ts[q]);
+            c.EH = left ? HIGH : eh;
+            int code = (!left && endh) ? LEAN_END_H : 0;
+            const int ev = bmin_le(up.CB + L.sgo[q], up.EV + L.sg[q], &endv);
+            const bool right = (T == L.Tr[q]);
+            c.EV = right ? HIGH : ev;
+            code |= (!right && endv) ? LEAN_END_V : 0;
             if (j > 0) {
-                const int ext = dg.EB + HIGH, open = dg.CB + HIGH;
-                c.EB = tmin(ext, open);
-                dir |= ext < open ? BEG_B : END_B;
-                const int dgc = t.csw[L.srb[q] + L.J[q]];
-                const int a0 = dg.CB + dgc, a1 = dg.EV + dgc, a2 = dg.EH + dgc;
-                const int a3 = dg.EB + dgc + go;
-                const int v = tmin(tmin(a0, a1), tmin(a2, a3));
-                c.CB = v;
-                dir |= (a0 == v ? A2A : 0) | (a1 == v ? A2V : 0) | (a2 == v ? A2H : 0) |
-                       (a3 == v ? A2D : 0);
+                const int m3 = min3(dg.CB, dg.EV, dg.EH);
+                c.CB = m3 + t.csw[L.srb[q] + L.J[q]];
+                code |= (dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0);
             } else {
                 c.CB = HIGH;
-                c.EB = HIGH;
             }
-            const int f = tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB));
+            const int f = min3(c.EH, c.EV, c.CB);
             const bool hh = c.EH == f, vv = c.EV == f;
-            dir |= (hh ? DO_H : 0) | (vv ? DO_V : 0) | (c.EB == f ? DO_D : 0) |
-                   (c.CB == f ? DO_A : 0) | ((hh && vv) ? H_EQ_V : 0);
-            uint32_t gm = (dir & (DO_A | DO_D)) ? dg.GM : 0u;
+            code |= (hh ? LEAN_DO_H : 0) | (vv ? LEAN_DO_V : 0) | ((hh && vv) ? LEAN_H_EQ_V : 0);
+            uint32_t gm = (c.CB == f) ? dg.GM : 0u;
             if (hh) gm = vmax2(gm, lf.GM + 1u);
             if (vv) gm = vmax2(gm, up.GM + 0x10000u);
             c.GM = gm;
             VP[q] = c;
-            dcode[q] = dir;
+            dcode[q] = code;
         } else {
             VP[q] = VC[q];  // keep the row's last state (read as diag/left)
         }
     }
 }
+
+// Final cost and gap count of the lean corner cell.
+PA_HD int lean_final(const LeanCell& c) { return min3(c.EH, c.EV, c.CB); }
+PA_HD int lean_gapnum(const LeanCell& c) { return tmax((int)(c.GM & 0xFFFF), (int)(c.GM >> 16)); }
 
 // Final cost of the affine corner cell from its four states.
 PA_HD int aff_final(const AffCell& c) { return tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB)); }
@@ -1093,10 +1136,18 @@ PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
     return r;
 }
 
-PA_HD int aff_dm(const uint16_t* dm, int P, int R, int i, int j)
-{
-    return dm[dm_index(P, R, i, j)];
-}
+// Direction flags of cell (i, j) from a slab of aff_step words or of lean
+// bytes.
+struct AffDmWords {
+    const uint16_t* dm;
+    int P, R;
+    PA_HDM int operator()(int i, int j) const { return dm[dm_index(P, R, i, j)]; }
+};
+struct AffDmLean {
+    const uint8_t* dm;
+    int P, R;
+    PA_HDM int operator()(int i, int j) const { return lean_flags(dm[dm_index(P, R, i, j)]); }
+};
 
 // algn_calculate_from_2_aligned on the worst table, bitset alphabet
 PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int L)
@@ -1126,9 +1177,9 @@ PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int
 
 // backtrace_aff (src/algn.c:1714-1819) in internal order (x shorter), then
 // the caller-order aligned pair and max_cost_2 on it.
-PA_HD PairRes aff_traceback(const uint16_t* dm, int P, int R, const Tables& t,
-                            const uint8_t* x, int m, const uint8_t* y, int n,
-                            int swaped, const PairOut& o)
+template <class DM>
+PA_HD PairRes aff_traceback_dm(const DM& aff_dm, const Tables& t, const uint8_t* x, int m,
+                               const uint8_t* y, int n, int swaped, const PairOut& o)
 {
     PairRes r = {0, 0, 0, 0, 0};
     uint8_t* ri = swaped ? o.eb : o.ea;  // aligned x in caller order slot
@@ -1141,7 +1192,7 @@ PA_HD PairRes aff_traceback(const uint16_t* dm, int P, int R, const Tables& t,
 #define PA_PUT(buf, k, v) do { if ((k) <= 0) { r.status = -2; return r; } (buf)[--(k)] = (uint8_t)(v); } while (0)
 #define PA_PUTR(a, b) do { if (kr <= 0) { r.status = -2; return r; } kr--; ri[kr] = (uint8_t)(a); rj[kr] = (uint8_t)(b); } while (0)
     while (i != 0 && j != 0) {
-        const int d = aff_dm(dm, P, R, i, j);
+        const int d = aff_dm(i, j);
         if (mode == 0) {
             int fv = d & DO_V, fh = d & DO_H, fd = d & DO_D;
             if (!swaped) mode = fv ? 1 : fh ? 2 : fd ? 3 : 4;
@@ -1214,6 +1265,20 @@ PA_HD PairRes aff_traceback(const uint16_t* dm, int P, int R, const Tables& t,
     }
     r.maxcost = (nga && ngb) ? worst_aligned(t, ea, eb, r.alen) : 0;
     return r;
+}
+
+PA_HD PairRes aff_traceback(const uint16_t* dm, int P, int R, const Tables& t,
+                            const uint8_t* x, int m, const uint8_t* y, int n, int swaped,
+                            const PairOut& o)
+{
+    return aff_traceback_dm(AffDmWords{dm, P, R}, t, x, m, y, n, swaped, o);
+}
+
+PA_HD PairRes aff_traceback_lean(const uint8_t* dm, int P, int R, const Tables& t,
+                                 const uint8_t* x, int m, const uint8_t* y, int n, int swaped,
+                                 const PairOut& o)
+{
+    return aff_traceback_dm(AffDmLean{dm, P, R}, t, x, m, y, n, swaped, o);
 }
 
 }  // namespace pa

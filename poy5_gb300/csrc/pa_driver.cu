@@ -1,0 +1,254 @@
+// Device-resident node sequences (poyalgn_store) and the level-batched tree
+// downpass built on them.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "pa_runtime.h"
+
+using namespace pa;
+
+namespace {
+
+constexpr long long kAlign = 16;
+
+long long align_up(long long x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+bool valid_node(const poyalgn_store* s, int node)
+{
+    return node >= 0 && node < (int)s->len.size();
+}
+
+// Enqueue DOS.median for n resident pairs and wait for the per-pair ints.
+// Medians land in the arena after `used` (keep) or in scratch.
+int store_batch(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* na,
+                const int32_t* nb, int keep, int32_t* median_node, int32_t* cost,
+                int32_t* maxcost, int32_t* status)
+{
+    poyalgn_ctx* c = s->ctx;
+    int rc;
+    if ((rc = ensure_device(c))) return rc;
+    const size_t ni = (size_t)n;
+    // metadata block: offa | offb | out_off (int64) | lena | lenb (int32)
+    s->hmeta.resize(ni * 32);
+    long long* offa = reinterpret_cast<long long*>(s->hmeta.data());
+    long long* offb = offa + ni;
+    long long* oo = offb + ni;
+    int* lena = reinterpret_cast<int*>(oo + ni);
+    int* lenb = lena + ni;
+    long long total = 0;
+    int maxmn = 2;
+    for (int k = 0; k < n; k++) {
+        if (!valid_node(s, na[k]) || !valid_node(s, nb[k]))
+            return set_err(POYALGN_EINVAL, "pair %d: unknown node (%d, %d)", k, na[k], nb[k]);
+        offa[k] = s->off[na[k]];
+        offb[k] = s->off[nb[k]];
+        lena[k] = s->len[na[k]];
+        lenb[k] = s->len[nb[k]];
+        oo[k] = total;
+        total += align_up((long long)lena[k] + lenb[k] + 2);
+        maxmn = std::max(maxmn, lena[k] + lenb[k]);
+    }
+    const long long base = align_up(s->used);
+    if (keep && base + total > s->cap)
+        return set_err(POYALGN_ENOMEM, "store full: %lld of %lld bytes used, batch needs %lld",
+                       s->used, s->cap, total);
+    if ((rc = reserve(s->meta, ni * 32))) return rc;
+    if ((rc = reserve(s->ints, ni * 4 * 7))) return rc;
+    if ((rc = reserve(s->bytes, (size_t)total * (keep ? 3 : 4)))) return rc;
+    cudaStream_t st = c->stream;
+    CU(cudaMemcpyAsync(s->meta.p, s->hmeta.data(), ni * 32, cudaMemcpyHostToDevice, st));
+    const long long* d_offa = as<long long>(s->meta);
+    const int* d_lena = reinterpret_cast<const int*>(d_offa + 3 * ni);
+    int* I = as<int>(s->ints);
+    uint8_t* B = as<uint8_t>(s->bytes);
+    uint8_t* arena = as<uint8_t>(s->arena);
+    uint8_t* med = keep ? arena + base : B + 3 * total;
+    if ((rc = run_batch(c, cm, cm->h.cost_model == 1, n, maxmn, total, arena, d_offa, d_lena,
+                        d_offa + ni, d_lena + ni, d_offa + 2 * ni, I, I + ni, I + 2 * ni,
+                        I + 3 * ni, I + 4 * ni, I + 5 * ni, B, B + total, med, B + 2 * total,
+                        I + 6 * ni, nullptr, nullptr, 1, st)))
+        return rc;
+    // cost | maxcost | alen | mlen | wlen | status
+    s->hints.resize(ni * 6);
+    CU(cudaMemcpyAsync(s->hints.data(), I, ni * 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    const int* h = s->hints.data();
+    int failed = -1;
+    for (int k = 0; k < n; k++) {
+        if (cost) cost[k] = h[k];
+        if (maxcost) maxcost[k] = h[ni + k];
+        if (status) status[k] = h[5 * ni + k];
+        if (h[5 * ni + k] != 0 && failed < 0) failed = k;
+    }
+    if (keep) {
+        for (int k = 0; k < n; k++) {
+            const int ml = h[3 * ni + k];
+            const bool ok = h[5 * ni + k] == 0 && ml > 0;
+            if (median_node) median_node[k] = ok ? (int)s->len.size() : -1;
+            if (!ok) continue;
+            s->off.push_back(base + oo[k] + lena[k] + lenb[k] + 2 - ml);
+            s->len.push_back(ml);
+        }
+        s->used = base + total;
+    }
+    if (failed >= 0)
+        return set_err(POYALGN_EPAIR, "pair %d failed with status %d", failed,
+                       h[5 * ni + failed]);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int poyalgn_store_create(poyalgn_ctx* ctx, int64_t capacity_bytes, poyalgn_store** out)
+{
+    if (!ctx || !out || capacity_bytes < 1) return set_err(POYALGN_EINVAL, "bad store arguments");
+    *out = nullptr;
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    poyalgn_store* s = new (std::nothrow) poyalgn_store;
+    if (!s) return set_err(POYALGN_ENOMEM, "store allocation");
+    s->ctx = ctx;
+    if ((rc = reserve(s->arena, (size_t)capacity_bytes))) {
+        delete s;
+        return rc;
+    }
+    s->cap = capacity_bytes;
+    *out = s;
+    return 0;
+}
+
+void poyalgn_store_free(poyalgn_store* s)
+{
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    release(s->arena);
+    release(s->meta);
+    release(s->ints);
+    release(s->bytes);
+    delete s;
+}
+
+int poyalgn_store_add(poyalgn_store* s, const uint8_t* seq, int len, int32_t* node)
+{
+    if (!s || !seq || !node || len < 1) return set_err(POYALGN_EINVAL, "bad sequence");
+    const long long at = align_up(s->used);
+    if (at + len > s->cap)
+        return set_err(POYALGN_ENOMEM, "store full: %lld of %lld bytes used, sequence needs %d",
+                       s->used, s->cap, len);
+    int rc;
+    if ((rc = ensure_device(s->ctx))) return rc;
+    CU(cudaMemcpy(as<uint8_t>(s->arena) + at, seq, (size_t)len, cudaMemcpyHostToDevice));
+    s->off.push_back(at);
+    s->len.push_back(len);
+    s->used = at + len;
+    *node = (int32_t)(s->len.size() - 1);
+    return 0;
+}
+
+int poyalgn_store_count(const poyalgn_store* s) { return s ? (int)s->len.size() : 0; }
+
+int poyalgn_store_length(const poyalgn_store* s, int node)
+{
+    if (!s || !valid_node(s, node)) return set_err(POYALGN_EINVAL, "unknown node %d", node);
+    return s->len[node];
+}
+
+int poyalgn_store_read(poyalgn_store* s, int node, uint8_t* out, int cap)
+{
+    if (!s || !out || !valid_node(s, node)) return set_err(POYALGN_EINVAL, "unknown node %d", node);
+    if (cap < s->len[node]) return set_err(POYALGN_EINVAL, "capacity %d < %d", cap, s->len[node]);
+    int rc;
+    if ((rc = ensure_device(s->ctx))) return rc;
+    CU(cudaStreamSynchronize(s->ctx->stream));
+    CU(cudaMemcpy(out, as<uint8_t>(s->arena) + s->off[node], (size_t)s->len[node],
+                  cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int poyalgn_store_truncate(poyalgn_store* s, int nodes)
+{
+    if (!s || nodes < 0 || nodes > (int)s->len.size())
+        return set_err(POYALGN_EINVAL, "bad node count %d", nodes);
+    s->off.resize(nodes);
+    s->len.resize(nodes);
+    long long end = 0;
+    for (int k = 0; k < nodes; k++) end = std::max(end, s->off[k] + s->len[k]);
+    s->used = end;
+    return 0;
+}
+
+int poyalgn_store_median_batch(poyalgn_store* s, const poyalgn_cm* cm, int npairs,
+                               const int32_t* node_a, const int32_t* node_b, int keep,
+                               int32_t* median_node, int32_t* cost, int32_t* maxcost,
+                               int32_t* status)
+{
+    if (!s || !cm || npairs < 0 || (npairs > 0 && (!node_a || !node_b || !cost)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (npairs == 0) return 0;
+    return store_batch(s, cm, npairs, node_a, node_b, keep, median_node, cost, maxcost, status);
+}
+
+int poyalgn_downpass(poyalgn_store* s, const poyalgn_cm* cm, int nleaves,
+                     const int32_t* leaf_node, int ninternal, const int32_t* left,
+                     const int32_t* right, int32_t* internal_node, int32_t* internal_cost,
+                     int64_t* total_cost, int32_t* levels)
+{
+    if (!s || !cm || nleaves < 1 || ninternal < 0 || !leaf_node ||
+        (ninternal > 0 && (!left || !right || !internal_node || !internal_cost)) || !total_cost)
+        return set_err(POYALGN_EINVAL, "null argument");
+    // level of each internal node: 1 + the deeper child's level (leaves 0)
+    std::vector<int> level(ninternal, 0);
+    int depth = 0;
+    for (int k = 0; k < ninternal; k++) {
+        int lv = 0;
+        for (int ch : {left[k], right[k]}) {
+            if (ch < 0 || ch >= nleaves + k)
+                return set_err(POYALGN_EINVAL, "internal node %d: child %d is not an earlier node",
+                               k, ch);
+            if (ch < nleaves) {
+                if (!valid_node(s, leaf_node[ch]))
+                    return set_err(POYALGN_EINVAL, "leaf %d: unknown node %d", ch, leaf_node[ch]);
+            } else {
+                lv = std::max(lv, level[ch - nleaves]);
+            }
+        }
+        level[k] = lv + 1;
+        depth = std::max(depth, level[k]);
+    }
+    auto node_of = [&](int ch) { return ch < nleaves ? leaf_node[ch] : internal_node[ch - nleaves]; };
+    std::vector<int> idx, na, nb, med, cst;
+    long long total = 0;
+    for (int lv = 1; lv <= depth; lv++) {
+        idx.clear();
+        na.clear();
+        nb.clear();
+        for (int k = 0; k < ninternal; k++) {
+            if (level[k] != lv) continue;
+            idx.push_back(k);
+            na.push_back(node_of(left[k]));
+            nb.push_back(node_of(right[k]));
+        }
+        const int n = (int)idx.size();
+        med.assign(n, -1);
+        cst.assign(n, 0);
+        int rc = store_batch(s, cm, n, na.data(), nb.data(), 1, med.data(), cst.data(), nullptr,
+                             nullptr);
+        if (rc) return rc;
+        for (int t = 0; t < n; t++) {
+            internal_node[idx[t]] = med[t];
+            internal_cost[idx[t]] = cst[t];
+            total += cst[t];
+        }
+    }
+    *total_cost = total;
+    if (levels) *levels = depth;
+    return 0;
+}
+
+}  // extern "C"

@@ -96,11 +96,11 @@ void aff_pass_fast(const AffBand& b, int P, const Tables& t, const uint8_t* x,
 
 template <int R>
 void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
-                   const uint8_t* y, uint16_t* dm, int shadowEH0, int* cost, int* gapnum)
+                   const uint8_t* y, uint8_t* dm, int shadowEH0, int* cost, int* gapnum)
 {
     std::vector<AffLean<R>> L(P);
     for (int g = 0; g < P; g++) aff_lean_init(L[g], b, t, x, g, P);
-    std::vector<AffCell> sv(P);
+    std::vector<LeanCell> sv(P);
     const int Tlast = (b.m - 1) + (b.n - 1);
     for (int T = 1; T <= Tlast; T++) {
         const bool odd = T & 1;
@@ -115,14 +115,14 @@ void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
             else
                 aff_lean_step<R>(l, l.V1, l.V0, l.R1, l.R0, l.G1, l.G0, b, t, x, y, P, T, sv[src],
                                  shadowEH0, dc);
-            for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint16_t)dc[q];
+            for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint8_t)dc[q];
         }
     }
     const int i = b.m - 1;
     const int blk = (i - 1) / R, g = blk % P, q = (i - 1) - blk * R;
-    const AffCell c = (Tlast & 1) ? L[g].V1[q] : L[g].V0[q];
-    *cost = aff_final(c);
-    *gapnum = aff_gapnum(c);
+    const LeanCell c = (Tlast & 1) ? L[g].V1[q] : L[g].V0[q];
+    *cost = lean_final(c);
+    *gapnum = lean_gapnum(c);
 }
 
 struct Emul {
@@ -189,6 +189,8 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     const int m = pl.m, n = pl.n;
     if (m == 1 && n == 1) return -4;
     std::vector<uint16_t> dm;
+    std::vector<uint8_t> dm8;  // lean passes
+    bool lean_last = false;
     std::vector<int> shadow(n, HIGH);
     bool gapfree = t.gap == TMPGAP;
     for (int i = 1; i < la; i++) gapfree = gapfree && !(a[i] & TMPGAP);
@@ -205,6 +207,8 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
         R = class_R(1, c);
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);
+        dm8.assign((size_t)(m + n + 1) * P * R, 0);
+        lean_last = false;
         (*passes)++;
         if (m == 1) {  // leni = 0: the initial row is the whole alignment
             int s = t.go;
@@ -213,10 +217,11 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
             g = 0xFFFF;
         } else {
             if (gapfree && aff_lean_ok(t, n)) {
+                lean_last = true;
                 switch (R) {
-                    case 1: aff_pass_lean<1>(bd, P, t, x, y, dm.data(), shadowEH0, cost, &g); break;
-                    case 2: aff_pass_lean<2>(bd, P, t, x, y, dm.data(), shadowEH0, cost, &g); break;
-                    default: aff_pass_lean<4>(bd, P, t, x, y, dm.data(), shadowEH0, cost, &g); break;
+                    case 1: aff_pass_lean<1>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    case 2: aff_pass_lean<2>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    default: aff_pass_lean<4>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
                 }
             } else if (gapfree) {
                 switch (R) {
@@ -237,7 +242,8 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
         T *= 2;
     }
     PairOut o = {ea, eb, med, mwg, cap};
-    PairRes r = aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    PairRes r = lean_last ? aff_traceback_lean(dm8.data(), P, R, t, x, m, y, n, pl.swaped, o)
+                          : aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
     res[0] = r.alen;
     res[1] = r.mlen;
     res[2] = r.wlen;

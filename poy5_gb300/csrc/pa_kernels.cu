@@ -426,24 +426,24 @@ __device__ void aff_fill(const AffBand& b, const Tables& st, const uint8_t* x,
 }
 
 
-// Lean affine fill (gap-free pairs within aff_lean_ok): the step loop is
-// unrolled by two so the two register sets of AffLean swap roles statically.
+// Lean affine fill (gap-free pairs within aff_lean_ok): one direction byte
+// per cell, no block-diagonal state; the step loop is unrolled by two so the
+// two register sets of AffLean swap roles statically.
 template <int R>
 __device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t* x,
-                              const uint8_t* y, uint16_t* dm, int shadowEH0, const Pipe& p,
-                              bool active, int Tmax, AffCell (*xc)[32], int* sres, int& cost,
+                              const uint8_t* y, uint8_t* dm, int shadowEH0, const Pipe& p,
+                              bool active, int Tmax, LeanCell (*xc)[32], int* sres, int& cost,
                               int& gapnum)
 {
     AffLean<R> L;
-    L.V0[R - 1] = AffCell{0, 0, 0, 0, 0u};
-    L.V1[R - 1] = AffCell{0, 0, 0, 0, 0u};
+    L.V0[R - 1] = LeanCell{0, 0, 0, 0u};
+    L.V1[R - 1] = LeanCell{0, 0, 0, 0u};
     if (active) aff_lean_init(L, b, st, x, p.gl, p.P);
     const int Tlast = active ? (b.m - 1) + (b.n - 1) : 0;
-    auto exchange = [&](const AffCell& sv, int T) {
-        AffCell rc;
+    auto exchange = [&](const LeanCell& sv, int T) {
+        LeanCell rc;
         rc.EH = rot_prev(p, sv.EH);
         rc.EV = rot_prev(p, sv.EV);
-        rc.EB = rot_prev(p, sv.EB);
         rc.CB = rot_prev(p, sv.CB);
         rc.GM = rot_prev(p, sv.GM);
         if (p.K > 1) {
@@ -455,32 +455,32 @@ __device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t*
     };
     for (int T = 1; T <= Tmax; T += 2) {
         {
-            const AffCell rc = exchange(L.V0[R - 1], T);
+            const LeanCell rc = exchange(L.V0[R - 1], T);
             if (active && T <= Tlast) {
                 int dc[R];
                 aff_lean_step<R>(L, L.V0, L.V1, L.R0, L.R1, L.G0, L.G1, b, st, x, y, p.P, T,
                                  rc, shadowEH0, dc);
-                store_u16<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+                store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
             }
         }
         if (T + 1 <= Tmax) {
-            const AffCell rc = exchange(L.V1[R - 1], T + 1);
+            const LeanCell rc = exchange(L.V1[R - 1], T + 1);
             if (active && T + 1 <= Tlast) {
                 int dc[R];
                 aff_lean_step<R>(L, L.V1, L.V0, L.R1, L.R0, L.G1, L.G0, b, st, x, y, p.P,
                                  T + 1, rc, shadowEH0, dc);
-                store_u16<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
+                store_u8<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
             }
         }
     }
     const int i = active ? b.m - 1 : 1;
     const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
-    AffCell c = L.V0[0];
+    LeanCell c = L.V0[0];
     const bool odd = (Tlast & 1) != 0;  // odd last step wrote V1
 #pragma unroll
     for (int r = 0; r < R; r++)
         if (r == oq) c = odd ? L.V1[r] : L.V0[r];
-    int f = aff_final(c), g = aff_gapnum(c);
+    int f = lean_final(c), g = lean_gapnum(c);
     if (p.K == 1) {
         f = from_lane(p, f, og);
         g = from_lane(p, g, og);
@@ -504,6 +504,7 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
     constexpr int VARIANT = FAST ? 1 : 0;
     __shared__ Tables st;
     __shared__ AffCell xc[2][32];
+    __shared__ LeanCell xl[2][32];
     __shared__ int sres[2];
     __shared__ int sitem;
     load_tables(st, A.tables);
@@ -539,7 +540,8 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
             int fc = 0, fg = 0;
             if (Tmax > 0) {
                 if constexpr (FAST)
-                    aff_fill_lean<R>(b, st, w.x, w.y, dm, eh0, p, act, Tmax, xc, sres, fc, fg);
+                    aff_fill_lean<R>(b, st, w.x, w.y, reinterpret_cast<uint8_t*>(dm), eh0, p,
+                                     act, Tmax, xl, sres, fc, fg);
                 else
                     aff_fill<R, false>(b, st, w.x, w.y, dm, shadow, eh0, p, act, Tmax, xc, sres,
                                        fc, fg);
@@ -567,11 +569,14 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
             pipe_sync(p);
         }
         if (finished && p.gl == 0) {
-            A.lastcls[w.k] = cls;
+            A.lastcls[w.k] = cls | (FAST ? LASTCLS_LEAN : 0);
             A.slab_cta[w.k] = p.slot;
             if (A.do_traceback) {
-                const PairRes r = aff_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
-                                                pair_out(A, w.k));
+                const PairRes r =
+                    FAST ? aff_traceback_lean(reinterpret_cast<const uint8_t*>(dm), p.P, R, st,
+                                              w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k))
+                         : aff_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
+                                         pair_out(A, w.k));
                 finish_pair(A, w.k, cost, r);
             } else {
                 A.cost[w.k] = cost;
@@ -666,11 +671,13 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
     const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
     const int m = swaped ? lb : la, n = swaped ? la : lb;
     const int tie = A.swap_override ? A.swap_override[k] : swaped;
-    const int cls = A.lastcls[k];
+    const int cls = A.lastcls[k] & LASTCLS_MASK;
+    const bool lean = (A.lastcls[k] & LASTCLS_LEAN) != 0;
     const int P = class_P(A.affine, cls), R = class_R(A.affine, cls);
     const uint8_t* base = A.slab + (long long)A.slab_cta[k] * strides[cls];
     PairRes r;
-    if (A.affine) r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, tie, pair_out(A, k));
+    if (A.affine && lean) r = aff_traceback_lean(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
+    else if (A.affine) r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, tie, pair_out(A, k));
     else r = lin_traceback(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
     finish_pair(A, k, A.cost[k], r);
 }

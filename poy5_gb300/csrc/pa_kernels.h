@@ -7,6 +7,11 @@
 
 namespace pa {
 
+// lastcls[k]: class of pair k's final fill, plus LASTCLS_LEAN when that fill
+// wrote lean direction bytes (aff_lean_step) instead of aff_step words
+constexpr int LASTCLS_LEAN = 0x100;
+constexpr int LASTCLS_MASK = 0xFF;
+
 // Everything a batch launch needs, all device pointers.
 struct BatchArgs {
     const uint8_t* seqs;       // concatenated input sequences
@@ -35,7 +40,7 @@ struct BatchArgs {
     int* wlen;
     int* status;               // 1 pending, 0 done, < 0 error
     int* passes;               // band iterations run
-    int* lastcls;              // class of the final iteration
+    int* lastcls;              // class of the final iteration (| LASTCLS_LEAN)
     int* slab_cta;             // pipeline whose slab holds the final fill
     const int* deltawh_override;  // per-call linear stub: caller's deltawh, no reordering
     const int* swap_override;     // per-call stubs: caller's tie preference

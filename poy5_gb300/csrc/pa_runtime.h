@@ -1,0 +1,106 @@
+// Runtime internals shared by the C ABI units (pa_capi.cu, pa_driver.cu):
+// error text, growable device buffers, the context and cost-matrix objects
+// and the batch launcher.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/poyalgn.h"
+#include "pa_kernels.h"
+#include "pa_tables.h"
+
+namespace pa {
+
+// Format the calling thread's error text (poyalgn_last_error); returns code.
+int set_err(int code, const char* fmt, ...);
+
+#define CU(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return ::pa::set_err(POYALGN_ECUDA, "%s: %s (%s:%d)", #call,                \
+                                 cudaGetErrorString(e_), __FILE__, __LINE__);           \
+    } while (0)
+
+// A device buffer that only grows.
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+int reserve(DevBuf& b, size_t bytes);
+void release(DevBuf& b);
+
+template <class T>
+T* as(DevBuf& b) { return reinterpret_cast<T*>(b.p); }
+
+}  // namespace pa
+
+struct poyalgn_cm {
+    pa::HostCM h;
+    pa::Tables t;
+    pa::Tables* d = nullptr;
+};
+
+struct poyalgn_ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    int bps[2][pa::NCLASS][2] = {};
+    // host-pointer batches: staging of inputs and outputs
+    pa::DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
+    // per-batch scratch
+    pa::DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
+    pa::DevBuf dwh, swp, order, order_scratch;
+    int last_launches = 0;
+    // upper bound on the direction-slab arena of one batch (0: half the free
+    // device memory, at most 64 GB)
+    long long slab_budget = 0;
+    // optional per-launch timing: one event before the prep launch and one
+    // after each launch of a batch, for up to prof_cap batches
+    std::vector<cudaEvent_t> prof_ev;
+    int prof_cap = 0, prof_used = 0;
+    // per-call stub state: the fill of the last simple_2 / align_affine_3
+    bool call_valid = false;
+    int call_affine = 0, call_l1 = 0, call_l2 = 0;
+    const poyalgn_cm* call_cm = nullptr;
+    std::vector<uint8_t> call_s1, call_s2;
+    long long call_strides[pa::NCLASS] = {0};
+};
+
+// Device-resident node sequences (poyalgn_store_*, pa_driver.cu).
+struct poyalgn_store {
+    poyalgn_ctx* ctx = nullptr;
+    pa::DevBuf arena;             // node bytes, bump-allocated
+    long long cap = 0, used = 0;
+    std::vector<long long> off;   // per node: arena offset and length
+    std::vector<int> len;
+    // batch scratch: pair metadata, per-pair ints, ea/eb/mwg (and discarded
+    // medians), plus pinned host mirrors
+    pa::DevBuf meta, ints, bytes;
+    std::vector<unsigned char> hmeta;
+    std::vector<int> hints;
+};
+
+namespace pa {
+
+int ensure_device(poyalgn_ctx* c);
+
+// Enqueue one DOS.median batch on `st` (all pointers on the device); see
+// pa_capi.cu.
+int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs, int maxmn,
+              long long out_total, const uint8_t* seqs, const long long* offa,
+              const int* lena, const long long* offb, const int* lenb,
+              const long long* out_off, int* cost, int* maxcost, int* alen, int* mlen,
+              int* wlen, int* status, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
+              int* passes, const int* dwh, const int* swp, int do_traceback, cudaStream_t st);
+
+// Reserve the per-batch scratch of run_batch for batches of up to max_pairs
+// pairs, out_total output bytes and a slab arena of slab_bytes, so that such
+// batches allocate nothing.
+int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
+               long long slab_bytes);
+
+}  // namespace pa

@@ -145,3 +145,83 @@ def serving_pairs(n_pairs: int, seed: int = SEED_BASE + 4) -> PairWorkload:
             b = random_bases(rng, 1)
         pairs.append((with_gap(a), with_gap(b)))
     return PairWorkload(f"serving_pairs_{n_pairs}", pairs, 1, 1, 3)
+
+
+@dataclass
+class TreeWorkload:
+    """A rooted binary tree with sequences at the leaves.
+
+    Leaves are 0..n-1; internal node k has children ``left[k]``, ``right[k]``
+    (leaf index, or n + internal index), children before parents, and the
+    last internal node is the root.
+    """
+    name: str
+    leaves: list         # bitset sequences with leading gap
+    left: np.ndarray
+    right: np.ndarray
+    subs: int
+    indel: int
+    gap_open: int
+
+    @property
+    def affine(self) -> bool:
+        return self.gap_open > 0
+
+
+def jc69_change(t: float) -> float:
+    """Jukes-Cantor probability that a site differs after branch length t."""
+    return 0.75 * (1.0 - np.exp(-4.0 * t / 3.0))
+
+
+def yule_tree(n_taxa: int = 256, root_len: int = 1500, mean_branch: float = 0.05,
+              indel_ratio: float = 0.2, seed: int = SEED_BASE + 3) -> TreeWorkload:
+    """Yule topology, exponential branch lengths, sequences evolved from a
+    uniform random root by JC69 substitutions and indels at indel_ratio x
+    the substitution rate (geometric lengths, mean 3)."""
+    rng = np.random.default_rng(seed)
+    # grow the topology: split a uniformly chosen tip until n_taxa tips
+    children = {0: None}
+    tips = [0]
+    nxt = 1
+    while len(tips) < n_taxa:
+        v = tips.pop(int(rng.integers(0, len(tips))))
+        children[v] = (nxt, nxt + 1)
+        children[nxt] = children[nxt + 1] = None
+        tips += [nxt, nxt + 1]
+        nxt += 2
+    seq = {0: random_bases(rng, root_len)}
+    order = [0]
+    for v in order:  # parents before children
+        if children[v] is None:
+            continue
+        for ch in children[v]:
+            t = rng.exponential(mean_branch)
+            s = substitute(rng, seq[v], jc69_change(t))
+            seq[ch] = indels(rng, s, indel_ratio * t) if len(s) else s
+            order.append(ch)
+    # number leaves 0..n-1 and internal nodes in post-order
+    leaf_id, int_id, left, right, leaves = {}, {}, [], [], []
+
+    def visit(v):
+        stack = [(v, False)]
+        while stack:
+            u, done = stack.pop()
+            if children[u] is None:
+                leaf_id[u] = len(leaves)
+                s = seq[u] if len(seq[u]) else random_bases(rng, 1)
+                leaves.append(with_gap(s))
+            elif done:
+                a, b = children[u]
+                ref = lambda w: leaf_id[w] if w in leaf_id else n_taxa + int_id[w]
+                int_id[u] = len(left)
+                left.append(ref(a))
+                right.append(ref(b))
+            else:
+                stack.append((u, True))
+                a, b = children[u]
+                stack.append((b, False))
+                stack.append((a, False))
+
+    visit(0)
+    return TreeWorkload(f"yule_tree_{n_taxa}_root{root_len}", leaves,
+                        np.array(left, np.int32), np.array(right, np.int32), 1, 2, 0)
