@@ -347,6 +347,40 @@ int poyalgn_server_replay(poyalgn_server *s, int nreq, const double *arrival_s,
 int poyalgn_server_stats(const poyalgn_server *s, int64_t *batches,
                          int64_t *pairs, int64_t *refused);
 
+/* ---- pipeline ladders and the autotuner ------------------------------------- */
+
+/*
+ * No counterpart in the reference. A context aligns each band pass on a
+ * pipeline class picked from a ladder of POYALGN_NCLASS shapes: class c has
+ * P[c] lanes (a power of two, 4..512) and R[c] rows per lane (2 or 4 for the
+ * affine model, 2, 4 or 8 for the linear one) and takes bands up to
+ * 2 (P[c] - 1) R[c] + 1 cells wide; capacities must not decrease along the
+ * ladder. Results never depend on the ladder, only the speed does.
+ */
+#define POYALGN_NCLASS 10
+
+int poyalgn_set_ladder(poyalgn_ctx *ctx, int affine, const int32_t *P,
+                       const int32_t *R);
+int poyalgn_get_ladder(const poyalgn_ctx *ctx, int affine, int32_t *P,
+                       int32_t *R);
+
+/*
+ * Time ncand candidate ladders (cand_P, cand_R: ncand rows of
+ * POYALGN_NCLASS) on a sample batch given as for poyalgn_median_batch (host
+ * pointers; copied to the device once), each run reps times after one
+ * warm-up run; keep the fastest for cm's cost model. ms[k] receives the
+ * median batch time of candidate k and *best its index. Every candidate's
+ * per-pair costs and statuses are checked against the first candidate's;
+ * a difference is reported as POYALGN_EINVAL (and the ladder is left
+ * unchanged).
+ */
+int poyalgn_autotune(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
+                     const uint8_t *seqs, const int64_t *offa,
+                     const int32_t *lena, const int64_t *offb,
+                     const int32_t *lenb, int ncand, const int32_t *cand_P,
+                     const int32_t *cand_R, int reps, float *ms,
+                     int32_t *best);
+
 /* Number of kernel launches the last batch enqueued (for accounting). */
 int poyalgn_last_launches(const poyalgn_ctx *ctx);
 

@@ -64,6 +64,9 @@ _SIGS = {
     "poyalgn_server_wait": (_I, [_P, _I64, _I, _P, _P, _P, _P, _I64, _P]),
     "poyalgn_server_replay": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "poyalgn_server_stats": (_I, [_P, _P, _P, _P]),
+    "poyalgn_set_ladder": (_I, [_P, _I, _P, _P]),
+    "poyalgn_get_ladder": (_I, [_P, _I, _P, _P]),
+    "poyalgn_autotune": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P]),
     "poyalgn_last_launches": (_I, [_P]),
     "poyalgn_profile_begin": (_I, [_P, _I]),
     "poyalgn_profile_end": (_I, [_P, _P, _P]),

@@ -94,8 +94,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     long long strides[NCLASS];
     long long arena = 0;
     for (int k = 0; k < NCLASS; k++) {
-        const int pipes = class_pipes_per_cta(affine, k);
-        strides[k] = class_slab_bytes(affine, k, maxmn);
+        const int pipes = class_pipes_per_cta(c->lad[affine], k);
+        strides[k] = class_slab_bytes(c->lad[affine], affine, k, maxmn);
         for (int v = 0; v < 2; v++) {
             long long g = (long long)c->nsm * std::max(1, c->bps[affine][k][v]);
             g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
@@ -119,6 +119,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.npairs = npairs;
     A.affine = affine;
     A.do_traceback = do_traceback;
+    A.lad = c->lad[affine];
     A.tables = cm->d;
     A.pfull = as<int>(c->pfull);
     A.shadow = as<int>(c->shadow);
@@ -275,6 +276,7 @@ int trace_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
     A.out_off = offa + 2;
     A.npairs = 1;
     A.affine = affine;
+    A.lad = c->lad[affine];
     A.tables = cm->d;
     A.slab = as<uint8_t>(c->slab);
     A.cost = ints + 0;
@@ -325,7 +327,7 @@ int poyalgn_init(int device, poyalgn_ctx** out)
     }
     for (int a = 0; a < 2; a++)
         for (int k = 0; k < NCLASS; k++)
-            for (int v = 0; v < 2; v++) c->bps[a][k][v] = class_blocks_per_sm(a, k, v);
+            for (int v = 0; v < 2; v++) c->bps[a][k][v] = class_blocks_per_sm(c->lad[a], a, k, v);
     *out = c;
     return 0;
 }
@@ -653,6 +655,147 @@ int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
 
 int poyalgn_num_classes(void) { return NCLASS; }
 
+int poyalgn_set_ladder(poyalgn_ctx* ctx, int affine, const int32_t* P, const int32_t* R)
+{
+    if (!ctx || !P || !R || (affine != 0 && affine != 1)) return set_err(POYALGN_EINVAL, "null argument");
+    Ladder L;
+    for (int k = 0; k < NCLASS; k++) {
+        L.P[k] = P[k];
+        L.R[k] = R[k];
+    }
+    if (!ladder_valid(L, affine)) return set_err(POYALGN_EINVAL, "ladder not supported");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    ctx->lad[affine] = L;
+    for (int k = 0; k < NCLASS; k++)
+        for (int v = 0; v < 2; v++) ctx->bps[affine][k][v] = class_blocks_per_sm(L, affine, k, v);
+    CU(cudaGetLastError());
+    ctx->call_valid = false;  // a kept per-call fill was laid out for the old ladder
+    return 0;
+}
+
+int poyalgn_get_ladder(const poyalgn_ctx* ctx, int affine, int32_t* P, int32_t* R)
+{
+    if (!ctx || !P || !R || (affine != 0 && affine != 1)) return set_err(POYALGN_EINVAL, "null argument");
+    for (int k = 0; k < NCLASS; k++) {
+        P[k] = ctx->lad[affine].P[k];
+        R[k] = ctx->lad[affine].R[k];
+    }
+    return 0;
+}
+
+int poyalgn_autotune(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs, const uint8_t* seqs,
+                     const int64_t* offa, const int32_t* lena, const int64_t* offb,
+                     const int32_t* lenb, int ncand, const int32_t* cand_P,
+                     const int32_t* cand_R, int reps, float* ms, int32_t* best)
+{
+    if (!ctx || !cm || npairs < 1 || !seqs || !offa || !lena || !offb || !lenb || ncand < 1 ||
+        !cand_P || !cand_R || reps < 1 || !ms || !best)
+        return set_err(POYALGN_EINVAL, "null argument");
+    const int affine = cm->h.cost_model == 1;
+    for (int q = 0; q < ncand; q++) {
+        Ladder L;
+        for (int k = 0; k < NCLASS; k++) {
+            L.P[k] = cand_P[q * NCLASS + k];
+            L.R[k] = cand_R[q * NCLASS + k];
+        }
+        if (!ladder_valid(L, affine)) return set_err(POYALGN_EINVAL, "candidate %d not supported", q);
+    }
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    // stage the sample once
+    long long seq_bytes = 0, out_total = 0;
+    int maxmn = 2;
+    std::vector<long long> oo(npairs);
+    for (int k = 0; k < npairs; k++) {
+        if (lena[k] < 1 || lenb[k] < 1) return set_err(POYALGN_EINVAL, "pair %d: empty sequence", k);
+        seq_bytes = std::max<long long>(seq_bytes, std::max(offa[k] + lena[k], offb[k] + lenb[k]));
+        oo[k] = out_total;
+        out_total += lena[k] + lenb[k] + 2;
+        maxmn = std::max(maxmn, lena[k] + lenb[k]);
+    }
+    const size_t ni = (size_t)npairs;
+    if ((rc = reserve(ctx->seqs, (size_t)seq_bytes))) return rc;
+    if ((rc = reserve(ctx->offa, ni * 8))) return rc;
+    if ((rc = reserve(ctx->offb, ni * 8))) return rc;
+    if ((rc = reserve(ctx->lena, ni * 4))) return rc;
+    if ((rc = reserve(ctx->lenb, ni * 4))) return rc;
+    if ((rc = reserve(ctx->outoff, ni * 8))) return rc;
+    if ((rc = reserve(ctx->ints, ni * 4 * 7))) return rc;
+    if ((rc = reserve(ctx->bytes, (size_t)out_total * 4))) return rc;
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(ctx->seqs.p, seqs, (size_t)seq_bytes, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->offa.p, offa, ni * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->offb.p, offb, ni * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->lena.p, lena, ni * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->lenb.p, lenb, ni * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->outoff.p, oo.data(), ni * 8, cudaMemcpyHostToDevice, st));
+    int* I = as<int>(ctx->ints);
+    uint8_t* B = as<uint8_t>(ctx->bytes);
+    const size_t ot = (size_t)out_total;
+    auto batch = [&]() {
+        return run_batch(ctx, cm, affine, npairs, maxmn, out_total, as<uint8_t>(ctx->seqs),
+                         as<long long>(ctx->offa), as<int>(ctx->lena), as<long long>(ctx->offb),
+                         as<int>(ctx->lenb), as<long long>(ctx->outoff), I, I + ni, I + 2 * ni,
+                         I + 3 * ni, I + 4 * ni, I + 5 * ni, B, B + ot, B + 2 * ot, B + 3 * ot,
+                         I + 6 * ni, nullptr, nullptr, 1, st);
+    };
+    const Ladder saved = ctx->lad[affine];
+    int saved_bps[NCLASS][2];
+    memcpy(saved_bps, ctx->bps[affine], sizeof(saved_bps));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    std::vector<int> first(2 * ni), got(2 * ni);
+    std::vector<float> t(reps);
+    int bi = 0;
+    rc = 0;
+    for (int q = 0; q < ncand && !rc; q++) {
+        Ladder L;
+        for (int k = 0; k < NCLASS; k++) {
+            L.P[k] = cand_P[q * NCLASS + k];
+            L.R[k] = cand_R[q * NCLASS + k];
+            for (int v = 0; v < 2; v++)
+                ctx->bps[affine][k][v] = class_blocks_per_sm(L, affine, k, v);
+        }
+        ctx->lad[affine] = L;
+        if ((rc = batch())) break;
+        for (int r = 0; r < reps && !rc; r++) {
+            if (cudaEventRecord(e0, st) != cudaSuccess) rc = set_err(POYALGN_ECUDA, "event");
+            if (!rc) rc = batch();
+            if (!rc && cudaEventRecord(e1, st) != cudaSuccess) rc = set_err(POYALGN_ECUDA, "event");
+            if (!rc && (cudaEventSynchronize(e1) != cudaSuccess ||
+                        cudaEventElapsedTime(&t[r], e0, e1) != cudaSuccess))
+                rc = set_err(POYALGN_ECUDA, "timing candidate %d", q);
+        }
+        if (rc) break;
+        std::vector<float> sorted(t);
+        std::sort(sorted.begin(), sorted.end());
+        ms[q] = sorted[reps / 2];
+        // cost and status of every pair must not depend on the ladder
+        std::vector<int>& dst = q == 0 ? first : got;
+        if (cudaMemcpy(dst.data(), I, ni * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(dst.data() + ni, I + 5 * ni, ni * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = set_err(POYALGN_ECUDA, "reading candidate %d", q);
+            break;
+        }
+        if (q > 0 && got != first) {
+            rc = set_err(POYALGN_EINVAL, "candidate %d changed a result", q);
+            break;
+        }
+        if (ms[q] < ms[bi]) bi = q;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) {
+        ctx->lad[affine] = saved;
+        memcpy(ctx->bps[affine], saved_bps, sizeof(saved_bps));
+        return rc;
+    }
+    *best = bi;
+    return poyalgn_set_ladder(ctx, affine, cand_P + bi * NCLASS, cand_R + bi * NCLASS);
+}
+
 }  // extern "C"
 
 // ---- poyalgn_median_batch_device_noalloc ----------------------------------
@@ -689,7 +832,8 @@ int noalloc_device(int dev, const NoAllocDevice** out)
         CU(cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, dev));
         for (int a = 0; a < 2; a++)
             for (int k = 0; k < NCLASS; k++)
-                for (int v = 0; v < 2; v++) d.bps[a][k][v] = class_blocks_per_sm(a, k, v);
+                for (int v = 0; v < 2; v++)
+                    d.bps[a][k][v] = class_blocks_per_sm(default_ladder(a), a, k, v);
         CU(cudaGetLastError());
         d.base = static_cast<unsigned char*>(p);
         d.ready = true;
@@ -751,6 +895,7 @@ extern "C" int poyalgn_median_batch_device_noalloc(
     if ((rc = noalloc_device(dev, &d))) return rc;
 
     const int affine = cm->h.cost_model == 1;
+    const Ladder lad = default_ladder(affine);
     const size_t ni = (size_t)npairs;
     Carve cv{d->base, 0, (size_t)POYALGN_NOALLOC_SCRATCH_BYTES};
     int* qctr = static_cast<int*>(cv.take(2 * NQUEUE * sizeof(int)));
@@ -772,8 +917,8 @@ extern "C" int poyalgn_median_batch_device_noalloc(
     long long strides[NCLASS];
     long long arena = 0;
     for (int k = 0; k < NCLASS; k++) {
-        const int pipes = class_pipes_per_cta(affine, k);
-        strides[k] = class_slab_bytes(affine, k, max_pair_len);
+        const int pipes = class_pipes_per_cta(lad, k);
+        strides[k] = class_slab_bytes(lad, affine, k, max_pair_len);
         if (strides[k] * pipes > budget)
             return set_err(POYALGN_EINVAL,
                            "max_pair_len %d leaves no room for class %d in POYALGN_NOALLOC_SCRATCH_BYTES",
@@ -802,6 +947,7 @@ extern "C" int poyalgn_median_batch_device_noalloc(
     A.npairs = npairs;
     A.affine = affine;
     A.do_traceback = 1;
+    A.lad = lad;
     A.tables = cm->d;
     A.pfull = pfull;
     A.shadow = shadow;

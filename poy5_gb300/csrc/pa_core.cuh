@@ -81,32 +81,37 @@ PA_HD uint32_t vmax2(uint32_t a, uint32_t b)
 }
 
 // ---------------------------------------------------------------------------
-// Pipeline shapes. A "class" is a (K warps, R rows per lane) shape; a pair
-// moves up the ladder as its band doubles. Linear and affine use different
-// ladders because affine lanes hold more state per row.
+// Pipeline shapes. A "class" is a (P lanes, R rows per lane) shape; a pair
+// moves up its ladder as its band doubles. P < 32: 32/P pipelines share a
+// warp (one pair each, shuffles of width P); P >= 32: P/32 warps of one CTA.
+// Ladders are runtime data (a context may retune them; results do not
+// depend on the ladder), drawn from the shapes the kernels are compiled for:
+// P in {4, 8, ..., 512}, R in {2, 4} (affine) or {2, 4, 8} (linear). Wider
+// shapes are bounded by registers: a 512-thread CTA leaves 128 registers per
+// thread, enough for 8 linear or 4 affine rows per lane.
 
 constexpr int NCLASS = 10;
-// Pipeline of P lanes with R rows per lane. P < 32: 32/P pipelines share a
-// warp (one pair each, shuffles of width P); P >= 32: P/32 warps of one CTA.
-// Wider shapes are bounded by registers: a 512-thread CTA leaves 128
-// registers per thread, enough for 8 linear or 4 affine rows per lane.
-PA_HD int class_P(int affine, int c)
+
+struct Ladder {
+    int P[NCLASS];
+    int R[NCLASS];
+};
+
+PA_HD Ladder default_ladder(int affine)
 {
+    Ladder L;
     const int lp[NCLASS] = {4, 8, 16, 32, 32, 32, 64, 128, 256, 512};
-    const int ap[NCLASS] = {4, 8, 16, 32, 32, 64, 128, 256, 512, 512};
-    return affine ? ap[c] : lp[c];
-}
-PA_HD int class_R(int affine, int c)
-{
     const int lr[NCLASS] = {2, 2, 2, 2, 4, 8, 8, 8, 8, 8};
+    const int ap[NCLASS] = {4, 8, 16, 32, 32, 64, 128, 256, 512, 512};
     const int ar[NCLASS] = {2, 2, 2, 2, 4, 4, 4, 4, 4, 4};
-    return affine ? ar[c] : lr[c];
+    for (int c = 0; c < NCLASS; c++) {
+        L.P[c] = affine ? ap[c] : lp[c];
+        L.R[c] = affine ? ar[c] : lr[c];
+    }
+    return L;
 }
-PA_HD int class_K(int affine, int c)
-{
-    const int P = class_P(affine, c);
-    return P >= 32 ? P / 32 : 1;
-}
+
+PA_HD int ladder_K(const Ladder& L, int c) { return L.P[c] >= 32 ? L.P[c] / 32 : 1; }
 
 // A (P, R) pipeline processes a band of unclipped width wu over n columns
 // without two blocks of one lane overlapping in time when either bound holds
@@ -117,14 +122,28 @@ PA_HD bool band_fits(int P, int R, long long wu, int n)
     return (wu <= 2 * pr + 1) || (pr >= n);
 }
 
-// Smallest class for a band; -1 if none. wu < 0 means "full plane".
-PA_HD int pick_class(int affine, long long wu, int n)
+// Smallest class of the ladder for a band; -1 if none. wu < 0: full plane.
+PA_HD int pick_class(const Ladder& L, long long wu, int n)
 {
-    for (int c = 0; c < NCLASS; c++) {
-        int P = class_P(affine, c);
-        if (band_fits(P, class_R(affine, c), wu < 0 ? (1LL << 40) : wu, n)) return c;
-    }
+    for (int c = 0; c < NCLASS; c++)
+        if (band_fits(L.P[c], L.R[c], wu < 0 ? (1LL << 40) : wu, n)) return c;
     return -1;
+}
+
+// A ladder the kernels can run: compiled shapes, and band capacity
+// 2 (P - 1) R + 1 non-decreasing so that the last class is the widest.
+PA_HD bool ladder_valid(const Ladder& L, int affine)
+{
+    long long prev = 0;
+    for (int c = 0; c < NCLASS; c++) {
+        const int P = L.P[c], R = L.R[c];
+        if (P < 4 || P > 512 || (P & (P - 1))) return false;
+        if (!(R == 2 || R == 4 || (!affine && R == 8))) return false;
+        const long long cap = 2LL * (P - 1) * R + 1;
+        if (cap < prev) return false;
+        prev = cap;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -807,6 +826,15 @@ PA_HD int min3(int a, int b, int c)
     return tmin(tmin(a, b), c);
 #endif
 }
+// per-halfword unsigned max of three packed u16 pairs
+PA_HD uint32_t vmax3(uint32_t a, uint32_t b, uint32_t c)
+{
+#if defined(__CUDA_ARCH__)
+    return __vimax3_u16x2(a, b, c);
+#else
+    return vmax2(vmax2(a, b), c);
+#endif
+}
 
 template <int R>
 struct AffLean {
@@ -877,8 +905,10 @@ PA_HD bool aff_lean_ok(const Tables& t, int n)
 
 // One anti-diagonal step. VC/RC/GC hold step T-1 (up, left), VP/RP/GP hold
 // step T-2 (diagonal); the step's results overwrite VP/RP/GP, which the
-// caller then passes as VC/RC/GC of the next step.
-template <int R>
+// caller then passes as VC/RC/GC of the next step. GEN = false promises that
+// lane 0 has left its first block (T >= lean_gen_steps), so no lane
+// generates row 0 any more.
+template <int R, bool GEN>
 PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
                          LeanCell& RC, LeanCell& RP, LeanCell& GC, LeanCell& GP,
                          const AffBand& b, const Tables& t, const uint8_t* si,
@@ -889,7 +919,7 @@ PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
     const bool moved = (T >= L.nstart);
     if (moved) aff_lean_enter(L, b, t, si, L.itop + P * R, P);
     const int go = t.go;
-    const bool gen = (L.itop == 1);
+    const bool gen = GEN && (L.itop == 1);
     if (gen) {  // row 0 at column T-1
         const int j0 = T - 1;
         if (j0 <= b.n - 1) {
@@ -949,26 +979,32 @@ PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
             const bool right = (T == L.Tr[q]);
             c.EV = right ? HIGH : ev;
             code |= (!right && endv) ? LEAN_END_V : 0;
-            if (j > 0) {
-                const int m3 = min3(dg.CB, dg.EV, dg.EH);
-                c.CB = m3 + t.csw[L.srb[q] + L.J[q]];
-                code |= (dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0);
-            } else {
-                c.CB = HIGH;
-            }
+            // column 0 has no diagonal (CB = HIGH); J = sj[0] keeps the
+            // lookup in range
+            const int m3 = min3(dg.CB, dg.EV, dg.EH);
+            const int dgc = t.csw[L.srb[q] + L.J[q]];
+            c.CB = j > 0 ? m3 + dgc : HIGH;
+            code |= j > 0 ? ((dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0)) : 0;
             const int f = min3(c.EH, c.EV, c.CB);
             const bool hh = c.EH == f, vv = c.EV == f;
             code |= (hh ? LEAN_DO_H : 0) | (vv ? LEAN_DO_V : 0) | ((hh && vv) ? LEAN_H_EQ_V : 0);
-            uint32_t gm = (c.CB == f) ? dg.GM : 0u;
-            if (hh) gm = vmax2(gm, lf.GM + 1u);
-            if (vv) gm = vmax2(gm, up.GM + 0x10000u);
-            c.GM = gm;
+            c.GM = vmax3(c.CB == f ? dg.GM : 0u, hh ? lf.GM + 1u : 0u,
+                         vv ? up.GM + 0x10000u : 0u);
             VP[q] = c;
             dcode[q] = code;
         } else {
             VP[q] = VC[q];  // keep the row's last state (read as diag/left)
         }
     }
+}
+
+// Steps during which lane 0 still generates row 0 (its first block), rounded
+// up to an even count so the step loop's register-set pairing is kept.
+PA_HD int lean_gen_steps(const AffBand& b, int P, int R)
+{
+    const long long s = block_start_step_aff(b, 1 + P * R);
+    const long long t = s > 0x7ffffff0LL ? 0x7ffffff0LL : s;
+    return (int)((t + 1) & ~1LL);
 }
 
 // Final cost and gap count of the lean corner cell.

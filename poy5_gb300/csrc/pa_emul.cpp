@@ -102,6 +102,8 @@ void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
     for (int g = 0; g < P; g++) aff_lean_init(L[g], b, t, x, g, P);
     std::vector<LeanCell> sv(P);
     const int Tlast = (b.m - 1) + (b.n - 1);
+    // row 0 is generated only up to step Tg, as in the kernel
+    const int Tg = tmin((Tlast + 1) & ~1, lean_gen_steps(b, P, R));
     for (int T = 1; T <= Tlast; T++) {
         const bool odd = T & 1;
         for (int g = 0; g < P; g++) sv[g] = odd ? L[g].V0[R - 1] : L[g].V1[R - 1];
@@ -109,12 +111,18 @@ void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
             const int src = (g + P - 1) % P;
             int dc[R];
             AffLean<R>& l = L[g];
-            if (odd)
-                aff_lean_step<R>(l, l.V0, l.V1, l.R0, l.R1, l.G0, l.G1, b, t, x, y, P, T, sv[src],
-                                 shadowEH0, dc);
+            if (odd && T <= Tg)
+                aff_lean_step<R, true>(l, l.V0, l.V1, l.R0, l.R1, l.G0, l.G1, b, t, x, y, P, T,
+                                       sv[src], shadowEH0, dc);
+            else if (odd)
+                aff_lean_step<R, false>(l, l.V0, l.V1, l.R0, l.R1, l.G0, l.G1, b, t, x, y, P, T,
+                                        sv[src], shadowEH0, dc);
+            else if (T <= Tg)
+                aff_lean_step<R, true>(l, l.V1, l.V0, l.R1, l.R0, l.G1, l.G0, b, t, x, y, P, T,
+                                       sv[src], shadowEH0, dc);
             else
-                aff_lean_step<R>(l, l.V1, l.V0, l.R1, l.R0, l.G1, l.G0, b, t, x, y, P, T, sv[src],
-                                 shadowEH0, dc);
+                aff_lean_step<R, false>(l, l.V1, l.V0, l.R1, l.R0, l.G1, l.G0, b, t, x, y, P, T,
+                                        sv[src], shadowEH0, dc);
             for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint8_t)dc[q];
         }
     }
@@ -128,6 +136,7 @@ void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
 struct Emul {
     HostCM cm;
     Tables t;
+    Ladder lad[2] = {default_ladder(0), default_ladder(1)};
 };
 
 int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb,
@@ -146,10 +155,10 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     *last_class = -1;
     for (;;) {
         LinBand bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
-        int c = pick_class(0, lin_wu(bd), n);
+        int c = pick_class(E.lad[0], lin_wu(bd), n);
         if (c < 0) return -5;
-        P = class_P(0, c);
-        R = class_R(0, c);
+        P = E.lad[0].P[c];
+        R = E.lad[0].R[c];
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);
         (*passes)++;
@@ -201,10 +210,10 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     *last_class = -1;
     for (;;) {
         AffBand bd = aff_band(m, n, band_p(T, m, n));
-        int c = pick_class(1, aff_wu(bd), n);
+        int c = pick_class(E.lad[1], aff_wu(bd), n);
         if (c < 0) return -5;
-        P = class_P(1, c);
-        R = class_R(1, c);
+        P = E.lad[1].P[c];
+        R = E.lad[1].R[c];
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);
         dm8.assign((size_t)(m + n + 1) * P * R, 0);

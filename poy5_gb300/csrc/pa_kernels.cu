@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
     __shared__ int sitem;
     load_tables(st, A.tables);
     __syncthreads();
-    const Pipe p = make_pipe(class_P(0, cls));
+    const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
     uint8_t* dm = A.slab + (long long)p.slot * A.slab_stride;
     for (;;) {
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
         for (;;) {
             const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
             if (live) {
-                const int c = pick_class(0, lin_wu(b), w.n);
+                const int c = pick_class(A.lad, lin_wu(b), w.n);
                 if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
                     if (p.gl == 0) {
                         if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
@@ -453,26 +453,35 @@ __device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t*
         }
         return rc;
     };
-    for (int T = 1; T <= Tmax; T += 2) {
-        {
-            const LeanCell rc = exchange(L.V0[R - 1], T);
-            if (active && T <= Tlast) {
-                int dc[R];
-                aff_lean_step<R>(L, L.V0, L.V1, L.R0, L.R1, L.G0, L.G1, b, st, x, y, p.P, T,
-                                 rc, shadowEH0, dc);
-                store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+    // two step pairs per iteration: V0 -> V1 at odd T, V1 -> V0 at even T
+    auto steps = [&](auto gen, int T0, int T1) {
+        constexpr bool GEN = decltype(gen)::value;
+        for (int T = T0; T <= T1; T += 2) {
+            {
+                const LeanCell rc = exchange(L.V0[R - 1], T);
+                if (active && T <= Tlast) {
+                    int dc[R];
+                    aff_lean_step<R, GEN>(L, L.V0, L.V1, L.R0, L.R1, L.G0, L.G1, b, st, x, y,
+                                          p.P, T, rc, shadowEH0, dc);
+                    store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+                }
+            }
+            if (T + 1 <= Tmax) {
+                const LeanCell rc = exchange(L.V1[R - 1], T + 1);
+                if (active && T + 1 <= Tlast) {
+                    int dc[R];
+                    aff_lean_step<R, GEN>(L, L.V1, L.V0, L.R1, L.R0, L.G1, L.G0, b, st, x, y,
+                                          p.P, T + 1, rc, shadowEH0, dc);
+                    store_u8<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
+                }
             }
         }
-        if (T + 1 <= Tmax) {
-            const LeanCell rc = exchange(L.V1[R - 1], T + 1);
-            if (active && T + 1 <= Tlast) {
-                int dc[R];
-                aff_lean_step<R>(L, L.V1, L.V0, L.R1, L.R0, L.G1, L.G0, b, st, x, y, p.P,
-                                 T + 1, rc, shadowEH0, dc);
-                store_u8<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
-            }
-        }
-    }
+    };
+    // lane 0 generates row 0 only while in its first block (both bounds even)
+    const int tg = group_max(p, active ? lean_gen_steps(b, p.P, R) : 0);
+    const int Tg = tmin((Tmax + 1) & ~1, tg);
+    steps(std::true_type{}, 1, Tg - 1);
+    steps(std::false_type{}, (Tg & ~1) + 1, Tmax);
     const int i = active ? b.m - 1 : 1;
     const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
     LeanCell c = L.V0[0];
@@ -509,7 +518,7 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
     __shared__ int sitem;
     load_tables(st, A.tables);
     __syncthreads();
-    const Pipe p = make_pipe(class_P(1, cls));
+    const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
     uint16_t* dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
     for (;;) {
@@ -524,7 +533,7 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
         for (;;) {
             const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
             if (live) {
-                const int c = pick_class(1, aff_wu(b), w.n);
+                const int c = pick_class(A.lad, aff_wu(b), w.n);
                 if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
                     if (p.gl == 0) {
                         if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
@@ -649,8 +658,8 @@ __global__ void prep_kernel(BatchArgs A)
         return;
     }
     int c;
-    if (A.affine) c = pick_class(1, aff_wu(aff_band(pl.m, pl.n, band_p(pl.T0, pl.m, pl.n))), pl.n);
-    else c = pick_class(0, lin_wu(lin_band(pl.m, pl.n, pl.full, pl.full ? 0 : band_p(pl.T0, pl.m, pl.n))), pl.n);
+    if (A.affine) c = pick_class(A.lad, aff_wu(aff_band(pl.m, pl.n, band_p(pl.T0, pl.m, pl.n))), pl.n);
+    else c = pick_class(A.lad, lin_wu(lin_band(pl.m, pl.n, pl.full, pl.full ? 0 : band_p(pl.T0, pl.m, pl.n))), pl.n);
     if (c < 0) {
         A.status[k] = -5;
         return;
@@ -673,7 +682,7 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
     const int tie = A.swap_override ? A.swap_override[k] : swaped;
     const int cls = A.lastcls[k] & LASTCLS_MASK;
     const bool lean = (A.lastcls[k] & LASTCLS_LEAN) != 0;
-    const int P = class_P(A.affine, cls), R = class_R(A.affine, cls);
+    const int P = A.lad.P[cls], R = A.lad.R[cls];
     const uint8_t* base = A.slab + (long long)A.slab_cta[k] * strides[cls];
     PairRes r;
     if (A.affine && lean) r = aff_traceback_lean(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
@@ -745,9 +754,9 @@ __global__ void aligned_medians_kernel(const Tables* tg, const uint8_t* x, const
 
 }  // namespace
 
-int class_blocks_per_sm(int affine, int cls, int variant)
+int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant)
 {
-    const int K = class_K(affine, cls), R = class_R(affine, cls);
+    const int K = ladder_K(lad, cls), R = lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     int n = 0;
     if (affine) {
@@ -765,9 +774,9 @@ int class_blocks_per_sm(int affine, int cls, int variant)
     return n;
 }
 
-long long class_slab_bytes(int affine, int cls, int maxmn)
+long long class_slab_bytes(const Ladder& lad, int affine, int cls, int maxmn)
 {
-    const long long PR = (long long)class_P(affine, cls) * class_R(affine, cls);
+    const long long PR = (long long)lad.P[cls] * lad.R[cls];
     long long b = (long long)(maxmn + 1) * PR * (affine ? 2 : 1);
     return (b + 255) & ~255LL;
 }
@@ -816,7 +825,7 @@ void launch_prep(const BatchArgs& a, cudaStream_t s)
 
 void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream_t s)
 {
-    const int K = class_K(a.affine, cls), R = class_R(a.affine, cls);
+    const int K = ladder_K(a.lad, cls), R = a.lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     if (a.affine) {
         switch (R) {
@@ -855,9 +864,9 @@ __global__ void order_keys_kernel(const int* lena, const int* lenb, int n, unsig
     idx[k] = k;
 }
 
-int class_pipes_per_cta(int affine, int cls)
+int class_pipes_per_cta(const Ladder& lad, int cls)
 {
-    const int P = class_P(affine, cls);
+    const int P = lad.P[cls];
     return P >= 64 ? 1 : NARROW_WARPS * (P < 32 ? 32 / P : 1);
 }
 

@@ -22,6 +22,7 @@ struct BatchArgs {
     int npairs;
     int affine;
     int do_traceback;          // 0: keep the last fill in the slab (per-call stubs)
+    Ladder lad;                // pipeline classes of this model
     const Tables* tables;
     int* pfull;                // linear plane choice per pair
     int* shadow;               // affine: row-0 EB left by earlier iterations (n per pair)
@@ -54,9 +55,10 @@ struct BatchArgs {
 // Work queues: 2 per class (variant 1 = affine gap-free fast path).
 constexpr int NQUEUE = 2 * NCLASS;
 // Persistent CTAs per SM a class kernel can keep resident.
-int class_blocks_per_sm(int affine, int cls, int variant);
-// Bytes of direction slab one CTA of a class needs for pairs up to maxmn = m + n.
-long long class_slab_bytes(int affine, int cls, int maxmn);
+int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant);
+// Bytes of direction slab one pipeline of a class needs for pairs up to
+// maxmn = m + n.
+long long class_slab_bytes(const Ladder& lad, int affine, int cls, int maxmn);
 
 void launch_prep(const BatchArgs& a, cudaStream_t s);
 // Longest-first order of the pairs (by len(a) * len(b)) into `order`.
@@ -69,7 +71,7 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
 // path); d_strides[c] = slab bytes per pipeline of class c.
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
 // Pipelines per CTA of a class launch.
-int class_pipes_per_cta(int affine, int cls);
+int class_pipes_per_cta(const Ladder& lad, int cls);
 // Column-wise medians of already aligned pairs (ancestor_2 / with-gaps / worst).
 void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
                             int len, uint8_t* anc, uint8_t* mwg, int* out3,

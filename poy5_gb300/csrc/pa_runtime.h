@@ -48,7 +48,8 @@ struct poyalgn_ctx {
     int device = 0;
     int nsm = 0;
     cudaStream_t stream = nullptr;
-    int bps[2][pa::NCLASS][2] = {};
+    pa::Ladder lad[2] = {pa::default_ladder(0), pa::default_ladder(1)};
+    int bps[2][pa::NCLASS][2] = {};  // resident CTAs per SM: [affine][class][variant]
     // host-pointer batches: staging of inputs and outputs
     pa::DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
     // per-batch scratch

@@ -46,3 +46,14 @@ def test_python_layer_fails_loudly_without_gpu():
     import poy5_gb300 as pg
     with pytest.raises(pg.PoyAlgnError):
         pg.Context(0)
+
+
+def test_candidate_ladders_are_valid():
+    from poy5_gb300 import tune
+    for affine in (False, True):
+        cands = tune.candidate_ladders(affine)
+        assert cands[0] == tune.default_ladder(affine)
+        assert all(tune.ladder_valid(P, R, affine) for P, R in cands)
+    assert not tune.ladder_valid([4] * 9 + [3], [2] * 10, True)
+    assert not tune.ladder_valid([512] + [4] * 9, [4] * 10, True)   # capacity drops
+    assert not tune.ladder_valid([4] * 10, [8] * 10, True)          # affine R <= 4
