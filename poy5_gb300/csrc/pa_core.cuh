@@ -222,16 +222,17 @@ PA_HD long long dm_index(int P, int R, int i, int j)
 
 template <int R>
 struct LinLane {
-    int V[R], Vp[R];        // cost at steps T-1, T-2 of each row
-    uint32_t N[R], Np[R];   // forward gap counts (#ins | #del << 16)
+    int V0[R], V1[R];       // cost of each row at two consecutive steps
+    uint32_t N0[R], N1[R];  // forward gap counts (#ins | #del << 16), same steps
     int J[R], G[R];         // column symbol s2[j] and its insert cost
-    int rb[R], dc[R];       // cost-row offset and delete cost of the row symbol
-    int ic[R];
+    int rb[R], dc[R], tl[R];// cost-row offset, delete and tail cost of the row symbol
+    int Ts[R], Te[R];       // first / last step of each row (Ts > Te: no cell)
+    int hr;                 // bit q: row q has a right border (no DELETE at Te)
+    int R0, R1;             // neighbour's bottom row, two consecutive steps
+    uint32_t RN0, RN1;
+    int G0, G1;             // row 0 (lane 0 of the first block)
     int itop;               // first row of the current block
     int nstart;             // step at which the lane moves to its next block
-    int sV, sVp;            // neighbour bottom row at T-1 / T-2
-    uint32_t sN, sNp;
-    int gV, gVp;            // row-0 generator (lane 0, first block)
 };
 
 PA_HD int block_start_step_lin(const LinBand& b, int itop)
@@ -244,13 +245,18 @@ PA_HD void lin_enter_block(LinLane<R>& L, const LinBand& b, const Tables& t,
                            const uint8_t* s1, int itop, int P)
 {
     L.itop = itop;
+    L.hr = 0;
 #pragma unroll
     for (int q = 0; q < R; q++) {
-        int i = itop + q;
-        int c = i <= b.m - 1 ? s1[i] : 0;
-        L.ic[q] = c;
+        const int i = itop + q;
+        const bool real = i <= b.m - 1;
+        const int c = real ? s1[i] : 0;
         L.rb[q] = t.rowoff[c];
         L.dc[q] = t.csw[t.rowoff[c] + t.gap];
+        L.tl[q] = t.tail[c];
+        L.Ts[q] = real ? i + lin_s(b, i) : 0x7fffffff;
+        L.Te[q] = real ? i + lin_e(b, i) : -1;
+        L.hr |= (real && lin_hasR(b, i)) ? 1 << q : 0;
     }
     L.nstart = block_start_step_lin(b, itop + P * R);
 }
@@ -261,42 +267,60 @@ PA_HD void lin_lane_init(LinLane<R>& L, const LinBand& b, const Tables& t,
 {
 #pragma unroll
     for (int q = 0; q < R; q++) {
-        L.V[q] = L.Vp[q] = 0;
-        L.N[q] = L.Np[q] = 0;
+        L.V0[q] = L.V1[q] = 0;
+        L.N0[q] = L.N1[q] = 0;
         L.J[q] = 0;
         L.G[q] = 0;
     }
-    L.sV = L.sVp = L.gV = L.gVp = 0;
-    L.sN = L.sNp = 0;
+    L.R0 = L.R1 = L.G0 = L.G1 = 0;
+    L.RN0 = L.RN1 = 0;
     lin_enter_block(L, b, t, s1, 1 + g * R, P);
 }
 
-// One anti-diagonal step of one lane. recvV/recvN: bottom row of lane g-1
-// after step T-1. dcode[q] receives the direction code of row q (0 when the
-// row has no cell in the band at this step).
-template <int R>
-PA_HD void lin_step(LinLane<R>& L, const LinBand& b, const Tables& t,
-                    const uint8_t* s1, const uint8_t* s2, int P, int T,
-                    int recvV, uint32_t recvN, int (&dcode)[R])
+// Steps during which lane 0 still generates row 0 (its first block), rounded
+// up to an even count so the step loop's register-set pairing is kept.
+PA_HD int lin_gen_steps(const LinBand& b, int P, int R)
 {
-    L.sVp = L.sV;
-    L.sNp = L.sN;
-    L.sV = recvV;
-    L.sN = recvN;
+    const long long s = block_start_step_lin(b, 1 + P * R);
+    const long long t = s > 0x7ffffff0LL ? 0x7ffffff0LL : s;
+    return (int)((t + 1) & ~1LL);
+}
+
+// One anti-diagonal step of one lane (algn_fill_row and its border variants,
+// src/algn.c:458-730). VC/NC/RC/RNC/GC hold step T-1, VP/NP/RP/RNP/GP step
+// T-2; the step overwrites the latter, which become the caller's "T-1" set
+// of the next step. recvV/recvN: bottom row of lane g-1 after step T-1.
+// Each cell is the minimum of its candidates with the flags of every
+// candidate equal to it (the reference's strict/equal comparison chains):
+//  * column 0: DELETE only, costing the tail (band) or the gap cost (full);
+//  * left border (j = s > 0): no INSERT; right border: no DELETE;
+//  * last column without right border: the tail DELETE joins the DELETE
+//    candidate (algn_fill_last_column).
+// GEN = false promises that lane 0 has left its first block.
+template <int R, bool GEN>
+PA_HD void lin_step(LinLane<R>& L, int (&VC)[R], int (&VP)[R], uint32_t (&NC)[R],
+                    uint32_t (&NP)[R], int& RC, int& RP, uint32_t& RNC, uint32_t& RNP,
+                    int& GC, int& GP, const LinBand& b, const Tables& t, const uint8_t* s1,
+                    const uint8_t* s2, int P, int T, int recvV, uint32_t recvN,
+                    int (&dcode)[R])
+{
+    constexpr int BIG = 0x3fffffff;
+    RP = recvV;
+    RNP = recvN;
     const bool moved = (T >= L.nstart);
     if (moved) lin_enter_block(L, b, t, s1, L.itop + P * R, P);
-    const bool gen = (L.itop == 1);
+    const bool gen = GEN && (L.itop == 1);
     if (gen) {  // row 0 at column T-1: prefix sums of the prepend costs
-        int j0 = T - 1;
-        L.gVp = L.gV;
-        if (j0 == 0) L.gV = 0;
-        else if (j0 < b.first) L.gV += t.prepend[s2[j0]];
+        const int j0 = T - 1;
+        if (j0 == 0) GP = 0;
+        else if (j0 < b.first) GP = GC + t.prepend[s2[j0]];
+        else GP = GC;
     }
     if (moved) {  // a new block: every row needs its own column
 #pragma unroll
         for (int q = 0; q < R; q++) {
-            int j = T - L.itop - q;
-            int c = (j >= 0 && j < b.n) ? s2[j] : 0;
+            const int j = T - L.itop - q;
+            const int c = (j >= 0 && j < b.n) ? s2[j] : 0;
             L.J[q] = c;
             L.G[q] = tcost(t, t.gap, c);
         }
@@ -306,78 +330,47 @@ PA_HD void lin_step(LinLane<R>& L, const LinBand& b, const Tables& t,
             L.J[q] = L.J[q - 1];
             L.G[q] = L.G[q - 1];
         }
-        int j = T - L.itop;
-        int c = (j >= 0 && j < b.n) ? s2[j] : 0;
+        const int j = T - L.itop;
+        const int c = (j >= 0 && j < b.n) ? s2[j] : 0;
         L.J[0] = c;
         L.G[0] = tcost(t, t.gap, c);
     }
 #pragma unroll
     for (int q = R - 1; q >= 0; q--) {
-        const int i = L.itop + q;
-        const int j = T - i;
         int upV, dgV;
         uint32_t upN, dgN;
         if (q > 0) {
-            upV = L.V[q - 1]; upN = L.N[q - 1];
-            dgV = L.Vp[q - 1]; dgN = L.Np[q - 1];
+            upV = VC[q - 1]; upN = NC[q - 1];
+            dgV = VP[q - 1]; dgN = NP[q - 1];
         } else if (gen) {
-            upV = L.gV; upN = (uint32_t)(T - 1);
-            dgV = L.gVp; dgN = (uint32_t)(T - 2);
+            upV = GP; upN = (uint32_t)(T - 1);
+            dgV = GC; dgN = (uint32_t)(T - 2);
         } else {
-            upV = L.sV; upN = L.sN;
-            dgV = L.sVp; dgN = L.sNp;
+            upV = RP; upN = RNP;
+            dgV = RC; dgN = RNC;
         }
-        const int lfV = L.V[q];
-        const uint32_t lfN = L.N[q];
-        L.Vp[q] = L.V[q];
-        L.Np[q] = L.N[q];
         dcode[q] = 0;
-        if (i <= b.m - 1) {
-            const int hasL = lin_hasL(b, i), hasR = lin_hasR(b, i);
-            const int s = hasL ? i - b.newk : 0;
-            const int e = hasR ? i + b.D + b.newk : b.n - 1;
-            if (j >= s && j <= e) {
-                int v, d;
-                const int ic = L.ic[q];
-                if (j == 0) {
-                    v = upV + (b.full ? L.dc[q] : t.tail[ic]);
-                    d = L_DELETE;
-                } else {
-                    const int aln = dgV + t.csw[L.rb[q] + L.J[q]];
-                    if (hasL && j == s) {
-                        if (hasR && e == s) {
-                            v = aln;
-                            d = L_ALIGN;
-                        } else {
-                            const int del = upV + L.dc[q];
-                            if (del < aln) { v = del; d = L_DELETE; }
-                            else if (aln < del) { v = aln; d = L_ALIGN; }
-                            else { v = del; d = L_ALIGN | L_DELETE; }
-                        }
-                    } else if (hasR && j == e) {
-                        const int ins = lfV + L.G[q];
-                        if (ins < aln) { v = ins; d = L_INSERT; }
-                        else if (aln < ins) { v = aln; d = L_ALIGN; }
-                        else { v = aln; d = L_ALIGN | L_INSERT; }
-                    } else {
-                        const int del = upV + L.dc[q];
-                        const int ins = lfV + L.G[q];
-                        v = tmin(tmin(aln, ins), del);
-                        d = (aln == v ? L_ALIGN : 0) | (ins == v ? L_INSERT : 0) |
-                            (del == v ? L_DELETE : 0);
-                    }
-                }
-                if (!hasR && j == b.n - 1 && j > 0) {  // last column: tail delete
-                    const int cst = t.tail[ic] + upV;
-                    if (cst < v) { v = cst; d = L_DELETE; }
-                    else if (cst == v) d |= L_DELETE;
-                }
-                // forward gap count along the path backtrace_2d_gaps follows
-                const uint32_t cn = (d & L_ALIGN) ? dgN : (d & L_INSERT) ? lfN + 1u : upN + 0x10000u;
-                L.V[q] = v;
-                L.N[q] = cn;
-                dcode[q] = d;
-            }
+        if (T >= L.Ts[q] && T <= L.Te[q]) {
+            const int i = L.itop + q;
+            const bool c0 = (T == i);
+            const bool hasR = (L.hr >> q) & 1;
+            const bool lft = (T == L.Ts[q]) && !c0;
+            const bool edge = (T == L.Te[q]);
+            const int dlc = c0 ? (b.full ? L.dc[q] : L.tl[q]) : L.dc[q];
+            const int aln = c0 ? BIG : dgV + t.csw[L.rb[q] + L.J[q]];
+            const int ins = (c0 || lft) ? BIG : VC[q] + L.G[q];
+            int del = (edge && hasR) ? BIG : upV + dlc;
+            if (edge && !hasR && !c0) del = tmin(del, upV + L.tl[q]);
+            const int v = tmin(tmin(aln, ins), del);
+            const int d = (aln == v ? L_ALIGN : 0) | (ins == v ? L_INSERT : 0) |
+                          (del == v ? L_DELETE : 0);
+            // forward gap count along the path backtrace_2d_gaps follows
+            NP[q] = (d & L_ALIGN) ? dgN : (d & L_INSERT) ? NC[q] + 1u : upN + 0x10000u;
+            VP[q] = v;
+            dcode[q] = d;
+        } else {
+            VP[q] = VC[q];  // keep the row's last state (read as diag/left)
+            NP[q] = NC[q];
         }
     }
 }

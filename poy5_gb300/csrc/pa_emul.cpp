@@ -26,22 +26,38 @@ void lin_pass(const LinBand& b, int P, const Tables& t, const uint8_t* x,
     std::vector<int> sv(P);
     std::vector<uint32_t> sn(P);
     const int Tlast = (b.m - 1) + (b.n - 1);
+    // row 0 is generated only up to step Tg, as in the kernel
+    const int Tg = tmin((Tlast + 1) & ~1, lin_gen_steps(b, P, R));
     for (int T = 1; T <= Tlast; T++) {
+        const bool odd = T & 1;
         for (int g = 0; g < P; g++) {
-            sv[g] = L[g].V[R - 1];
-            sn[g] = L[g].N[R - 1];
+            sv[g] = odd ? L[g].V0[R - 1] : L[g].V1[R - 1];
+            sn[g] = odd ? L[g].N0[R - 1] : L[g].N1[R - 1];
         }
         for (int g = 0; g < P; g++) {
-            int src = (g + P - 1) % P;
+            const int src = (g + P - 1) % P;
             int dc[R];
-            lin_step<R>(L[g], b, t, x, y, P, T, sv[src], sn[src], dc);
+            LinLane<R>& l = L[g];
+            if (odd && T <= Tg)
+                lin_step<R, true>(l, l.V0, l.V1, l.N0, l.N1, l.R0, l.R1, l.RN0, l.RN1, l.G0,
+                                  l.G1, b, t, x, y, P, T, sv[src], sn[src], dc);
+            else if (odd)
+                lin_step<R, false>(l, l.V0, l.V1, l.N0, l.N1, l.R0, l.R1, l.RN0, l.RN1, l.G0,
+                                   l.G1, b, t, x, y, P, T, sv[src], sn[src], dc);
+            else if (T <= Tg)
+                lin_step<R, true>(l, l.V1, l.V0, l.N1, l.N0, l.R1, l.R0, l.RN1, l.RN0, l.G1,
+                                  l.G0, b, t, x, y, P, T, sv[src], sn[src], dc);
+            else
+                lin_step<R, false>(l, l.V1, l.V0, l.N1, l.N0, l.R1, l.R0, l.RN1, l.RN0, l.G1,
+                                   l.G0, b, t, x, y, P, T, sv[src], sn[src], dc);
             for (int q = 0; q < R; q++) dm[(long long)T * P * R + g * R + q] = (uint8_t)dc[q];
         }
     }
     const int i = b.m - 1;
     const int blk = (i - 1) / R, g = blk % P, q = (i - 1) - blk * R;
-    *cost = L[g].V[q];
-    const uint32_t N = L[g].N[q];
+    const bool odd = Tlast & 1;
+    *cost = odd ? L[g].V1[q] : L[g].V0[q];
+    const uint32_t N = odd ? L[g].N1[q] : L[g].N0[q];
     *gapnum = tmax((int)(N & 0xFFFF), (int)(N >> 16));
 }
 

@@ -232,15 +232,13 @@ __device__ void lin_fill(const LinBand& b, const Tables& st, const uint8_t* x,
                          int& cost, int& gapnum)
 {
     LinLane<R> L;
-    L.V[R - 1] = 0;
-    L.N[R - 1] = 0;
+    L.V0[R - 1] = L.V1[R - 1] = 0;
+    L.N0[R - 1] = L.N1[R - 1] = 0;
     if (active) lin_lane_init(L, b, st, x, p.gl, p.P);
     const int Tlast = active ? (b.m - 1) + (b.n - 1) : 0;
-    for (int T = 1; T <= Tmax; T++) {
-        const int sv = L.V[R - 1];
-        const uint32_t sn = L.N[R - 1];
-        int rv = rot_prev(p, sv);
-        uint32_t rn = rot_prev(p, sn);
+    auto exchange = [&](int sv, uint32_t sn, int T, int& rv, uint32_t& rn) {
+        rv = rot_prev(p, sv);
+        rn = rot_prev(p, sn);
         if (p.K > 1) {
             if (p.lane == 31) {
                 xv[T & 1][p.warp] = sv;
@@ -253,22 +251,51 @@ __device__ void lin_fill(const LinBand& b, const Tables& st, const uint8_t* x,
                 rn = xn[T & 1][w];
             }
         }
-        if (active && T <= Tlast) {
-            int dc[R];
-            lin_step<R>(L, b, st, x, y, p.P, T, rv, rn, dc);
-            store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+    };
+    // two steps per iteration: set 0 -> 1 at odd T, set 1 -> 0 at even T
+    auto steps = [&](auto gen, int T0, int T1) {
+        constexpr bool GEN = decltype(gen)::value;
+        for (int T = T0; T <= T1; T += 2) {
+            {
+                int rv;
+                uint32_t rn;
+                exchange(L.V0[R - 1], L.N0[R - 1], T, rv, rn);
+                if (active && T <= Tlast) {
+                    int dc[R];
+                    lin_step<R, GEN>(L, L.V0, L.V1, L.N0, L.N1, L.R0, L.R1, L.RN0, L.RN1,
+                                     L.G0, L.G1, b, st, x, y, p.P, T, rv, rn, dc);
+                    store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+                }
+            }
+            if (T + 1 <= Tmax) {
+                int rv;
+                uint32_t rn;
+                exchange(L.V1[R - 1], L.N1[R - 1], T + 1, rv, rn);
+                if (active && T + 1 <= Tlast) {
+                    int dc[R];
+                    lin_step<R, GEN>(L, L.V1, L.V0, L.N1, L.N0, L.R1, L.R0, L.RN1, L.RN0,
+                                     L.G1, L.G0, b, st, x, y, p.P, T + 1, rv, rn, dc);
+                    store_u8<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
+                }
+            }
         }
-    }
+    };
+    // lane 0 generates row 0 only while in its first block (both bounds even)
+    const int tg = group_max(p, active ? lin_gen_steps(b, p.P, R) : 0);
+    const int Tg = tmin((Tmax + 1) & ~1, tg);
+    steps(std::true_type{}, 1, Tg - 1);
+    steps(std::false_type{}, (Tg & ~1) + 1, Tmax);
     // the lane owning the corner row reports cost and gap count
     const int i = active ? b.m - 1 : 1;
     const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
+    const bool odd = (Tlast & 1) != 0;  // odd last step wrote set 1
     int v = 0;
     uint32_t nn = 0;
 #pragma unroll
     for (int r = 0; r < R; r++)
         if (r == oq) {
-            v = L.V[r];
-            nn = L.N[r];
+            v = odd ? L.V1[r] : L.V0[r];
+            nn = odd ? L.N1[r] : L.N0[r];
         }
     if (p.K == 1) {
         v = from_lane(p, v, og);
