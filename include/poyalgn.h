@@ -223,6 +223,40 @@ int poyalgn_median_batch_device_noalloc(const poyalgn_cm *cm, int npairs,
                                         uint8_t *med, uint8_t *mwg, int32_t *passes,
                                         void *stream);
 
+/* ---- cost-only scoring (SeqCS.DOS.distance) ---------------------------------- */
+
+/*
+ * algn_CAML_cost_affine_3 (src/algn.c:2456-2515): cost of the full unbanded
+ * affine fill without traceback (algn_fill_plane_3_aff_nobt,
+ * src/algn.c:1986-2110), the shorter sequence down the rows. This is the
+ * cost SeqCS.DOS.distance reports under affine gap costs; it can differ from
+ * the banded poyalgn_align_affine_3 cost, as in POY.
+ */
+int poyalgn_cost_affine_3(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                          const uint8_t *si, int li, const uint8_t *sj, int lj,
+                          int32_t *cost);
+
+/*
+ * SeqCS.DOS.distance (src/seqCS.ml:701-774, Algn_Normal) of many pairs:
+ * pairs in which either sequence is all gaps (Sequence.is_empty) cost
+ * missing_distance; otherwise the affine model runs algn_CAML_cost_affine_3
+ * and the linear model Align.cost_2 ~deltaw:(max 8 |la - lb|)
+ * (src/sequence.ml:868-925) -> algn_CAML_simple_2's band doubling, without
+ * traceback. Layout as poyalgn_median_batch; per-pair cost and status.
+ * The _device form takes device pointers and a stream and only enqueues.
+ */
+int poyalgn_distance_batch(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
+                           const uint8_t *seqs, const int64_t *offa,
+                           const int32_t *lena, const int64_t *offb,
+                           const int32_t *lenb, int32_t missing_distance,
+                           int32_t *cost, int32_t *status);
+int poyalgn_distance_batch_device(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                                  int npairs, int max_pair_len,
+                                  const uint8_t *seqs, const int64_t *offa,
+                                  const int32_t *lena, const int64_t *offb,
+                                  const int32_t *lenb, int32_t missing_distance,
+                                  int32_t *cost, int32_t *status, void *stream);
+
 /* ---- device-resident sequences and the tree downpass ------------------------ */
 
 /*

@@ -5,13 +5,13 @@ The compute path is the CUDA library ``libpoyalgn.so`` built from
 host-side interface.
 """
 from .align import (Align, BatchResult, Context, CostMatrix, DOSMedian, PackedPairs,
-                    PoyAlgnError, count_gaps, deltaw_calc, dos_median, encode,
-                    median_batch, pack_pairs)
+                    PoyAlgnError, count_gaps, deltaw_calc, distance_batch, dos_median,
+                    encode, median_batch, pack_pairs)
 from .serve import ReplayResult, Reply, Server, Trace, poisson_trace
 from .tree import DownpassResult, Store, downpass, tree_levels
 
 __all__ = ["Align", "BatchResult", "Context", "CostMatrix", "DOSMedian", "PackedPairs",
            "PoyAlgnError", "count_gaps", "deltaw_calc", "dos_median", "encode",
-           "median_batch", "pack_pairs", "DownpassResult", "Store", "downpass",
+           "median_batch", "pack_pairs", "distance_batch", "DownpassResult", "Store", "downpass",
            "tree_levels", "ReplayResult", "Reply", "Server", "Trace", "poisson_trace"]
 __version__ = "0.1.0"

@@ -280,6 +280,14 @@ class Align:
     def median_2_with_gaps(self, a, b, cm: CostMatrix) -> np.ndarray:
         return self._aligned(a, b, cm)[1]
 
+    def cost_affine_3(self, si, sj, cm: CostMatrix) -> int:
+        """algn_CAML_cost_affine_3: full unbanded affine cost, no traceback."""
+        si, sj = _u8(si), _u8(sj)
+        c = C.c_int32()
+        check(_lib.load().poyalgn_cost_affine_3(self.ctx.handle, cm.handle, _ptr(si), len(si),
+                                                _ptr(sj), len(sj), C.byref(c)))
+        return c.value
+
     def max_cost_2(self, a, b, cm: CostMatrix) -> int:
         a, b = _u8(a), _u8(b)
         if np.all(a == cm.gap) or np.all(b == cm.gap):
@@ -382,6 +390,20 @@ def pack_pairs(pairs) -> PackedPairs:
     if len(lena) > 1:
         out_off[1:] = np.cumsum(cap)[:-1]
     return PackedPairs(seqs, offa, lena, offb, lenb, out_off, cap)
+
+
+def distance_batch(ctx: Context, cm: CostMatrix, pairs, missing_distance: int = 0):
+    """SeqCS.DOS.distance of many pairs; returns (cost, status) arrays."""
+    pk = pairs if isinstance(pairs, PackedPairs) else pack_pairs(pairs)
+    n = pk.npairs
+    cost = np.zeros(n, np.int32)
+    status = np.zeros(n, np.int32)
+    rc = _lib.load().poyalgn_distance_batch(
+        ctx.handle, cm.handle, n, _ptr(pk.seqs), _ptr(pk.offa), _ptr(pk.lena), _ptr(pk.offb),
+        _ptr(pk.lenb), int(missing_distance), _ptr(cost), _ptr(status))
+    if rc not in (0, _lib.EPAIR):
+        check(rc)
+    return cost, status
 
 
 def median_batch(ctx: Context, cm: CostMatrix, pairs) -> BatchResult:

@@ -11,6 +11,7 @@
 #include <new>
 #include <vector>
 
+#include "pa_cost.h"
 #include "pa_runtime.h"
 
 using namespace pa;
@@ -68,7 +69,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
               const int* lenb, const long long* out_off, int* cost, int* maxcost,
               int* alen, int* mlen, int* wlen, int* status, uint8_t* ea,
               uint8_t* eb, uint8_t* med, uint8_t* mwg, int* passes,
-              const int* dwh, const int* swp, int do_traceback, cudaStream_t st)
+              const int* dwh, const int* swp, int do_traceback, cudaStream_t st,
+              int distance, int missing_distance)
 {
     int rc;
     if (npairs <= 0) return 0;
@@ -119,6 +121,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.npairs = npairs;
     A.affine = affine;
     A.do_traceback = do_traceback;
+    A.distance = distance;
+    A.missing_distance = missing_distance;
     A.lad = c->lad[affine];
     A.tables = cm->d;
     A.pfull = as<int>(c->pfull);
@@ -190,6 +194,49 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
     if ((rc = reserve(c->order_scratch, order_scratch_bytes((int)n)))) return rc;
     if ((rc = reserve(c->slab, (size_t)slab_bytes))) return rc;
+    return 0;
+}
+
+// Enqueue the cost-only affine fill of npairs pairs (device pointers).
+// min_len bounds the shorter length of every pair.
+int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
+             const uint8_t* seqs, const long long* offa, const int* lena,
+             const long long* offb, const int* lenb, int missing, int* cost, int* status,
+             cudaStream_t st)
+{
+    int rc;
+    if (npairs <= 0) return 0;
+    const int per_sm = std::max(1, nobt_blocks_per_sm());
+    const int grid = std::max(1, std::min(c->nsm * per_sm,
+                                          (npairs + nobt_warps_per_cta() - 1) / nobt_warps_per_cta()));
+    const int stride = std::max(min_len, 1);
+    const size_t warps = (size_t)grid * nobt_warps_per_cta();
+    if ((rc = reserve(c->nobt_bnd, warps * (size_t)stride * sizeof(int4)))) return rc;
+    if ((rc = reserve(c->nobt_ctr, sizeof(int)))) return rc;
+    if ((rc = reserve(c->order, (size_t)npairs * 4))) return rc;
+    if ((rc = reserve(c->order_scratch, order_scratch_bytes(npairs)))) return rc;
+    CU(cudaMemsetAsync(c->nobt_ctr.p, 0, sizeof(int), st));
+    if (launch_order(lena, lenb, npairs, as<int>(c->order), c->order_scratch.p, st) != 0)
+        return set_err(POYALGN_ECUDA, "ordering pairs failed");
+    NobtArgs A;
+    memset(&A, 0, sizeof(A));
+    A.seqs = seqs;
+    A.offa = offa;
+    A.lena = lena;
+    A.offb = offb;
+    A.lenb = lenb;
+    A.npairs = npairs;
+    A.tables = cm->d;
+    A.order = as<int>(c->order);
+    A.missing_distance = missing;
+    A.next = as<int>(c->nobt_ctr);
+    A.bnd = as<int4>(c->nobt_bnd);
+    A.bnd_stride = stride;
+    A.cost = cost;
+    A.status = status;
+    launch_nobt(A, grid, st);
+    CU(cudaGetLastError());
+    c->last_launches = 3;
     return 0;
 }
 
@@ -339,7 +386,8 @@ void poyalgn_free(poyalgn_ctx* c)
     DevBuf* bufs[] = {&c->seqs, &c->offa, &c->lena, &c->offb, &c->lenb, &c->outoff,
                       &c->ints, &c->bytes, &c->pfull, &c->eh0, &c->lastcls, &c->slabcta,
                       &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
-                      &c->dwh, &c->swp, &c->order, &c->order_scratch};
+                      &c->dwh, &c->swp, &c->order, &c->order_scratch, &c->nobt_bnd,
+                      &c->nobt_ctr};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
@@ -654,6 +702,95 @@ int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
 }
 
 int poyalgn_num_classes(void) { return NCLASS; }
+
+int poyalgn_cost_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* si, int li,
+                          const uint8_t* sj, int lj, int32_t* cost)
+{
+    if (!ctx || !cm || !si || !sj || !cost || li < 1 || lj < 1)
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (cm->h.cost_model != 1) return set_err(POYALGN_EINVAL, "cost matrix is not affine");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    if ((rc = stage_pair(ctx, si, li, sj, lj))) return rc;
+    int* I = as<int>(ctx->ints);
+    if ((rc = run_nobt(ctx, cm, 1, std::min(li, lj), as<uint8_t>(ctx->seqs),
+                       as<long long>(ctx->offa), as<int>(ctx->lena), as<long long>(ctx->offa) + 1,
+                       as<int>(ctx->lena) + 1, NOBT_NO_MISSING, I, I + 1, ctx->stream)))
+        return rc;
+    int h[2];
+    CU(cudaMemcpyAsync(h, I, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (h[1] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[1]);
+    *cost = h[0];
+    return 0;
+}
+
+int poyalgn_distance_batch_device(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
+                                  int max_pair_len, const uint8_t* seqs, const int64_t* offa,
+                                  const int32_t* lena, const int64_t* offb, const int32_t* lenb,
+                                  int32_t missing_distance, int32_t* cost, int32_t* status,
+                                  void* stream)
+{
+    if (!ctx || !cm) return set_err(POYALGN_EINVAL, "null argument");
+    if (npairs < 0 || max_pair_len < 2) return set_err(POYALGN_EINVAL, "bad batch shape");
+    if (npairs == 0) return 0;
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    const long long* oa = reinterpret_cast<const long long*>(offa);
+    const long long* ob = reinterpret_cast<const long long*>(offb);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cm->h.cost_model == 1)
+        return run_nobt(ctx, cm, npairs, max_pair_len / 2, seqs, oa, lena, ob, lenb,
+                        missing_distance, cost, status, st);
+    return run_batch(ctx, cm, 0, npairs, max_pair_len, 1, seqs, oa, lena, ob, lenb, nullptr,
+                     cost, nullptr, nullptr, nullptr, nullptr, status, nullptr, nullptr, nullptr,
+                     nullptr, nullptr, nullptr, nullptr, 0, st, 1, missing_distance);
+}
+
+int poyalgn_distance_batch(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
+                           const uint8_t* seqs, const int64_t* offa, const int32_t* lena,
+                           const int64_t* offb, const int32_t* lenb, int32_t missing_distance,
+                           int32_t* cost, int32_t* status)
+{
+    if (!ctx || !cm || (npairs > 0 && (!seqs || !offa || !lena || !offb || !lenb || !cost ||
+                                       !status)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (npairs <= 0) return 0;
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    long long seq_bytes = 0;
+    int maxmn = 2;
+    for (int k = 0; k < npairs; k++) {
+        if (lena[k] < 1 || lenb[k] < 1) return set_err(POYALGN_EINVAL, "pair %d: empty sequence", k);
+        seq_bytes = std::max<long long>(seq_bytes, std::max(offa[k] + lena[k], offb[k] + lenb[k]));
+        maxmn = std::max(maxmn, lena[k] + lenb[k]);
+    }
+    const size_t ni = (size_t)npairs;
+    if ((rc = reserve(ctx->seqs, (size_t)seq_bytes))) return rc;
+    if ((rc = reserve(ctx->offa, ni * 8))) return rc;
+    if ((rc = reserve(ctx->offb, ni * 8))) return rc;
+    if ((rc = reserve(ctx->lena, ni * 4))) return rc;
+    if ((rc = reserve(ctx->lenb, ni * 4))) return rc;
+    if ((rc = reserve(ctx->ints, ni * 4 * 2))) return rc;
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(ctx->seqs.p, seqs, (size_t)seq_bytes, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->offa.p, offa, ni * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->offb.p, offb, ni * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->lena.p, lena, ni * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(ctx->lenb.p, lenb, ni * 4, cudaMemcpyHostToDevice, st));
+    int* I = as<int>(ctx->ints);
+    if ((rc = poyalgn_distance_batch_device(
+             ctx, cm, npairs, maxmn, as<uint8_t>(ctx->seqs), as<int64_t>(ctx->offa),
+             as<int>(ctx->lena), as<int64_t>(ctx->offb), as<int>(ctx->lenb), missing_distance, I,
+             I + ni, st)))
+        return rc;
+    CU(cudaMemcpyAsync(cost, I, ni * 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(status, I + ni, ni * 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    for (int k = 0; k < npairs; k++)
+        if (status[k] != 0) return set_err(POYALGN_EPAIR, "pair %d failed with status %d", k, status[k]);
+    return 0;
+}
 
 int poyalgn_set_ladder(poyalgn_ctx* ctx, int affine, const int32_t* P, const int32_t* R)
 {

@@ -1050,6 +1050,28 @@ PA_HD PairPlan plan_linear(const Tables& t, int gaps_a, int la, int gaps_b, int 
     return p;
 }
 
+// SeqCS.DOS.distance (src/seqCS.ml:738-751) -> Sequence.Align.cost_2
+// ~deltaw:(max 8 |la - lb|) (src/sequence.ml:868-925, the Some branch of
+// deltaw_calc) feeding algn_nw_limit.
+PA_HD PairPlan plan_linear_distance(const Tables& t, int gaps_a, int la, int gaps_b, int lb)
+{
+    PairPlan p;
+    p.swaped = la <= lb ? 0 : 1;
+    p.m = p.swaped ? lb : la;
+    p.n = p.swaped ? la : lb;
+    const int v = tmax(8, p.n - p.m);
+    const int lower = p.m / 10;
+    const int dw = (p.m - p.n) < lower ? lower : v;
+    const int deltawh = tmax(gaps_a, gaps_b) + dw;
+    int height = (p.m - p.n) + 50 + deltawh;
+    if (height > p.m) height = p.m;
+    if (2LL * p.m >= 3LL * p.n) p.full = 1;
+    else if (2 * height < p.m) p.full = 0;
+    else p.full = (8 >= p.m - height) ? 1 : 0;
+    p.T0 = (p.n - p.m + 1) * t.mnz;
+    return p;
+}
+
 // algn_nw called directly with s1 = a, s2 = b and the caller's deltawh
 // (the algn_CAML_simple_2 external): no reordering.
 PA_HD PairPlan plan_linear_deltawh(const Tables& t, int la, int lb, int deltawh)

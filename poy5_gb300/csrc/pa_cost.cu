@@ -1,0 +1,377 @@
+// Cost-only affine alignment: algn_CAML_cost_affine_3 (src/algn.c:2456-2515)
+// -> algn_fill_plane_3_aff_nobt (src/algn.c:1986-2110), the full unbanded
+// four-state fill SeqCS.DOS.distance uses for affine cost models.
+//
+// One warp per pair. The columns are cut into blocks of 32 * K; each lane
+// keeps the previous row of its K columns in registers, so a block sweeps
+// all rows with no memory traffic but its left boundary column (one int4 per
+// row, written by the previous block). Within a row, EV, EB and CB depend on
+// the previous row only; the horizontal state EH[j] = min(EH[j-1] + x_j, t_j)
+// is a min-plus recurrence, solved per row by composing each lane's K maps
+// and an inclusive warp scan of the compositions.
+//
+// The reference keeps its rows in one buffer whose current and previous rows
+// overlap by a few words (the previous row starts lenj + 2 ints after the
+// current one, arrays of 2 * largest ints). For lenj >= 2 the only effect is
+// that every even row writes HIGH into the previous row's EV[lenj] and
+// CB[lenj] before reading them; sequences of at most 2 positions are replayed
+// word for word instead.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pa_cost.h"
+
+namespace pa {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int BIG = 1 << 29;  // "no path" inside a composed map; + HIGH stays < 2^31
+
+__device__ __forceinline__ int gap_open_cost(int idx, int prev, int curr, int gap, int go)
+{
+    if (idx == 1 && (gap & curr)) return 0;
+    if (idx > 1 && !(gap & prev) && (gap & curr)) return 0;
+    return go;
+}
+
+// The reference's buffer, word for word, for sequences of at most 2 positions.
+__device__ int nobt_tiny(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj)
+{
+    const int gap = t.gap, go = t.go;
+    const int largest = lj;
+    const int leni = li - 1, lenj = lj - 1;
+    const int off = lenj + 2;
+    int mat[12 * 2 + 4];
+    for (int k = 0; k < 12 * largest + 4; k++) mat[k] = 0;
+    int cb = 0, eb = 2 * largest, ev = 4 * largest, eh = 6 * largest;
+    const int gopc = 10 * largest, shx = 11 * largest;
+    mat[cb] = 0;
+    mat[eb] = HIGH;
+    mat[eh] = go;
+    mat[ev] = go;
+    for (int j = 1; j <= lenj; j++) {
+        mat[eh + j] = mat[eh + j - 1] + t.prepend[sj[j]];
+        mat[cb + j] = HIGH;
+        mat[eb + j] = HIGH;
+        mat[ev + j] = HIGH;
+    }
+    int peh = eh + off, pev = ev + off, peb = eb + off, pcb = cb + off;
+    mat[shx] = 0;
+    for (int j = 1; j <= lenj; j++) {
+        mat[gopc + j] = gap_open_cost(j, sj[j - 1], sj[j], gap, go);
+        mat[shx + j] = ((sj[j - 1] & gap) && !(sj[j] & gap)) ? mat[gopc + j] + t.prepend[sj[j]]
+                                                               : t.prepend[sj[j]];
+    }
+    if (lenj >= 1) mat[shx + 1] = t.prepend[sj[1]];
+    int ic = si[0];
+    for (int i = 1; i <= leni; i++) {
+        int x;
+        x = peh; peh = eh; eh = x;
+        x = pev; pev = ev; ev = x;
+        x = peb; peb = eb; eb = x;
+        x = pcb; pcb = cb; cb = x;
+        mat[eh] = HIGH;
+        const int ip = ic;
+        ic = si[i];
+        const int sgext = tcost(t, ic, gap);
+        const int sgop = gap_open_cost(i, ip, ic, gap, go);
+        const int sng = ic & NTMPGAP;
+        const int svext = (i > 1 && (ip & gap) && !(ic & gap)) ? sgop + sgext : sgext;
+        const int r = mat[pev] + svext;
+        mat[eh] = HIGH;
+        mat[cb] = r;
+        mat[eb] = HIGH;
+        mat[ev] = r;
+        mat[cb] = HIGH;
+        int jc = sj[0];
+        for (int j = 1; j <= lenj; j++) {
+            const int jp = jc;
+            jc = sj[j];
+            const int jng = jc & NTMPGAP;
+            const int jgr = t.prepend[jc], jgo = mat[gopc + j];
+            mat[eh + j] = tmin(mat[eh + j - 1] + mat[shx + j], mat[cb + j - 1] + jgo + jgr);
+            mat[ev + j] = tmin(mat[pev + j] + svext, mat[pcb + j] + sgop + sgext);
+            const bool flag = (TMPGAP & ic) && (TMPGAP & jc);
+            const bool flag2 = !(TMPGAP & ip) && !(TMPGAP & jp);
+            const int d = flag ? 0 : HIGH;
+            const int od = flag ? (flag2 ? 0 : 2 * go) : HIGH;
+            mat[eb + j] = tmin(mat[peb + j - 1] + d, mat[pcb + j - 1] + od);
+            const int dg = tcost(t, sng, jng);
+            const int xgo = tmax(jgo, sgop);
+            const int a0 = mat[pcb + j - 1] + dg;
+            const int a1 = (ic == sng) ? mat[pev + j - 1] + dg : mat[pev + j - 1] + dg + jgo;
+            const int a2 = (jc == jng) ? mat[peh + j - 1] + dg : mat[peh + j - 1] + dg + sgop;
+            const int a3 = mat[peb + j - 1] + dg + xgo;
+            mat[cb + j] = tmin(tmin(a0, a1), tmin(a2, a3));
+        }
+    }
+    return tmin(tmin(mat[eh + lenj], mat[ev + lenj]), tmin(mat[eb + lenj], mat[cb + lenj]));
+}
+
+// min(x + s, t) maps composed along a row: apply f then g
+struct MinPlus {
+    int s, t;
+};
+__device__ __forceinline__ MinPlus compose(MinPlus f, MinPlus g)
+{
+    return MinPlus{tmin(f.s + g.s, BIG), tmin(tmin(f.t + g.s, BIG), g.t)};
+}
+__device__ __forceinline__ int apply(MinPlus f, int x) { return tmin(x + f.s, f.t); }
+
+// Inclusive scan over the warp: lane l gets f_l o ... o f_0 (f_0 first).
+__device__ __forceinline__ MinPlus warp_scan(MinPlus f, int lane)
+{
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int ps = __shfl_up_sync(FULL, f.s, d);
+        const int pt = __shfl_up_sync(FULL, f.t, d);
+        if (lane >= d) f = compose(MinPlus{ps, pt}, f);
+    }
+    return f;
+}
+
+template <int K>
+__device__ int nobt_warp(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
+                         int4* bnd, int lane)
+{
+    const int gap = t.gap, go = t.go;
+    const int leni = li - 1, lenj = lj - 1;
+    constexpr int W = 32 * K;
+    const int nblk = (lenj + 1 + W - 1) / W;
+    int result = 0;
+    for (int blk = 0; blk < nblk; blk++) {
+        const int c0 = blk * W + lane * K;  // this lane's first column
+        // column constants
+        int jc[K], jgr[K], gop[K], shx[K];
+        unsigned jpgap = 0;  // bit q: sj[j - 1] has the gap bit
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            const int j = c0 + q;
+            const bool real = j <= lenj;
+            const int c = real ? sj[j] : 0;
+            const int cp = (real && j > 0) ? sj[j - 1] : 0;
+            jc[q] = c;
+            jgr[q] = t.prepend[c];
+            gop[q] = (real && j > 0) ? gap_open_cost(j, cp, c, gap, go) : 0;
+            shx[q] = (j > 1 && (cp & gap) && !(c & gap)) ? gop[q] + jgr[q] : jgr[q];
+            jpgap |= (cp & TMPGAP) ? 1u << q : 0u;
+        }
+        // row 0
+        int pEH[K], pEV[K], pEB[K], pCB[K];
+        {
+            MinPlus f{0, BIG};
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const int j = c0 + q;
+                const MinPlus g = j == 0 ? MinPlus{BIG, go} : MinPlus{jgr[q], BIG};
+                f = compose(f, g);
+            }
+            const MinPlus pre = warp_scan(f, lane);
+            MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
+            const int left = blk > 0 ? bnd[0].x : 0;
+            int x = lane == 0 ? left : apply(ex, left);
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const int j = c0 + q;
+                x = j == 0 ? go : x + jgr[q];
+                pEH[q] = x;
+                pEV[q] = j == 0 ? go : HIGH;
+                pEB[q] = HIGH;
+                pCB[q] = j == 0 ? 0 : HIGH;
+            }
+        }
+        const int last_col = tmin(lenj, blk * W + W - 1);
+        const int last_lane = (last_col - blk * W) / K, last_q = (last_col - blk * W) % K;
+        auto write_bnd = [&](int i) {
+#pragma unroll
+            for (int q = 0; q < K; q++)
+                if (lane == last_lane && q == last_q) bnd[i] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
+        };
+        // previous row's value of column c0 - 1 (the diagonal of column c0)
+        int4 dprev = make_int4(HIGH, HIGH, HIGH, HIGH);
+        if (blk > 0 && lane == 0) dprev = bnd[0];
+        __syncwarp();
+        write_bnd(0);
+        int ic = si[0];
+        for (int i = 1; i <= leni; i++) {
+            const int ip = ic;
+            ic = si[i];
+            const int sgext = tcost(t, ic, gap);
+            const int sgop = gap_open_cost(i, ip, ic, gap, go);
+            const int sng = ic & NTMPGAP;
+            const int srow = t.rowoff[sng];
+            const int svext = (i > 1 && (ip & gap) && !(ic & gap)) ? sgop + sgext : sgext;
+            const bool even = (i & 1) == 0 && lenj >= 2;
+            // left neighbour: previous row's last column of lane - 1 (lane 0:
+            // the block boundary of row i - 1) and, for EH, the current row's
+            int4 dg;
+            dg.x = __shfl_up_sync(FULL, pEH[K - 1], 1);
+            dg.y = __shfl_up_sync(FULL, pEV[K - 1], 1);
+            dg.z = __shfl_up_sync(FULL, pEB[K - 1], 1);
+            dg.w = __shfl_up_sync(FULL, pCB[K - 1], 1);
+            int4 lb = make_int4(HIGH, HIGH, HIGH, HIGH);  // block boundary, row i
+            if (lane == 0) {
+                dg = dprev;
+                if (blk > 0) lb = bnd[i];
+                dprev = lb;
+            }
+            int nEV[K], nEB[K], nCB[K];
+            int dEH = dg.x, dEV = dg.y, dEB = dg.z, dCB = dg.w;
+            int jprev = (c0 > 0 && c0 - 1 <= lenj) ? sj[c0 - 1] : 0;
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const int j = c0 + q;
+                const int c = jc[q];
+                const int jng = c & NTMPGAP;
+                const bool lastc = even && j == lenj;
+                const int uEV = lastc ? HIGH : pEV[q], uCB = lastc ? HIGH : pCB[q];
+                if (j == 0) {
+                    nEV[q] = pEV[q] + svext;
+                    nEB[q] = HIGH;
+                    nCB[q] = HIGH;
+                } else {
+                    nEV[q] = tmin(uEV + svext, uCB + sgop + sgext);
+                    const bool flag = (TMPGAP & ic) && (TMPGAP & c);
+                    const bool flag2 = !(TMPGAP & ip) && !((jpgap >> q) & 1);
+                    const int d = flag ? 0 : HIGH;
+                    const int od = flag ? (flag2 ? 0 : 2 * go) : HIGH;
+                    nEB[q] = tmin(dEB + d, dCB + od);
+                    const int dgc = t.csw[srow + jng];
+                    const int xgo = tmax(gop[q], sgop);
+                    const int a0 = dCB + dgc;
+                    const int a1 = dEV + dgc + (ic == sng ? 0 : gop[q]);
+                    const int a2 = dEH + dgc + (c == jng ? 0 : sgop);
+                    const int a3 = dEB + dgc + xgo;
+                    nCB[q] = tmin(tmin(a0, a1), tmin(a2, a3));
+                }
+                dEH = pEH[q];
+                dEV = pEV[q];
+                dEB = pEB[q];
+                dCB = pCB[q];
+                jprev = c;
+            }
+            (void)jprev;
+            // EH along the row: EH[j] = min(EH[j-1] + shx_j, CB[j-1] + gop_j + jgr_j)
+            const int cbl = __shfl_up_sync(FULL, nCB[K - 1], 1);
+            MinPlus f{0, BIG};
+            int cprev = lane == 0 ? lb.w : cbl;
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const int j = c0 + q;
+                const MinPlus g = j == 0 ? MinPlus{BIG, HIGH}
+                                         : MinPlus{shx[q], tmin(cprev + gop[q] + jgr[q], BIG)};
+                f = compose(f, g);
+                cprev = nCB[q];
+            }
+            const MinPlus pre = warp_scan(f, lane);
+            const MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
+            const int lbx = __shfl_sync(FULL, lb.x, 0);  // only lane 0 read the boundary
+            const int left = lane == 0 ? lbx : apply(ex, lbx);
+            int x = left;
+            cprev = lane == 0 ? lb.w : cbl;
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const int j = c0 + q;
+                x = j == 0 ? HIGH : tmin(x + shx[q], cprev + gop[q] + jgr[q]);
+                pEH[q] = x;
+                pEV[q] = nEV[q];
+                pEB[q] = nEB[q];
+                pCB[q] = nCB[q];
+                cprev = nCB[q];
+            }
+            __syncwarp();
+            write_bnd(i);
+        }
+        __syncwarp();
+        if (blk == nblk - 1) {
+#pragma unroll
+            for (int q = 0; q < K; q++)
+                if (lane == last_lane && q == last_q)
+                    result = tmin(tmin(pEH[q], pEV[q]), tmin(pEB[q], pCB[q]));
+            result = __shfl_sync(FULL, result, last_lane);
+        }
+    }
+    return result;
+}
+
+constexpr int NOBT_K = 8;
+constexpr int NOBT_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * NOBT_WARPS) nobt_kernel(NobtArgs A)
+{
+    __shared__ Tables st;
+    for (int k = threadIdx.x; k < (int)(sizeof(Tables) / 4); k += blockDim.x)
+        reinterpret_cast<int*>(&st)[k] = reinterpret_cast<const int*>(A.tables)[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int4* bnd = A.bnd + (long long)gw * A.bnd_stride;
+    for (;;) {
+        int w = 0;
+        if (lane == 0) w = atomicAdd(A.next, 1);
+        w = __shfl_sync(FULL, w, 0);
+        if (w >= A.npairs) break;
+        const int k = A.order ? A.order[w] : w;
+        const int la = A.lena[k], lb = A.lenb[k];
+        const uint8_t* a = A.seqs + A.offa[k];
+        const uint8_t* b = A.seqs + A.offb[k];
+        // states must index the tables; distance: all-gap sequences are "missing"
+        int bad = 0, ga = 1, gb = 1;
+        const int ns = 1 << st.lcm;
+        for (int i = lane; i < la; i += 32) {
+            bad |= a[i] >= ns;
+            ga &= a[i] == st.gap;
+        }
+        for (int i = lane; i < lb; i += 32) {
+            bad |= b[i] >= ns;
+            gb &= b[i] == st.gap;
+        }
+        bad = __any_sync(FULL, bad);
+        ga = __all_sync(FULL, ga);
+        gb = __all_sync(FULL, gb);
+        int cost = 0, status = 0;
+        if (la < 1 || lb < 1) {
+            status = -4;
+        } else if (bad) {
+            status = -7;
+        } else if (A.missing_distance != NOBT_NO_MISSING && (ga || gb)) {
+            cost = A.missing_distance;
+        } else if (la > 65535 || lb > 65535 || tmin(la, lb) > A.bnd_stride) {
+            status = -6;
+        } else {
+            const bool sw = la > lb;  // the shorter sequence runs down the rows
+            const uint8_t* si = sw ? b : a;
+            const uint8_t* sj = sw ? a : b;
+            const int li = sw ? lb : la, lj = sw ? la : lb;
+            if (lj <= 2) {
+                if (lane == 0) cost = nobt_tiny(st, si, li, sj, lj);
+                cost = __shfl_sync(FULL, cost, 0);
+            } else {
+                cost = nobt_warp<NOBT_K>(st, si, li, sj, lj, bnd, lane);
+            }
+        }
+        if (lane == 0) {
+            A.cost[k] = cost;
+            A.status[k] = status;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+int nobt_warps_per_cta() { return NOBT_WARPS; }
+
+int nobt_blocks_per_sm()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nobt_kernel, 32 * NOBT_WARPS, 0);
+    return n;
+}
+
+void launch_nobt(const NobtArgs& a, int grid, cudaStream_t s)
+{
+    nobt_kernel<<<grid, 32 * NOBT_WARPS, 0, s>>>(a);
+}
+
+}  // namespace pa

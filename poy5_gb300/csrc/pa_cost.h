@@ -1,0 +1,34 @@
+// Launch interface of the cost-only affine fill (pa_cost.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pa_core.cuh"
+
+namespace pa {
+
+// missing_distance value meaning "no all-gap rule" (per-call cost_affine_3)
+constexpr int NOBT_NO_MISSING = -0x7fffffff;
+
+struct NobtArgs {
+    const uint8_t* seqs;
+    const long long* offa;
+    const int* lena;
+    const long long* offb;
+    const int* lenb;
+    int npairs;
+    const Tables* tables;
+    const int* order;         // optional visiting order (longest first)
+    int missing_distance;     // cost of pairs with an all-gap sequence
+    int* next;                // work counter, zero before the launch
+    int4* bnd;                // per warp: block boundary column, bnd_stride rows
+    int bnd_stride;           // >= the shorter length of every pair
+    int* cost;
+    int* status;              // 0 ok, -4 empty, -6 too long, -7 bad state
+};
+
+int nobt_warps_per_cta();
+int nobt_blocks_per_sm();
+void launch_nobt(const NobtArgs& a, int grid, cudaStream_t s);
+
+}  // namespace pa

@@ -665,8 +665,24 @@ __global__ void prep_kernel(BatchArgs A)
             gb += __shfl_xor_sync(FULL, gb, o);
         }
         if (A.deltawh_override) pl = plan_linear_deltawh(t, la, lb, A.deltawh_override[k]);
+        else if (A.distance) pl = plan_linear_distance(t, ga, la, gb, lb);
         else pl = plan_linear(t, ga, la, gb, lb);
         if (lane == 0) A.pfull[k] = pl.full;
+    }
+    if (A.distance) {  // Sequence.is_empty: every position the gap
+        int ea = 1, eb = 1;
+        for (int i = lane; i < la; i += 32) ea &= a[i] == t.gap;
+        for (int i = lane; i < lb; i += 32) eb &= b[i] == t.gap;
+        const bool empty = __all_sync(FULL, ea) || __all_sync(FULL, eb);
+        if (empty) {
+            if (lane == 0) {
+                A.passes[k] = 0;
+                A.lastcls[k] = -1;
+                A.cost[k] = A.missing_distance;
+                A.status[k] = 0;
+            }
+            return;
+        }
     }
     if (lane != 0) return;
     A.passes[k] = 0;

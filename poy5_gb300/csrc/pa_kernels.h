@@ -22,6 +22,8 @@ struct BatchArgs {
     int npairs;
     int affine;
     int do_traceback;          // 0: keep the last fill in the slab (per-call stubs)
+    int distance;              // DOS.distance: deltaw = max 8 |la - lb|, all-gap -> missing
+    int missing_distance;
     Ladder lad;                // pipeline classes of this model
     const Tables* tables;
     int* pfull;                // linear plane choice per pair

@@ -55,6 +55,7 @@ struct poyalgn_ctx {
     // per-batch scratch
     pa::DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
     pa::DevBuf dwh, swp, order, order_scratch;
+    pa::DevBuf nobt_bnd, nobt_ctr;  // cost-only affine fill: boundary columns, work counter
     int last_launches = 0;
     // upper bound on the direction-slab arena of one batch (0: half the free
     // device memory, at most 64 GB)
@@ -96,7 +97,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs, int 
               const int* lena, const long long* offb, const int* lenb,
               const long long* out_off, int* cost, int* maxcost, int* alen, int* mlen,
               int* wlen, int* status, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
-              int* passes, const int* dwh, const int* swp, int do_traceback, cudaStream_t st);
+              int* passes, const int* dwh, const int* swp, int do_traceback, cudaStream_t st,
+              int distance = 0, int missing_distance = 0);
 
 // Reserve the per-batch scratch of run_batch for batches of up to max_pairs
 // pairs, out_total output bytes and a slab arena of slab_bytes, so that such
