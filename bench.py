@@ -375,28 +375,35 @@ def run_serving(local: int, seconds: float = 1.0) -> dict:
     nb = np.array([store.add(b) for _, b in w.pairs], np.int32)
     pair_cells = np.array([len(a) * len(b) for a, b in w.pairs], np.int64)
     cfg = dict(nslots=3, max_batch_pairs=2048, max_waiting_pairs=16384)
-    srv = pg.Server(store, cm, hbm_budget=24 << 30, **cfg)
     rng = np.random.default_rng(wl.SEED_BASE + 4)
-    srv.replay(pg.poisson_trace(rng, 2000.0, 200, na, nb))  # warm-up
-    points = []
-    for rate in (1000, 5000, 20000, 50000, 100000, 200000):
-        nreq = int(min(rate * seconds, 40000))
-        tr = pg.poisson_trace(rng, float(rate), nreq, na, nb)
-        res = srv.replay(tr)
-        ok = res.served()
-        lat = res.latency_s[ok] * 1e3
-        pair_ok = np.repeat(ok, tr.npairs)
-        cells = int(pair_cells[tr.node_a[pair_ok]].sum())
-        points.append({"rate_req_s": rate, "requests": nreq, "refused": int((~ok).sum()),
-                       "p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
-                       "p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
-                       "alignments_per_s": round(int(pair_ok.sum()) / res.wall_s, 1),
-                       "gcups": round(cells / res.wall_s / 1e9, 3)})
-    st = srv.stats()
-    srv.close()
+
+    def sweep(kind, rates):
+        srv = pg.Server(store, cm, hbm_budget=24 << 30, kind=kind, **cfg)
+        srv.replay(pg.poisson_trace(rng, 2000.0, 200, na, nb))  # warm-up
+        points = []
+        for rate in rates:
+            nreq = int(min(rate * seconds, 40000))
+            tr = pg.poisson_trace(rng, float(rate), nreq, na, nb)
+            res = srv.replay(tr)
+            ok = res.served()
+            lat = res.latency_s[ok] * 1e3
+            pair_ok = np.repeat(ok, tr.npairs)
+            cells = int(pair_cells[tr.node_a[pair_ok]].sum())
+            points.append({"rate_req_s": rate, "requests": nreq, "refused": int((~ok).sum()),
+                           "p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
+                           "p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
+                           "alignments_per_s": round(int(pair_ok.sum()) / res.wall_s, 1),
+                           "gcups": round(cells / res.wall_s / 1e9, 3)})
+        st = srv.stats()
+        srv.close()
+        return {"batches": st["batches"], "points": points}
+
+    from poy5_gb300.serve import DISTANCE, MEDIAN
+    dist = sweep(DISTANCE, (250, 1000, 5000, 20000, 50000, 100000, 200000))
+    med = sweep(MEDIAN, (250, 1000, 5000))
     store.close()
     return {"workload": "serving_requests_poisson_1-64pairs_lognormal1000", **cfg,
-            "batches": st["batches"], "points": points}
+            "distance": dist, "median": med}
 
 
 def _reduce(x: float, world: int, op: str) -> float:

@@ -341,12 +341,18 @@ int poyalgn_downpass(poyalgn_store *s, const poyalgn_cm *cm, int nleaves,
  */
 #define POYALGN_EBUSY -6 /* server admission refused: too many waiting pairs */
 
+/* What a server computes per pair: DOS.median (cost, median) or
+ * DOS.distance (cost only, as poyalgn_distance_batch; missing_distance for
+ * pairs with an all-gap sequence). */
+#define POYALGN_SERVE_MEDIAN 0
+#define POYALGN_SERVE_DISTANCE 1
+
 typedef struct poyalgn_server poyalgn_server;
 
-int poyalgn_server_create(poyalgn_store *store, const poyalgn_cm *cm,
-                          int nslots, int max_batch_pairs,
-                          int max_waiting_pairs, int64_t hbm_budget,
-                          poyalgn_server **out);
+int poyalgn_server_create(poyalgn_store *store, const poyalgn_cm *cm, int kind,
+                          int32_t missing_distance, int nslots,
+                          int max_batch_pairs, int max_waiting_pairs,
+                          int64_t hbm_budget, poyalgn_server **out);
 void poyalgn_server_free(poyalgn_server *s);
 
 /* Queue a request of npairs pairs (node ids); non-blocking. */
@@ -355,8 +361,8 @@ int poyalgn_server_submit(poyalgn_server *s, int npairs, const int32_t *node_a,
 
 /*
  * Wait up to timeout_ms (< 0: no limit; POYALGN_EBUSY on timeout) for a
- * ticket, then release it. Per pair: cost, status and the median's length;
- * the medians themselves are concatenated into medians (NULL to skip;
+ * ticket, then release it. Per pair: cost, status and the median's length
+ * (0 for a distance server); the medians are concatenated into medians (NULL to skip;
  * POYALGN_EINVAL if med_cap is too small). latency_s: submission to
  * completion of the batch that carried the request.
  */

@@ -197,8 +197,23 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     return 0;
 }
 
-// Enqueue the cost-only affine fill of npairs pairs (device pointers).
-// min_len bounds the shorter length of every pair.
+static int nobt_grid(const poyalgn_ctx* c, int npairs)
+{
+    const int per_sm = std::max(1, nobt_blocks_per_sm());
+    return std::max(1, std::min(c->nsm * per_sm,
+                                (npairs + nobt_warps_per_cta() - 1) / nobt_warps_per_cta()));
+}
+
+int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int min_len)
+{
+    int rc;
+    const size_t warps = (size_t)nobt_grid(c, max_pairs) * nobt_warps_per_cta();
+    if ((rc = reserve(c->nobt_bnd, warps * (size_t)std::max(min_len, 1) * sizeof(int4)))) return rc;
+    if ((rc = reserve(c->nobt_ctr, sizeof(int)))) return rc;
+    if ((rc = reserve(c->order, (size_t)std::max(max_pairs, 1) * 4))) return rc;
+    return reserve(c->order_scratch, order_scratch_bytes(std::max(max_pairs, 1)));
+}
+
 int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
              const uint8_t* seqs, const long long* offa, const int* lena,
              const long long* offb, const int* lenb, int missing, int* cost, int* status,
@@ -206,9 +221,7 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
 {
     int rc;
     if (npairs <= 0) return 0;
-    const int per_sm = std::max(1, nobt_blocks_per_sm());
-    const int grid = std::max(1, std::min(c->nsm * per_sm,
-                                          (npairs + nobt_warps_per_cta() - 1) / nobt_warps_per_cta()));
+    const int grid = nobt_grid(c, npairs);
     const int stride = std::max(min_len, 1);
     const size_t warps = (size_t)grid * nobt_warps_per_cta();
     if ((rc = reserve(c->nobt_bnd, warps * (size_t)stride * sizeof(int4)))) return rc;

@@ -100,6 +100,17 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs, int 
               int* passes, const int* dwh, const int* swp, int do_traceback, cudaStream_t st,
               int distance = 0, int missing_distance = 0);
 
+// Enqueue the cost-only affine fill (algn_CAML_cost_affine_3 semantics) of
+// npairs pairs; min_len bounds the shorter length of every pair. missing:
+// cost of pairs with an all-gap sequence (NOBT_NO_MISSING: no such rule).
+int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
+             const uint8_t* seqs, const long long* offa, const int* lena,
+             const long long* offb, const int* lenb, int missing, int* cost, int* status,
+             cudaStream_t st);
+// Reserve run_nobt's scratch for up to max_pairs pairs of shorter length up
+// to min_len.
+int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int min_len);
+
 // Reserve the per-batch scratch of run_batch for batches of up to max_pairs
 // pairs, out_total output bytes and a slab arena of slab_bytes, so that such
 // batches allocate nothing.

@@ -61,6 +61,8 @@ struct Slot {
 struct poyalgn_server {
     const poyalgn_cm* cm = nullptr;
     int affine = 0;
+    int kind = POYALGN_SERVE_MEDIAN;
+    int missing = 0;                  // DOS.distance's missing_distance
     int device = 0;
     const uint8_t* arena = nullptr;
     std::vector<long long> off;       // node table snapshot
@@ -136,13 +138,29 @@ int launch(poyalgn_server* s, Slot& sl, std::vector<Req*>& batch)
     int* I = as<int>(sl.ints);
     uint8_t* B = as<uint8_t>(sl.bytes);
     const long long oc = s->out_cap;
-    int rc = run_batch(c, s->cm, s->affine, n, maxmn, total, s->arena, d_offa, d_lena,
+    int rc;
+    if (s->kind == POYALGN_SERVE_DISTANCE) {
+        // cost at I, status at I + 5 ni, like the median layout; no medians
+        CU(cudaMemsetAsync(I + 3 * ni, 0, ni * sizeof(int), st));
+        if (s->affine)
+            rc = run_nobt(c, s->cm, n, maxmn / 2, s->arena, d_offa, d_lena, d_offa + ni,
+                          d_lena + ni, s->missing, I, I + 5 * ni, st);
+        else
+            rc = run_batch(c, s->cm, 0, n, maxmn, 1, s->arena, d_offa, d_lena, d_offa + ni,
+                           d_lena + ni, nullptr, I, nullptr, nullptr, nullptr, nullptr,
+                           I + 5 * ni, nullptr, nullptr, nullptr, nullptr, I + 6 * ni, nullptr,
+                           nullptr, 0, st, 1, s->missing);
+        if (rc) return rc;
+        CU(cudaMemcpyAsync(sl.hints, I, ni * 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    } else {
+        rc = run_batch(c, s->cm, s->affine, n, maxmn, total, s->arena, d_offa, d_lena,
                        d_offa + ni, d_lena + ni, d_offa + 2 * ni, I, I + ni, I + 2 * ni,
                        I + 3 * ni, I + 4 * ni, I + 5 * ni, B, B + oc, B + 2 * oc, B + 3 * oc,
                        I + 6 * ni, nullptr, nullptr, 1, st);
-    if (rc) return rc;
-    CU(cudaMemcpyAsync(sl.hints, I, ni * 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(sl.hmed, B + 2 * oc, (size_t)total, cudaMemcpyDeviceToHost, st));
+        if (rc) return rc;
+        CU(cudaMemcpyAsync(sl.hints, I, ni * 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(sl.hmed, B + 2 * oc, (size_t)total, cudaMemcpyDeviceToHost, st));
+    }
     CU(cudaEventRecord(sl.done, st));
     sl.busy = true;
     return 0;
@@ -285,12 +303,13 @@ int submit_at(poyalgn_server* s, int npairs, const int32_t* na, const int32_t* n
 
 extern "C" {
 
-int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int nslots,
-                          int max_batch_pairs, int max_waiting_pairs, int64_t hbm_budget,
-                          poyalgn_server** out)
+int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int kind,
+                          int32_t missing_distance, int nslots, int max_batch_pairs,
+                          int max_waiting_pairs, int64_t hbm_budget, poyalgn_server** out)
 {
     if (!store || !cm || !out || nslots < 1 || nslots > 64 || max_batch_pairs < 1 ||
-        max_waiting_pairs < max_batch_pairs || hbm_budget < 0)
+        max_waiting_pairs < max_batch_pairs || hbm_budget < 0 ||
+        (kind != POYALGN_SERVE_MEDIAN && kind != POYALGN_SERVE_DISTANCE))
         return set_err(POYALGN_EINVAL, "bad server arguments");
     *out = nullptr;
     int rc;
@@ -304,6 +323,8 @@ int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int nslots
     if (!s) return set_err(POYALGN_ENOMEM, "server allocation");
     s->cm = cm;
     s->affine = cm->h.cost_model == 1;
+    s->kind = kind;
+    s->missing = missing_distance;
     s->device = store->ctx->device;
     s->arena = as<uint8_t>(store->arena);
     s->off = store->off;
@@ -318,10 +339,14 @@ int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int nslots
     s->out_cap &= ~(kAlign - 1);
     s->slots.resize(nslots);
     const size_t ni = (size_t)max_batch_pairs;
+    int maxlen = 1;
+    for (int L : s->len) maxlen = std::max(maxlen, L);
     for (Slot& sl : s->slots) {
         if ((rc = poyalgn_init(s->device, &sl.ctx))) break;
         sl.ctx->slab_budget = slab;
         if ((rc = prereserve(sl.ctx, s->affine, max_batch_pairs, s->out_cap, slab))) break;
+        if (kind == POYALGN_SERVE_DISTANCE && s->affine &&
+            (rc = prereserve_nobt(sl.ctx, max_batch_pairs, maxlen))) break;
         if ((rc = reserve(sl.meta, ni * 32))) break;
         if ((rc = reserve(sl.ints, ni * 4 * 7))) break;
         if ((rc = reserve(sl.bytes, (size_t)s->out_cap * 4))) break;

@@ -60,14 +60,22 @@ def poisson_trace(rng: np.random.Generator, rate: float, nreq: int, pool_a, pool
                  np.asarray(pool_b, np.int32)[pick])
 
 
+MEDIAN, DISTANCE = 0, 1   # POYALGN_SERVE_*
+
+
 class Server:
+    """kind MEDIAN serves DOS.median (cost and median per pair), DISTANCE
+    serves DOS.distance (cost only; missing_distance for all-gap pairs)."""
+
     def __init__(self, store: Store, cm: CostMatrix, nslots: int = 3,
                  max_batch_pairs: int = 4096, max_waiting_pairs: int = 65536,
-                 hbm_budget: int = 16 << 30):
+                 hbm_budget: int = 16 << 30, kind: int = MEDIAN, missing_distance: int = 0):
         self.store = store
         self.cm = cm
+        self.kind = kind
         h = C.c_void_p()
-        check(_lib.load().poyalgn_server_create(store.handle, cm.handle, nslots,
+        check(_lib.load().poyalgn_server_create(store.handle, cm.handle, int(kind),
+                                                int(missing_distance), nslots,
                                                 max_batch_pairs, max_waiting_pairs,
                                                 int(hbm_budget), C.byref(h)))
         self._h = h

@@ -89,3 +89,23 @@ def test_admission_refuses_beyond_waiting_bound(ctx):
     with pytest.raises(pg.PoyAlgnError):
         srv.submit(np.zeros(65, np.int32), np.zeros(65, np.int32))  # larger than a batch
     srv.close()
+
+
+@pytest.mark.gpu
+def test_distance_server_matches_distance_batch(ctx):
+    from poy5_gb300.serve import DISTANCE
+    w, cm, store, na, nb = _pool(ctx, n=40, seed=13)
+    want, st = pg.distance_batch(ctx, cm, w.pairs)
+    assert np.all(st == 0)
+    srv = pg.Server(store, cm, nslots=2, max_batch_pairs=64, max_waiting_pairs=4096,
+                    hbm_budget=1 << 30, kind=DISTANCE)
+    pick = np.array([3, 9, 27, 0], np.int32)
+    alone = srv.wait(srv.submit(na[pick], nb[pick]))
+    assert np.array_equal(alone.cost, want[pick])
+    assert all(len(m) == 0 for m in alone.medians)
+    rng = np.random.default_rng(8)
+    tr = pg.poisson_trace(rng, 5000.0, 120, na, nb, max_pairs=12)
+    res = srv.replay(tr)
+    assert np.all(res.served()) and np.all(res.status == 0)
+    assert np.array_equal(res.cost, want[np.searchsorted(na, tr.node_a)])
+    srv.close()
