@@ -361,6 +361,69 @@ def run_downpass(local: int, reps: int = 5) -> dict:
             "total_cost_matches_cpu": tot == res.total_cost}
 
 
+def run_long(local: int, cpu_pairs: int = 1) -> dict:
+    """The long-pair stress workload (512 pairs of 20-50 kb, 15% substitutions,
+    2% indels, linear 1/2): one timed batch with inputs resident on the
+    device, direction bytes written per filled cell as the HBM figure, and
+    the host implementation on the first pair(s) beside it."""
+    import ctypes as C
+    import torch
+    import poy5_gb300 as pg
+    from poy5_gb300 import _lib, schedule
+    from poy5_gb300 import workloads as wl
+    w = wl.long_pairs()
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    lib = _lib.load()
+    pk = pg.pack_pairs(w.pairs)
+    n = pk.npairs
+    dev = torch.device("cuda", local)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_in = [t(pk.seqs), t(pk.offa), t(pk.lena), t(pk.offb), t(pk.lenb), t(pk.out_off)]
+    d_int = [torch.zeros(n, dtype=torch.int32, device=dev) for _ in range(7)]
+    d_out = [torch.zeros(pk.out_bytes, dtype=torch.uint8, device=dev) for _ in range(4)]
+    P = lambda x: C.c_void_p(x.data_ptr())
+    st = torch.cuda.current_stream(dev)
+
+    def step():
+        _lib.check(lib.poyalgn_median_batch_device(
+            ctx.handle, cm.handle, n, pk.max_pair_len, pk.out_bytes, *(P(x) for x in d_in),
+            *(P(x) for x in d_int[:6]), *(P(x) for x in d_out), P(d_int[6]),
+            C.c_void_p(st.cuda_stream)))
+
+    step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    step()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    status = d_int[5].cpu().numpy()
+    passes = d_int[6].cpu().numpy()
+    cells = cells_full(w)
+    gaps = lambda s: int(np.count_nonzero((s >= 16) & ((s & 16) != 0)))
+    full = schedule.linear_full_plane(pk.lena, pk.lenb, [gaps(a) for a, _ in w.pairs],
+                                      [gaps(b) for _, b in w.pairs])
+    mnz = cm.tables()["min_non0_cost"]
+    computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, False, full).sum())
+    # host implementation on the first pair(s), single pair at a time
+    orc, kind = host_oracle()
+    ocm = orc.cm(subs=w.subs, indel=w.indel)
+    c0 = time.perf_counter()
+    ccells = 0
+    for a, b in w.pairs[:cpu_pairs]:
+        orc.median(ocm, a, b, False)
+        ccells += len(a) * len(b)
+    cpu_s = time.perf_counter() - c0
+    return {"workload": w.name, "pairs": n, "ms": round(ms, 2),
+            "status_ok": int((status == 0).sum()), "gcups": round(cells / ms / 1e6, 2),
+            "gcups_computed_cells": round(computed / ms / 1e6, 2),
+            "dm_write_gbs": round(computed / ms / 1e6, 2), "passes_mean": round(float(passes.mean()), 2),
+            "cpu_baseline": {"gcups": round(ccells / cpu_s / 1e9, 4), "kind": kind, "cores": 1,
+                             "sample": f"first {cpu_pairs} pair(s), one thread"}}
+
+
 def run_serving(local: int, seconds: float = 1.0) -> dict:
     """Open-loop Poisson replay against the continuous-batching server: each
     request has U{1..64} pairs of a resident pool (lognormal lengths, median
@@ -538,6 +601,7 @@ def main(argv=None):
             "alignments_per_s": round(cpu["pairs_per_s"], 2)}
         if world == 1 and not args.no_extras:
             line["downpass"] = run_downpass(local)
+            line["long_pairs"] = run_long(local)
             line["serving"] = run_serving(local, args.serve_seconds)
         print(json.dumps(line))
     if world > 1:
