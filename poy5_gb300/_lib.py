@@ -11,7 +11,8 @@ import os
 import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpoyalgn.so")
+# POYALGN_LIBRARY selects another build of the library (same C ABI)
+LIB_PATH = os.environ.get("POYALGN_LIBRARY") or os.path.join(HERE, "libpoyalgn.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "poyalgn.h")
 
 _P = C.c_void_p

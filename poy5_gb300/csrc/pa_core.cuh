@@ -208,12 +208,25 @@ PA_HD int gap_opening(int idx, int prev, int curr, int gap, int go)
     return go;
 }
 
-// Slab addressing shared by the fills and the tracebacks.
+// log2 of a power of two
+PA_HD int log2_pow2(int x)
+{
+#if defined(__CUDA_ARCH__)
+    return __ffs(x) - 1;
+#else
+    return __builtin_ctz((unsigned)x);
+#endif
+}
+
+// Slab addressing shared by the fills and the tracebacks: row i >= 1 is row
+// q of block b = (i - 1) / R, held by lane g = b mod P (P and R are powers
+// of two in every ladder).
 PA_HD long long dm_index(int P, int R, int i, int j)
 {
-    int b = (i - 1) / R;
-    int g = b % P;
-    int q = (i - 1) - b * R;
+    const int lr = log2_pow2(R);
+    const int b = (i - 1) >> lr;
+    const int g = b & (P - 1);
+    const int q = (i - 1) & (R - 1);
     return (long long)(i + j) * (P * R) + g * R + q;
 }
 
@@ -1132,18 +1145,22 @@ struct PairRes {
     int alen, mlen, wlen, maxcost, status;
 };
 
-PA_HD int lin_dm(const uint8_t* dm, int P, int R, int i, int j)
-{
-    if (i == 0) return j == 0 ? L_ALIGN : L_INSERT;
-    return dm[dm_index(P, R, i, j)];
-}
+// Direction code of cell (i >= 1, j) of a linear slab.
+struct LinDmBytes {
+    const uint8_t* dm;
+    int P, R;
+    PA_HDM int operator()(int i, int j) const { return dm[dm_index(P, R, i, j)]; }
+};
 
 // backtrace_2d + algn_ancestor_2 + seq_get_median_2d_with_gaps + algn_worst_2
 // (src/algn.c:3277-3327, 3602-3626, 3002-3105; src/seq.c:241-252), linear
 // model. x = shorter (rows), y = longer; `swaped` = the caller passed y first.
-PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
-                            const uint8_t* x, int m, const uint8_t* y, int n,
-                            int swaped, const PairOut& o)
+// The traceback reads its codes through `rd`, which may be a shared-memory
+// window that the calling warp refills together (every lane then runs the
+// same traceback on the same data, so control flow stays uniform).
+template <class DM>
+PA_HD PairRes lin_traceback_dm(DM& rd, const Tables& t, const uint8_t* x, int m,
+                               const uint8_t* y, int n, int swaped, const PairOut& o)
 {
     PairRes r = {0, 0, 0, 0, 0};
     const int gap = t.gap, lcm = t.lcm;
@@ -1153,7 +1170,7 @@ PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
     int a = 0, bsym = 0;
     while (i >= 0) {
         if (k <= 0) { r.status = -2; return r; }
-        int d = lin_dm(dm, P, R, i, j);
+        const int d = i == 0 ? (j == 0 ? L_ALIGN : L_INSERT) : rd(i, j);
         int xs, ys;
         if (d & L_ALIGN) {
             xs = x[i--];
@@ -1185,6 +1202,14 @@ PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
     r.mlen = o.cap - ka;
     r.maxcost = (nga && ngb) ? worst : 0;
     return r;
+}
+
+PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
+                            const uint8_t* x, int m, const uint8_t* y, int n,
+                            int swaped, const PairOut& o)
+{
+    LinDmBytes rd{dm, P, R};
+    return lin_traceback_dm(rd, t, x, m, y, n, swaped, o);
 }
 
 // Direction flags of cell (i, j) from a slab of aff_step words or of lean
@@ -1229,7 +1254,7 @@ PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int
 // backtrace_aff (src/algn.c:1714-1819) in internal order (x shorter), then
 // the caller-order aligned pair and max_cost_2 on it.
 template <class DM>
-PA_HD PairRes aff_traceback_dm(const DM& aff_dm, const Tables& t, const uint8_t* x, int m,
+PA_HD PairRes aff_traceback_dm(DM& aff_dm, const Tables& t, const uint8_t* x, int m,
                                const uint8_t* y, int n, int swaped, const PairOut& o)
 {
     PairRes r = {0, 0, 0, 0, 0};
@@ -1322,14 +1347,16 @@ PA_HD PairRes aff_traceback(const uint16_t* dm, int P, int R, const Tables& t,
                             const uint8_t* x, int m, const uint8_t* y, int n, int swaped,
                             const PairOut& o)
 {
-    return aff_traceback_dm(AffDmWords{dm, P, R}, t, x, m, y, n, swaped, o);
+    AffDmWords rd{dm, P, R};
+    return aff_traceback_dm(rd, t, x, m, y, n, swaped, o);
 }
 
 PA_HD PairRes aff_traceback_lean(const uint8_t* dm, int P, int R, const Tables& t,
                                  const uint8_t* x, int m, const uint8_t* y, int n, int swaped,
                                  const PairOut& o)
 {
-    return aff_traceback_dm(AffDmLean{dm, P, R}, t, x, m, y, n, swaped, o);
+    AffDmLean rd{dm, P, R};
+    return aff_traceback_dm(rd, t, x, m, y, n, swaped, o);
 }
 
 }  // namespace pa

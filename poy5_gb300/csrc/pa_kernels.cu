@@ -314,8 +314,14 @@ __device__ void lin_fill(const LinBand& b, const Tables& st, const uint8_t* x,
     gapnum = tmax((int)(nn & 0xFFFF), (int)(nn >> 16));
 }
 
-template <int R>
-__global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
+// Resident CTAs per SM the compiler must allow for the 128-thread (P <= 32)
+// launches of each shape; the wide launches (up to 512 threads) keep 1.
+constexpr int lin_narrow_minb(int R) { return R == 2 ? 6 : R == 4 ? 5 : 4; }
+constexpr int aff_narrow_minb(int) { return 4; }  // higher counts spill more than they gain
+
+template <int R, bool NARROW>
+__global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R) : 1)
+    lin_class_kernel(BatchArgs A, int cls)
 {
     constexpr int VARIANT = 0;
     __shared__ Tables st;
@@ -372,16 +378,20 @@ __global__ void __launch_bounds__(512) lin_class_kernel(BatchArgs A, int cls)
                 }
             }
         }
-        if (finished && p.gl == 0) {
-            A.lastcls[w.k] = cls;
-            A.slab_cta[w.k] = p.slot;
-            if (A.do_traceback) {
+        if (finished) {
+            if (p.gl == 0) {
+                A.lastcls[w.k] = cls;
+                A.slab_cta[w.k] = p.slot;
+            }
+            if (!A.do_traceback) {
+                if (p.gl == 0) {
+                    A.cost[w.k] = cost;
+                    A.status[w.k] = 0;
+                }
+            } else if (p.gl == 0) {
                 const PairRes r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
                                                 pair_out(A, w.k));
                 finish_pair(A, w.k, cost, r);
-            } else {
-                A.cost[w.k] = cost;
-                A.status[w.k] = 0;
             }
         }
         pipe_sync(p);
@@ -534,8 +544,9 @@ __device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t*
     gapnum = g;
 }
 
-template <int R, bool FAST>
-__global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
+template <int R, bool FAST, bool NARROW>
+__global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R) : 1)
+    aff_class_kernel(BatchArgs A, int cls)
 {
     constexpr int VARIANT = FAST ? 1 : 0;
     __shared__ Tables st;
@@ -604,19 +615,23 @@ __global__ void __launch_bounds__(512) aff_class_kernel(BatchArgs A, int cls)
             }
             pipe_sync(p);
         }
-        if (finished && p.gl == 0) {
-            A.lastcls[w.k] = cls | (FAST ? LASTCLS_LEAN : 0);
-            A.slab_cta[w.k] = p.slot;
-            if (A.do_traceback) {
+        if (finished) {
+            if (p.gl == 0) {
+                A.lastcls[w.k] = cls | (FAST ? LASTCLS_LEAN : 0);
+                A.slab_cta[w.k] = p.slot;
+            }
+            if (!A.do_traceback) {
+                if (p.gl == 0) {
+                    A.cost[w.k] = cost;
+                    A.status[w.k] = 0;
+                }
+            } else if (p.gl == 0) {
                 const PairRes r =
                     FAST ? aff_traceback_lean(reinterpret_cast<const uint8_t*>(dm), p.P, R, st,
                                               w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k))
                          : aff_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
                                          pair_out(A, w.k));
                 finish_pair(A, w.k, cost, r);
-            } else {
-                A.cost[w.k] = cost;
-                A.status[w.k] = 0;
             }
         }
         pipe_sync(p);
@@ -797,23 +812,30 @@ __global__ void aligned_medians_kernel(const Tables* tg, const uint8_t* x, const
 
 }  // namespace
 
+using ClassKernel = void (*)(BatchArgs, int);
+
+// The compiled kernel for a class shape (narrow: a 128-thread CTA).
+static ClassKernel class_kernel(int affine, int R, int variant, bool narrow)
+{
+    if (affine) {
+        if (R == 2)
+            return variant ? (narrow ? aff_class_kernel<2, true, true> : aff_class_kernel<2, true, false>)
+                           : (narrow ? aff_class_kernel<2, false, true> : aff_class_kernel<2, false, false>);
+        return variant ? (narrow ? aff_class_kernel<4, true, true> : aff_class_kernel<4, true, false>)
+                       : (narrow ? aff_class_kernel<4, false, true> : aff_class_kernel<4, false, false>);
+    }
+    if (R == 2) return narrow ? lin_class_kernel<2, true> : lin_class_kernel<2, false>;
+    if (R == 4) return narrow ? lin_class_kernel<4, true> : lin_class_kernel<4, false>;
+    return narrow ? lin_class_kernel<8, true> : lin_class_kernel<8, false>;
+}
+
 int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant)
 {
     const int K = ladder_K(lad, cls), R = lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     int n = 0;
-    if (affine) {
-        switch (R) {
-            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<2, true> : aff_class_kernel<2, false>, threads, 0); break;
-            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, variant ? aff_class_kernel<4, true> : aff_class_kernel<4, false>, threads, 0); break;
-        }
-    } else {
-        switch (R) {
-            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<2>, threads, 0); break;
-            case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<4>, threads, 0); break;
-            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lin_class_kernel<8>, threads, 0); break;
-        }
-    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, class_kernel(affine, R, variant, K == 1),
+                                                  threads, 0);
     return n;
 }
 
@@ -870,24 +892,7 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
 {
     const int K = ladder_K(a.lad, cls), R = a.lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
-    if (a.affine) {
-        switch (R) {
-            case 2:
-                if (variant) aff_class_kernel<2, true><<<grid, threads, 0, s>>>(a, cls);
-                else aff_class_kernel<2, false><<<grid, threads, 0, s>>>(a, cls);
-                break;
-            default:
-                if (variant) aff_class_kernel<4, true><<<grid, threads, 0, s>>>(a, cls);
-                else aff_class_kernel<4, false><<<grid, threads, 0, s>>>(a, cls);
-                break;
-        }
-    } else {
-        switch (R) {
-            case 2: lin_class_kernel<2><<<grid, threads, 0, s>>>(a, cls); break;
-            case 4: lin_class_kernel<4><<<grid, threads, 0, s>>>(a, cls); break;
-            default: lin_class_kernel<8><<<grid, threads, 0, s>>>(a, cls); break;
-        }
-    }
+    class_kernel(a.affine, R, a.affine ? variant : 0, K == 1)<<<grid, threads, 0, s>>>(a, cls);
 }
 
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s)
