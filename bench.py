@@ -35,7 +35,11 @@ sys.path.insert(0, ROOT)
 METRIC = ("GCUPS & alignments/s batched+served vs plain per-pair kernel, 1 GB300, "
           "bit-exact; p50/p99")
 OPS_PER_CELL = {"affine": 51, "linear": 8}   # int32 ops per DP cell
-DM_BYTES = {"affine": 2, "linear": 1}        # direction bytes written per cell
+DM_BYTES = {"affine": 1, "linear": 1}        # direction bytes written per cell (lean affine: 1)
+# DRAM bytes (read + write) the class kernels moved per computed cell in one
+# ncu capture of the 8,192-pair affine batch (5.5 GB for 3.12 G cells); the
+# traffic grows with the computed cells, so it scales to the full batch.
+DRAM_BYTES_PER_CELL = {"affine": 1.77}
 
 
 def parse_args(argv=None):
@@ -54,6 +58,8 @@ def parse_args(argv=None):
                     help="skip the downpass and serving measurements")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="arrival window of each serving rate")
+    ap.add_argument("--leg", choices=["main", "downpass", "long", "serving", "distance"],
+                    default="main", help="run one measurement alone and print its object")
     return ap.parse_args(argv)
 
 
@@ -424,6 +430,48 @@ def run_long(local: int, cpu_pairs: int = 1) -> dict:
                              "sample": f"first {cpu_pairs} pair(s), one thread"}}
 
 
+def run_distance(local: int, n_pairs: int = 8192, reps: int = 3) -> dict:
+    """DOS.distance (cost only) of serving-distribution pairs, affine: the
+    full unbanded fill of algn_CAML_cost_affine_3, inputs resident."""
+    import ctypes as C
+    import torch
+    import poy5_gb300 as pg
+    from poy5_gb300 import _lib
+    from poy5_gb300 import workloads as wl
+    w = wl.serving_pairs(n_pairs=n_pairs)
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    lib = _lib.load()
+    pk = pg.pack_pairs(w.pairs)
+    dev = torch.device("cuda", local)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_in = [t(pk.seqs), t(pk.offa), t(pk.lena), t(pk.offb), t(pk.lenb)]
+    cost = torch.zeros(pk.npairs, dtype=torch.int32, device=dev)
+    status = torch.zeros(pk.npairs, dtype=torch.int32, device=dev)
+    P = lambda x: C.c_void_p(x.data_ptr())
+    st = torch.cuda.current_stream(dev)
+
+    def step():
+        _lib.check(lib.poyalgn_distance_batch_device(
+            ctx.handle, cm.handle, pk.npairs, pk.max_pair_len, *(P(x) for x in d_in), 0,
+            P(cost), P(status), C.c_void_p(st.cuda_stream)))
+
+    step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    cells = cells_full(w)
+    ok = int((status.cpu().numpy() == 0).sum())
+    return {"workload": f"serving_pairs_{n_pairs}_distance", "pairs": pk.npairs,
+            "status_ok": ok, "ms": round(ms, 2), "gcups": round(cells / ms / 1e6, 2),
+            "alignments_per_s": round(pk.npairs / ms * 1e3, 1)}
+
+
 def run_serving(local: int, seconds: float = 1.0) -> dict:
     """Open-loop Poisson replay against the continuous-batching server: each
     request has U{1..64} pairs of a resident pool (lognormal lengths, median
@@ -537,7 +585,11 @@ def gpu_line(args, r) -> dict:
         "roofline": {"bound": "hbm", "kernel": "class kernels (fill+traceback), dominant "
                      + dom, "achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                      "frac": round(gbs / hbm_peak, 4) if hbm_peak else None,
-                     "traffic": None, "peak_source": "measured" if hbm_peak else None},
+                     "traffic": (round(r["computed"] * DRAM_BYTES_PER_CELL[model])
+                                 if model in DRAM_BYTES_PER_CELL else None),
+                     "traffic_source": "ncu dram bytes per computed cell, 8,192-pair batch, "
+                                       "scaled by computed cells",
+                     "peak_source": "measured" if hbm_peak else None},
         "roofline_int32": {"bound": "int32 ALU", "ops_per_cell": OPS_PER_CELL[model],
                            "achieved": round(int_ach, 2), "peak": round(int_peak, 2),
                            "unit": "Tops", "frac": round(int_ach / int_peak, 4),
@@ -563,6 +615,19 @@ def gpu_line(args, r) -> dict:
 def main(argv=None):
     args = parse_args(argv)
     rank, world, local = dist_info()
+    if args.leg != "main" and args.impl == "gpu":
+        import torch
+        torch.cuda.set_device(local)
+        if args.leg == "downpass":
+            out = run_downpass(local)
+        elif args.leg == "long":
+            out = run_long(local)
+        elif args.leg == "serving":
+            out = run_serving(local, args.serve_seconds)
+        else:
+            out = run_distance(local, args.pairs or 8192)
+        print(json.dumps({"leg": args.leg, **out}))
+        return 0
     if args.impl == "reference":
         if rank != 0:
             return 0
@@ -602,6 +667,7 @@ def main(argv=None):
         if world == 1 and not args.no_extras:
             line["downpass"] = run_downpass(local)
             line["long_pairs"] = run_long(local)
+            line["distance"] = run_distance(local)
             line["serving"] = run_serving(local, args.serve_seconds)
         print(json.dumps(line))
     if world > 1:

@@ -204,31 +204,50 @@ static int nobt_grid(const poyalgn_ctx* c, int npairs)
                                 (npairs + nobt_warps_per_cta() - 1) / nobt_warps_per_cta()));
 }
 
-int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int min_len)
+// Small batches run one pair per CTA (all its warps on one pair, lower
+// latency); large ones one pair per warp.
+static int nobt_ncoop(const poyalgn_ctx* c, int npairs) { return npairs <= 2 * c->nsm ? npairs : 0; }
+
+static int nobt_reserve(poyalgn_ctx* c, int npairs, int max_pair_len, int* grid, int* cgrid,
+                        int* stride, long long* cstride)
 {
     int rc;
-    const size_t warps = (size_t)nobt_grid(c, max_pairs) * nobt_warps_per_cta();
-    if ((rc = reserve(c->nobt_bnd, warps * (size_t)std::max(min_len, 1) * sizeof(int4)))) return rc;
-    if ((rc = reserve(c->nobt_ctr, sizeof(int)))) return rc;
-    if ((rc = reserve(c->order, (size_t)std::max(max_pairs, 1) * 4))) return rc;
-    return reserve(c->order_scratch, order_scratch_bytes(std::max(max_pairs, 1)));
+    *stride = std::max(max_pair_len / 2, 1);  // rows: the shorter length
+    *grid = nobt_grid(c, npairs);
+    const int ncoop = nobt_ncoop(c, npairs);
+    *cgrid = std::max(1, std::min(ncoop, c->nsm));
+    *cstride = (long long)nobt_coop_columns(max_pair_len) * *stride;
+    const size_t warps = (size_t)*grid * nobt_warps_per_cta();
+    if ((rc = reserve(c->nobt_bnd, warps * (size_t)*stride * sizeof(int4)))) return rc;
+    if ((rc = reserve(c->nobt_coop, ncoop > 0 ? (size_t)*cgrid * (size_t)*cstride * sizeof(int4)
+                                              : sizeof(int4))))
+        return rc;
+    if ((rc = reserve(c->nobt_ctr, 2 * sizeof(int)))) return rc;
+    if ((rc = reserve(c->order, (size_t)std::max(npairs, 1) * 4))) return rc;
+    return reserve(c->order_scratch, order_scratch_bytes(std::max(npairs, 1)));
 }
 
-int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
+int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int max_len)
+{
+    int g, cg, st;
+    long long cs;
+    // both kernels' scratch: the largest per-warp and per-CTA layouts
+    int rc = nobt_reserve(c, max_pairs, 2 * max_len, &g, &cg, &st, &cs);
+    if (rc) return rc;
+    return nobt_reserve(c, std::min(max_pairs, 2 * c->nsm), 2 * max_len, &g, &cg, &st, &cs);
+}
+
+int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
              const uint8_t* seqs, const long long* offa, const int* lena,
              const long long* offb, const int* lenb, int missing, int* cost, int* status,
              cudaStream_t st)
 {
     int rc;
     if (npairs <= 0) return 0;
-    const int grid = nobt_grid(c, npairs);
-    const int stride = std::max(min_len, 1);
-    const size_t warps = (size_t)grid * nobt_warps_per_cta();
-    if ((rc = reserve(c->nobt_bnd, warps * (size_t)stride * sizeof(int4)))) return rc;
-    if ((rc = reserve(c->nobt_ctr, sizeof(int)))) return rc;
-    if ((rc = reserve(c->order, (size_t)npairs * 4))) return rc;
-    if ((rc = reserve(c->order_scratch, order_scratch_bytes(npairs)))) return rc;
-    CU(cudaMemsetAsync(c->nobt_ctr.p, 0, sizeof(int), st));
+    int grid, cgrid, stride;
+    long long cstride;
+    if ((rc = nobt_reserve(c, npairs, max_pair_len, &grid, &cgrid, &stride, &cstride))) return rc;
+    CU(cudaMemsetAsync(c->nobt_ctr.p, 0, 2 * sizeof(int), st));
     if (launch_order(lena, lenb, npairs, as<int>(c->order), c->order_scratch.p, st) != 0)
         return set_err(POYALGN_ECUDA, "ordering pairs failed");
     NobtArgs A;
@@ -243,13 +262,17 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
     A.order = as<int>(c->order);
     A.missing_distance = missing;
     A.next = as<int>(c->nobt_ctr);
+    A.next_coop = as<int>(c->nobt_ctr) + 1;
+    A.ncoop = nobt_ncoop(c, npairs);
     A.bnd = as<int4>(c->nobt_bnd);
     A.bnd_stride = stride;
+    A.coop_cols = as<int4>(c->nobt_coop);
+    A.coop_stride = cstride;
     A.cost = cost;
     A.status = status;
-    launch_nobt(A, grid, st);
+    launch_nobt(A, grid, cgrid, st);
     CU(cudaGetLastError());
-    c->last_launches = 3;
+    c->last_launches = 3 + (A.ncoop > 0 && A.ncoop < npairs ? 1 : 0);
     return 0;
 }
 
@@ -400,7 +423,7 @@ void poyalgn_free(poyalgn_ctx* c)
                       &c->ints, &c->bytes, &c->pfull, &c->eh0, &c->lastcls, &c->slabcta,
                       &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
                       &c->dwh, &c->swp, &c->order, &c->order_scratch, &c->nobt_bnd,
-                      &c->nobt_ctr};
+                      &c->nobt_ctr, &c->nobt_coop};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
@@ -726,7 +749,7 @@ int poyalgn_cost_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t*
     if ((rc = ensure_device(ctx))) return rc;
     if ((rc = stage_pair(ctx, si, li, sj, lj))) return rc;
     int* I = as<int>(ctx->ints);
-    if ((rc = run_nobt(ctx, cm, 1, std::min(li, lj), as<uint8_t>(ctx->seqs),
+    if ((rc = run_nobt(ctx, cm, 1, li + lj, as<uint8_t>(ctx->seqs),
                        as<long long>(ctx->offa), as<int>(ctx->lena), as<long long>(ctx->offa) + 1,
                        as<int>(ctx->lena) + 1, NOBT_NO_MISSING, I, I + 1, ctx->stream)))
         return rc;
@@ -753,7 +776,7 @@ int poyalgn_distance_batch_device(poyalgn_ctx* ctx, const poyalgn_cm* cm, int np
     const long long* ob = reinterpret_cast<const long long*>(offb);
     cudaStream_t st = (cudaStream_t)stream;
     if (cm->h.cost_model == 1)
-        return run_nobt(ctx, cm, npairs, max_pair_len / 2, seqs, oa, lena, ob, lenb,
+        return run_nobt(ctx, cm, npairs, max_pair_len, seqs, oa, lena, ob, lenb,
                         missing_distance, cost, status, st);
     return run_batch(ctx, cm, 0, npairs, max_pair_len, 1, seqs, oa, lena, ob, lenb, nullptr,
                      cost, nullptr, nullptr, nullptr, nullptr, status, nullptr, nullptr, nullptr,

@@ -130,231 +130,360 @@ __device__ __forceinline__ MinPlus warp_scan(MinPlus f, int lane)
     return f;
 }
 
+// One lane's K columns of a column block: column constants (jc, jgr, gop,
+// shx, jpgap), the previous row of every state (pEH, pEV, pEB, pCB), the
+// block geometry and, in lane 0, the previous row's value of column c0 - 1.
+// Kept as separate arrays in the caller so that they stay in registers.
+#define NOBT_LANE_PARAMS                                                                   \
+    int (&jc)[K], int (&jgr)[K], int (&gop)[K], int (&shx)[K], unsigned& jpgap,            \
+        int (&pEH)[K], int (&pEV)[K], int (&pEB)[K], int (&pCB)[K], int &c0, int &last_lane, \
+        int &last_q, int4 &dprev, int &ic_last
+#define NOBT_LANE_DECL                                                                     \
+    int jc[K], jgr[K], gop[K], shx[K];                                                     \
+    unsigned jpgap;                                                                        \
+    int pEH[K], pEV[K], pEB[K], pCB[K];                                                    \
+    int c0, last_lane, last_q;                                                             \
+    int4 dprev;                                                                            \
+    int ic_last
+#define NOBT_LANE_ARGS jc, jgr, gop, shx, jpgap, pEH, pEV, pEB, pCB, c0, last_lane, last_q, dprev, ic_last
+
+// Start column block `blk`: constants and row 0. left: the previous block's
+// last column (row 0 read here; unused for blk 0); out: this block's last
+// column (row 0 written here). All 32 lanes call it.
 template <int K>
-__device__ int nobt_warp(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
-                         int4* bnd, int lane)
+__device__ __forceinline__ void nobt_block_begin(NOBT_LANE_PARAMS, const Tables& t,
+                                                 const uint8_t* si, const uint8_t* sj, int lenj,
+                                                 int blk, int lane, const int4* left, int4* out)
 {
     const int gap = t.gap, go = t.go;
-    const int leni = li - 1, lenj = lj - 1;
     constexpr int W = 32 * K;
-    const int nblk = (lenj + 1 + W - 1) / W;
+    c0 = blk * W + lane * K;
+    jpgap = 0;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = c0 + q;
+        const bool real = j <= lenj;
+        const int c = real ? sj[j] : 0;
+        const int cp = (real && j > 0) ? sj[j - 1] : 0;
+        jc[q] = c;
+        jgr[q] = t.prepend[c];
+        gop[q] = (real && j > 0) ? gap_open_cost(j, cp, c, gap, go) : 0;
+        shx[q] = (j > 1 && (cp & gap) && !(c & gap)) ? gop[q] + jgr[q] : jgr[q];
+        jpgap |= (cp & TMPGAP) ? 1u << q : 0u;
+    }
+    MinPlus f{0, BIG};
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = c0 + q;
+        f = compose(f, j == 0 ? MinPlus{BIG, go} : MinPlus{jgr[q], BIG});
+    }
+    const MinPlus pre = warp_scan(f, lane);
+    const MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
+    const int4 l0 = blk > 0 ? left[0] : make_int4(HIGH, HIGH, HIGH, HIGH);
+    int x = lane == 0 ? l0.x : apply(ex, l0.x);
+    if (blk == 0) x = lane == 0 ? 0 : apply(ex, 0);
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = c0 + q;
+        x = j == 0 ? go : x + jgr[q];
+        pEH[q] = x;
+        pEV[q] = j == 0 ? go : HIGH;
+        pEB[q] = HIGH;
+        pCB[q] = j == 0 ? 0 : HIGH;
+    }
+    const int last_col = tmin(lenj, blk * W + W - 1);
+    last_lane = (last_col - blk * W) / K;
+    last_q = (last_col - blk * W) % K;
+    dprev = l0;
+    ic_last = si[0];
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < K; q++)
+        if (lane == last_lane && q == last_q)
+            out[0] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
+}
+
+// Row i >= 1 of the block. Reads left[i] (lane 0) before writing out[i]
+// (the last lane), so left and out may be the same column.
+template <int K>
+__device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t,
+                                               const uint8_t* si, int i, int lenj, int blk,
+                                               int lane, const int4* left, int4* out)
+{
+    const int gap = t.gap, go = t.go;
+    const int ip = ic_last;
+    const int ic = si[i];
+    ic_last = ic;
+    const int sgext = tcost(t, ic, gap);
+    const int sgop = gap_open_cost(i, ip, ic, gap, go);
+    const int sng = ic & NTMPGAP;
+    const int srow = t.rowoff[sng];
+    const int svext = (i > 1 && (ip & gap) && !(ic & gap)) ? sgop + sgext : sgext;
+    const bool even = (i & 1) == 0 && lenj >= 2;
+    // left neighbour: previous row's last column of lane - 1 (lane 0: the
+    // block boundary of row i - 1) and, for EH, the current row's
+    int4 dg;
+    dg.x = __shfl_up_sync(FULL, pEH[K - 1], 1);
+    dg.y = __shfl_up_sync(FULL, pEV[K - 1], 1);
+    dg.z = __shfl_up_sync(FULL, pEB[K - 1], 1);
+    dg.w = __shfl_up_sync(FULL, pCB[K - 1], 1);
+    int4 lb = make_int4(HIGH, HIGH, HIGH, HIGH);  // block boundary, row i
+    if (lane == 0) {
+        dg = dprev;
+        if (blk > 0) lb = left[i];
+        dprev = lb;
+    }
+    int nEV[K], nEB[K], nCB[K];
+    int dEH = dg.x, dEV = dg.y, dEB = dg.z, dCB = dg.w;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = c0 + q;
+        const int c = jc[q];
+        const int jng = c & NTMPGAP;
+        const bool lastc = even && j == lenj;
+        const int uEV = lastc ? HIGH : pEV[q], uCB = lastc ? HIGH : pCB[q];
+        if (j == 0) {
+            nEV[q] = pEV[q] + svext;
+            nEB[q] = HIGH;
+            nCB[q] = HIGH;
+        } else {
+            nEV[q] = tmin(uEV + svext, uCB + sgop + sgext);
+            const bool flag = (TMPGAP & ic) && (TMPGAP & c);
+            const bool flag2 = !(TMPGAP & ip) && !((jpgap >> q) & 1);
+            const int d = flag ? 0 : HIGH;
+            const int od = flag ? (flag2 ? 0 : 2 * go) : HIGH;
+            nEB[q] = tmin(dEB + d, dCB + od);
+            const int dgc = t.csw[srow + jng];
+            const int xgo = tmax(gop[q], sgop);
+            const int a0 = dCB + dgc;
+            const int a1 = dEV + dgc + (ic == sng ? 0 : gop[q]);
+            const int a2 = dEH + dgc + (c == jng ? 0 : sgop);
+            const int a3 = dEB + dgc + xgo;
+            nCB[q] = tmin(tmin(a0, a1), tmin(a2, a3));
+        }
+        dEH = pEH[q];
+        dEV = pEV[q];
+        dEB = pEB[q];
+        dCB = pCB[q];
+    }
+    // EH along the row: EH[j] = min(EH[j-1] + shx_j, CB[j-1] + gop_j + jgr_j)
+    const int cbl = __shfl_up_sync(FULL, nCB[K - 1], 1);
+    MinPlus f{0, BIG};
+    int cprev = lane == 0 ? lb.w : cbl;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = c0 + q;
+        const MinPlus g = j == 0 ? MinPlus{BIG, HIGH}
+                                 : MinPlus{shx[q], tmin(cprev + gop[q] + jgr[q], BIG)};
+        f = compose(f, g);
+        cprev = nCB[q];
+    }
+    const MinPlus pre = warp_scan(f, lane);
+    const MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
+    const int lbx = __shfl_sync(FULL, lb.x, 0);  // only lane 0 read the boundary
+    int x = lane == 0 ? lbx : apply(ex, lbx);
+    cprev = lane == 0 ? lb.w : cbl;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = c0 + q;
+        x = j == 0 ? HIGH : tmin(x + shx[q], cprev + gop[q] + jgr[q]);
+        pEH[q] = x;
+        pEV[q] = nEV[q];
+        pEB[q] = nEB[q];
+        pCB[q] = nCB[q];
+        cprev = nCB[q];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < K; q++)
+        if (lane == last_lane && q == last_q)
+            out[i] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
+}
+
+// min of the four states of the block's last column (valid in every lane)
+template <int K>
+__device__ __forceinline__ int nobt_block_result(NOBT_LANE_PARAMS, int lane)
+{
+    int r = 0;
+#pragma unroll
+    for (int q = 0; q < K; q++)
+        if (lane == last_lane && q == last_q)
+            r = tmin(tmin(pEH[q], pEV[q]), tmin(pEB[q], pCB[q]));
+    return __shfl_sync(FULL, r, last_lane);
+}
+
+// One warp, blocks in sequence; bnd: one column (the block boundary).
+template <int K>
+__device__ __forceinline__ int nobt_warp(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
+                         int4* bnd, int lane)
+{
+    const int leni = li - 1, lenj = lj - 1;
+    const int nblk = (lenj + 1 + 32 * K - 1) / (32 * K);
+    NOBT_LANE_DECL;
     int result = 0;
     for (int blk = 0; blk < nblk; blk++) {
-        const int c0 = blk * W + lane * K;  // this lane's first column
-        // column constants
-        int jc[K], jgr[K], gop[K], shx[K];
-        unsigned jpgap = 0;  // bit q: sj[j - 1] has the gap bit
-#pragma unroll
-        for (int q = 0; q < K; q++) {
-            const int j = c0 + q;
-            const bool real = j <= lenj;
-            const int c = real ? sj[j] : 0;
-            const int cp = (real && j > 0) ? sj[j - 1] : 0;
-            jc[q] = c;
-            jgr[q] = t.prepend[c];
-            gop[q] = (real && j > 0) ? gap_open_cost(j, cp, c, gap, go) : 0;
-            shx[q] = (j > 1 && (cp & gap) && !(c & gap)) ? gop[q] + jgr[q] : jgr[q];
-            jpgap |= (cp & TMPGAP) ? 1u << q : 0u;
-        }
-        // row 0
-        int pEH[K], pEV[K], pEB[K], pCB[K];
-        {
-            MinPlus f{0, BIG};
-#pragma unroll
-            for (int q = 0; q < K; q++) {
-                const int j = c0 + q;
-                const MinPlus g = j == 0 ? MinPlus{BIG, go} : MinPlus{jgr[q], BIG};
-                f = compose(f, g);
-            }
-            const MinPlus pre = warp_scan(f, lane);
-            MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
-            const int left = blk > 0 ? bnd[0].x : 0;
-            int x = lane == 0 ? left : apply(ex, left);
-#pragma unroll
-            for (int q = 0; q < K; q++) {
-                const int j = c0 + q;
-                x = j == 0 ? go : x + jgr[q];
-                pEH[q] = x;
-                pEV[q] = j == 0 ? go : HIGH;
-                pEB[q] = HIGH;
-                pCB[q] = j == 0 ? 0 : HIGH;
-            }
-        }
-        const int last_col = tmin(lenj, blk * W + W - 1);
-        const int last_lane = (last_col - blk * W) / K, last_q = (last_col - blk * W) % K;
-        auto write_bnd = [&](int i) {
-#pragma unroll
-            for (int q = 0; q < K; q++)
-                if (lane == last_lane && q == last_q) bnd[i] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
-        };
-        // previous row's value of column c0 - 1 (the diagonal of column c0)
-        int4 dprev = make_int4(HIGH, HIGH, HIGH, HIGH);
-        if (blk > 0 && lane == 0) dprev = bnd[0];
+        nobt_block_begin<K>(NOBT_LANE_ARGS, t, si, sj, lenj, blk, lane, bnd, bnd);
+        for (int i = 1; i <= leni; i++)
+            nobt_block_row<K>(NOBT_LANE_ARGS, t, si, i, lenj, blk, lane, bnd, bnd);
         __syncwarp();
-        write_bnd(0);
-        int ic = si[0];
-        for (int i = 1; i <= leni; i++) {
-            const int ip = ic;
-            ic = si[i];
-            const int sgext = tcost(t, ic, gap);
-            const int sgop = gap_open_cost(i, ip, ic, gap, go);
-            const int sng = ic & NTMPGAP;
-            const int srow = t.rowoff[sng];
-            const int svext = (i > 1 && (ip & gap) && !(ic & gap)) ? sgop + sgext : sgext;
-            const bool even = (i & 1) == 0 && lenj >= 2;
-            // left neighbour: previous row's last column of lane - 1 (lane 0:
-            // the block boundary of row i - 1) and, for EH, the current row's
-            int4 dg;
-            dg.x = __shfl_up_sync(FULL, pEH[K - 1], 1);
-            dg.y = __shfl_up_sync(FULL, pEV[K - 1], 1);
-            dg.z = __shfl_up_sync(FULL, pEB[K - 1], 1);
-            dg.w = __shfl_up_sync(FULL, pCB[K - 1], 1);
-            int4 lb = make_int4(HIGH, HIGH, HIGH, HIGH);  // block boundary, row i
-            if (lane == 0) {
-                dg = dprev;
-                if (blk > 0) lb = bnd[i];
-                dprev = lb;
-            }
-            int nEV[K], nEB[K], nCB[K];
-            int dEH = dg.x, dEV = dg.y, dEB = dg.z, dCB = dg.w;
-            int jprev = (c0 > 0 && c0 - 1 <= lenj) ? sj[c0 - 1] : 0;
-#pragma unroll
-            for (int q = 0; q < K; q++) {
-                const int j = c0 + q;
-                const int c = jc[q];
-                const int jng = c & NTMPGAP;
-                const bool lastc = even && j == lenj;
-                const int uEV = lastc ? HIGH : pEV[q], uCB = lastc ? HIGH : pCB[q];
-                if (j == 0) {
-                    nEV[q] = pEV[q] + svext;
-                    nEB[q] = HIGH;
-                    nCB[q] = HIGH;
-                } else {
-                    nEV[q] = tmin(uEV + svext, uCB + sgop + sgext);
-                    const bool flag = (TMPGAP & ic) && (TMPGAP & c);
-                    const bool flag2 = !(TMPGAP & ip) && !((jpgap >> q) & 1);
-                    const int d = flag ? 0 : HIGH;
-                    const int od = flag ? (flag2 ? 0 : 2 * go) : HIGH;
-                    nEB[q] = tmin(dEB + d, dCB + od);
-                    const int dgc = t.csw[srow + jng];
-                    const int xgo = tmax(gop[q], sgop);
-                    const int a0 = dCB + dgc;
-                    const int a1 = dEV + dgc + (ic == sng ? 0 : gop[q]);
-                    const int a2 = dEH + dgc + (c == jng ? 0 : sgop);
-                    const int a3 = dEB + dgc + xgo;
-                    nCB[q] = tmin(tmin(a0, a1), tmin(a2, a3));
-                }
-                dEH = pEH[q];
-                dEV = pEV[q];
-                dEB = pEB[q];
-                dCB = pCB[q];
-                jprev = c;
-            }
-            (void)jprev;
-            // EH along the row: EH[j] = min(EH[j-1] + shx_j, CB[j-1] + gop_j + jgr_j)
-            const int cbl = __shfl_up_sync(FULL, nCB[K - 1], 1);
-            MinPlus f{0, BIG};
-            int cprev = lane == 0 ? lb.w : cbl;
-#pragma unroll
-            for (int q = 0; q < K; q++) {
-                const int j = c0 + q;
-                const MinPlus g = j == 0 ? MinPlus{BIG, HIGH}
-                                         : MinPlus{shx[q], tmin(cprev + gop[q] + jgr[q], BIG)};
-                f = compose(f, g);
-                cprev = nCB[q];
-            }
-            const MinPlus pre = warp_scan(f, lane);
-            const MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
-            const int lbx = __shfl_sync(FULL, lb.x, 0);  // only lane 0 read the boundary
-            const int left = lane == 0 ? lbx : apply(ex, lbx);
-            int x = left;
-            cprev = lane == 0 ? lb.w : cbl;
-#pragma unroll
-            for (int q = 0; q < K; q++) {
-                const int j = c0 + q;
-                x = j == 0 ? HIGH : tmin(x + shx[q], cprev + gop[q] + jgr[q]);
-                pEH[q] = x;
-                pEV[q] = nEV[q];
-                pEB[q] = nEB[q];
-                pCB[q] = nCB[q];
-                cprev = nCB[q];
-            }
-            __syncwarp();
-            write_bnd(i);
-        }
-        __syncwarp();
-        if (blk == nblk - 1) {
-#pragma unroll
-            for (int q = 0; q < K; q++)
-                if (lane == last_lane && q == last_q)
-                    result = tmin(tmin(pEH[q], pEV[q]), tmin(pEB[q], pCB[q]));
-            result = __shfl_sync(FULL, result, last_lane);
-        }
+        if (blk == nblk - 1) result = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
     }
     return result;
 }
 
-constexpr int NOBT_K = 8;
-constexpr int NOBT_WARPS = 4;
+// All NW warps of the CTA on one pair: warp w takes blocks w, w + NW, ...
+// and the warps advance one row per barrier, warp w a row behind warp w - 1,
+// so block b + 1 reads block b's last column one row after it is written.
+// cols: one column (rows 0..leni) per block.
+template <int K, int NW>
+__device__ __forceinline__ int nobt_coop(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
+                         int4* cols, int col_stride, int warp, int lane, int* sres)
+{
+    const int leni = li - 1, lenj = lj - 1;
+    const int nblk = (lenj + 1 + 32 * K - 1) / (32 * K);
+    const int rows = leni + 1;
+    const long long total = (long long)((nblk - 1) / NW) * rows + rows + (nblk - 1) % NW;
+    NOBT_LANE_DECL;
+    for (long long it = 0; it < total; it++) {
+        const long long u = it - warp;
+        if (u >= 0) {
+            const int bi = (int)(u / rows), i = (int)(u % rows);
+            const int blk = warp + bi * NW;
+            if (blk < nblk) {
+                const int4* left = cols + (long long)(blk > 0 ? blk - 1 : 0) * col_stride;
+                int4* out = cols + (long long)blk * col_stride;
+                if (i == 0) nobt_block_begin<K>(NOBT_LANE_ARGS, t, si, sj, lenj, blk, lane, left, out);
+                else nobt_block_row<K>(NOBT_LANE_ARGS, t, si, i, lenj, blk, lane, left, out);
+                if (blk == nblk - 1 && i == leni) {
+                    const int r = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
+                    if (lane == 0) *sres = r;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    return *sres;
+}
 
+constexpr int NOBT_K = 8;
+constexpr int NOBT_WARPS = 4;   // one pair per warp
+constexpr int COOP_WARPS = 8;   // one pair per CTA
+
+__device__ __forceinline__ void load_tables_smem(Tables& st, const Tables* g)
+{
+    for (int k = threadIdx.x; k < (int)(sizeof(Tables) / 4); k += blockDim.x)
+        reinterpret_cast<int*>(&st)[k] = reinterpret_cast<const int*>(g)[k];
+    __syncthreads();
+}
+
+// Pair k's screening, as DOS.distance / cost_affine_3 need it (warp-uniform).
+struct NobtPair {
+    const uint8_t *si, *sj;
+    int li, lj, k;
+    int cost, status;
+    bool run;  // the fill has to run
+};
+
+__device__ NobtPair nobt_screen(const NobtArgs& A, const Tables& st, int k, int lane)
+{
+    NobtPair q;
+    q.k = k;
+    const int la = A.lena[k], lb = A.lenb[k];
+    const uint8_t* a = A.seqs + A.offa[k];
+    const uint8_t* b = A.seqs + A.offb[k];
+    // states must index the tables; distance: all-gap sequences are "missing"
+    int bad = 0, ga = 1, gb = 1;
+    const int ns = 1 << st.lcm;
+    for (int i = lane; i < la; i += 32) {
+        bad |= a[i] >= ns;
+        ga &= a[i] == st.gap;
+    }
+    for (int i = lane; i < lb; i += 32) {
+        bad |= b[i] >= ns;
+        gb &= b[i] == st.gap;
+    }
+    bad = __any_sync(FULL, bad);
+    ga = __all_sync(FULL, ga);
+    gb = __all_sync(FULL, gb);
+    q.cost = 0;
+    q.status = 0;
+    q.run = false;
+    const bool sw = la > lb;  // the shorter sequence runs down the rows
+    q.si = sw ? b : a;
+    q.sj = sw ? a : b;
+    q.li = sw ? lb : la;
+    q.lj = sw ? la : lb;
+    if (la < 1 || lb < 1) q.status = -4;
+    else if (bad) q.status = -7;
+    else if (A.missing_distance != NOBT_NO_MISSING && (ga || gb)) q.cost = A.missing_distance;
+    else if (la > 65535 || lb > 65535 || q.li > A.bnd_stride) q.status = -6;
+    else q.run = true;
+    return q;
+}
+
+// Pairs ncoop .. npairs - 1 of the visiting order, one warp each.
 __global__ void __launch_bounds__(32 * NOBT_WARPS) nobt_kernel(NobtArgs A)
 {
     __shared__ Tables st;
-    for (int k = threadIdx.x; k < (int)(sizeof(Tables) / 4); k += blockDim.x)
-        reinterpret_cast<int*>(&st)[k] = reinterpret_cast<const int*>(A.tables)[k];
-    __syncthreads();
+    load_tables_smem(st, A.tables);
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int4* bnd = A.bnd + (long long)gw * A.bnd_stride;
     for (;;) {
         int w = 0;
-        if (lane == 0) w = atomicAdd(A.next, 1);
+        if (lane == 0) w = A.ncoop + atomicAdd(A.next, 1);
         w = __shfl_sync(FULL, w, 0);
         if (w >= A.npairs) break;
-        const int k = A.order ? A.order[w] : w;
-        const int la = A.lena[k], lb = A.lenb[k];
-        const uint8_t* a = A.seqs + A.offa[k];
-        const uint8_t* b = A.seqs + A.offb[k];
-        // states must index the tables; distance: all-gap sequences are "missing"
-        int bad = 0, ga = 1, gb = 1;
-        const int ns = 1 << st.lcm;
-        for (int i = lane; i < la; i += 32) {
-            bad |= a[i] >= ns;
-            ga &= a[i] == st.gap;
-        }
-        for (int i = lane; i < lb; i += 32) {
-            bad |= b[i] >= ns;
-            gb &= b[i] == st.gap;
-        }
-        bad = __any_sync(FULL, bad);
-        ga = __all_sync(FULL, ga);
-        gb = __all_sync(FULL, gb);
-        int cost = 0, status = 0;
-        if (la < 1 || lb < 1) {
-            status = -4;
-        } else if (bad) {
-            status = -7;
-        } else if (A.missing_distance != NOBT_NO_MISSING && (ga || gb)) {
-            cost = A.missing_distance;
-        } else if (la > 65535 || lb > 65535 || tmin(la, lb) > A.bnd_stride) {
-            status = -6;
-        } else {
-            const bool sw = la > lb;  // the shorter sequence runs down the rows
-            const uint8_t* si = sw ? b : a;
-            const uint8_t* sj = sw ? a : b;
-            const int li = sw ? lb : la, lj = sw ? la : lb;
-            if (lj <= 2) {
-                if (lane == 0) cost = nobt_tiny(st, si, li, sj, lj);
-                cost = __shfl_sync(FULL, cost, 0);
+        NobtPair q = nobt_screen(A, st, A.order ? A.order[w] : w, lane);
+        if (q.run) {
+            if (q.lj <= 2) {
+                if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
+                q.cost = __shfl_sync(FULL, q.cost, 0);
             } else {
-                cost = nobt_warp<NOBT_K>(st, si, li, sj, lj, bnd, lane);
+                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, bnd, lane);
             }
         }
         if (lane == 0) {
-            A.cost[k] = cost;
-            A.status[k] = status;
+            A.cost[q.k] = q.cost;
+            A.status[q.k] = q.status;
         }
         __syncwarp();
+    }
+}
+
+// Pairs 0 .. ncoop - 1 of the visiting order (the longest), one CTA each:
+// lower latency for small batches of long pairs.
+__global__ void __launch_bounds__(32 * COOP_WARPS) nobt_coop_kernel(NobtArgs A)
+{
+    __shared__ Tables st;
+    __shared__ int sw, sres;
+    load_tables_smem(st, A.tables);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int4* cols = A.coop_cols + (long long)blockIdx.x * A.coop_stride;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) sw = atomicAdd(A.next_coop, 1);
+        __syncthreads();
+        const int w = sw;
+        if (w >= A.ncoop) break;
+        NobtPair q = nobt_screen(A, st, A.order ? A.order[w] : w, lane);
+        const int nblk = (q.lj + 32 * NOBT_K - 1) / (32 * NOBT_K);
+        if (q.run && q.lj > 2 && q.li >= COOP_WARPS &&
+            (long long)nblk * A.bnd_stride <= A.coop_stride) {
+            q.cost = nobt_coop<NOBT_K, COOP_WARPS>(st, q.si, q.li, q.sj, q.lj, cols,
+                                                    A.bnd_stride, warp, lane, &sres);
+        } else if (q.run && warp == 0) {  // short or narrow pairs: warp 0 alone
+            if (q.lj <= 2) {
+                if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
+                q.cost = __shfl_sync(FULL, q.cost, 0);
+            } else {
+                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, cols, lane);
+            }
+        }
+        if (threadIdx.x == 0) {
+            A.cost[q.k] = q.cost;
+            A.status[q.k] = q.status;
+        }
     }
 }
 
@@ -369,9 +498,12 @@ int nobt_blocks_per_sm()
     return n;
 }
 
-void launch_nobt(const NobtArgs& a, int grid, cudaStream_t s)
+int nobt_coop_columns(int maxlen) { return (maxlen + 32 * NOBT_K - 1) / (32 * NOBT_K); }
+
+void launch_nobt(const NobtArgs& a, int grid, int coop_grid, cudaStream_t s)
 {
-    nobt_kernel<<<grid, 32 * NOBT_WARPS, 0, s>>>(a);
+    if (a.ncoop > 0) nobt_coop_kernel<<<coop_grid, 32 * COOP_WARPS, 0, s>>>(a);
+    if (a.ncoop < a.npairs) nobt_kernel<<<grid, 32 * NOBT_WARPS, 0, s>>>(a);
 }
 
 }  // namespace pa

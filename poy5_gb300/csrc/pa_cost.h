@@ -20,15 +20,21 @@ struct NobtArgs {
     const Tables* tables;
     const int* order;         // optional visiting order (longest first)
     int missing_distance;     // cost of pairs with an all-gap sequence
-    int* next;                // work counter, zero before the launch
+    int* next;                // work counters (one pair per warp; one per CTA), zero
+    int* next_coop;           // before the launch
+    int ncoop;                // the first ncoop pairs of the order go one per CTA
     int4* bnd;                // per warp: block boundary column, bnd_stride rows
     int bnd_stride;           // >= the shorter length of every pair
+    int4* coop_cols;          // per CTA of the cooperative kernel: one column per
+    long long coop_stride;    // column block, bnd_stride rows each
     int* cost;
     int* status;              // 0 ok, -4 empty, -6 too long, -7 bad state
 };
 
 int nobt_warps_per_cta();
 int nobt_blocks_per_sm();
-void launch_nobt(const NobtArgs& a, int grid, cudaStream_t s);
+// column blocks of a pair whose longer sequence has maxlen positions
+int nobt_coop_columns(int maxlen);
+void launch_nobt(const NobtArgs& a, int grid, int coop_grid, cudaStream_t s);
 
 }  // namespace pa

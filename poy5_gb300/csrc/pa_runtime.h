@@ -55,7 +55,7 @@ struct poyalgn_ctx {
     // per-batch scratch
     pa::DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
     pa::DevBuf dwh, swp, order, order_scratch;
-    pa::DevBuf nobt_bnd, nobt_ctr;  // cost-only affine fill: boundary columns, work counter
+    pa::DevBuf nobt_bnd, nobt_ctr, nobt_coop;  // cost-only affine fill scratch
     int last_launches = 0;
     // upper bound on the direction-slab arena of one batch (0: half the free
     // device memory, at most 64 GB)
@@ -101,15 +101,15 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs, int 
               int distance = 0, int missing_distance = 0);
 
 // Enqueue the cost-only affine fill (algn_CAML_cost_affine_3 semantics) of
-// npairs pairs; min_len bounds the shorter length of every pair. missing:
+// npairs pairs; max_pair_len bounds la + lb of every pair. missing:
 // cost of pairs with an all-gap sequence (NOBT_NO_MISSING: no such rule).
-int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int min_len,
+int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
              const uint8_t* seqs, const long long* offa, const int* lena,
              const long long* offb, const int* lenb, int missing, int* cost, int* status,
              cudaStream_t st);
-// Reserve run_nobt's scratch for up to max_pairs pairs of shorter length up
-// to min_len.
-int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int min_len);
+// Reserve run_nobt's scratch for up to max_pairs pairs of lengths up to
+// max_len.
+int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int max_len);
 
 // Reserve the per-batch scratch of run_batch for batches of up to max_pairs
 // pairs, out_total output bytes and a slab arena of slab_bytes, so that such

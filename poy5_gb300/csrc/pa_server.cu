@@ -143,7 +143,7 @@ int launch(poyalgn_server* s, Slot& sl, std::vector<Req*>& batch)
         // cost at I, status at I + 5 ni, like the median layout; no medians
         CU(cudaMemsetAsync(I + 3 * ni, 0, ni * sizeof(int), st));
         if (s->affine)
-            rc = run_nobt(c, s->cm, n, maxmn / 2, s->arena, d_offa, d_lena, d_offa + ni,
+            rc = run_nobt(c, s->cm, n, maxmn, s->arena, d_offa, d_lena, d_offa + ni,
                           d_lena + ni, s->missing, I, I + 5 * ni, st);
         else
             rc = run_batch(c, s->cm, 0, n, maxmn, 1, s->arena, d_offa, d_lena, d_offa + ni,
