@@ -421,6 +421,15 @@ int poyalgn_autotune(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
                      const int32_t *cand_R, int reps, float *ms,
                      int32_t *best);
 
+/*
+ * Lean affine passes (gap-free pairs) with bands up to 512 cells wide run
+ * either on the lane pipeline (throughput) or on a row tile, one pair per
+ * warp swept row by row (latency). mode 0: lane pipeline; 1: row tile;
+ * 2 (default): row tile for batches of at most 2 pairs per SM. Results are
+ * identical. No counterpart in the reference.
+ */
+int poyalgn_set_row_tile(poyalgn_ctx *ctx, int mode);
+
 /* Number of kernel launches the last batch enqueued (for accounting). */
 int poyalgn_last_launches(const poyalgn_ctx *ctx);
 

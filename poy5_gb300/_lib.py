@@ -71,6 +71,7 @@ _SIGS = {
     "poyalgn_cost_affine_3": (_I, [_P, _P, _P, _I, _P, _I, _P]),
     "poyalgn_distance_batch": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P]),
     "poyalgn_distance_batch_device": (_I, [_P, _P, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
+    "poyalgn_set_row_tile": (_I, [_P, _I]),
     "poyalgn_last_launches": (_I, [_P]),
     "poyalgn_profile_begin": (_I, [_P, _I]),
     "poyalgn_profile_end": (_I, [_P, _P, _P]),

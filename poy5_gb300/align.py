@@ -73,6 +73,10 @@ class Context:
     def last_launches(self) -> int:
         return _lib.load().poyalgn_last_launches(self._h)
 
+    def set_row_tile(self, mode: int):
+        """0: lane pipeline, 1: row tile, 2: by batch size (lean affine passes)."""
+        check(_lib.load().poyalgn_set_row_tile(self._h, int(mode)))
+
     def profile_begin(self, max_batches: int):
         """Record per-launch CUDA events for the next `max_batches` batches."""
         check(_lib.load().poyalgn_profile_begin(self._h, int(max_batches)))

@@ -61,6 +61,8 @@ int ensure_device(poyalgn_ctx* c)
     return 0;
 }
 
+constexpr int ROW_TILE_MAX_PAIRS = 2;  // per SM, for row_tile_mode 2
+
 // Enqueue one batch on `st`. All pointers are device pointers. `out_total`
 // bounds out_off[k] + cap_k (sizes the affine row-0 scratch).
 int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
@@ -74,6 +76,10 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
 {
     int rc;
     if (npairs <= 0) return 0;
+    // the row tile has the lower latency per pair, the lane pipeline the
+    // higher throughput: small batches take the row tile
+    const int row_tile = affine && (c->row_tile_mode == 1 ||
+                                    (c->row_tile_mode == 2 && npairs <= ROW_TILE_MAX_PAIRS * c->nsm));
     if ((rc = reserve(c->pfull, (size_t)npairs * 4))) return rc;
     if ((rc = reserve(c->eh0, (size_t)npairs * 4))) return rc;
     if ((rc = reserve(c->lastcls, (size_t)npairs * 4))) return rc;
@@ -96,10 +102,12 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     long long strides[NCLASS];
     long long arena = 0;
     for (int k = 0; k < NCLASS; k++) {
-        const int pipes = class_pipes_per_cta(c->lad[affine], k);
-        strides[k] = class_slab_bytes(c->lad[affine], affine, k, maxmn);
+        strides[k] = class_slab_bytes(c->lad[affine], affine, k, maxmn, row_tile);
         for (int v = 0; v < 2; v++) {
-            long long g = (long long)c->nsm * std::max(1, c->bps[affine][k][v]);
+            const int pipes = class_pipes_per_cta(c->lad[affine], affine, k, v, row_tile);
+            const int bps = class_row_tile(c->lad[affine], affine, k, v, row_tile)
+                                ? c->bps_rt[k] : c->bps[affine][k][v];
+            long long g = (long long)c->nsm * std::max(1, bps);
             g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
             g = std::min<long long>(g, std::max<long long>(1, budget / (strides[k] * pipes)));
             grid[k][v] = (int)std::max<long long>(1, g);
@@ -124,6 +132,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.distance = distance;
     A.missing_distance = missing_distance;
     A.lad = c->lad[affine];
+    A.row_tile = row_tile;
     A.tables = cm->d;
     A.pfull = as<int>(c->pfull);
     A.shadow = as<int>(c->shadow);
@@ -368,6 +377,7 @@ int trace_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
     A.mlen = ints + 3;
     A.wlen = ints + 4;
     A.status = ints + 5;
+    A.passes = ints + 6;  // written by the fill (fill_pair): locates the final band
     A.lastcls = as<int>(c->lastcls);
     A.slab_cta = as<int>(c->slabcta);
     A.swap_override = as<int>(c->swp);
@@ -410,7 +420,8 @@ int poyalgn_init(int device, poyalgn_ctx** out)
     }
     for (int a = 0; a < 2; a++)
         for (int k = 0; k < NCLASS; k++)
-            for (int v = 0; v < 2; v++) c->bps[a][k][v] = class_blocks_per_sm(c->lad[a], a, k, v);
+            for (int v = 0; v < 2; v++) c->bps[a][k][v] = class_blocks_per_sm(c->lad[a], a, k, v, 0);
+    for (int k = 0; k < NCLASS; k++) c->bps_rt[k] = class_blocks_per_sm(c->lad[1], 1, k, 1, 1);
     *out = c;
     return 0;
 }
@@ -739,6 +750,14 @@ int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
 
 int poyalgn_num_classes(void) { return NCLASS; }
 
+int poyalgn_set_row_tile(poyalgn_ctx* ctx, int mode)
+{
+    if (!ctx || mode < 0 || mode > 2) return set_err(POYALGN_EINVAL, "bad row tile mode");
+    ctx->row_tile_mode = mode;
+    ctx->call_valid = false;
+    return 0;
+}
+
 int poyalgn_cost_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* si, int li,
                           const uint8_t* sj, int lj, int32_t* cost)
 {
@@ -840,8 +859,10 @@ int poyalgn_set_ladder(poyalgn_ctx* ctx, int affine, const int32_t* P, const int
     int rc;
     if ((rc = ensure_device(ctx))) return rc;
     ctx->lad[affine] = L;
-    for (int k = 0; k < NCLASS; k++)
-        for (int v = 0; v < 2; v++) ctx->bps[affine][k][v] = class_blocks_per_sm(L, affine, k, v);
+    for (int k = 0; k < NCLASS; k++) {
+        for (int v = 0; v < 2; v++) ctx->bps[affine][k][v] = class_blocks_per_sm(L, affine, k, v, 0);
+        if (affine) ctx->bps_rt[k] = class_blocks_per_sm(L, 1, k, 1, 1);
+    }
     CU(cudaGetLastError());
     ctx->call_valid = false;  // a kept per-call fill was laid out for the old ladder
     return 0;
@@ -929,7 +950,8 @@ int poyalgn_autotune(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs, const u
             L.P[k] = cand_P[q * NCLASS + k];
             L.R[k] = cand_R[q * NCLASS + k];
             for (int v = 0; v < 2; v++)
-                ctx->bps[affine][k][v] = class_blocks_per_sm(L, affine, k, v);
+                ctx->bps[affine][k][v] = class_blocks_per_sm(L, affine, k, v, 0);
+            if (affine) ctx->bps_rt[k] = class_blocks_per_sm(L, 1, k, 1, 1);
         }
         ctx->lad[affine] = L;
         if ((rc = batch())) break;
@@ -1006,7 +1028,7 @@ int noalloc_device(int dev, const NoAllocDevice** out)
         for (int a = 0; a < 2; a++)
             for (int k = 0; k < NCLASS; k++)
                 for (int v = 0; v < 2; v++)
-                    d.bps[a][k][v] = class_blocks_per_sm(default_ladder(a), a, k, v);
+                    d.bps[a][k][v] = class_blocks_per_sm(default_ladder(a), a, k, v, 0);
         CU(cudaGetLastError());
         d.base = static_cast<unsigned char*>(p);
         d.ready = true;
@@ -1090,13 +1112,13 @@ extern "C" int poyalgn_median_batch_device_noalloc(
     long long strides[NCLASS];
     long long arena = 0;
     for (int k = 0; k < NCLASS; k++) {
-        const int pipes = class_pipes_per_cta(lad, k);
-        strides[k] = class_slab_bytes(lad, affine, k, max_pair_len);
-        if (strides[k] * pipes > budget)
-            return set_err(POYALGN_EINVAL,
-                           "max_pair_len %d leaves no room for class %d in POYALGN_NOALLOC_SCRATCH_BYTES",
-                           max_pair_len, k);
+        strides[k] = class_slab_bytes(lad, affine, k, max_pair_len, 0);
         for (int v = 0; v < 2; v++) {
+            const int pipes = class_pipes_per_cta(lad, affine, k, v, 0);
+            if (strides[k] * pipes > budget)
+                return set_err(POYALGN_EINVAL,
+                               "max_pair_len %d leaves no room for class %d in POYALGN_NOALLOC_SCRATCH_BYTES",
+                               max_pair_len, k);
             long long g = (long long)d->nsm * std::max(1, d->bps[affine][k][v]);
             g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
             g = std::min<long long>(g, budget / (strides[k] * pipes));

@@ -122,11 +122,36 @@ PA_HD bool band_fits(int P, int R, long long wu, int n)
     return (wu <= 2 * pr + 1) || (pr >= n);
 }
 
+// Band capacity of class c: 2 (P - 1) R + 1.
+PA_HD long long ladder_cap(const Ladder& L, int c) { return 2LL * (L.P[c] - 1) * L.R[c] + 1; }
+
 // Smallest class of the ladder for a band; -1 if none. wu < 0: full plane.
 PA_HD int pick_class(const Ladder& L, long long wu, int n)
 {
     for (int c = 0; c < NCLASS; c++)
         if (band_fits(L.P[c], L.R[c], wu < 0 ? (1LL << 40) : wu, n)) return c;
+    return -1;
+}
+
+// Class of a lean affine band: classes up to 32 * RK_MAXK wide run on the
+// row tile (band of unclipped width wu <= 32 K), wider ones on the lane
+// pipeline.
+constexpr int RK_MAXK = 16;  // widest row tile: 512 positions
+
+// The tile width a class of capacity cap (2 (P - 1) R + 1) runs on, or 0
+// for classes wider than RK_MAXK * 32 (lane pipeline).
+PA_HD int rk_k_for(long long cap)
+{
+    for (int k = 1; k <= RK_MAXK; k <<= 1)
+        if (32LL * k >= cap) return k;
+    return 0;
+}
+PA_HD int pick_class_lean(const Ladder& L, long long wu, int n)
+{
+    for (int c = 0; c < NCLASS; c++) {
+        const int k = rk_k_for(2LL * (L.P[c] - 1) * L.R[c] + 1);
+        if (k > 0 ? wu <= 32LL * k : band_fits(L.P[c], L.R[c], wu, n)) return c;
+    }
     return -1;
 }
 
@@ -1017,6 +1042,182 @@ PA_HD int lean_gen_steps(const AffBand& b, int P, int R)
 PA_HD int lean_final(const LeanCell& c) { return min3(c.EH, c.EV, c.CB); }
 PA_HD int lean_gapnum(const LeanCell& c) { return tmax((int)(c.GM & 0xFFFF), (int)(c.GM >> 16)); }
 
+// ---------------------------------------------------------------------------
+// Row tile for the lean affine band ("row kernel"): one pair per warp, row
+// after row. Lane l holds the band cells of skewed positions
+// d = l * K + q (q < K), d = j - i + newk, so the band of every row lies in
+// d in [0, 32 K) when its unclipped width wu = D + 2 newk + 1 <= 32 K. In
+// skewed positions a cell's diagonal neighbour (i-1, j-1) sits at the same
+// d and its up neighbour (i-1, j) at d + 1, both in the previous row, which
+// the lanes keep in registers; the left neighbour (i, j-1) at d - 1 is in
+// the same row: EH[j] = min(EH[j-1] + jgr, CB[j-1] + go + jgr) and the gap
+// numbers GM[j] = max(a_j, hh_j ? GM[j-1] + 1 : 0) are solved per row by
+// composing each lane's K maps and scanning the compositions across the
+// warp (min-plus maps for EH, per-halfword max-plus maps for GM). Cells and
+// flags are those of aff_lean_step; direction bytes are stored row-major,
+// code(i, j) at dm[i * 32 K + d].
+
+// x -> min(x + s, t), composed left to right
+struct MinPlus {
+    int s, t;
+};
+constexpr int MP_BIG = 1 << 29;  // "no path" inside a composed map; + HIGH stays < 2^31
+PA_HD MinPlus mp_then(MinPlus f, MinPlus g)  // g after f
+{
+    return MinPlus{tmin(f.s + g.s, MP_BIG), tmin(tmin(f.t + g.s, MP_BIG), g.t)};
+}
+PA_HD int mp_apply(MinPlus f, int x) { return tmin(x + f.s, f.t); }
+
+// x -> act ? vmax2(floor, x + add) : floor on packed u16 pairs (counts stay
+// below 2^16, so max distributes over the addition)
+struct GmMap {
+    int act;
+    uint32_t add, floor;
+};
+PA_HD GmMap gm_then(GmMap f, GmMap g)  // g after f
+{
+    if (!g.act) return g;
+    if (!f.act) return GmMap{0, 0u, vmax2(g.floor, f.floor + g.add)};
+    return GmMap{1, f.add + g.add, vmax2(g.floor, f.floor + g.add)};
+}
+PA_HD uint32_t gm_apply(GmMap g, uint32_t x) { return g.act ? vmax2(g.floor, x + g.add) : g.floor; }
+
+
+// Row constants shared by the warp.
+struct RkRow {
+    int i, ic, sg, sgo, srow;
+    int s, e, tr;  // band [s, e] of the row, right-border column tr
+};
+PA_HD RkRow rk_row(const AffBand& b, const Tables& t, const uint8_t* si, int i)
+{
+    RkRow r;
+    r.i = i;
+    r.ic = si[i];
+    r.sg = tcost(t, r.ic, t.gap);
+    r.sgo = r.sg + t.go;
+    r.srow = t.rowoff[r.ic];
+    r.s = tmax(0, i - b.newk);
+    r.tr = i + b.D + b.newk;
+    r.e = tmin(b.n - 1, r.tr);
+    return r;
+}
+
+// Row 0 cell of position d (prefix sums of the prepend costs; CB and EH
+// from the caller's scan). GM = j insertions.
+PA_HD LeanCell rk_row0(int j, int cb, int shadowEH0)
+{
+    LeanCell c;
+    c.CB = j == 0 ? 0 : cb;
+    c.EH = j == 0 ? shadowEH0 : cb;
+    c.EV = HIGH;
+    c.GM = (uint32_t)tmax(j, 0);
+    return c;
+}
+// prepend term of row 0's column j (j >= 1)
+PA_HD int rk_row0_term(const Tables& t, const uint8_t* sj, int j)
+{
+    const int gr = t.prepend[sj[j]];
+    return (j == 1 && (sj[0] & t.gap)) ? t.go + gr : gr;
+}
+
+// Phase A of one lane's K cells of row r (first column j0): EV and CB from
+// the previous row (P: this lane's previous row, upn: the next lane's P[0]).
+template <int K>
+PA_HD void rk_phase_a(const LeanCell (&P)[K], const LeanCell& upn, const int (&J)[K],
+                      const RkRow& r, const Tables& t, int j0, int (&EV)[K], int (&CB)[K],
+                      int (&code)[K])
+{
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = j0 + q;
+        const LeanCell& up = q + 1 < K ? P[q + 1] : upn;
+        const LeanCell& dg = P[q];
+        bool endv;
+        const int ev = bmin_le(up.CB + r.sgo, up.EV + r.sg, &endv);
+        const bool right = j == r.tr;
+        EV[q] = right ? HIGH : ev;
+        const int m3 = min3(dg.CB, dg.EV, dg.EH);
+        const int dgc = t.csw[r.srow + J[q]];
+        CB[q] = j > 0 ? m3 + dgc : HIGH;
+        code[q] = ((!right && endv) ? LEAN_END_V : 0) |
+                  (j > 0 ? ((dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0)) : 0);
+    }
+}
+
+// The lane's composed EH map (cbl: the current row's CB at this lane's
+// d - 1, i.e. the previous lane's last CB).
+template <int K>
+PA_HD MinPlus rk_eh_map(const int (&JG)[K], const int (&CB)[K], const RkRow& r, int go, int j0,
+                        int cbl)
+{
+    MinPlus f{0, MP_BIG};
+    int cprev = cbl;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const bool left = j0 + q == r.s;
+        f = mp_then(f, left ? MinPlus{MP_BIG, HIGH}
+                            : MinPlus{JG[q], tmin(cprev + go + JG[q], MP_BIG)});
+        cprev = CB[q];
+    }
+    return f;
+}
+
+// Phase B: EH from the incoming EH[d-1] (x), the cell minima and flags, and
+// the lane's composed gap-number map.
+template <int K>
+PA_HD GmMap rk_phase_b(const LeanCell (&P)[K], const LeanCell& upn, const int (&JG)[K],
+                       const RkRow& r, const Tables& t, int j0, int x, int cbl,
+                       const int (&EV)[K], const int (&CB)[K], int (&EH)[K], int (&code)[K],
+                       int (&hv)[K], uint32_t (&fl)[K])
+{
+    const int go = t.go;
+    GmMap g{1, 0u, 0u};
+    int cprev = cbl;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = j0 + q;
+        const LeanCell& up = q + 1 < K ? P[q + 1] : upn;
+        const LeanCell& dg = P[q];
+        bool endh;
+        const int eh = bmin_le(cprev + go + JG[q], x + JG[q], &endh);
+        const bool left = j == r.s;
+        EH[q] = left ? HIGH : eh;
+        x = EH[q];
+        cprev = CB[q];
+        const int f = min3(EH[q], EV[q], CB[q]);
+        const bool hh = EH[q] == f, vv = EV[q] == f;
+        code[q] |= ((!left && endh) ? LEAN_END_H : 0) | (hh ? LEAN_DO_H : 0) |
+                   (vv ? LEAN_DO_V : 0) | ((hh && vv) ? LEAN_H_EQ_V : 0);
+        fl[q] = vmax2(CB[q] == f ? dg.GM : 0u, vv ? up.GM + 0x10000u : 0u);
+        hv[q] = hh;
+        g = gm_then(g, GmMap{hh ? 1 : 0, hh ? 1u : 0u, fl[q]});
+    }
+    return g;
+}
+
+// Phase C: gap numbers from the incoming GM[d-1] (y); the new row replaces P
+// in band cells (cells outside the band keep their old state).
+template <int K>
+PA_HD void rk_phase_c(LeanCell (&P)[K], const RkRow& r, int j0, uint32_t y, const int (&EH)[K],
+                      const int (&EV)[K], const int (&CB)[K], const int (&hv)[K],
+                      const uint32_t (&fl)[K], int (&code)[K])
+{
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = j0 + q;
+        y = hv[q] ? vmax2(fl[q], y + 1u) : fl[q];
+        const bool in = j >= r.s && j <= r.e;
+        if (in) {
+            P[q].EH = EH[q];
+            P[q].EV = EV[q];
+            P[q].CB = CB[q];
+            P[q].GM = y;
+        } else {
+            code[q] = 0;
+        }
+    }
+}
+
 // Final cost of the affine corner cell from its four states.
 PA_HD int aff_final(const AffCell& c) { return tmin(tmin(c.EH, c.EV), tmin(c.EB, c.CB)); }
 PA_HD int aff_gapnum(const AffCell& c) { return tmax((int)(c.GM & 0xFFFF), (int)(c.GM >> 16)); }
@@ -1224,6 +1425,15 @@ struct AffDmLean {
     int P, R;
     PA_HDM int operator()(int i, int j) const { return lean_flags(dm[dm_index(P, R, i, j)]); }
 };
+// row tile: code(i, j) at dm[i * S + j - i + newk]
+struct AffDmRow {
+    const uint8_t* dm;
+    int S, newk;
+    PA_HDM int operator()(int i, int j) const
+    {
+        return lean_flags(dm[(long long)i * S + (j - i + newk)]);
+    }
+};
 
 // algn_calculate_from_2_aligned on the worst table, bitset alphabet
 PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int L)
@@ -1356,6 +1566,14 @@ PA_HD PairRes aff_traceback_lean(const uint8_t* dm, int P, int R, const Tables& 
                                  const PairOut& o)
 {
     AffDmLean rd{dm, P, R};
+    return aff_traceback_dm(rd, t, x, m, y, n, swaped, o);
+}
+
+PA_HD PairRes aff_traceback_rowtile(const uint8_t* dm, int S, int newk, const Tables& t,
+                                    const uint8_t* x, int m, const uint8_t* y, int n, int swaped,
+                                    const PairOut& o)
+{
+    AffDmRow rd{dm, S, newk};
     return aff_traceback_dm(rd, t, x, m, y, n, swaped, o);
 }
 

@@ -8,6 +8,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <array>
 #include <vector>
 
 #include "pa_core.cuh"
@@ -149,6 +150,135 @@ void aff_pass_lean(const AffBand& b, int P, const Tables& t, const uint8_t* x,
     *gapnum = lean_gapnum(c);
 }
 
+// The row tile, lane by lane: each cross-lane step of the kernel (shuffles,
+// exclusive scans of the composed maps) is done over arrays of the 32 lanes.
+template <int K>
+void aff_pass_rk(const AffBand& b, const Tables& t, const uint8_t* x, const uint8_t* y,
+                 uint8_t* dm, int shadowEH0, int* cost, int* gapnum)
+{
+    constexpr int S = 32 * K;
+    const int newk = b.newk, n = b.n;
+    std::vector<std::array<LeanCell, K>> P(32);
+    std::vector<std::array<int, K>> J(32), JG(32);
+    // row 0: prefix sums of the prepend terms
+    {
+        int run = 0;
+        for (int l = 0; l < 32; l++)
+            for (int q = 0; q < K; q++) {
+                const int j = l * K + q - newk;
+                run += (j >= 1 && j < n) ? rk_row0_term(t, y, j) : 0;
+                P[l][q] = rk_row0(j, run, shadowEH0);
+            }
+    }
+    for (int l = 0; l < 32; l++)
+        for (int q = 0; q < K; q++) {
+            const int j = 1 + l * K + q - newk;
+            J[l][q] = (j >= 0 && j < n) ? y[j] : 0;
+            JG[l][q] = t.prepend[J[l][q]];
+        }
+    for (int i = 1; i <= b.m - 1; i++) {
+        if (i > 1) {
+            for (int l = 0; l < 32; l++) {
+                for (int q = 0; q + 1 < K; q++) {
+                    J[l][q] = J[l][q + 1];
+                    JG[l][q] = JG[l][q + 1];
+                }
+                if (l < 31) {
+                    J[l][K - 1] = J[l + 1][0];
+                    JG[l][K - 1] = JG[l + 1][0];
+                } else {
+                    const int j = i + S - 1 - newk;
+                    J[l][K - 1] = (j >= 0 && j < n) ? y[j] : 0;
+                    JG[l][K - 1] = t.prepend[J[l][K - 1]];
+                }
+            }
+        }
+        const RkRow r = rk_row(b, t, x, i);
+        std::vector<std::array<int, K>> EV(32), CB(32), EH(32), code(32), hv(32);
+        std::vector<std::array<uint32_t, K>> fl(32);
+        std::vector<LeanCell> upn(32);
+        std::vector<MinPlus> F(32);
+        std::vector<GmMap> G(32);
+        std::vector<int> cbl(32);
+        for (int l = 0; l < 32; l++) upn[l] = l < 31 ? P[l + 1][0] : P[l][0];
+        for (int l = 0; l < 32; l++) {
+            LeanCell Pl[K];
+            int Jl[K], EVl[K], CBl[K], codel[K];
+            for (int q = 0; q < K; q++) {
+                Pl[q] = P[l][q];
+                Jl[q] = J[l][q];
+            }
+            rk_phase_a<K>(Pl, upn[l], Jl, r, t, i + l * K - newk, EVl, CBl, codel);
+            for (int q = 0; q < K; q++) {
+                EV[l][q] = EVl[q];
+                CB[l][q] = CBl[q];
+                code[l][q] = codel[q];
+            }
+        }
+        for (int l = 0; l < 32; l++) {
+            cbl[l] = l == 0 ? HIGH : CB[l - 1][K - 1];
+            int JGl[K], CBl[K];
+            for (int q = 0; q < K; q++) {
+                JGl[q] = JG[l][q];
+                CBl[q] = CB[l][q];
+            }
+            F[l] = rk_eh_map<K>(JGl, CBl, r, t.go, i + l * K - newk, cbl[l]);
+        }
+        MinPlus pre{0, MP_BIG};
+        std::vector<int> xin(32);
+        for (int l = 0; l < 32; l++) {
+            xin[l] = l == 0 ? HIGH : mp_apply(pre, HIGH);
+            pre = l == 0 ? F[0] : mp_then(pre, F[l]);
+        }
+        for (int l = 0; l < 32; l++) {
+            LeanCell Pl[K];
+            int JGl[K], EVl[K], CBl[K], EHl[K], codel[K], hvl[K];
+            uint32_t fll[K];
+            for (int q = 0; q < K; q++) {
+                Pl[q] = P[l][q];
+                JGl[q] = JG[l][q];
+                EVl[q] = EV[l][q];
+                CBl[q] = CB[l][q];
+                codel[q] = code[l][q];
+            }
+            G[l] = rk_phase_b<K>(Pl, upn[l], JGl, r, t, i + l * K - newk, xin[l], cbl[l], EVl,
+                                 CBl, EHl, codel, hvl, fll);
+            for (int q = 0; q < K; q++) {
+                EH[l][q] = EHl[q];
+                code[l][q] = codel[q];
+                hv[l][q] = hvl[q];
+                fl[l][q] = fll[q];
+            }
+        }
+        GmMap gpre{1, 0u, 0u};
+        for (int l = 0; l < 32; l++) {
+            const uint32_t yin = l == 0 ? 0u : gm_apply(gpre, 0u);
+            LeanCell Pl[K];
+            int EHl[K], EVl[K], CBl[K], hvl[K], codel[K];
+            uint32_t fll[K];
+            for (int q = 0; q < K; q++) {
+                Pl[q] = P[l][q];
+                EHl[q] = EH[l][q];
+                EVl[q] = EV[l][q];
+                CBl[q] = CB[l][q];
+                hvl[q] = hv[l][q];
+                fll[q] = fl[l][q];
+                codel[q] = code[l][q];
+            }
+            rk_phase_c<K>(Pl, r, i + l * K - newk, yin, EHl, EVl, CBl, hvl, fll, codel);
+            for (int q = 0; q < K; q++) {
+                P[l][q] = Pl[q];
+                dm[(long long)i * S + l * K + q] = (uint8_t)codel[q];
+            }
+            gpre = l == 0 ? G[0] : gm_then(gpre, G[l]);
+        }
+    }
+    const int dc = b.n - 1 - (b.m - 1) + newk;
+    const LeanCell c = P[dc / K][dc % K];
+    *cost = lean_final(c);
+    *gapnum = lean_gapnum(c);
+}
+
 struct Emul {
     HostCM cm;
     Tables t;
@@ -224,15 +354,19 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     int P = 32, R = 1, T = pl.T0, g = 0;
     *passes = 0;
     *last_class = -1;
+    const bool lean = gapfree && aff_lean_ok(t, tmax(la, lb));
+    int rk = 0, rk_newk = 0;
     for (;;) {
         AffBand bd = aff_band(m, n, band_p(T, m, n));
-        int c = pick_class(E.lad[1], aff_wu(bd), n);
+        int c = lean ? pick_class_lean(E.lad[1], aff_wu(bd), n) : pick_class(E.lad[1], aff_wu(bd), n);
         if (c < 0) return -5;
         P = E.lad[1].P[c];
         R = E.lad[1].R[c];
+        rk = lean ? rk_k_for(ladder_cap(E.lad[1], c)) : 0;
+        rk_newk = bd.newk;
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);
-        dm8.assign((size_t)(m + n + 1) * P * R, 0);
+        dm8.assign(std::max((size_t)(m + n + 1) * P * R, (size_t)m * 32 * (rk ? rk : 1)), 0);
         lean_last = false;
         (*passes)++;
         if (m == 1) {  // leni = 0: the initial row is the whole alignment
@@ -241,7 +375,16 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
             *cost = s;
             g = 0xFFFF;
         } else {
-            if (gapfree && aff_lean_ok(t, n)) {
+            if (lean && rk) {
+                lean_last = true;
+                switch (rk) {
+                    case 1: aff_pass_rk<1>(bd, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    case 2: aff_pass_rk<2>(bd, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    case 4: aff_pass_rk<4>(bd, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    case 8: aff_pass_rk<8>(bd, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    default: aff_pass_rk<16>(bd, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                }
+            } else if (lean) {
                 lean_last = true;
                 switch (R) {
                     case 1: aff_pass_lean<1>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
@@ -267,8 +410,10 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
         T *= 2;
     }
     PairOut o = {ea, eb, med, mwg, cap};
-    PairRes r = lean_last ? aff_traceback_lean(dm8.data(), P, R, t, x, m, y, n, pl.swaped, o)
-                          : aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    PairRes r = (lean_last && rk) ? aff_traceback_rowtile(dm8.data(), 32 * rk, rk_newk, t, x, m,
+                                                          y, n, pl.swaped, o)
+                : lean_last ? aff_traceback_lean(dm8.data(), P, R, t, x, m, y, n, pl.swaped, o)
+                            : aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
     res[0] = r.alen;
     res[1] = r.mlen;
     res[2] = r.wlen;

@@ -16,6 +16,8 @@
 // shared-memory tables are shared.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cub/device/device_radix_sort.cuh>
 #include <type_traits>
 
@@ -571,7 +573,8 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
         for (;;) {
             const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
             if (live) {
-                const int c = pick_class(A.lad, aff_wu(b), w.n);
+                const int c = (FAST && A.row_tile) ? pick_class_lean(A.lad, aff_wu(b), w.n)
+                                                   : pick_class(A.lad, aff_wu(b), w.n);
                 if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
                     if (p.gl == 0) {
                         if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
@@ -635,6 +638,202 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
             }
         }
         pipe_sync(p);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Row tile for lean affine bands up to 32 K wide: one pair per warp, the
+// band swept row by row (rk_* cell phases in pa_core.cuh). Direction bytes
+// are stored row-major, 32 K per row.
+
+template <int K>
+__device__ __forceinline__ void store_codes(uint8_t* p, const int (&c)[K])
+{
+    if constexpr (K == 16) {
+        uint32_t w[4];
+#pragma unroll
+        for (int h = 0; h < 4; h++)
+            w[h] = (uint32_t)c[4 * h] | ((uint32_t)c[4 * h + 1] << 8) |
+                   ((uint32_t)c[4 * h + 2] << 16) | ((uint32_t)c[4 * h + 3] << 24);
+        *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+    } else {
+        store_u8<K>(p, c);
+    }
+}
+
+template <int K>
+__device__ void aff_rk_fill(const AffBand& b, const Tables& st, const uint8_t* x,
+                            const uint8_t* y, uint8_t* dm, int shadowEH0, int lane, int& cost,
+                            int& gapnum)
+{
+    constexpr int S = 32 * K;
+    const int newk = b.newk, n = b.n, go = st.go;
+    LeanCell P[K];
+    int J[K], JG[K];
+    {  // row 0: prefix sums of the prepend terms
+        const int j0 = lane * K - newk;
+        int pre[K], run = 0;
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            const int j = j0 + q;
+            run += (j >= 1 && j < n) ? rk_row0_term(st, y, j) : 0;
+            pre[q] = run;
+        }
+        int incl = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int base = incl - run;
+#pragma unroll
+        for (int q = 0; q < K; q++) P[q] = rk_row0(j0 + q, base + pre[q], shadowEH0);
+    }
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int j = 1 + lane * K + q - newk;
+        J[q] = (j >= 0 && j < n) ? y[j] : 0;
+        JG[q] = st.prepend[J[q]];
+    }
+    for (int i = 1; i <= b.m - 1; i++) {
+        if (i > 1) {  // row i's column at d is row i-1's at d + 1
+            const int nj = __shfl_down_sync(FULL, J[0], 1);
+            const int ng = __shfl_down_sync(FULL, JG[0], 1);
+#pragma unroll
+            for (int q = 0; q + 1 < K; q++) {
+                J[q] = J[q + 1];
+                JG[q] = JG[q + 1];
+            }
+            J[K - 1] = nj;
+            JG[K - 1] = ng;
+            if (lane == 31) {
+                const int j = i + S - 1 - newk;
+                J[K - 1] = (j >= 0 && j < n) ? y[j] : 0;
+                JG[K - 1] = st.prepend[J[K - 1]];
+            }
+        }
+        const RkRow r = rk_row(b, st, x, i);
+        const int j0 = i + lane * K - newk;
+        LeanCell upn;
+        upn.EH = __shfl_down_sync(FULL, P[0].EH, 1);
+        upn.EV = __shfl_down_sync(FULL, P[0].EV, 1);
+        upn.CB = __shfl_down_sync(FULL, P[0].CB, 1);
+        upn.GM = __shfl_down_sync(FULL, P[0].GM, 1);
+        int EV[K], CB[K], EH[K], code[K], hv[K];
+        uint32_t fl[K];
+        rk_phase_a<K>(P, upn, J, r, st, j0, EV, CB, code);
+        int cbl = __shfl_up_sync(FULL, CB[K - 1], 1);
+        if (lane == 0) cbl = HIGH;
+        // EH: exclusive scan of the lanes' min-plus maps
+        MinPlus f = rk_eh_map<K>(JG, CB, r, go, j0, cbl);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ps = __shfl_up_sync(FULL, f.s, o);
+            const int pt = __shfl_up_sync(FULL, f.t, o);
+            if (lane >= o) f = mp_then(MinPlus{ps, pt}, f);
+        }
+        const MinPlus ex{__shfl_up_sync(FULL, f.s, 1), __shfl_up_sync(FULL, f.t, 1)};
+        const int xin = lane == 0 ? HIGH : mp_apply(ex, HIGH);
+        GmMap g = rk_phase_b<K>(P, upn, JG, r, st, j0, xin, cbl, EV, CB, EH, code, hv, fl);
+        // GM: a lane's composition is a constant unless every cell of it extends
+        // horizontally; scan only when some lane's is not
+        uint32_t yin;
+        if (__any_sync(FULL, g.act)) {
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int pa = __shfl_up_sync(FULL, g.act, o);
+                const uint32_t pd = __shfl_up_sync(FULL, g.add, o);
+                const uint32_t pf = __shfl_up_sync(FULL, g.floor, o);
+                if (lane >= o) g = gm_then(GmMap{pa, pd, pf}, g);
+            }
+            const GmMap ge{__shfl_up_sync(FULL, g.act, 1), __shfl_up_sync(FULL, g.add, 1),
+                           __shfl_up_sync(FULL, g.floor, 1)};
+            yin = lane == 0 ? 0u : gm_apply(ge, 0u);
+        } else {
+            yin = __shfl_up_sync(FULL, g.floor, 1);
+            if (lane == 0) yin = 0u;
+        }
+        rk_phase_c<K>(P, r, j0, yin, EH, EV, CB, hv, fl, code);
+        store_codes<K>(dm + (long long)i * S + lane * K, code);
+    }
+    const int dc = n - 1 - (b.m - 1) + newk;
+    const int cl = dc / K, cq = dc % K;
+    int f = 0, g = 0;
+#pragma unroll
+    for (int q = 0; q < K; q++)
+        if (q == cq) {
+            f = lean_final(P[q]);
+            g = lean_gapnum(P[q]);
+        }
+    cost = __shfl_sync(FULL, f, cl);
+    gapnum = __shfl_sync(FULL, g, cl);
+}
+
+// Class kernel of the row tile (lean queue of class cls, one pair per warp).
+template <int K>
+__global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, int cls)
+{
+    __shared__ Tables st;
+    __shared__ int sitem;
+    load_tables(st, A.tables);
+    __syncthreads();
+    const Pipe p = make_pipe(32);
+    const int q = 2 * cls + 1;
+    uint8_t* dm = A.slab + (long long)p.slot * A.slab_stride;
+    for (;;) {
+        const int base = pop_items(A, q, p, &sitem);
+        if (base < 0) break;
+        const int it = base + p.grp;
+        bool live = it < A.qcount[q];
+        Item w = live ? load_item(A, q, it) : empty_item(A);
+        bool finished = false;
+        int cost = 0, newk = 0;
+        while (live) {  // uniform across the warp: one pair
+            const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
+            const int c = pick_class_lean(A.lad, aff_wu(b), w.n);
+            if (c != cls || w.npass >= MAX_PASSES) {
+                if (p.lane == 0) {
+                    if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + 1, w.k, w.T);
+                    else A.status[w.k] = c < 0 ? -5 : -8;
+                }
+                live = false;
+                break;
+            }
+            int gapnum;
+            if (w.m == 1) {  // leni = 0: the initial row is the whole alignment
+                int s = st.go;
+                for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
+                cost = s;
+                gapnum = 0xFFFF;
+            } else {
+                aff_rk_fill<K>(b, st, w.x, w.y, dm, A.shadowEH0[w.k], p.lane, cost, gapnum);
+                if (p.lane == 0 && tmin(w.m - 1, b.newk) >= 2) A.shadowEH0[w.k] = HIGH;
+            }
+            newk = b.newk;
+            w.npass++;
+            if (p.lane == 0) A.passes[w.k] = w.npass;
+            __syncwarp();
+            if (aff_done(w.T, w.m, w.n, gapnum)) {
+                finished = true;
+                break;
+            }
+            w.T *= 2;
+        }
+        if (finished) {
+            if (p.lane == 0) {
+                A.lastcls[w.k] = cls | LASTCLS_LEAN | LASTCLS_ROW;
+                A.slab_cta[w.k] = p.slot;
+                if (!A.do_traceback) {
+                    A.cost[w.k] = cost;
+                    A.status[w.k] = 0;
+                } else {
+                    const PairRes r = aff_traceback_rowtile(dm, 32 * K, newk, st, w.x, w.m, w.y,
+                                                            w.n, w.swaped, pair_out(A, w.k));
+                    finish_pair(A, w.k, cost, r);
+                }
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -716,7 +915,11 @@ __global__ void prep_kernel(BatchArgs A)
         return;
     }
     int c;
-    if (A.affine) c = pick_class(A.lad, aff_wu(aff_band(pl.m, pl.n, band_p(pl.T0, pl.m, pl.n))), pl.n);
+    if (A.affine) {
+        const long long wu = aff_wu(aff_band(pl.m, pl.n, band_p(pl.T0, pl.m, pl.n)));
+        c = ((A.pfull[k] & 2) && A.row_tile) ? pick_class_lean(A.lad, wu, pl.n)
+                                              : pick_class(A.lad, wu, pl.n);
+    }
     else c = pick_class(A.lad, lin_wu(lin_band(pl.m, pl.n, pl.full, pl.full ? 0 : band_p(pl.T0, pl.m, pl.n))), pl.n);
     if (c < 0) {
         A.status[k] = -5;
@@ -740,10 +943,18 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
     const int tie = A.swap_override ? A.swap_override[k] : swaped;
     const int cls = A.lastcls[k] & LASTCLS_MASK;
     const bool lean = (A.lastcls[k] & LASTCLS_LEAN) != 0;
+    const bool row = (A.lastcls[k] & LASTCLS_ROW) != 0;
     const int P = A.lad.P[cls], R = A.lad.R[cls];
     const uint8_t* base = A.slab + (long long)A.slab_cta[k] * strides[cls];
     PairRes r;
-    if (A.affine && lean) r = aff_traceback_lean(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
+    if (A.affine && row) {
+        // the final pass's band: T doubled once per pass after the first
+        const PairPlan pl = plan_affine(t, la, lb);
+        const long long T = (long long)pl.T0 << tmax(A.passes[k] - 1, 0);
+        const AffBand b = aff_band(m, n, band_p((int)T, m, n));
+        r = aff_traceback_rowtile(base, 32 * rk_k_for(ladder_cap(A.lad, cls)), b.newk, t, x, m, y,
+                                  n, tie, pair_out(A, k));
+    } else if (A.affine && lean) r = aff_traceback_lean(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
     else if (A.affine) r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, tie, pair_out(A, k));
     else r = lin_traceback(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
     finish_pair(A, k, A.cost[k], r);
@@ -829,20 +1040,43 @@ static ClassKernel class_kernel(int affine, int R, int variant, bool narrow)
     return narrow ? lin_class_kernel<8, true> : lin_class_kernel<8, false>;
 }
 
-int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant)
+int class_row_tile(const Ladder& lad, int affine, int cls, int variant, int row_tile)
 {
+    return (affine && variant == 1 && row_tile) ? rk_k_for(ladder_cap(lad, cls)) : 0;
+}
+
+static ClassKernel row_tile_kernel(int k)
+{
+    switch (k) {
+        case 1: return aff_rk_kernel<1>;
+        case 2: return aff_rk_kernel<2>;
+        case 4: return aff_rk_kernel<4>;
+        case 8: return aff_rk_kernel<8>;
+        default: return aff_rk_kernel<16>;
+    }
+}
+
+int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant, int row_tile)
+{
+    int n = 0;
+    const int rk = class_row_tile(lad, affine, cls, variant, row_tile);
+    if (rk) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, row_tile_kernel(rk), 32 * NARROW_WARPS, 0);
+        return n;
+    }
     const int K = ladder_K(lad, cls), R = lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
-    int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, class_kernel(affine, R, variant, K == 1),
                                                   threads, 0);
     return n;
 }
 
-long long class_slab_bytes(const Ladder& lad, int affine, int cls, int maxmn)
+long long class_slab_bytes(const Ladder& lad, int affine, int cls, int maxmn, int row_tile)
 {
     const long long PR = (long long)lad.P[cls] * lad.R[cls];
     long long b = (long long)(maxmn + 1) * PR * (affine ? 2 : 1);
+    const int rk = class_row_tile(lad, affine, cls, 1, row_tile);  // 32 K bytes per row
+    b = std::max<long long>(b, (long long)(maxmn + 1) * 32 * rk);
     return (b + 255) & ~255LL;
 }
 
@@ -890,6 +1124,11 @@ void launch_prep(const BatchArgs& a, cudaStream_t s)
 
 void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream_t s)
 {
+    const int rk = class_row_tile(a.lad, a.affine, cls, variant, a.row_tile);
+    if (rk) {
+        row_tile_kernel(rk)<<<grid, 32 * NARROW_WARPS, 0, s>>>(a, cls);
+        return;
+    }
     const int K = ladder_K(a.lad, cls), R = a.lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     class_kernel(a.affine, R, a.affine ? variant : 0, K == 1)<<<grid, threads, 0, s>>>(a, cls);
@@ -912,8 +1151,9 @@ __global__ void order_keys_kernel(const int* lena, const int* lenb, int n, unsig
     idx[k] = k;
 }
 
-int class_pipes_per_cta(const Ladder& lad, int cls)
+int class_pipes_per_cta(const Ladder& lad, int affine, int cls, int variant, int row_tile)
 {
+    if (class_row_tile(lad, affine, cls, variant, row_tile)) return NARROW_WARPS;
     const int P = lad.P[cls];
     return P >= 64 ? 1 : NARROW_WARPS * (P < 32 ? 32 / P : 1);
 }

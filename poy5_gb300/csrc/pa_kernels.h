@@ -10,6 +10,7 @@ namespace pa {
 // lastcls[k]: class of pair k's final fill, plus LASTCLS_LEAN when that fill
 // wrote lean direction bytes (aff_lean_step) instead of aff_step words
 constexpr int LASTCLS_LEAN = 0x100;
+constexpr int LASTCLS_ROW = 0x200;  // lean fill on the row tile (row-major bytes)
 constexpr int LASTCLS_MASK = 0xFF;
 
 // Everything a batch launch needs, all device pointers.
@@ -25,6 +26,7 @@ struct BatchArgs {
     int distance;              // DOS.distance: deltaw = max 8 |la - lb|, all-gap -> missing
     int missing_distance;
     Ladder lad;                // pipeline classes of this model
+    int row_tile;              // lean affine classes up to 512 wide run on the row tile
     const Tables* tables;
     int* pfull;                // linear plane choice per pair
     int* shadow;               // affine: row-0 EB left by earlier iterations (n per pair)
@@ -57,10 +59,12 @@ struct BatchArgs {
 // Work queues: 2 per class (variant 1 = affine gap-free fast path).
 constexpr int NQUEUE = 2 * NCLASS;
 // Persistent CTAs per SM a class kernel can keep resident.
-int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant);
+int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant, int row_tile);
+// The row tile width of a class's lean queue (0: lane pipeline).
+int class_row_tile(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // Bytes of direction slab one pipeline of a class needs for pairs up to
 // maxmn = m + n.
-long long class_slab_bytes(const Ladder& lad, int affine, int cls, int maxmn);
+long long class_slab_bytes(const Ladder& lad, int affine, int cls, int maxmn, int row_tile);
 
 void launch_prep(const BatchArgs& a, cudaStream_t s);
 // Longest-first order of the pairs (by len(a) * len(b)) into `order`.
@@ -73,7 +77,7 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
 // path); d_strides[c] = slab bytes per pipeline of class c.
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
 // Pipelines per CTA of a class launch.
-int class_pipes_per_cta(const Ladder& lad, int cls);
+int class_pipes_per_cta(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // Column-wise medians of already aligned pairs (ancestor_2 / with-gaps / worst).
 void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
                             int len, uint8_t* anc, uint8_t* mwg, int* out3,

@@ -50,6 +50,8 @@ struct poyalgn_ctx {
     cudaStream_t stream = nullptr;
     pa::Ladder lad[2] = {pa::default_ladder(0), pa::default_ladder(1)};
     int bps[2][pa::NCLASS][2] = {};  // resident CTAs per SM: [affine][class][variant]
+    int bps_rt[pa::NCLASS] = {};     // the same for the row tile (affine, lean)
+    int row_tile_mode = 2;           // 0 lane pipeline, 1 row tile, 2 by batch size
     // host-pointer batches: staging of inputs and outputs
     pa::DevBuf seqs, offa, lena, offb, lenb, outoff, ints, bytes;
     // per-batch scratch

@@ -39,3 +39,35 @@ def test_every_candidate_ladder_gives_the_same_results(workload):
     with pytest.raises(pg.PoyAlgnError):
         tune.set_ladder(ctx, w.affine, [4] * 10, [3] * 10)
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_lean_paths_match_oracle(oracle, mode):
+    """Gap-free affine pairs on the lane pipeline (0) and on the row tile (1)."""
+    import poy5_gb300 as pg
+    from cases import random_pairs
+    ctx = pg.Context(0)
+    ctx.set_row_tile(mode)
+    w = wl.affine_pairs(n_pairs=160, seed=wl.SEED_BASE + 60)
+    rng = np.random.default_rng(61)
+    pairs = w.pairs + [(a, b) for a, b in random_pairs(rng, 200, maxlen=700, kinds=1)]
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    ocm = oracle.cm(subs=w.subs, indel=w.indel, gap_open=w.gap_open)
+    res = pg.median_batch(ctx, cm, pairs)
+    for k, (a, b) in enumerate(pairs):
+        try:
+            r = oracle.median(ocm, a, b, True)
+        except Exception as e:
+            assert "empty" in str(e) and res.status[k] == -4, (k, res.status[k], e)
+            continue
+        assert res.status[k] == 0, (k, res.status[k])
+        d = res.pair(k)
+        assert (d.cost, d.maxcost) == (r.cost, r.maxcost), k
+        assert np.array_equal(d.median, r.median) and np.array_equal(d.median_wg, r.medianwg), k
+        assert np.array_equal(d.aligned_a, r.ea) and np.array_equal(d.aligned_b, r.eb), k
+    al = pg.Align(ctx)  # per-call stubs keep a fill of either layout for the traceback
+    for a, b in pairs[:12]:
+        x = pg.dos_median(al, a, b, cm)
+        r = oracle.median(ocm, a, b, True)
+        assert x.cost == r.cost and np.array_equal(x.median, r.median)
+    ctx.close()
