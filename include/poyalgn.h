@@ -430,6 +430,26 @@ int poyalgn_autotune(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
  */
 int poyalgn_set_row_tile(poyalgn_ctx *ctx, int mode);
 
+/*
+ * A CUDA graph of poyalgn_median_batch_device's launch sequence for fixed
+ * buffers and shapes (no counterpart in the reference). Create runs the
+ * batch once (reserving all scratch) and captures a second run; each
+ * launch then replays the whole batch on `stream` with whatever the buffers
+ * hold at that time (same pair count, max_pair_len and out_bytes).
+ */
+typedef struct poyalgn_graph poyalgn_graph;
+int poyalgn_batch_graph_create(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
+                               int max_pair_len, int64_t out_bytes,
+                               const uint8_t *seqs, const int64_t *offa,
+                               const int32_t *lena, const int64_t *offb,
+                               const int32_t *lenb, const int64_t *out_off,
+                               int32_t *cost, int32_t *maxcost, int32_t *alen,
+                               int32_t *mlen, int32_t *wlen, int32_t *status,
+                               uint8_t *ea, uint8_t *eb, uint8_t *med, uint8_t *mwg,
+                               int32_t *passes, poyalgn_graph **out);
+int poyalgn_batch_graph_launch(poyalgn_graph *g, void *stream);
+void poyalgn_batch_graph_free(poyalgn_graph *g);
+
 /* Number of kernel launches the last batch enqueued (for accounting). */
 int poyalgn_last_launches(const poyalgn_ctx *ctx);
 

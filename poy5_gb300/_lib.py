@@ -72,6 +72,9 @@ _SIGS = {
     "poyalgn_distance_batch": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P]),
     "poyalgn_distance_batch_device": (_I, [_P, _P, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "poyalgn_set_row_tile": (_I, [_P, _I]),
+    "poyalgn_batch_graph_create": (_I, [_P, _P, _I, _I, _I64] + [_P] * 17 + [C.POINTER(_P)]),
+    "poyalgn_batch_graph_launch": (_I, [_P, _P]),
+    "poyalgn_batch_graph_free": (None, [_P]),
     "poyalgn_last_launches": (_I, [_P]),
     "poyalgn_profile_begin": (_I, [_P, _I]),
     "poyalgn_profile_end": (_I, [_P, _P, _P]),

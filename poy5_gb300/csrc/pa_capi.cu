@@ -93,11 +93,20 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if ((rc = reserve(c->qctr, 2 * NQUEUE * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
 
+    // a capture (poyalgn_batch_graph_create) records the launches only: the
+    // budget of the run before it, and no host-memory copies
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
     // persistent grid per class, bounded by a slab budget
-    size_t free_b = 0, total_b = 0;
-    CU(cudaMemGetInfo(&free_b, &total_b));
-    long long budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
-    if (c->slab_budget > 0) budget = std::min(budget, c->slab_budget);
+    long long budget = c->last_budget;
+    if (!capturing) {
+        size_t free_b = 0, total_b = 0;
+        CU(cudaMemGetInfo(&free_b, &total_b));
+        budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
+        if (c->slab_budget > 0) budget = std::min(budget, c->slab_budget);
+        c->last_budget = budget;
+    }
     int grid[NCLASS][2];
     long long strides[NCLASS];
     long long arena = 0;
@@ -115,7 +124,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         }
     }
     if ((rc = reserve(c->slab, (size_t)arena))) return rc;
-    CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
+    if (!capturing)  // slab strides for the per-call traceback
+        CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
     memcpy(c->call_strides, strides, sizeof(strides));
     CU(cudaMemsetAsync(c->qctr.p, 0, 2 * NQUEUE * sizeof(int), st));
 
@@ -168,7 +178,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
 
     int launches = 0;
     cudaEvent_t* ev = nullptr;
-    if (c->prof_used < c->prof_cap) {
+    if (!capturing && c->prof_used < c->prof_cap) {
         ev = &c->prof_ev[(size_t)c->prof_used * (NCLASS + 2)];
         c->prof_used++;
         CU(cudaEventRecord(ev[0], st));
@@ -749,6 +759,77 @@ int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
 }
 
 int poyalgn_num_classes(void) { return NCLASS; }
+
+struct poyalgn_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int device = 0;
+};
+
+int poyalgn_batch_graph_create(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
+                               int max_pair_len, int64_t out_bytes, const uint8_t* seqs,
+                               const int64_t* offa, const int32_t* lena, const int64_t* offb,
+                               const int32_t* lenb, const int64_t* out_off, int32_t* cost,
+                               int32_t* maxcost, int32_t* alen, int32_t* mlen, int32_t* wlen,
+                               int32_t* status, uint8_t* ea, uint8_t* eb, uint8_t* med,
+                               uint8_t* mwg, int32_t* passes, poyalgn_graph** out)
+{
+    if (!ctx || !cm || !out || npairs < 1 || max_pair_len < 2 || out_bytes < 1)
+        return set_err(POYALGN_EINVAL, "bad graph arguments");
+    *out = nullptr;
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    const int affine = cm->h.cost_model == 1;
+    auto batch = [&](cudaStream_t st) {
+        return run_batch(ctx, cm, affine, npairs, max_pair_len, out_bytes, seqs,
+                         reinterpret_cast<const long long*>(offa), lena,
+                         reinterpret_cast<const long long*>(offb), lenb,
+                         reinterpret_cast<const long long*>(out_off), cost, maxcost, alen, mlen,
+                         wlen, status, ea, eb, med, mwg, passes, nullptr, nullptr, 1, st);
+    };
+    // one plain run reserves every buffer the captured launches use
+    if ((rc = batch(ctx->stream))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    poyalgn_graph* g = new (std::nothrow) poyalgn_graph;
+    if (!g) return set_err(POYALGN_ENOMEM, "graph allocation");
+    g->device = ctx->device;
+    CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = batch(ctx->stream);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        delete g;
+        cudaGetLastError();
+        return rc ? rc : set_err(POYALGN_ECUDA, "capture: %s", cudaGetErrorString(e));
+    }
+    g->graph = graph;
+    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        delete g;
+        cudaGetLastError();
+        return set_err(POYALGN_ECUDA, "graph instantiation failed");
+    }
+    *out = g;
+    return 0;
+}
+
+int poyalgn_batch_graph_launch(poyalgn_graph* g, void* stream)
+{
+    if (!g) return set_err(POYALGN_EINVAL, "null graph");
+    CU(cudaSetDevice(g->device));
+    CU(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    return 0;
+}
+
+void poyalgn_batch_graph_free(poyalgn_graph* g)
+{
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+}
 
 int poyalgn_set_row_tile(poyalgn_ctx* ctx, int mode)
 {

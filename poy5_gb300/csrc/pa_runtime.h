@@ -62,6 +62,7 @@ struct poyalgn_ctx {
     // upper bound on the direction-slab arena of one batch (0: half the free
     // device memory, at most 64 GB)
     long long slab_budget = 0;
+    long long last_budget = 1LL << 30;  // slab budget of the last uncaptured batch
     // optional per-launch timing: one event before the prep launch and one
     // after each launch of a batch, for up to prof_cap batches
     std::vector<cudaEvent_t> prof_ev;

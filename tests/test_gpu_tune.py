@@ -71,3 +71,50 @@ def test_lean_paths_match_oracle(oracle, mode):
         r = oracle.median(ocm, a, b, True)
         assert x.cost == r.cost and np.array_equal(x.median, r.median)
     ctx.close()
+
+
+def test_batch_graph_replays_match_plain_calls():
+    """A captured batch replayed on new contents of the same buffers."""
+    import ctypes as C
+    import torch
+    import poy5_gb300 as pg
+    from poy5_gb300 import _lib
+    lib = _lib.load()
+    ctx = pg.Context(0)
+    w = wl.affine_pairs(n_pairs=300, seed=wl.SEED_BASE + 80)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    pk = pg.pack_pairs(w.pairs)
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_in = [t(pk.seqs), t(pk.offa), t(pk.lena), t(pk.offb), t(pk.lenb), t(pk.out_off)]
+    d_int = [torch.zeros(pk.npairs, dtype=torch.int32, device=dev) for _ in range(7)]
+    d_out = [torch.zeros(pk.out_bytes, dtype=torch.uint8, device=dev) for _ in range(4)]
+    P = lambda x: C.c_void_p(x.data_ptr())
+    g = C.c_void_p()
+    _lib.check(lib.poyalgn_batch_graph_create(
+        ctx.handle, cm.handle, pk.npairs, pk.max_pair_len, pk.out_bytes, *(P(x) for x in d_in),
+        *(P(x) for x in d_int[:6]), *(P(x) for x in d_out), P(d_int[6]), C.byref(g)))
+    stream = torch.cuda.current_stream(0)
+    rng = np.random.default_rng(81)
+    for rnd in range(2):
+        seqs = pk.seqs.copy()
+        if rnd:  # new bases, same lengths and leading gaps
+            pos = np.flatnonzero(seqs != 16)
+            seqs[pos] = np.array([1, 2, 4, 8], np.uint8)[rng.integers(0, 4, len(pos))]
+        d_in[0].copy_(torch.from_numpy(seqs))
+        for x in d_out:
+            x.zero_()
+        _lib.check(lib.poyalgn_batch_graph_launch(g, C.c_void_p(stream.cuda_stream)))
+        torch.cuda.synchronize()
+        pairs = [(seqs[o:o + la], seqs[ob:ob + lb]) for o, la, ob, lb in
+                 zip(pk.offa, pk.lena, pk.offb, pk.lenb)]
+        ref = pg.median_batch(ctx, cm, pairs)
+        assert np.array_equal(d_int[5].cpu().numpy(), ref.status)
+        assert np.array_equal(d_int[0].cpu().numpy(), ref.cost)
+        med = d_out[2].cpu().numpy()
+        for k in range(pk.npairs):
+            end = int(pk.out_off[k] + pk.cap[k])
+            ml = int(ref.mlen[k])
+            assert np.array_equal(med[end - ml:end], ref.pair(k).median), (rnd, k)
+    lib.poyalgn_batch_graph_free(g)
+    ctx.close()
