@@ -98,15 +98,19 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     CU(cudaStreamIsCapturing(st, &cap));
     const bool capturing = cap != cudaStreamCaptureStatusNone;
-    // persistent grid per class, bounded by a slab budget
-    long long budget = c->last_budget;
+    // persistent grid per class, bounded by a slab budget; with deferred
+    // tracebacks the fills go to the direction arena and the slabs are only
+    // the fallback when it is full
+    const bool defer = do_traceback && c->defer_traceback;
+    long long total_budget = c->last_budget;
     if (!capturing) {
         size_t free_b = 0, total_b = 0;
         CU(cudaMemGetInfo(&free_b, &total_b));
-        budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
-        if (c->slab_budget > 0) budget = std::min(budget, c->slab_budget);
-        c->last_budget = budget;
+        total_budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
+        if (c->slab_budget > 0) total_budget = std::min(total_budget, c->slab_budget);
+        c->last_budget = total_budget;
     }
+    const long long budget = defer ? std::min(total_budget / 4, 8LL << 30) : total_budget;
     int grid[NCLASS][2];
     long long strides[NCLASS];
     long long arena = 0;
@@ -124,6 +128,16 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         }
     }
     if ((rc = reserve(c->slab, (size_t)arena))) return rc;
+    long long dm_cap = 0;
+    if (defer) {
+        const long long want = (long long)npairs * (maxmn + 1) * 1024;
+        dm_cap = std::max<long long>(0, std::min(total_budget - arena, want));
+        if (capturing) dm_cap = std::min<long long>(dm_cap, (long long)c->dmarena.n);
+        if ((rc = reserve(c->dmarena, (size_t)std::max<long long>(dm_cap, 256)))) return rc;
+        if ((rc = reserve(c->dmoff, (size_t)npairs * 8))) return rc;
+        if ((rc = reserve(c->dmctr, 8))) return rc;
+        CU(cudaMemsetAsync(c->dmctr.p, 0, 8, st));
+    }
     if (!capturing)  // slab strides for the per-call traceback
         CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
     memcpy(c->call_strides, strides, sizeof(strides));
@@ -168,6 +182,12 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.eb = eb;
     A.med = med;
     A.mwg = mwg;
+    if (defer && dm_cap > 0) {
+        A.dm_arena = as<uint8_t>(c->dmarena);
+        A.dm_cap = dm_cap;
+        A.dm_used = as<unsigned long long>(c->dmctr);
+        A.dm_off = as<long long>(c->dmoff);
+    }
 
     // longest pairs enter the queues first so the persistent grid drains evenly
     if ((rc = reserve(c->order, (size_t)npairs * 4))) return rc;
@@ -193,6 +213,10 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
             launches++;
         }
         if (ev) CU(cudaEventRecord(ev[k + 2], st));
+    }
+    if (A.dm_cap > 0) {
+        launch_deferred_traceback(A, st);
+        launches++;
     }
     CU(cudaGetLastError());
     c->last_launches = launches;
@@ -444,7 +468,7 @@ void poyalgn_free(poyalgn_ctx* c)
                       &c->ints, &c->bytes, &c->pfull, &c->eh0, &c->lastcls, &c->slabcta,
                       &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
                       &c->dwh, &c->swp, &c->order, &c->order_scratch, &c->nobt_bnd,
-                      &c->nobt_ctr, &c->nobt_coop};
+                      &c->nobt_ctr, &c->nobt_coop, &c->dmarena, &c->dmoff, &c->dmctr};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);

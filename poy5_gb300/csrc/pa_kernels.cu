@@ -182,6 +182,35 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& A, int k, int cost,
     A.status[k] = r.status;
 }
 
+// Arena region of `bytes` for one pair's fills in one class; -1 when the
+// arena is off or full (the fill then uses the pipeline's own slab and the
+// traceback runs in the class kernel).
+__device__ __forceinline__ long long arena_take(const BatchArgs& A, long long bytes)
+{
+    if (A.dm_cap <= 0) return -1;
+    const unsigned long long b = ((unsigned long long)bytes + 255ull) & ~255ull;
+    const unsigned long long off = atomicAdd(A.dm_used, b);
+    return off + b <= (unsigned long long)A.dm_cap ? (long long)off : -1;
+}
+
+// An arena region for the pipeline's item: its leader takes it, every lane of
+// the pipeline gets it. Pipeline-uniform call (a CTA barrier when K > 1).
+__device__ __forceinline__ long long pipe_take(const BatchArgs& A, const Pipe& p, bool want,
+                                               long long bytes, long long* sh)
+{
+    long long off = -1;
+    if (p.gl == 0 && want) off = arena_take(A, bytes);
+    if (p.K == 1) {
+        off = __shfl_sync(FULL, off, p.lane - p.gl);
+    } else {
+        __syncthreads();
+        if (p.gl == 0) *sh = off;
+        __syncthreads();
+        off = *sh;
+    }
+    return off;
+}
+
 // Work item of one pipeline: the pair in internal order and its band state.
 struct Item {
     int k, T, m, n, swaped, full, npass;
@@ -331,11 +360,12 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
     __shared__ uint32_t xn[2][32];
     __shared__ int sres[2];
     __shared__ int sitem;
+    __shared__ long long soff;
     load_tables(st, A.tables);
     __syncthreads();
     const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
-    uint8_t* dm = A.slab + (long long)p.slot * A.slab_stride;
+    uint8_t* const slot_dm = A.slab + (long long)p.slot * A.slab_stride;
     for (;;) {
         const int base = pop_items(A, q, p, &sitem);
         if (base < 0) break;
@@ -344,6 +374,8 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
         Item w = live ? load_item(A, q, it) : empty_item(A);
         bool finished = false;
         int cost = 0;
+        long long off = -2;  // arena region: not taken yet
+        uint8_t* dm = slot_dm;
         for (;;) {
             const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
             if (live) {
@@ -357,6 +389,11 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                 }
             }
             if (!any_live(p, live)) break;
+            if (off == -2) {  // first pass in this class: the arena region
+                off = pipe_take(A, p, live && A.do_traceback,
+                                (long long)(w.m + w.n + 1) * p.P * R, &soff);
+                dm = off >= 0 ? A.dm_arena + off : slot_dm;
+            }
             const bool act = live && w.m > 1;
             const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
             int fc = 0, fg = 0;
@@ -385,8 +422,9 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                 A.lastcls[w.k] = cls;
                 A.slab_cta[w.k] = p.slot;
             }
-            if (!A.do_traceback) {
+            if (!A.do_traceback || off >= 0) {  // no traceback, or after all fills
                 if (p.gl == 0) {
+                    if (off >= 0) A.dm_off[w.k] = off;
                     A.cost[w.k] = cost;
                     A.status[w.k] = 0;
                 }
@@ -556,11 +594,12 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
     __shared__ LeanCell xl[2][32];
     __shared__ int sres[2];
     __shared__ int sitem;
+    __shared__ long long soff;
     load_tables(st, A.tables);
     __syncthreads();
     const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
-    uint16_t* dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
+    uint16_t* const slot_dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
     for (;;) {
         const int base = pop_items(A, q, p, &sitem);
         if (base < 0) break;
@@ -570,6 +609,8 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
         int* shadow = A.shadow + (live ? A.out_off[w.k] : 0);
         bool finished = false;
         int cost = 0;
+        long long off = -2;  // arena region: not taken yet
+        uint16_t* dm = slot_dm;
         for (;;) {
             const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
             if (live) {
@@ -584,6 +625,11 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
                 }
             }
             if (!any_live(p, live)) break;
+            if (off == -2) {  // first pass in this class: the arena region
+                off = pipe_take(A, p, live && A.do_traceback,
+                                (long long)(w.m + w.n + 1) * p.P * R * (FAST ? 1 : 2), &soff);
+                dm = off >= 0 ? reinterpret_cast<uint16_t*>(A.dm_arena + off) : slot_dm;
+            }
             const bool act = live && w.m > 1;
             const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
             const int eh0 = live ? A.shadowEH0[w.k] : 0;
@@ -623,8 +669,9 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
                 A.lastcls[w.k] = cls | (FAST ? LASTCLS_LEAN : 0);
                 A.slab_cta[w.k] = p.slot;
             }
-            if (!A.do_traceback) {
+            if (!A.do_traceback || off >= 0) {  // no traceback, or after all fills
                 if (p.gl == 0) {
+                    if (off >= 0) A.dm_off[w.k] = off;
                     A.cost[w.k] = cost;
                     A.status[w.k] = 0;
                 }
@@ -779,7 +826,7 @@ __global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, 
     __syncthreads();
     const Pipe p = make_pipe(32);
     const int q = 2 * cls + 1;
-    uint8_t* dm = A.slab + (long long)p.slot * A.slab_stride;
+    uint8_t* const slot_dm = A.slab + (long long)p.slot * A.slab_stride;
     for (;;) {
         const int base = pop_items(A, q, p, &sitem);
         if (base < 0) break;
@@ -788,6 +835,8 @@ __global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, 
         Item w = live ? load_item(A, q, it) : empty_item(A);
         bool finished = false;
         int cost = 0, newk = 0;
+        long long off = -2;  // arena region: not taken yet
+        uint8_t* dm = slot_dm;
         while (live) {  // uniform across the warp: one pair
             const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
             const int c = pick_class_lean(A.lad, aff_wu(b), w.n);
@@ -798,6 +847,11 @@ __global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, 
                 }
                 live = false;
                 break;
+            }
+            if (off == -2) {  // first pass in this class: the arena region
+                if (p.lane == 0) off = A.do_traceback ? arena_take(A, (long long)w.m * 32 * K) : -1;
+                off = __shfl_sync(FULL, off, 0);
+                dm = off >= 0 ? A.dm_arena + off : slot_dm;
             }
             int gapnum;
             if (w.m == 1) {  // leni = 0: the initial row is the whole alignment
@@ -823,7 +877,8 @@ __global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, 
             if (p.lane == 0) {
                 A.lastcls[w.k] = cls | LASTCLS_LEAN | LASTCLS_ROW;
                 A.slab_cta[w.k] = p.slot;
-                if (!A.do_traceback) {
+                if (!A.do_traceback || off >= 0) {  // no traceback, or after all fills
+                    if (off >= 0) A.dm_off[w.k] = off;
                     A.cost[w.k] = cost;
                     A.status[w.k] = 0;
                 } else {
@@ -902,6 +957,7 @@ __global__ void prep_kernel(BatchArgs A)
     A.passes[k] = 0;
     A.status[k] = 1;
     A.lastcls[k] = -1;
+    if (A.dm_off) A.dm_off[k] = -1;
     if (la < 1 || lb < 1 || (A.affine && la == 1 && lb == 1)) {
         A.status[k] = -4;
         return;
@@ -957,6 +1013,41 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
     } else if (A.affine && lean) r = aff_traceback_lean(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
     else if (A.affine) r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, tie, pair_out(A, k));
     else r = lin_traceback(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
+    finish_pair(A, k, A.cost[k], r);
+}
+
+// Tracebacks of the pairs whose final fill sits in the arena, one thread per
+// pair (after all class kernels, so no fill waits on a traceback).
+__global__ void deferred_traceback_kernel(BatchArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
+    const Tables& t = *A.tables;
+    const int la = A.lena[k], lb = A.lenb[k];
+    const int swaped = la <= lb ? 0 : 1;
+    const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
+    const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
+    const int m = swaped ? lb : la, n = swaped ? la : lb;
+    const int cls = A.lastcls[k] & LASTCLS_MASK;
+    const bool lean = (A.lastcls[k] & LASTCLS_LEAN) != 0;
+    const bool row = (A.lastcls[k] & LASTCLS_ROW) != 0;
+    const int P = A.lad.P[cls], R = A.lad.R[cls];
+    const uint8_t* base = A.dm_arena + A.dm_off[k];
+    PairRes r;
+    if (A.affine && row) {
+        const PairPlan pl = plan_affine(t, la, lb);
+        const long long T = (long long)pl.T0 << tmax(A.passes[k] - 1, 0);
+        const AffBand b = aff_band(m, n, band_p((int)T, m, n));
+        r = aff_traceback_rowtile(base, 32 * rk_k_for(ladder_cap(A.lad, cls)), b.newk, t, x, m, y,
+                                  n, swaped, pair_out(A, k));
+    } else if (A.affine && lean) {
+        r = aff_traceback_lean(base, P, R, t, x, m, y, n, swaped, pair_out(A, k));
+    } else if (A.affine) {
+        r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, swaped,
+                          pair_out(A, k));
+    } else {
+        r = lin_traceback(base, P, R, t, x, m, y, n, swaped, pair_out(A, k));
+    }
     finish_pair(A, k, A.cost[k], r);
 }
 
@@ -1132,6 +1223,13 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
     const int K = ladder_K(a.lad, cls), R = a.lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     class_kernel(a.affine, R, a.affine ? variant : 0, K == 1)<<<grid, threads, 0, s>>>(a, cls);
+}
+
+void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)
+{
+    if (a.npairs <= 0 || a.dm_cap <= 0) return;
+    const int threads = 128;
+    deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a);
 }
 
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s)

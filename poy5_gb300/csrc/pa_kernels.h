@@ -54,6 +54,12 @@ struct BatchArgs {
     uint8_t* eb;
     uint8_t* med;
     uint8_t* mwg;
+    // deferred tracebacks: each pair's fills in a class get their own arena
+    // region, and the tracebacks run after all fills (dm_cap 0: in-kernel)
+    uint8_t* dm_arena;
+    long long dm_cap;
+    unsigned long long* dm_used;  // bump counter, zero before the batch
+    long long* dm_off;            // per pair: arena offset of the final fill, -1 if none
 };
 
 // Work queues: 2 per class (variant 1 = affine gap-free fast path).
@@ -76,6 +82,8 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
 // Traceback + medians of pairs whose fill was left in the slab (per-call
 // path); d_strides[c] = slab bytes per pipeline of class c.
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
+// Tracebacks + medians of the pairs whose final fill sits in the arena.
+void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s);
 // Pipelines per CTA of a class launch.
 int class_pipes_per_cta(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // Column-wise medians of already aligned pairs (ancestor_2 / with-gaps / worst).

@@ -58,6 +58,8 @@ struct poyalgn_ctx {
     pa::DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
     pa::DevBuf dwh, swp, order, order_scratch;
     pa::DevBuf nobt_bnd, nobt_ctr, nobt_coop;  // cost-only affine fill scratch
+    pa::DevBuf dmarena, dmoff, dmctr;          // deferred tracebacks
+    int defer_traceback = 1;                   // 0: trace back inside the class kernels
     int last_launches = 0;
     // upper bound on the direction-slab arena of one batch (0: half the free
     // device memory, at most 64 GB)

@@ -344,6 +344,7 @@ int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int kind,
     for (Slot& sl : s->slots) {
         if ((rc = poyalgn_init(s->device, &sl.ctx))) break;
         sl.ctx->slab_budget = slab;
+        sl.ctx->defer_traceback = 0;  // no arena growth while serving
         if ((rc = prereserve(sl.ctx, s->affine, max_batch_pairs, s->out_cap, slab))) break;
         if (kind == POYALGN_SERVE_DISTANCE && s->affine &&
             (rc = prereserve_nobt(sl.ctx, max_batch_pairs, maxlen))) break;
