@@ -62,6 +62,9 @@ int ensure_device(poyalgn_ctx* c)
 }
 
 constexpr int ROW_TILE_MAX_PAIRS = 2;  // per SM, for row_tile_mode 2
+// Largest arena region one pair's fills in one class may take; wider fills
+// (long pairs) keep the pipeline's slab and trace back in the class kernel.
+constexpr long long DM_MAX_REGION = 64LL << 20;
 
 // Enqueue one batch on `st`. All pointers are device pointers. `out_total`
 // bounds out_off[k] + cap_k (sizes the affine row-0 scratch).
@@ -110,7 +113,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         if (c->slab_budget > 0) total_budget = std::min(total_budget, c->slab_budget);
         c->last_budget = total_budget;
     }
-    const long long budget = defer ? std::min(total_budget / 4, 8LL << 30) : total_budget;
+    const long long budget = total_budget;
     int grid[NCLASS][2];
     long long strides[NCLASS];
     long long arena = 0;
@@ -130,9 +133,19 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if ((rc = reserve(c->slab, (size_t)arena))) return rc;
     long long dm_cap = 0;
     if (defer) {
-        const long long want = (long long)npairs * (maxmn + 1) * 1024;
-        dm_cap = std::max<long long>(0, std::min(total_budget - arena, want));
+        // the arena takes what is free after the slabs (16 GB kept back), at
+        // most 64 GB and DM_MAX_REGION per pair
+        long long free_now = c->last_free;
+        if (!capturing) {
+            size_t fr = 0, tot = 0;
+            CU(cudaMemGetInfo(&fr, &tot));
+            free_now = (long long)fr + (long long)c->dmarena.n;  // the arena may be re-reserved
+            c->last_free = free_now;
+        }
+        const long long want = (long long)npairs * DM_MAX_REGION;
+        dm_cap = std::max<long long>(0, std::min({free_now - (16LL << 30), 64LL << 30, want}));
         if (capturing) dm_cap = std::min<long long>(dm_cap, (long long)c->dmarena.n);
+        if (c->dm_fixed > 0) dm_cap = std::min(dm_cap, c->dm_fixed);
         if ((rc = reserve(c->dmarena, (size_t)std::max<long long>(dm_cap, 256)))) return rc;
         if ((rc = reserve(c->dmoff, (size_t)npairs * 8))) return rc;
         if ((rc = reserve(c->dmctr, 8))) return rc;
@@ -185,6 +198,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if (defer && dm_cap > 0) {
         A.dm_arena = as<uint8_t>(c->dmarena);
         A.dm_cap = dm_cap;
+        A.dm_max_region = DM_MAX_REGION;
         A.dm_used = as<unsigned long long>(c->dmctr);
         A.dm_off = as<long long>(c->dmoff);
     }
@@ -237,6 +251,11 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
     if ((rc = reserve(c->order_scratch, order_scratch_bytes((int)n)))) return rc;
     if ((rc = reserve(c->slab, (size_t)slab_bytes))) return rc;
+    if (c->dm_fixed > 0) {
+        if ((rc = reserve(c->dmarena, (size_t)c->dm_fixed))) return rc;
+        if ((rc = reserve(c->dmoff, n * 8))) return rc;
+        if ((rc = reserve(c->dmctr, 8))) return rc;
+    }
     return 0;
 }
 

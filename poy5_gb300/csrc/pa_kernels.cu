@@ -187,7 +187,7 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& A, int k, int cost,
 // traceback runs in the class kernel).
 __device__ __forceinline__ long long arena_take(const BatchArgs& A, long long bytes)
 {
-    if (A.dm_cap <= 0) return -1;
+    if (A.dm_cap <= 0 || bytes > A.dm_max_region) return -1;
     const unsigned long long b = ((unsigned long long)bytes + 255ull) & ~255ull;
     const unsigned long long off = atomicAdd(A.dm_used, b);
     return off + b <= (unsigned long long)A.dm_cap ? (long long)off : -1;

@@ -58,6 +58,7 @@ struct BatchArgs {
     // region, and the tracebacks run after all fills (dm_cap 0: in-kernel)
     uint8_t* dm_arena;
     long long dm_cap;
+    long long dm_max_region;      // larger fills keep the pipeline's slab
     unsigned long long* dm_used;  // bump counter, zero before the batch
     long long* dm_off;            // per pair: arena offset of the final fill, -1 if none
 };

@@ -60,11 +60,13 @@ struct poyalgn_ctx {
     pa::DevBuf nobt_bnd, nobt_ctr, nobt_coop;  // cost-only affine fill scratch
     pa::DevBuf dmarena, dmoff, dmctr;          // deferred tracebacks
     int defer_traceback = 1;                   // 0: trace back inside the class kernels
+    long long dm_fixed = 0;                    // > 0: arena reserved up front, never grown
     int last_launches = 0;
     // upper bound on the direction-slab arena of one batch (0: half the free
     // device memory, at most 64 GB)
     long long slab_budget = 0;
     long long last_budget = 1LL << 30;  // slab budget of the last uncaptured batch
+    long long last_free = 0;            // free memory seen by it (arena included)
     // optional per-launch timing: one event before the prep launch and one
     // after each launch of a batch, for up to prof_cap batches
     std::vector<cudaEvent_t> prof_ev;

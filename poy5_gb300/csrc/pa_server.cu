@@ -331,10 +331,12 @@ int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int kind,
     s->len = store->len;
     s->max_batch_pairs = max_batch_pairs;
     s->max_waiting_pairs = max_waiting_pairs;
-    // per slot: half of its share for direction slabs (at most 8 GB), the
-    // rest for pair data (4 output buffers and the affine row-0 scratch)
+    // per slot: half of its share for direction slabs (at most 8 GB), a
+    // quarter for the deferred-traceback arena (at most 8 GB), the rest for
+    // pair data (4 output buffers and the affine row-0 scratch)
     const long long share = hbm_budget / nslots;
     const long long slab = std::min<long long>(share / 2, 8LL << 30);
+    const long long dm = std::min<long long>(share / 4, 8LL << 30);
     s->out_cap = std::min<long long>(share / 16, (long long)max_batch_pairs * 16384);
     s->out_cap &= ~(kAlign - 1);
     s->slots.resize(nslots);
@@ -344,7 +346,7 @@ int poyalgn_server_create(poyalgn_store* store, const poyalgn_cm* cm, int kind,
     for (Slot& sl : s->slots) {
         if ((rc = poyalgn_init(s->device, &sl.ctx))) break;
         sl.ctx->slab_budget = slab;
-        sl.ctx->defer_traceback = 0;  // no arena growth while serving
+        sl.ctx->dm_fixed = dm;  // deferred tracebacks in an arena reserved here
         if ((rc = prereserve(sl.ctx, s->affine, max_batch_pairs, s->out_cap, slab))) break;
         if (kind == POYALGN_SERVE_DISTANCE && s->affine &&
             (rc = prereserve_nobt(sl.ctx, max_batch_pairs, maxlen))) break;
