@@ -264,6 +264,7 @@ struct LinLane {
     uint32_t N0[R], N1[R];  // forward gap counts (#ins | #del << 16), same steps
     int J[R], G[R];         // column symbol s2[j] and its insert cost
     int rb[R], dc[R], tl[R];// cost-row offset, delete and tail cost of the row symbol
+    int Jn;                 // next step's column symbol of row 0 (loaded a step ahead)
     int Ts[R], Te[R];       // first / last step of each row (Ts > Te: no cell)
     int hr;                 // bit q: row q has a right border (no DELETE at Te)
     int R0, R1;             // neighbour's bottom row, two consecutive steps
@@ -313,6 +314,8 @@ PA_HD void lin_lane_init(LinLane<R>& L, const LinBand& b, const Tables& t,
     L.R0 = L.R1 = L.G0 = L.G1 = 0;
     L.RN0 = L.RN1 = 0;
     lin_enter_block(L, b, t, s1, 1 + g * R, P);
+    // step 1 reaches at most column 0 (lane 0), whose symbol no cell reads
+    L.Jn = 0;
 }
 
 // Steps during which lane 0 still generates row 0 (its first block), rounded
@@ -368,10 +371,13 @@ PA_HD void lin_step(LinLane<R>& L, int (&VC)[R], int (&VP)[R], uint32_t (&NC)[R]
             L.J[q] = L.J[q - 1];
             L.G[q] = L.G[q - 1];
         }
-        const int j = T - L.itop;
-        const int c = (j >= 0 && j < b.n) ? s2[j] : 0;
+        const int c = L.Jn;
         L.J[0] = c;
         L.G[0] = tcost(t, t.gap, c);
+    }
+    {  // the next step's row-0 column, loaded now so its latency overlaps this step
+        const int jn = T + 1 - L.itop;
+        L.Jn = (jn >= 0 && jn < b.n) ? s2[jn] : 0;
     }
 #pragma unroll
     for (int q = R - 1; q >= 0; q--) {
@@ -877,6 +883,7 @@ struct AffLean {
     int sg[R], sgo[R];      // gap cost of the row symbol (and + go)
     int srb[R];             // cost row of the row symbol
     int itop, nstart, gCB;
+    int Jn;                 // next step's column symbol of row 0 (loaded a step ahead)
 };
 
 template <int R>
@@ -916,6 +923,8 @@ PA_HD void aff_lean_init(AffLean<R>& L, const AffBand& b, const Tables& t,
     L.R0 = L.R1 = L.G0 = L.G1 = z;
     L.gCB = 0;
     aff_lean_enter(L, b, t, si, 1 + g * R, P);
+    // step 1 reaches at most column 0 (lane 0), whose symbol no cell reads
+    L.Jn = 0;
 }
 
 // The lean path needs every in-band cell to keep a state below HIGH / 4: a
@@ -983,10 +992,13 @@ PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
             L.J[q] = L.J[q - 1];
             L.JG[q] = L.JG[q - 1];
         }
-        const int j = T - L.itop;
-        const int c = (j >= 0 && j < b.n) ? sj[j] : 0;
+        const int c = L.Jn;
         L.J[0] = c;
         L.JG[0] = t.prepend[c];
+    }
+    {  // the next step's row-0 column, loaded now so its latency overlaps this step
+        const int jn = T + 1 - L.itop;
+        L.Jn = (jn >= 0 && jn < b.n) ? sj[jn] : 0;
     }
     // the "up" neighbours of row 0 are this step's received / generated
     // values (already in RP / GP); the diagonals are last step's (RC / GC)
