@@ -392,12 +392,12 @@ int poyalgn_server_stats(const poyalgn_server *s, int64_t *batches,
 /*
  * No counterpart in the reference. A context aligns each band pass on a
  * pipeline class picked from a ladder of POYALGN_NCLASS shapes: class c has
- * P[c] lanes (a power of two, 4..512) and R[c] rows per lane (2 or 4 for the
- * affine model, 2, 4 or 8 for the linear one) and takes bands up to
+ * P[c] lanes (a power of two, 4..512) and R[c] rows per lane (2, 3 or 4 for
+ * the affine model, 2, 4 or 8 for the linear one) and takes bands up to
  * 2 (P[c] - 1) R[c] + 1 cells wide; capacities must not decrease along the
  * ladder. Results never depend on the ladder, only the speed does.
  */
-#define POYALGN_NCLASS 10
+#define POYALGN_NCLASS 12
 
 int poyalgn_set_ladder(poyalgn_ctx *ctx, int affine, const int32_t *P,
                        const int32_t *R);

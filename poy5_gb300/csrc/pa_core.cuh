@@ -86,11 +86,13 @@ PA_HD uint32_t vmax2(uint32_t a, uint32_t b)
 // warp (one pair each, shuffles of width P); P >= 32: P/32 warps of one CTA.
 // Ladders are runtime data (a context may retune them; results do not
 // depend on the ladder), drawn from the shapes the kernels are compiled for:
-// P in {4, 8, ..., 512}, R in {2, 4} (affine) or {2, 4, 8} (linear). Wider
-// shapes are bounded by registers: a 512-thread CTA leaves 128 registers per
-// thread, enough for 8 linear or 4 affine rows per lane.
+// P in {4, 8, ..., 512}, R in {2, 3, 4} (affine) or {2, 4, 8} (linear).
+// Wider shapes are bounded by registers: a 512-thread CTA leaves 128
+// registers per thread, enough for 8 linear or 4 affine rows per lane. A
+// band of width w keeps w / (2 P R) of a class's lane-row slots busy, so
+// the affine ladder interleaves R = 3 shapes between the powers of two.
 
-constexpr int NCLASS = 10;
+constexpr int NCLASS = 12;
 
 struct Ladder {
     int P[NCLASS];
@@ -100,10 +102,10 @@ struct Ladder {
 PA_HD Ladder default_ladder(int affine)
 {
     Ladder L;
-    const int lp[NCLASS] = {4, 8, 16, 32, 32, 32, 64, 128, 256, 512};
-    const int lr[NCLASS] = {2, 2, 2, 2, 4, 8, 8, 8, 8, 8};
-    const int ap[NCLASS] = {4, 8, 16, 32, 32, 64, 128, 256, 512, 512};
-    const int ar[NCLASS] = {2, 2, 2, 2, 4, 4, 4, 4, 4, 4};
+    const int lp[NCLASS] = {4, 8, 16, 32, 32, 32, 64, 128, 256, 512, 512, 512};
+    const int lr[NCLASS] = {2, 2, 2, 2, 4, 8, 8, 8, 8, 8, 8, 8};
+    const int ap[NCLASS] = {8, 8, 16, 16, 32, 32, 32, 64, 64, 128, 256, 512};
+    const int ar[NCLASS] = {2, 3, 2, 3, 2, 3, 4, 3, 4, 4, 4, 4};
     for (int c = 0; c < NCLASS; c++) {
         L.P[c] = affine ? ap[c] : lp[c];
         L.R[c] = affine ? ar[c] : lr[c];
@@ -163,7 +165,7 @@ PA_HD bool ladder_valid(const Ladder& L, int affine)
     for (int c = 0; c < NCLASS; c++) {
         const int P = L.P[c], R = L.R[c];
         if (P < 4 || P > 512 || (P & (P - 1))) return false;
-        if (!(R == 2 || R == 4 || (!affine && R == 8))) return false;
+        if (!(R == 2 || R == 4 || (affine ? R == 3 : R == 8))) return false;
         const long long cap = 2LL * (P - 1) * R + 1;
         if (cap < prev) return false;
         prev = cap;
@@ -244,14 +246,13 @@ PA_HD int log2_pow2(int x)
 }
 
 // Slab addressing shared by the fills and the tracebacks: row i >= 1 is row
-// q of block b = (i - 1) / R, held by lane g = b mod P (P and R are powers
-// of two in every ladder).
+// q of block b = (i - 1) / R, held by lane g = b mod P (P is a power of two
+// in every ladder; R is 3 or a power of two).
 PA_HD long long dm_index(int P, int R, int i, int j)
 {
-    const int lr = log2_pow2(R);
-    const int b = (i - 1) >> lr;
+    const int b = R == 3 ? (i - 1) / 3 : (i - 1) >> log2_pow2(R);
     const int g = b & (P - 1);
-    const int q = (i - 1) & (R - 1);
+    const int q = (i - 1) - b * R;
     return (long long)(i + j) * (P * R) + g * R + q;
 }
 

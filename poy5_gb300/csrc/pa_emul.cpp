@@ -283,6 +283,7 @@ struct Emul {
     HostCM cm;
     Tables t;
     Ladder lad[2] = {default_ladder(0), default_ladder(1)};
+    int row_tile = 1;  // lean bands up to 512 wide on the row tile (0: lane pipeline)
 };
 
 int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb,
@@ -358,11 +359,12 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     int rk = 0, rk_newk = 0;
     for (;;) {
         AffBand bd = aff_band(m, n, band_p(T, m, n));
-        int c = lean ? pick_class_lean(E.lad[1], aff_wu(bd), n) : pick_class(E.lad[1], aff_wu(bd), n);
+        const bool rt = lean && E.row_tile;
+        int c = rt ? pick_class_lean(E.lad[1], aff_wu(bd), n) : pick_class(E.lad[1], aff_wu(bd), n);
         if (c < 0) return -5;
         P = E.lad[1].P[c];
         R = E.lad[1].R[c];
-        rk = lean ? rk_k_for(ladder_cap(E.lad[1], c)) : 0;
+        rk = rt ? rk_k_for(ladder_cap(E.lad[1], c)) : 0;
         rk_newk = bd.newk;
         *last_class = c;
         dm.assign((size_t)(m + n + 1) * P * R, 0);
@@ -389,18 +391,21 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
                 switch (R) {
                     case 1: aff_pass_lean<1>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
                     case 2: aff_pass_lean<2>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
+                    case 3: aff_pass_lean<3>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
                     default: aff_pass_lean<4>(bd, P, t, x, y, dm8.data(), shadowEH0, cost, &g); break;
                 }
             } else if (gapfree) {
                 switch (R) {
                     case 1: aff_pass_fast<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                     case 2: aff_pass_fast<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                    case 3: aff_pass_fast<3>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                     default: aff_pass_fast<4>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                 }
             } else {
                 switch (R) {
                     case 1: aff_pass<1>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                     case 2: aff_pass<2>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
+                    case 3: aff_pass<3>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                     default: aff_pass<4>(bd, P, t, x, y, dm.data(), shadow.data(), shadowEH0, cost, &g); break;
                 }
             }
@@ -437,6 +442,10 @@ void* pa_emul_new(const int* tcm, int alph, int gap_open)
 }
 
 void pa_emul_free(void* e) { delete (Emul*)e; }
+
+// 0: lean affine passes on the lane pipeline only; 1: on the row tile up to
+// 512 wide (the default, as in a context).
+void pa_emul_set_row_tile(void* e, int mode) { ((Emul*)e)->row_tile = mode ? 1 : 0; }
 
 // Copies out the product's host tables for comparison with the oracle.
 int pa_emul_tables(void* h, int* cost, uint8_t* median, int* worst, int* tail,

@@ -46,6 +46,10 @@ __device__ __forceinline__ void store_u8(uint8_t* p, const int (&d)[R])
         p[0] = (uint8_t)d[0];
     } else if constexpr (R == 2) {
         *reinterpret_cast<uint16_t*>(p) = (uint16_t)(d[0] | (d[1] << 8));
+    } else if constexpr (R == 3) {  // 3 bytes at an odd offset for odd lanes
+        p[0] = (uint8_t)d[0];
+        p[1] = (uint8_t)d[1];
+        p[2] = (uint8_t)d[2];
     } else if constexpr (R == 4) {
         *reinterpret_cast<uint32_t*>(p) =
             (uint32_t)d[0] | ((uint32_t)d[1] << 8) | ((uint32_t)d[2] << 16) | ((uint32_t)d[3] << 24);
@@ -64,6 +68,10 @@ __device__ __forceinline__ void store_u16(uint16_t* p, const int (&d)[R])
         p[0] = (uint16_t)d[0];
     } else if constexpr (R == 2) {
         *reinterpret_cast<uint32_t*>(p) = (uint32_t)d[0] | ((uint32_t)d[1] << 16);
+    } else if constexpr (R == 3) {
+        p[0] = (uint16_t)d[0];
+        p[1] = (uint16_t)d[1];
+        p[2] = (uint16_t)d[2];
     } else {
         static_assert(R == 4, "rows per lane");
         *reinterpret_cast<uint2*>(p) = make_uint2((uint32_t)d[0] | ((uint32_t)d[1] << 16),
@@ -152,6 +160,30 @@ __device__ __forceinline__ int pop_items(const BatchArgs& A, int q, const Pipe& 
         it = *sh;
     }
     return it < A.qcount[q] ? it : -1;
+}
+
+// Pipelines that want an item take the next ones of queue q, one each (one
+// atomic per warp, or per CTA for a multi-warp pipeline); `want` is uniform
+// within a pipeline. Returns the item index, or -1 when the queue is drained
+// (its count is fixed while the class kernel runs: items only move up).
+__device__ __forceinline__ int take_item(const BatchArgs& A, int q, const Pipe& p, bool want,
+                                         int* sh)
+{
+    int it = -1;
+    if (p.K == 1) {
+        const unsigned lead = __ballot_sync(FULL, want && p.gl == 0);
+        int base = 0;
+        if (p.lane == 0 && lead) base = atomicAdd(&A.qhead[q], __popc(lead));
+        base = __shfl_sync(FULL, base, 0);
+        const int leader = p.lane - p.gl;
+        it = base + __popc(lead & ((1u << leader) - 1u));
+    } else {
+        __syncthreads();
+        if (threadIdx.x == 0) *sh = want ? atomicAdd(&A.qhead[q], 1) : 0;
+        __syncthreads();
+        it = *sh;
+    }
+    return (want && it < A.qcount[q]) ? it : -1;
 }
 
 __device__ __forceinline__ void push_item(const BatchArgs& A, int q, int pair, int T)
@@ -366,57 +398,76 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
     const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
     uint8_t* const slot_dm = A.slab + (long long)p.slot * A.slab_stride;
+    Item w = empty_item(A);
+    bool live = false, drained = false;
+    int cost = 0;
+    long long off = -2;  // arena region of the item: not taken yet
+    uint8_t* dm = slot_dm;
+    // the item's band for its next pass: stays here, moves up the ladder, or fails
+    auto keep = [&]() {
+        const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
+        const int c = pick_class(A.lad, lin_wu(b), w.n);
+        if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
+            if (p.gl == 0) {
+                if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
+                else A.status[w.k] = c < 0 ? -5 : -8;
+            }
+            live = false;
+        }
+    };
     for (;;) {
-        const int base = pop_items(A, q, p, &sitem);
-        if (base < 0) break;
-        const int it = base + p.grp;
-        bool live = it < A.qcount[q];
-        Item w = live ? load_item(A, q, it) : empty_item(A);
-        bool finished = false;
-        int cost = 0;
-        long long off = -2;  // arena region: not taken yet
-        uint8_t* dm = slot_dm;
-        for (;;) {
-            const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
-            if (live) {
-                const int c = pick_class(A.lad, lin_wu(b), w.n);
-                if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
-                    if (p.gl == 0) {
-                        if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
-                        else A.status[w.k] = c < 0 ? -5 : -8;
-                    }
-                    live = false;
-                }
-            }
-            if (!any_live(p, live)) break;
-            if (off == -2) {  // first pass in this class: the arena region
-                off = pipe_take(A, p, live && A.do_traceback,
-                                (long long)(w.m + w.n + 1) * p.P * R, &soff);
-                dm = off >= 0 ? A.dm_arena + off : slot_dm;
-            }
-            const bool act = live && w.m > 1;
-            const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
-            int fc = 0, fg = 0;
-            if (Tmax > 0) lin_fill<R>(b, st, w.x, w.y, dm, p, act, Tmax, xv, xn, sres, fc, fg);
-            if (live) {
-                int gapnum = fg;
-                cost = fc;
-                if (w.m == 1) {  // no rows: row 0 is the whole alignment
-                    int s = 0;
-                    for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
-                    cost = s;
-                    gapnum = w.n - 1;
-                }
-                w.npass++;
-                if (p.gl == 0) A.passes[w.k] = w.npass;
-                if (w.full || lin_done(w.T, w.m, w.n, gapnum)) {
-                    live = false;
-                    finished = true;
+        for (;;) {  // refill between passes (pipeline-uniform decisions)
+            const bool want = !live && !drained;
+            if (!any_live(p, want)) break;
+            const int it = take_item(A, q, p, want, &sitem);
+            if (want) {
+                if (it < 0) {
+                    drained = true;
                 } else {
-                    w.T *= 2;
+                    w = load_item(A, q, it);
+                    live = true;
+                    off = -2;
+                    keep();
                 }
             }
         }
+        if (!any_live(p, live)) break;
+        const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
+        {  // first pass of an item in this class: its arena region (a warp-
+           // or CTA-wide call: pipelines of one warp admit items at different times)
+            const bool fresh = off == -2;
+            const long long o = pipe_take(A, p, fresh && live && A.do_traceback,
+                                          (long long)(w.m + w.n + 1) * p.P * R, &soff);
+            if (fresh) {
+                off = o;
+                dm = off >= 0 ? A.dm_arena + off : slot_dm;
+            }
+        }
+        const bool act = live && w.m > 1;
+        const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
+        int fc = 0, fg = 0;
+        if (Tmax > 0) lin_fill<R>(b, st, w.x, w.y, dm, p, act, Tmax, xv, xn, sres, fc, fg);
+        bool finished = false;
+        if (live) {
+            int gapnum = fg;
+            cost = fc;
+            if (w.m == 1) {  // no rows: row 0 is the whole alignment
+                int s = 0;
+                for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
+                cost = s;
+                gapnum = w.n - 1;
+            }
+            w.npass++;
+            if (p.gl == 0) A.passes[w.k] = w.npass;
+            if (w.full || lin_done(w.T, w.m, w.n, gapnum)) {
+                live = false;
+                finished = true;
+            } else {
+                w.T *= 2;
+                keep();
+            }
+        }
+        pipe_sync(p);
         if (finished) {
             if (p.gl == 0) {
                 A.lastcls[w.k] = cls;
@@ -600,70 +651,95 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
     const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
     uint16_t* const slot_dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
+    Item w = empty_item(A);
+    bool live = false, drained = false;
+    int cost = 0;
+    long long off = -2;  // arena region of the item: not taken yet
+    uint16_t* dm = slot_dm;
+    // A pipeline that has no item (or whose item left this class) takes the
+    // next one between passes, so the pipelines sharing a warp stay busy
+    // whatever the number of passes each of their pairs runs in this class.
+    auto admit = [&](int it) {
+        w = load_item(A, q, it);
+        live = true;
+        off = -2;
+    };
+    // the item's band for its next pass: stays here, moves up the ladder, or fails
+    auto keep = [&]() {
+        const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
+        const int c = (FAST && A.row_tile) ? pick_class_lean(A.lad, aff_wu(b), w.n)
+                                           : pick_class(A.lad, aff_wu(b), w.n);
+        if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
+            if (p.gl == 0) {
+                if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
+                else A.status[w.k] = c < 0 ? -5 : -8;
+            }
+            live = false;
+        }
+    };
     for (;;) {
-        const int base = pop_items(A, q, p, &sitem);
-        if (base < 0) break;
-        const int it = base + p.grp;
-        bool live = it < A.qcount[q];
-        Item w = live ? load_item(A, q, it) : empty_item(A);
-        int* shadow = A.shadow + (live ? A.out_off[w.k] : 0);
-        bool finished = false;
-        int cost = 0;
-        long long off = -2;  // arena region: not taken yet
-        uint16_t* dm = slot_dm;
-        for (;;) {
-            const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
-            if (live) {
-                const int c = (FAST && A.row_tile) ? pick_class_lean(A.lad, aff_wu(b), w.n)
-                                                   : pick_class(A.lad, aff_wu(b), w.n);
-                if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
-                    if (p.gl == 0) {
-                        if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
-                        else A.status[w.k] = c < 0 ? -5 : -8;
-                    }
-                    live = false;
+        for (;;) {  // refill (pipeline-uniform decisions)
+            const bool want = !live && !drained;
+            if (!any_live(p, want)) break;
+            const int it = take_item(A, q, p, want, &sitem);
+            if (want) {
+                if (it < 0) {
+                    drained = true;
+                } else {
+                    admit(it);
+                    keep();
                 }
             }
-            if (!any_live(p, live)) break;
-            if (off == -2) {  // first pass in this class: the arena region
-                off = pipe_take(A, p, live && A.do_traceback,
-                                (long long)(w.m + w.n + 1) * p.P * R * (FAST ? 1 : 2), &soff);
+        }
+        if (!any_live(p, live)) break;
+        const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
+        {  // first pass of an item in this class: its arena region (a warp-
+           // or CTA-wide call: pipelines of one warp admit items at different times)
+            const bool fresh = off == -2;
+            const long long o =
+                pipe_take(A, p, fresh && live && A.do_traceback,
+                          (long long)(w.m + w.n + 1) * p.P * R * (FAST ? 1 : 2), &soff);
+            if (fresh) {
+                off = o;
                 dm = off >= 0 ? reinterpret_cast<uint16_t*>(A.dm_arena + off) : slot_dm;
             }
-            const bool act = live && w.m > 1;
-            const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
-            const int eh0 = live ? A.shadowEH0[w.k] : 0;
-            int fc = 0, fg = 0;
-            if (Tmax > 0) {
-                if constexpr (FAST)
-                    aff_fill_lean<R>(b, st, w.x, w.y, reinterpret_cast<uint8_t*>(dm), eh0, p,
-                                     act, Tmax, xl, sres, fc, fg);
-                else
-                    aff_fill<R, false>(b, st, w.x, w.y, dm, shadow, eh0, p, act, Tmax, xc, sres,
-                                       fc, fg);
-            }
-            if (live) {
-                int gapnum = fg;
-                cost = fc;
-                if (w.m == 1) {  // leni = 0: the initial row is the whole alignment
-                    int s = st.go;
-                    for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
-                    cost = s;
-                    gapnum = 0xFFFF;
-                } else if (p.gl == 0 && tmin(w.m - 1, b.newk) >= 2) {
-                    A.shadowEH0[w.k] = HIGH;
-                }
-                w.npass++;
-                if (p.gl == 0) A.passes[w.k] = w.npass;
-                if (aff_done(w.T, w.m, w.n, gapnum)) {
-                    live = false;
-                    finished = true;
-                } else {
-                    w.T *= 2;
-                }
-            }
-            pipe_sync(p);
         }
+        int* shadow = A.shadow + (live ? A.out_off[w.k] : 0);
+        const bool act = live && w.m > 1;
+        const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
+        const int eh0 = live ? A.shadowEH0[w.k] : 0;
+        int fc = 0, fg = 0;
+        if (Tmax > 0) {
+            if constexpr (FAST)
+                aff_fill_lean<R>(b, st, w.x, w.y, reinterpret_cast<uint8_t*>(dm), eh0, p, act,
+                                 Tmax, xl, sres, fc, fg);
+            else
+                aff_fill<R, false>(b, st, w.x, w.y, dm, shadow, eh0, p, act, Tmax, xc, sres, fc,
+                                   fg);
+        }
+        bool finished = false;
+        if (live) {
+            int gapnum = fg;
+            cost = fc;
+            if (w.m == 1) {  // leni = 0: the initial row is the whole alignment
+                int s = st.go;
+                for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
+                cost = s;
+                gapnum = 0xFFFF;
+            } else if (p.gl == 0 && tmin(w.m - 1, b.newk) >= 2) {
+                A.shadowEH0[w.k] = HIGH;
+            }
+            w.npass++;
+            if (p.gl == 0) A.passes[w.k] = w.npass;
+            if (aff_done(w.T, w.m, w.n, gapnum)) {
+                live = false;
+                finished = true;
+            } else {
+                w.T *= 2;
+                keep();
+            }
+        }
+        pipe_sync(p);
         if (finished) {
             if (p.gl == 0) {
                 A.lastcls[w.k] = cls | (FAST ? LASTCLS_LEAN : 0);
@@ -1123,6 +1199,9 @@ static ClassKernel class_kernel(int affine, int R, int variant, bool narrow)
         if (R == 2)
             return variant ? (narrow ? aff_class_kernel<2, true, true> : aff_class_kernel<2, true, false>)
                            : (narrow ? aff_class_kernel<2, false, true> : aff_class_kernel<2, false, false>);
+        if (R == 3)
+            return variant ? (narrow ? aff_class_kernel<3, true, true> : aff_class_kernel<3, true, false>)
+                           : (narrow ? aff_class_kernel<3, false, true> : aff_class_kernel<3, false, false>);
         return variant ? (narrow ? aff_class_kernel<4, true, true> : aff_class_kernel<4, true, false>)
                        : (narrow ? aff_class_kernel<4, false, true> : aff_class_kernel<4, false, false>);
     }

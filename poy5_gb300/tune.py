@@ -13,14 +13,16 @@ import numpy as np
 from . import _lib
 from .align import Context, CostMatrix, PackedPairs, _ptr, check, pack_pairs
 
-NCLASS = 10
+NCLASS = 12
 P_ALLOWED = (4, 8, 16, 32, 64, 128, 256, 512)
 
 
 def default_ladder(affine: bool):
     if affine:
-        return ([4, 8, 16, 32, 32, 64, 128, 256, 512, 512], [2, 2, 2, 2, 4, 4, 4, 4, 4, 4])
-    return ([4, 8, 16, 32, 32, 32, 64, 128, 256, 512], [2, 2, 2, 2, 4, 8, 8, 8, 8, 8])
+        return ([8, 8, 16, 16, 32, 32, 32, 64, 64, 128, 256, 512],
+                [2, 3, 2, 3, 2, 3, 4, 3, 4, 4, 4, 4])
+    return ([4, 8, 16, 32, 32, 32, 64, 128, 256, 512, 512, 512],
+            [2, 2, 2, 2, 4, 8, 8, 8, 8, 8, 8, 8])
 
 
 def ladder_valid(P, R, affine: bool) -> bool:
@@ -29,7 +31,7 @@ def ladder_valid(P, R, affine: bool) -> bool:
         return False
     prev = 0
     for p, r in zip(P, R):
-        if p not in P_ALLOWED or r not in ((2, 4) if affine else (2, 4, 8)):
+        if p not in P_ALLOWED or r not in ((2, 3, 4) if affine else (2, 4, 8)):
             return False
         cap = 2 * (p - 1) * r + 1
         if cap < prev:
@@ -40,18 +42,23 @@ def ladder_valid(P, R, affine: bool) -> bool:
 
 def candidate_ladders(affine: bool) -> list:
     """A small search space around the default: rows per lane of the narrow
-    classes, and where the multi-warp pipelines start."""
+    classes, where the multi-warp pipelines start, and whether R = 3 shapes
+    fill the gaps between the power-of-two capacities. Every candidate ends
+    on the widest shape, so that no band a default ladder takes is refused."""
     out = [default_ladder(affine)]
     if affine:
         out += [
-            ([4, 8, 16, 32, 64, 128, 256, 512, 512, 512], [4] * 10),
-            ([4, 8, 16, 32, 32, 64, 128, 256, 512, 512], [4, 4, 4, 2, 4, 4, 4, 4, 4, 4]),
-            ([8, 16, 32, 32, 64, 128, 256, 512, 512, 512], [2, 2, 2, 4, 4, 4, 4, 4, 4, 4]),
+            ([4, 8, 8, 16, 16, 32, 32, 32, 64, 64, 128, 512],
+             [2, 2, 3, 2, 3, 2, 3, 4, 3, 4, 4, 4]),
+            ([8, 8, 16, 16, 32, 32, 32, 64, 64, 128, 128, 512],
+             [2, 3, 2, 3, 2, 3, 4, 3, 4, 3, 4, 4]),
+            ([8, 16, 32, 32, 64, 128, 256, 512, 512, 512, 512, 512], [2, 2, 2] + [4] * 9),
+            ([4, 8, 16, 32, 32, 64, 128, 256, 512, 512, 512, 512], [2, 2, 2, 2] + [4] * 8),
         ]
     else:
         out += [
-            ([4, 8, 16, 32, 32, 64, 128, 256, 512, 512], [4, 4, 4, 4, 8, 8, 8, 8, 8, 8]),
-            ([4, 8, 16, 32, 64, 128, 256, 512, 512, 512], [8] * 10),
+            ([4, 8, 16, 32, 32, 64, 128, 256, 512, 512, 512, 512], [4, 4, 4, 4] + [8] * 8),
+            ([4, 8, 16, 32, 64, 128, 256, 512, 512, 512, 512, 512], [8] * 12),
         ]
     assert all(ladder_valid(P, R, affine) for P, R in out)
     return out

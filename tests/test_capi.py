@@ -54,6 +54,10 @@ def test_candidate_ladders_are_valid():
         cands = tune.candidate_ladders(affine)
         assert cands[0] == tune.default_ladder(affine)
         assert all(tune.ladder_valid(P, R, affine) for P, R in cands)
-    assert not tune.ladder_valid([4] * 9 + [3], [2] * 10, True)
-    assert not tune.ladder_valid([512] + [4] * 9, [4] * 10, True)   # capacity drops
-    assert not tune.ladder_valid([4] * 10, [8] * 10, True)          # affine R <= 4
+    n = tune.NCLASS
+    assert not tune.ladder_valid([4] * (n - 1) + [3], [2] * n, True)
+    assert not tune.ladder_valid([512] + [4] * (n - 1), [4] * n, True)   # capacity drops
+    assert not tune.ladder_valid([4] * n, [8] * n, True)                 # affine R <= 4
+    assert tune.ladder_valid([4] * n, [3] * n, True)                     # R = 3: affine only
+    assert not tune.ladder_valid([4] * n, [3] * n, False)
+    assert not tune.ladder_valid([4] * 10, [2] * 10, True)               # one per class

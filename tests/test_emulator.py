@@ -24,6 +24,7 @@ def emul():
     lib.pa_emul_new.restype = _P
     lib.pa_emul_new.argtypes = [_P, C.c_int, C.c_int]
     lib.pa_emul_free.argtypes = [_P]
+    lib.pa_emul_set_row_tile.argtypes = [_P, C.c_int]
     return lib
 
 
@@ -32,11 +33,12 @@ def _ptr(a):
 
 
 class Emu:
-    def __init__(self, lib, tcm, go):
+    def __init__(self, lib, tcm, go, row_tile=1):
         self.lib = lib
         flat = np.ascontiguousarray(np.asarray(tcm, np.int32).reshape(-1))
         self.h = _P(lib.pa_emul_new(_ptr(flat), int(np.asarray(tcm).shape[0]), go))
         assert self.h
+        lib.pa_emul_set_row_tile(self.h, row_tile)
         self.affine = go > 0
 
     def tables(self):
@@ -81,11 +83,13 @@ def test_pipeline_matches_golden(emul, name):
         assert not bad, (name, k, bad)
 
 
-@pytest.mark.parametrize("affine", [False, True])
-def test_pipeline_matches_oracle_random(emul, oracle, affine):
+@pytest.mark.parametrize("affine,row_tile", [(False, 1), (True, 1), (True, 0)])
+def test_pipeline_matches_oracle_random(emul, oracle, affine, row_tile):
+    """row_tile 0 keeps lean (gap-free) affine pairs on the lane pipeline,
+    whose ladder interleaves R = 3 shapes with the R = 2 and 4 ones."""
     rng = np.random.default_rng(314 + affine)
     tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
-    e = Emu(emul, tcm, go)
+    e = Emu(emul, tcm, go, row_tile)
     cm = oracle.cm(tcm=tcm, gap_open=go)
     classes = set()
     for a, b in edge_pairs() + random_pairs(rng, 300, maxlen=700):

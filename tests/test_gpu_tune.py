@@ -37,7 +37,7 @@ def test_every_candidate_ladder_gives_the_same_results(workload):
     assert len(r["ms"]) == len(tune.candidate_ladders(w.affine)) and min(r["ms"]) > 0
     _same(ref, pg.median_batch(ctx, cm, w.pairs))
     with pytest.raises(pg.PoyAlgnError):
-        tune.set_ladder(ctx, w.affine, [4] * 10, [3] * 10)
+        tune.set_ladder(ctx, w.affine, [4] * tune.NCLASS, [5] * tune.NCLASS)
     ctx.close()
 
 
