@@ -92,8 +92,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         passes = as<int>(c->passes);
     }
     if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
-    if ((rc = reserve(c->qitems, (size_t)NQUEUE * npairs * sizeof(int2)))) return rc;
-    if ((rc = reserve(c->qctr, 2 * NQUEUE * sizeof(int)))) return rc;
+    if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * npairs * sizeof(int2)))) return rc;
+    if ((rc = reserve(c->qctr, QCTR_INTS * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
 
     // a capture (poyalgn_batch_graph_create) records the launches only: the
@@ -154,7 +154,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if (!capturing)  // slab strides for the per-call traceback
         CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
     memcpy(c->call_strides, strides, sizeof(strides));
-    CU(cudaMemsetAsync(c->qctr.p, 0, 2 * NQUEUE * sizeof(int), st));
+    CU(cudaMemsetAsync(c->qctr.p, 0, QCTR_INTS * sizeof(int), st));
 
     BatchArgs A;
     memset(&A, 0, sizeof(A));
@@ -178,6 +178,9 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.qcount = as<int>(c->qctr);
     A.qhead = as<int>(c->qctr) + NQUEUE;
     A.qcap = npairs;
+    A.qsorted = as<int2>(c->qitems) + (size_t)NQUEUE * npairs;
+    A.qhist = as<int>(c->qctr) + 2 * NQUEUE;
+    A.qcur = A.qhist + NQUEUE * NBUCKET;
     A.slab = as<uint8_t>(c->slab);
     A.out_off = out_off;
     A.cost = cost;
@@ -220,8 +223,11 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     launch_prep(A, st);
     launches++;
     if (ev) CU(cudaEventRecord(ev[1], st));
+    const int sort_grid = std::max(1, std::min(2 * c->nsm, (npairs + 255) / 256));
     for (int k = 0; k < NCLASS; k++) {
         A.slab_stride = strides[k];
+        launch_sort_queues(A, k, sort_grid, st);
+        launches += 2;
         for (int v = 0; v < (affine ? 2 : 1); v++) {
             launch_class(A, k, v, grid[k][v], st);
             launches++;
@@ -246,8 +252,8 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     for (DevBuf* b : per_pair)
         if ((rc = reserve(*b, n * 4))) return rc;
     if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
-    if ((rc = reserve(c->qitems, (size_t)NQUEUE * n * sizeof(int2)))) return rc;
-    if ((rc = reserve(c->qctr, 2 * NQUEUE * sizeof(int)))) return rc;
+    if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * n * sizeof(int2)))) return rc;
+    if ((rc = reserve(c->qctr, QCTR_INTS * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
     if ((rc = reserve(c->order_scratch, order_scratch_bytes((int)n)))) return rc;
     if ((rc = reserve(c->slab, (size_t)slab_bytes))) return rc;

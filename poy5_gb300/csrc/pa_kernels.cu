@@ -253,7 +253,7 @@ struct Item {
 __device__ __forceinline__ Item load_item(const BatchArgs& A, int q, int it)
 {
     Item w;
-    const int2 e = A.qitems[q * A.qcap + it];
+    const int2 e = (A.qsorted ? A.qsorted : A.qitems)[(long long)q * A.qcap + it];
     w.k = e.x;
     w.T = e.y;
     const int la = A.lena[w.k], lb = A.lenb[w.k];
@@ -969,6 +969,78 @@ __global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, 
 }
 
 // ---------------------------------------------------------------------------
+// Queue sort: a counting sort of a class's two queues by the pairs' length
+// m + n, longest first, so that the pipelines sharing a warp run pairs of
+// similar length and the persistent grid ends on short pairs.
+
+__device__ __forceinline__ int len_bucket(int x)
+{
+    x = x < 1 ? 1 : x;
+    const int e = 31 - __clz(x);
+    const int mant = e >= 3 ? (x >> (e - 3)) & 7 : (x << (3 - e)) & 7;
+    return NBUCKET - 1 - (e * 8 + mant);
+}
+
+__global__ void __launch_bounds__(256) queue_hist_kernel(BatchArgs A, int cls)
+{
+    __shared__ int h[2 * NBUCKET];
+    for (int i = threadIdx.x; i < 2 * NBUCKET; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (int v = 0; v < 2; v++) {
+        const int q = 2 * cls + v, n = A.qcount[q];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            const int k = A.qitems[(long long)q * A.qcap + i].x;
+            atomicAdd(&h[v * NBUCKET + len_bucket(A.lena[k] + A.lenb[k])], 1);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * NBUCKET; i += blockDim.x)
+        if (h[i]) atomicAdd(&A.qhist[2 * cls * NBUCKET + i], h[i]);
+}
+
+__global__ void __launch_bounds__(256) queue_scatter_kernel(BatchArgs A, int cls)
+{
+    static_assert(NBUCKET == 256, "one bucket per thread");
+    __shared__ int base[2 * NBUCKET];
+    const int t = threadIdx.x;
+    for (int v = 0; v < 2; v++) {  // exclusive prefix of each histogram (every block)
+        const int h = A.qhist[(2 * cls + v) * NBUCKET + t];
+        int* b = base + v * NBUCKET;
+        b[t] = h;
+        __syncthreads();
+        for (int o = 1; o < NBUCKET; o <<= 1) {
+            const int add = t >= o ? b[t - o] : 0;
+            __syncthreads();
+            b[t] += add;
+            __syncthreads();
+        }
+        b[t] -= h;
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (int v = 0; v < 2; v++) {
+        const int q = 2 * cls + v, n = A.qcount[q];
+        for (int w0 = wid * 32; w0 < n; w0 += warps * 32) {  // warp-uniform trips
+            const int i = w0 + lane;
+            const bool ok = i < n;
+            const int2 e = ok ? A.qitems[(long long)q * A.qcap + i] : make_int2(0, 0);
+            const int bk = ok ? len_bucket(A.lena[e.x] + A.lenb[e.x]) : -1;
+            const unsigned peers = __match_any_sync(FULL, bk);
+            const int leader = __ffs(peers) - 1;
+            int at = 0;
+            if (ok && lane == leader) at = atomicAdd(&A.qcur[q * NBUCKET + bk], __popc(peers));
+            at = __shfl_sync(FULL, at, leader);
+            if (ok) {
+                const int pos = base[v * NBUCKET + bk] + at + __popc(peers & ((1u << lane) - 1u));
+                A.qsorted[(long long)q * A.qcap + pos] = e;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // prep: one warp per pair
 
 __global__ void prep_kernel(BatchArgs A)
@@ -1302,6 +1374,13 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
     const int K = ladder_K(a.lad, cls), R = a.lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     class_kernel(a.affine, R, a.affine ? variant : 0, K == 1)<<<grid, threads, 0, s>>>(a, cls);
+}
+
+void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s)
+{
+    if (!a.qsorted) return;
+    queue_hist_kernel<<<grid, 256, 0, s>>>(a, cls);
+    queue_scatter_kernel<<<grid, 256, 0, s>>>(a, cls);
 }
 
 void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)

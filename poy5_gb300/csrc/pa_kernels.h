@@ -35,6 +35,11 @@ struct BatchArgs {
     int* qcount;
     int* qhead;
     int qcap;
+    // a class's queues sorted longest pair first just before it runs (null:
+    // the class kernels take qitems in push order)
+    int2* qsorted;             // same layout as qitems
+    int* qhist;                // NQUEUE x NBUCKET counts, zero before the batch
+    int* qcur;                 // NQUEUE x NBUCKET scatter cursors, zero before the batch
     uint8_t* slab;             // per-CTA direction slabs, reused class after class
     long long slab_stride;     // bytes per CTA for the class being launched
     const long long* out_off;  // pair k writes its outputs at out_off[k]
@@ -65,6 +70,12 @@ struct BatchArgs {
 
 // Work queues: 2 per class (variant 1 = affine gap-free fast path).
 constexpr int NQUEUE = 2 * NCLASS;
+// Length buckets of the queue sort (8 per octave of m + n).
+constexpr int NBUCKET = 256;
+// Queue counters: counts, heads, and the sort's histograms and cursors.
+constexpr int QCTR_INTS = 2 * NQUEUE * (1 + NBUCKET);
+// Sort the class's two queues longest pair first (no-op without qsorted).
+void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s);
 // Persistent CTAs per SM a class kernel can keep resident.
 int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // The row tile width of a class's lean queue (0: lane pipeline).
