@@ -36,10 +36,11 @@ METRIC = ("GCUPS & alignments/s batched+served vs plain per-pair kernel, 1 GB300
           "bit-exact; p50/p99")
 OPS_PER_CELL = {"affine": 51, "linear": 8}   # int32 ops per DP cell
 DM_BYTES = {"affine": 1, "linear": 1}        # direction bytes written per cell (lean affine: 1)
-# DRAM bytes (read + write) the class kernels moved per computed cell in one
-# ncu capture of the 8,192-pair affine batch (5.5 GB for 3.12 G cells); the
-# traffic grows with the computed cells, so it scales to the full batch.
-DRAM_BYTES_PER_CELL = {"affine": 1.77}
+# DRAM bytes (read + write) the class kernels and the deferred traceback moved
+# per computed cell in one ncu capture of the 8,192-pair affine batch (4.80 GB
+# for 3.12 G cells); the traffic grows with the computed cells, so it scales
+# to the full batch.
+DRAM_BYTES_PER_CELL = {"affine": 1.54}
 
 
 def parse_args(argv=None):
@@ -223,11 +224,13 @@ def run_gpu(args):
             P(d_int[6]), C.c_void_p(stream.cuda_stream))
         _lib.check(rc)
 
-    # pipeline shapes tuned on a sample of the workload (untimed setup)
+    # pipeline shapes tuned on the workload itself (untimed setup): a sample
+    # smaller than the batch favours the ladders whose narrow classes finish
+    # their longest pairs soonest, not the ones with the highest throughput
     tuned = None
     if not args.no_autotune:
         from poy5_gb300 import tune
-        tuned = tune.autotune(ctx, cm, w.pairs[:min(n, 8192)], reps=1)
+        tuned = tune.autotune(ctx, cm, pk, reps=1)
     # the whole batch captured once as a CUDA graph and replayed per step
     graph = C.c_void_p()
     _lib.check(lib.poyalgn_batch_graph_create(
