@@ -431,6 +431,23 @@ int poyalgn_autotune(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
 int poyalgn_set_row_tile(poyalgn_ctx *ctx, int mode);
 
 /*
+ * Speculative band passes, for batches too small to fill the GPU: the band
+ * doubling of a pair runs its passes one after another, each a full sweep of
+ * the pair's anti-diagonals, which bounds a small batch's latency. With
+ * speculation the first `passes` bands of every linear or gap-free affine
+ * pair run at once (each class of the ladder on its own stream), and the
+ * pair keeps the first pass that satisfies the doubling test (the one the
+ * sequential doubling stops at); pairs that need more, and gap-bearing
+ * affine pairs, continue sequentially. Costs extra cells, never changes a result.
+ * mode 0: off; 1: every batch; 2 (default): batches of at most one pair per
+ * SM. passes: 1 .. POYALGN_SPEC_MAX_PASSES (default 6). Only batches whose
+ * fills outlive the sweep speculate (tracebacks deferred to the arena, or
+ * cost-only distances). No counterpart in the reference.
+ */
+#define POYALGN_SPEC_MAX_PASSES 16
+int poyalgn_set_speculation(poyalgn_ctx *ctx, int mode, int passes);
+
+/*
  * A CUDA graph of poyalgn_median_batch_device's launch sequence for fixed
  * buffers and shapes (no counterpart in the reference). Create runs the
  * batch once (reserving all scratch) and captures a second run; each

@@ -38,6 +38,7 @@ def _compile(unit: str, verbose: bool) -> str:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(BUILD_DIR, unit + ".o")
     cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-Werror=return-type",
            "-I", CSRC, "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
     if unit.endswith(".cu") and verbose:
         cmd.insert(1, "-Xptxas=-v")

@@ -62,6 +62,7 @@ int ensure_device(poyalgn_ctx* c)
 }
 
 constexpr int ROW_TILE_MAX_PAIRS = 2;  // per SM, for row_tile_mode 2
+constexpr int SPEC_MAX_PAIRS = 1;      // per SM, for spec_mode 2
 // Largest arena region one pair's fills in one class may take; wider fills
 // (long pairs) keep the pipeline's slab and trace back in the class kernel.
 constexpr long long DM_MAX_REGION = 64LL << 20;
@@ -79,10 +80,21 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
 {
     int rc;
     if (npairs <= 0) return 0;
-    // the row tile has the lower latency per pair, the lane pipeline the
-    // higher throughput: small batches take the row tile
-    const int row_tile = affine && (c->row_tile_mode == 1 ||
-                                    (c->row_tile_mode == 2 && npairs <= ROW_TILE_MAX_PAIRS * c->nsm));
+    // Batches too small to fill the GPU run their pairs' first band passes
+    // at once (speculative sweep, then the sequential sweep for the pairs
+    // that need more). The fills must outlive the sweep: the arena holds
+    // them, or only the cost is wanted.
+    const bool spec_ok = distance || (do_traceback && c->defer_traceback);
+    const int spec_S = (spec_ok && (c->spec_mode == 1 ||
+                                    (c->spec_mode == 2 && npairs <= SPEC_MAX_PAIRS * c->nsm)))
+                           ? c->spec_passes : 0;
+    // the row tile has the lower latency per pass, the lane pipeline the
+    // higher throughput: small batches take the row tile (unless their
+    // passes run speculatively on the lane pipeline)
+    const int row_tile = affine && !spec_S &&
+                         (c->row_tile_mode == 1 ||
+                          (c->row_tile_mode == 2 && npairs <= ROW_TILE_MAX_PAIRS * c->nsm));
+    const int items = npairs * std::max(1, spec_S);  // queue capacity
     if ((rc = reserve(c->pfull, (size_t)npairs * 4))) return rc;
     if ((rc = reserve(c->eh0, (size_t)npairs * 4))) return rc;
     if ((rc = reserve(c->lastcls, (size_t)npairs * 4))) return rc;
@@ -92,9 +104,17 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         passes = as<int>(c->passes);
     }
     if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
-    if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * npairs * sizeof(int2)))) return rc;
+    if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * items * sizeof(int2)))) return rc;
     if ((rc = reserve(c->qctr, QCTR_INTS * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
+    if (spec_S) {
+        DevBuf* per_pair[] = {&c->spec_t0, &c->spec_n};
+        for (DevBuf* b : per_pair)
+            if ((rc = reserve(*b, (size_t)npairs * 4))) return rc;
+        if ((rc = reserve(c->spec_res, (size_t)items * sizeof(int4)))) return rc;
+        if ((rc = reserve(c->spec_off, (size_t)items * 8))) return rc;
+        CU(cudaMemsetAsync(c->spec_res.p, 0, (size_t)items * sizeof(int4), st));
+    }
 
     // a capture (poyalgn_batch_graph_create) records the launches only: the
     // budget of the run before it, and no host-memory copies
@@ -124,7 +144,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
             const int bps = class_row_tile(c->lad[affine], affine, k, v, row_tile)
                                 ? c->bps_rt[k] : c->bps[affine][k][v];
             long long g = (long long)c->nsm * std::max(1, bps);
-            g = std::min<long long>(g, (npairs + pipes - 1) / pipes);
+            g = std::min<long long>(g, (items + pipes - 1) / pipes);
             g = std::min<long long>(g, std::max<long long>(1, budget / (strides[k] * pipes)));
             grid[k][v] = (int)std::max<long long>(1, g);
             arena = std::max(arena, (long long)grid[k][v] * pipes * strides[k]);
@@ -142,7 +162,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
             free_now = (long long)fr + (long long)c->dmarena.n;  // the arena may be re-reserved
             c->last_free = free_now;
         }
-        const long long want = (long long)npairs * DM_MAX_REGION;
+        const long long want = (long long)items * DM_MAX_REGION;
         dm_cap = std::max<long long>(0, std::min({free_now - (16LL << 30), 64LL << 30, want}));
         if (capturing) dm_cap = std::min<long long>(dm_cap, (long long)c->dmarena.n);
         if (c->dm_fixed > 0) dm_cap = std::min(dm_cap, c->dm_fixed);
@@ -177,8 +197,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.qitems = as<int2>(c->qitems);
     A.qcount = as<int>(c->qctr);
     A.qhead = as<int>(c->qctr) + NQUEUE;
-    A.qcap = npairs;
-    A.qsorted = as<int2>(c->qitems) + (size_t)NQUEUE * npairs;
+    A.qcap = items;
+    A.qsorted = as<int2>(c->qitems) + (size_t)NQUEUE * items;
     A.qhist = as<int>(c->qctr) + 2 * NQUEUE;
     A.qcur = A.qhist + NQUEUE * NBUCKET;
     A.slab = as<uint8_t>(c->slab);
@@ -213,9 +233,17 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         return set_err(POYALGN_ECUDA, "ordering pairs failed");
     A.order = as<int>(c->order);
 
+    if (spec_S) {
+        A.spec_S = spec_S;
+        A.spec_T0 = as<int>(c->spec_t0);
+        A.spec_n = as<int>(c->spec_n);
+        A.spec_res = as<int4>(c->spec_res);
+        A.spec_off = as<long long>(c->spec_off);
+    }
+
     int launches = 0;
     cudaEvent_t* ev = nullptr;
-    if (!capturing && c->prof_used < c->prof_cap) {
+    if (!capturing && !spec_S && c->prof_used < c->prof_cap) {
         ev = &c->prof_ev[(size_t)c->prof_used * (NCLASS + 2)];
         c->prof_used++;
         CU(cudaEventRecord(ev[0], st));
@@ -223,17 +251,50 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     launch_prep(A, st);
     launches++;
     if (ev) CU(cudaEventRecord(ev[1], st));
-    const int sort_grid = std::max(1, std::min(2 * c->nsm, (npairs + 255) / 256));
-    for (int k = 0; k < NCLASS; k++) {
-        A.slab_stride = strides[k];
-        launch_sort_queues(A, k, sort_grid, st);
-        launches += 2;
-        for (int v = 0; v < (affine ? 2 : 1); v++) {
-            launch_class(A, k, v, grid[k][v], st);
-            launches++;
+    const int sort_grid = std::max(1, std::min(2 * c->nsm, (items + 255) / 256));
+    auto sweep = [&]() -> int {
+        for (int k = 0; k < NCLASS; k++) {
+            A.slab_stride = strides[k];
+            launch_sort_queues(A, k, sort_grid, st);
+            launches += 2;
+            for (int v = 0; v < (affine ? 2 : 1); v++) {
+                launch_class(A, k, v, grid[k][v], st);
+                launches++;
+            }
+            if (ev) CU(cudaEventRecord(ev[k + 2], st));
         }
-        if (ev) CU(cudaEventRecord(ev[k + 2], st));
+        return 0;
+    };
+    if (spec_S) {
+        // speculative sweep: only linear / lean items, which never move
+        // between classes, so the classes run concurrently (fork / join)
+        A.spec = 1;
+        if (!c->spec_fork) {
+            CU(cudaEventCreateWithFlags(&c->spec_fork, cudaEventDisableTiming));
+            for (int k = 0; k < NCLASS; k++) {
+                CU(cudaStreamCreateWithFlags(&c->spec_st[k], cudaStreamNonBlocking));
+                CU(cudaEventCreateWithFlags(&c->spec_join[k], cudaEventDisableTiming));
+            }
+        }
+        CU(cudaEventRecord(c->spec_fork, st));
+        const int v = affine ? 1 : 0;
+        for (int k = 0; k < NCLASS; k++) {
+            cudaStream_t sk = c->spec_st[k];
+            CU(cudaStreamWaitEvent(sk, c->spec_fork, 0));
+            A.slab_stride = strides[k];
+            launch_sort_queues(A, k, sort_grid, sk);
+            launch_class(A, k, v, grid[k][v], sk);
+            launches += 3;
+            CU(cudaEventRecord(c->spec_join[k], sk));
+            CU(cudaStreamWaitEvent(st, c->spec_join[k], 0));
+        }
+        // fresh queues for the sequential sweep, which the resolve fills
+        CU(cudaMemsetAsync(c->qctr.p, 0, QCTR_INTS * sizeof(int), st));
+        A.spec = 0;
+        launch_spec_resolve(A, st);
+        launches++;
     }
+    if ((rc = sweep())) return rc;
     if (A.dm_cap > 0) {
         launch_deferred_traceback(A, st);
         launches++;
@@ -493,10 +554,16 @@ void poyalgn_free(poyalgn_ctx* c)
                       &c->ints, &c->bytes, &c->pfull, &c->eh0, &c->lastcls, &c->slabcta,
                       &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
                       &c->dwh, &c->swp, &c->order, &c->order_scratch, &c->nobt_bnd,
-                      &c->nobt_ctr, &c->nobt_coop, &c->dmarena, &c->dmoff, &c->dmctr};
+                      &c->nobt_ctr, &c->nobt_coop, &c->dmarena, &c->dmoff, &c->dmctr,
+                      &c->spec_t0, &c->spec_n, &c->spec_res, &c->spec_off};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+    for (int k = 0; k < NCLASS; k++) {
+        if (c->spec_st[k]) cudaStreamDestroy(c->spec_st[k]);
+        if (c->spec_join[k]) cudaEventDestroy(c->spec_join[k]);
+    }
+    if (c->spec_fork) cudaEventDestroy(c->spec_fork);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -885,6 +952,15 @@ int poyalgn_set_row_tile(poyalgn_ctx* ctx, int mode)
     if (!ctx || mode < 0 || mode > 2) return set_err(POYALGN_EINVAL, "bad row tile mode");
     ctx->row_tile_mode = mode;
     ctx->call_valid = false;
+    return 0;
+}
+
+int poyalgn_set_speculation(poyalgn_ctx* ctx, int mode, int passes)
+{
+    if (!ctx || mode < 0 || mode > 2 || passes < 1 || passes > POYALGN_SPEC_MAX_PASSES)
+        return set_err(POYALGN_EINVAL, "bad speculation mode %d / passes %d", mode, passes);
+    ctx->spec_mode = mode;
+    ctx->spec_passes = passes;
     return 0;
 }
 

@@ -1347,6 +1347,11 @@ PA_HD bool aff_done(int T, int m, int n, int gapnum)
     return gapnum < p || newp - (n - 1) + 1 >= 0;
 }
 
+// The second clause of each stop rule alone: the doubling ends at band T
+// whatever that pass's gap count is.
+PA_HD bool lin_covers(int T, int m, int n) { return (2 * T - (n - m)) / 2 - n + 1 >= 0; }
+PA_HD bool aff_covers(int T, int m, int n) { return (2 * T - (n - m)) / 2 - (n - 1) + 1 >= 0; }
+
 // ---------------------------------------------------------------------------
 // Tracebacks and medians. Outputs are written back to front so that each
 // sequence ends at index cap-1 of its buffer, as seq_prepend leaves them.

@@ -282,6 +282,30 @@ __device__ __forceinline__ Item empty_item(const BatchArgs& A)
     return w;
 }
 
+// Pass index of a speculative item (T = T0 << j).
+__device__ __forceinline__ int spec_pass(const BatchArgs& A, const Item& w)
+{
+    return __ffs(w.T / A.spec_T0[w.k]) - 1;
+}
+
+// Row-0 EH at column 0 for lean affine pass j: HIGH once an earlier pass had
+// min(m - 1, newk) >= 2 (newk grows with T, so pass j - 1 decides), else the
+// value prep left.
+__device__ __forceinline__ int spec_eh0(const BatchArgs& A, const Item& w, int j)
+{
+    if (j == 0 || w.m - 1 < 2) return A.shadowEH0[w.k];
+    const AffBand pb = aff_band(w.m, w.n, band_p(A.spec_T0[w.k] << (j - 1), w.m, w.n));
+    return tmin(w.m - 1, pb.newk) >= 2 ? HIGH : A.shadowEH0[w.k];
+}
+
+__device__ __forceinline__ void spec_record(const BatchArgs& A, const Item& w, int j, int cost,
+                                            int gapnum, int cls_flags, long long off)
+{
+    const long long si = (long long)w.k * A.spec_S + j;
+    A.spec_res[si] = make_int4(cost, gapnum, cls_flags, 1);
+    A.spec_off[si] = off;
+}
+
 // ---------------------------------------------------------------------------
 // linear
 
@@ -398,9 +422,10 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
     const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
     uint8_t* const slot_dm = A.slab + (long long)p.slot * A.slab_stride;
+    const bool spec = A.spec != 0;  // every linear item of a speculative sweep
     Item w = empty_item(A);
     bool live = false, drained = false;
-    int cost = 0;
+    int cost = 0, sj = 0;
     long long off = -2;  // arena region of the item: not taken yet
     uint8_t* dm = slot_dm;
     // the item's band for its next pass: stays here, moves up the ladder, or fails
@@ -427,6 +452,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                     w = load_item(A, q, it);
                     live = true;
                     off = -2;
+                    if (spec) sj = spec_pass(A, w);
                     keep();
                 }
             }
@@ -457,14 +483,19 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                 cost = s;
                 gapnum = w.n - 1;
             }
-            w.npass++;
-            if (p.gl == 0) A.passes[w.k] = w.npass;
-            if (w.full || lin_done(w.T, w.m, w.n, gapnum)) {
+            if (spec) {  // one pass; spec_resolve_kernel decides
+                if (p.gl == 0) spec_record(A, w, sj, cost, gapnum, cls, off);
                 live = false;
-                finished = true;
             } else {
-                w.T *= 2;
-                keep();
+                w.npass++;
+                if (p.gl == 0) A.passes[w.k] = w.npass;
+                if (w.full || lin_done(w.T, w.m, w.n, gapnum)) {
+                    live = false;
+                    finished = true;
+                } else {
+                    w.T *= 2;
+                    keep();
+                }
             }
         }
         pipe_sync(p);
@@ -651,9 +682,10 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
     const Pipe p = make_pipe(A.lad.P[cls]);
     const int q = 2 * cls + VARIANT;
     uint16_t* const slot_dm = reinterpret_cast<uint16_t*>(A.slab + (long long)p.slot * A.slab_stride);
+    const bool spec = FAST && A.spec;  // lean items of a speculative sweep
     Item w = empty_item(A);
     bool live = false, drained = false;
-    int cost = 0;
+    int cost = 0, sj = 0;
     long long off = -2;  // arena region of the item: not taken yet
     uint16_t* dm = slot_dm;
     // A pipeline that has no item (or whose item left this class) takes the
@@ -663,6 +695,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
         w = load_item(A, q, it);
         live = true;
         off = -2;
+        if (spec) sj = spec_pass(A, w);
     };
     // the item's band for its next pass: stays here, moves up the ladder, or fails
     auto keep = [&]() {
@@ -707,7 +740,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
         int* shadow = A.shadow + (live ? A.out_off[w.k] : 0);
         const bool act = live && w.m > 1;
         const int Tmax = group_max(p, act ? (w.m - 1) + (w.n - 1) : 0);
-        const int eh0 = live ? A.shadowEH0[w.k] : 0;
+        const int eh0 = !live ? 0 : spec ? spec_eh0(A, w, sj) : A.shadowEH0[w.k];
         int fc = 0, fg = 0;
         if (Tmax > 0) {
             if constexpr (FAST)
@@ -726,17 +759,22 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
                 for (int j = 1; j < w.n; j++) s += st.prepend[w.y[j]];
                 cost = s;
                 gapnum = 0xFFFF;
-            } else if (p.gl == 0 && tmin(w.m - 1, b.newk) >= 2) {
+            } else if (!spec && p.gl == 0 && tmin(w.m - 1, b.newk) >= 2) {
                 A.shadowEH0[w.k] = HIGH;
             }
-            w.npass++;
-            if (p.gl == 0) A.passes[w.k] = w.npass;
-            if (aff_done(w.T, w.m, w.n, gapnum)) {
+            if (spec) {  // one pass; spec_resolve_kernel decides
+                if (p.gl == 0) spec_record(A, w, sj, cost, gapnum, cls | LASTCLS_LEAN, off);
                 live = false;
-                finished = true;
             } else {
-                w.T *= 2;
-                keep();
+                w.npass++;
+                if (p.gl == 0) A.passes[w.k] = w.npass;
+                if (aff_done(w.T, w.m, w.n, gapnum)) {
+                    live = false;
+                    finished = true;
+                } else {
+                    w.T *= 2;
+                    keep();
+                }
             }
         }
         pipe_sync(p);
@@ -1118,18 +1156,114 @@ __global__ void prep_kernel(BatchArgs A)
         A.status[k] = -6;
         return;
     }
-    int c;
-    if (A.affine) {
-        const long long wu = aff_wu(aff_band(pl.m, pl.n, band_p(pl.T0, pl.m, pl.n)));
-        c = ((A.pfull[k] & 2) && A.row_tile) ? pick_class_lean(A.lad, wu, pl.n)
-                                              : pick_class(A.lad, wu, pl.n);
-    }
-    else c = pick_class(A.lad, lin_wu(lin_band(pl.m, pl.n, pl.full, pl.full ? 0 : band_p(pl.T0, pl.m, pl.n))), pl.n);
+    const bool lean = A.affine && (A.pfull[k] & 2);
+    auto class_of = [&](int T) {
+        if (A.affine) {
+            const long long wu = aff_wu(aff_band(pl.m, pl.n, band_p(T, pl.m, pl.n)));
+            return (lean && A.row_tile) ? pick_class_lean(A.lad, wu, pl.n)
+                                        : pick_class(A.lad, wu, pl.n);
+        }
+        return pick_class(A.lad, lin_wu(lin_band(pl.m, pl.n, pl.full,
+                                                 pl.full ? 0 : band_p(T, pl.m, pl.n))), pl.n);
+    };
+    const int c = class_of(pl.T0);
     if (c < 0) {
         A.status[k] = -5;
         return;
     }
-    push_item(A, 2 * c + ((A.affine && (A.pfull[k] & 2)) ? 1 : 0), k, pl.T0);
+    if (A.spec_S > 0 && (lean || !A.affine) && pl.T0 > 0) {
+        // queue the first passes at once (the doubling's bands, up to the
+        // one that covers the plane), each as its own item
+        const int S = (!A.affine && pl.full) ? 1 : A.spec_S;
+        int T = pl.T0, nq = 0;
+        for (;;) {
+            const int cj = class_of(T);
+            if (cj < 0) {
+                nq |= SPEC_NOCLASS;
+                break;
+            }
+            push_item(A, 2 * cj + (lean ? 1 : 0), k, T);
+            nq++;
+            const bool last = A.affine ? aff_covers(T, pl.m, pl.n)
+                                       : (pl.full || lin_covers(T, pl.m, pl.n));
+            if (nq >= S || last) break;
+            T *= 2;
+        }
+        A.spec_T0[k] = pl.T0;
+        A.spec_n[k] = nq;
+        return;
+    }
+    if (A.spec_S > 0) {  // speculative batch: sequential pairs wait for the second sweep
+        A.spec_T0[k] = pl.T0;
+        A.spec_n[k] = -1;
+        return;
+    }
+    push_item(A, 2 * c + (lean ? 1 : 0), k, pl.T0);
+}
+
+// The sequential doubling resumed at pass j (band T) on the second sweep.
+__device__ void spec_requeue(const BatchArgs& A, int k, int m, int n, int j, int T, bool lean)
+{
+    A.passes[k] = j;
+    int c;
+    if (A.affine) {
+        if (j > 0 && m - 1 >= 2 &&
+            tmin(m - 1, aff_band(m, n, band_p(T / 2, m, n)).newk) >= 2)
+            A.shadowEH0[k] = HIGH;
+        c = pick_class(A.lad, aff_wu(aff_band(m, n, band_p(T, m, n))), n);
+    } else {
+        const int full = A.pfull[k] & 1;
+        c = pick_class(A.lad, lin_wu(lin_band(m, n, full, full ? 0 : band_p(T, m, n))), n);
+    }
+    if (c < 0) {
+        A.status[k] = -5;
+        return;
+    }
+    push_item(A, 2 * c + (lean ? 1 : 0), k, T);
+}
+
+// One thread per speculated pair: the first queued pass whose result
+// satisfies the doubling test is the pair's final pass (the sequential
+// doubling runs exactly the passes before it, in order, and stops there).
+__global__ void spec_resolve_kernel(BatchArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.npairs || A.status[k] != 1) return;
+    const int la = A.lena[k], lb = A.lenb[k];
+    const int m = la <= lb ? la : lb, n = la <= lb ? lb : la;
+    const bool lean = A.affine && (A.pfull[k] & 2);
+    int T = A.spec_T0[k];
+    if (A.spec_n[k] < 0) {  // not speculated (gap-bearing affine pair): sequential from pass 0
+        spec_requeue(A, k, m, n, 0, T, lean);
+        return;
+    }
+    const int S = A.spec_S, nq = A.spec_n[k] & ~SPEC_NOCLASS;
+    const bool full = !A.affine && (A.pfull[k] & 1);
+    for (int j = 0; j < nq; j++, T *= 2) {
+        const int4 r = A.spec_res[(long long)k * S + j];
+        if (r.w != 1) {  // a queued pass did not run
+            A.status[k] = -9;
+            return;
+        }
+        const bool done = A.affine ? aff_done(T, m, n, r.y) : (full || lin_done(T, m, n, r.y));
+        if (!done) continue;
+        const long long off = A.spec_off[(long long)k * S + j];
+        if (off >= 0 || !A.do_traceback) {
+            A.cost[k] = r.x;
+            A.passes[k] = j + 1;
+            A.lastcls[k] = r.z;
+            if (A.dm_off) A.dm_off[k] = off;
+            A.status[k] = 0;
+        } else {  // no arena region for its fill: the sequential sweep runs it again
+            spec_requeue(A, k, m, n, j, T, lean);
+        }
+        return;
+    }
+    if (A.spec_n[k] & SPEC_NOCLASS) {
+        A.status[k] = -5;
+        return;
+    }
+    spec_requeue(A, k, m, n, nq, T, lean);
 }
 
 // Traceback of fills kept in their slabs (per-call stub path); one thread
@@ -1381,6 +1515,11 @@ void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s)
     if (!a.qsorted) return;
     queue_hist_kernel<<<grid, 256, 0, s>>>(a, cls);
     queue_scatter_kernel<<<grid, 256, 0, s>>>(a, cls);
+}
+
+void launch_spec_resolve(const BatchArgs& a, cudaStream_t s)
+{
+    spec_resolve_kernel<<<(a.npairs + 127) / 128, 128, 0, s>>>(a);
 }
 
 void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)

@@ -66,7 +66,23 @@ struct BatchArgs {
     long long dm_max_region;      // larger fills keep the pipeline's slab
     unsigned long long* dm_used;  // bump counter, zero before the batch
     long long* dm_off;            // per pair: arena offset of the final fill, -1 if none
+    // Speculative band passes (small batches): the first spec_S passes of
+    // every linear or lean affine pair run at once as independent items (a
+    // pass depends on the earlier ones only through the stop decision and,
+    // for the affine model, a row-0 value that is a function of the pass
+    // index); spec_resolve_kernel then keeps the first pass that satisfies
+    // the doubling test, as the sequential doubling would have stopped there.
+    int spec;                     // this sweep's linear / lean items are speculative
+    int spec_S;                   // passes per pair (0: no speculation in this batch)
+    int* spec_T0;                 // per pair: T of pass 0 (0: not speculated)
+    int* spec_n;                  // per pair: passes queued (| SPEC_NOCLASS)
+    int4* spec_res;               // per pair x spec_S: cost, gap count, class flags, 1 = ran
+    long long* spec_off;          // per pair x spec_S: arena region of that pass (-1: none)
 };
+
+// spec_n: the pass after the queued ones has no class (the sequential
+// doubling would fail the pair there with status -5)
+constexpr int SPEC_NOCLASS = 1 << 30;
 
 // Work queues: 2 per class (variant 1 = affine gap-free fast path).
 constexpr int NQUEUE = 2 * NCLASS;
@@ -76,6 +92,9 @@ constexpr int NBUCKET = 256;
 constexpr int QCTR_INTS = 2 * NQUEUE * (1 + NBUCKET);
 // Sort the class's two queues longest pair first (no-op without qsorted).
 void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s);
+// After a speculative sweep: finish the pairs one of whose passes stopped,
+// queue the others for the sequential sweep.
+void launch_spec_resolve(const BatchArgs& a, cudaStream_t s);
 // Persistent CTAs per SM a class kernel can keep resident.
 int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // The row tile width of a class's lean queue (0: lane pipeline).
