@@ -439,8 +439,9 @@ int poyalgn_set_row_tile(poyalgn_ctx *ctx, int mode);
  * pair keeps the first pass that satisfies the doubling test (the one the
  * sequential doubling stops at); pairs that need more, and gap-bearing
  * affine pairs, continue sequentially. Costs extra cells, never changes a result.
- * mode 0: off; 1: every batch; 2 (default): batches of at most one pair per
- * SM. passes: 1 .. POYALGN_SPEC_MAX_PASSES (default 6). Only batches whose
+ * mode 0: off; 1: every batch; 2 (default): batches of at most 8 pairs per
+ * SM with `passes`, of at most 32 pairs per SM with passes - 2, larger
+ * batches without. passes: 1 .. POYALGN_SPEC_MAX_PASSES (default 8). Only batches whose
  * fills outlive the sweep speculate (tracebacks deferred to the arena, or
  * cost-only distances). No counterpart in the reference.
  */

@@ -77,9 +77,9 @@ class Context:
         """0: lane pipeline, 1: row tile, 2: by batch size (lean affine passes)."""
         check(_lib.load().poyalgn_set_row_tile(self._h, int(mode)))
 
-    def set_speculation(self, mode: int, passes: int = 6):
-        """Speculative band passes: 0 off, 1 every batch, 2 batches of at most
-        one pair per SM (default); `passes` bands of each pair run at once."""
+    def set_speculation(self, mode: int, passes: int = 8):
+        """Speculative band passes: 0 off, 1 every batch, 2 by batch size
+        (default); `passes` bands of each pair run at once."""
         check(_lib.load().poyalgn_set_speculation(self._h, int(mode), int(passes)))
 
     def profile_begin(self, max_batches: int):

@@ -62,7 +62,11 @@ int ensure_device(poyalgn_ctx* c)
 }
 
 constexpr int ROW_TILE_MAX_PAIRS = 2;  // per SM, for row_tile_mode 2
-constexpr int SPEC_MAX_PAIRS = 1;      // per SM, for spec_mode 2
+// spec_mode 2: batches of at most SPEC_FULL_PAIRS pairs per SM speculate
+// spec_passes passes, up to SPEC_MAX_PAIRS two fewer (measured on GB300: the
+// extra cells cost more than the latency saved beyond about 30 pairs per SM)
+constexpr int SPEC_FULL_PAIRS = 8;
+constexpr int SPEC_MAX_PAIRS = 32;
 // Largest arena region one pair's fills in one class may take; wider fills
 // (long pairs) keep the pipeline's slab and trace back in the class kernel.
 constexpr long long DM_MAX_REGION = 64LL << 20;
@@ -85,9 +89,12 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     // that need more). The fills must outlive the sweep: the arena holds
     // them, or only the cost is wanted.
     const bool spec_ok = distance || (do_traceback && c->defer_traceback);
-    const int spec_S = (spec_ok && (c->spec_mode == 1 ||
-                                    (c->spec_mode == 2 && npairs <= SPEC_MAX_PAIRS * c->nsm)))
-                           ? c->spec_passes : 0;
+    int spec_S = 0;
+    if (spec_ok && c->spec_mode == 1) spec_S = c->spec_passes;
+    if (spec_ok && c->spec_mode == 2) {
+        if (npairs <= SPEC_FULL_PAIRS * c->nsm) spec_S = c->spec_passes;
+        else if (npairs <= SPEC_MAX_PAIRS * c->nsm) spec_S = std::max(1, c->spec_passes - 2);
+    }
     // the row tile has the lower latency per pass, the lane pipeline the
     // higher throughput: small batches take the row tile (unless their
     // passes run speculatively on the lane pipeline)
@@ -313,10 +320,18 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     for (DevBuf* b : per_pair)
         if ((rc = reserve(*b, n * 4))) return rc;
     if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
-    if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * n * sizeof(int2)))) return rc;
+    // speculative batches queue up to spec_passes items per pair
+    const size_t items = n * (size_t)(c->spec_mode ? std::max(1, c->spec_passes) : 1);
+    if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * items * sizeof(int2)))) return rc;
     if ((rc = reserve(c->qctr, QCTR_INTS * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
     if ((rc = reserve(c->order_scratch, order_scratch_bytes((int)n)))) return rc;
+    if (c->spec_mode) {
+        if ((rc = reserve(c->spec_t0, n * 4))) return rc;
+        if ((rc = reserve(c->spec_n, n * 4))) return rc;
+        if ((rc = reserve(c->spec_res, items * sizeof(int4)))) return rc;
+        if ((rc = reserve(c->spec_off, items * 8))) return rc;
+    }
     if ((rc = reserve(c->slab, (size_t)slab_bytes))) return rc;
     if (c->dm_fixed > 0) {
         if ((rc = reserve(c->dmarena, (size_t)c->dm_fixed))) return rc;

@@ -61,8 +61,8 @@ struct poyalgn_ctx {
     pa::DevBuf dmarena, dmoff, dmctr;          // deferred tracebacks
     int defer_traceback = 1;                   // 0: trace back inside the class kernels
     pa::DevBuf spec_t0, spec_n, spec_res, spec_off;  // speculative band passes
-    int spec_mode = 2;     // 0 off, 1 every batch, 2 batches of at most one pair per SM
-    int spec_passes = 6;   // passes per pair run at once
+    int spec_mode = 2;     // 0 off, 1 every batch, 2 by batch size
+    int spec_passes = 8;   // passes per pair run at once
     // the speculative sweep runs every class at once, one stream per class
     cudaStream_t spec_st[pa::NCLASS] = {};
     cudaEvent_t spec_fork = nullptr, spec_join[pa::NCLASS] = {};

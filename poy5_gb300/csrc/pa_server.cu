@@ -99,13 +99,20 @@ void fail_all(poyalgn_server* s, int code, const char* msg)
     s->cv_done.notify_all();
 }
 
+// pairs per SM up to which a batch with no backlog speculates
+constexpr int SERVE_SPEC_PAIRS = 2;
+
 // Build and enqueue one batch on slot `sl` from the requests in `batch`.
 // Runs without the server lock; touches only the slot and the requests,
-// which no other thread reads until they are marked done.
-int launch(poyalgn_server* s, Slot& sl, std::vector<Req*>& batch)
+// which no other thread reads until they are marked done. Speculative band
+// passes only for a small batch with nothing waiting behind it: with a
+// backlog, or batches that with the other slots' fill the GPU, throughput
+// matters more than one batch's latency.
+int launch(poyalgn_server* s, Slot& sl, std::vector<Req*>& batch, bool backlog)
 {
     int n = 0;
     for (Req* r : batch) n += r->npairs;
+    sl.ctx->spec_mode = (backlog || n > SERVE_SPEC_PAIRS * sl.ctx->nsm) ? 0 : 2;
     const size_t ni = (size_t)n;
     long long* offa = reinterpret_cast<long long*>(sl.hmeta);
     long long* offb = offa + ni;
@@ -233,8 +240,9 @@ void scheduler(poyalgn_server* s)
                 s->waiting.pop_front();
             }
             s->waiting_pairs -= n;
+            const bool backlog = !s->waiting.empty();
             lk.unlock();
-            const int rc = launch(s, sl, batch);
+            const int rc = launch(s, sl, batch, backlog);
             lk.lock();
             if (rc) {
                 fail_all(s, rc, poyalgn_last_error());
