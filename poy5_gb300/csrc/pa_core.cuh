@@ -1036,9 +1036,13 @@ PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
                          vv ? up.GM + 0x10000u : 0u);
             VP[q] = c;
             dcode[q] = code;
-        } else {
-            VP[q] = VC[q];  // keep the row's last state (read as diag/left)
         }
+        // Outside its band a row's register keeps a stale state. No in-band
+        // cell reads it: a row's first cell ignores its left neighbour (EH =
+        // HIGH, END_H masked), an up neighbour beyond the row above's band
+        // only occurs at the right border (EV = HIGH), and a diagonal one
+        // outside the band only at column 0 (CB = HIGH); the gap numbers take
+        // each neighbour only with the state it decides.
     }
 }
 
