@@ -837,13 +837,15 @@ enum : int {
     LEAN_DO_V = 16, LEAN_DO_H = 32, LEAN_H_EQ_V = 64
 };
 
-// the flags of a lean direction byte in the aff_step encoding
+// the flags of a lean direction byte in the aff_step encoding (H_EQ_V: EH
+// and EV both minimal, i.e. DO_H and DO_V)
 PA_HD int lean_flags(int b)
 {
+    const bool hv = (b & (LEAN_DO_H | LEAN_DO_V)) == (LEAN_DO_H | LEAN_DO_V);
     return ((b & LEAN_A2V) ? A2V : 0) | ((b & LEAN_A2H) ? A2H : 0) |
            ((b & LEAN_END_V) ? END_V : 0) | ((b & LEAN_END_H) ? END_H : 0) |
            ((b & LEAN_DO_V) ? DO_V : 0) | ((b & LEAN_DO_H) ? DO_H : 0) |
-           ((b & LEAN_H_EQ_V) ? H_EQ_V : 0);
+           ((hv || (b & LEAN_H_EQ_V)) ? H_EQ_V : 0);
 }
 
 // min(a, b) and *le = (a <= b); min of three (DPX instructions on sm_90+)
@@ -1015,23 +1017,28 @@ PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
             LeanCell c;
             bool endh, endv;
             // EH: extend (left EH) vs open (left CB); END_H when open <= extend
+            // Flags a traceback can never read are left unmasked: a row's
+            // first cell (EH = HIGH) is never in the H state, a right-border
+            // cell (EV = HIGH) never in the V state, a column-0 cell (CB =
+            // HIGH) never in the D state; H_EQ_V is DO_H and DO_V together
+            // (lean_flags).
             const int eh = bmin_le(lf.CB + go + jgr, lf.EH + jgr, &endh);
             const bool left = (T == L.Ts[q]);
             c.EH = left ? HIGH : eh;
-            int code = (!left && endh) ? LEAN_END_H : 0;
+            int code = endh ? LEAN_END_H : 0;
             const int ev = bmin_le(up.CB + L.sgo[q], up.EV + L.sg[q], &endv);
             const bool right = (T == L.Tr[q]);
             c.EV = right ? HIGH : ev;
-            code |= (!right && endv) ? LEAN_END_V : 0;
+            code |= endv ? LEAN_END_V : 0;
             // column 0 has no diagonal (CB = HIGH); J = sj[0] keeps the
             // lookup in range
             const int m3 = min3(dg.CB, dg.EV, dg.EH);
             const int dgc = t.csw[L.srb[q] + L.J[q]];
             c.CB = j > 0 ? m3 + dgc : HIGH;
-            code |= j > 0 ? ((dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0)) : 0;
+            code |= (dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0);
             const int f = min3(c.EH, c.EV, c.CB);
             const bool hh = c.EH == f, vv = c.EV == f;
-            code |= (hh ? LEAN_DO_H : 0) | (vv ? LEAN_DO_V : 0) | ((hh && vv) ? LEAN_H_EQ_V : 0);
+            code |= (hh ? LEAN_DO_H : 0) | (vv ? LEAN_DO_V : 0);
             c.GM = vmax3(c.CB == f ? dg.GM : 0u, hh ? lf.GM + 1u : 0u,
                          vv ? up.GM + 0x10000u : 0u);
             VP[q] = c;
