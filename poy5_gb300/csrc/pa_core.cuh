@@ -1010,46 +1010,43 @@ PA_HD void aff_lean_step(AffLean<R>& L, LeanCell (&VC)[R], LeanCell (&VP)[R],
         const LeanCell up = q > 0 ? VC[q - 1] : (gen ? GP : RP);
         const LeanCell dg = q > 0 ? VP[q - 1] : (gen ? GC : RC);
         const LeanCell& lf = VC[q];
-        dcode[q] = 0;
-        if (T >= L.Ts[q] && T <= L.Te[q]) {
-            const int j = T - (L.itop + q);
-            const int jgr = L.JG[q];
-            LeanCell c;
-            bool endh, endv;
-            // EH: extend (left EH) vs open (left CB); END_H when open <= extend
-            // Flags a traceback can never read are left unmasked: a row's
-            // first cell (EH = HIGH) is never in the H state, a right-border
-            // cell (EV = HIGH) never in the V state, a column-0 cell (CB =
-            // HIGH) never in the D state; H_EQ_V is DO_H and DO_V together
-            // (lean_flags).
-            const int eh = bmin_le(lf.CB + go + jgr, lf.EH + jgr, &endh);
-            const bool left = (T == L.Ts[q]);
-            c.EH = left ? HIGH : eh;
-            int code = endh ? LEAN_END_H : 0;
-            const int ev = bmin_le(up.CB + L.sgo[q], up.EV + L.sg[q], &endv);
-            const bool right = (T == L.Tr[q]);
-            c.EV = right ? HIGH : ev;
-            code |= endv ? LEAN_END_V : 0;
-            // column 0 has no diagonal (CB = HIGH); J = sj[0] keeps the
-            // lookup in range
-            const int m3 = min3(dg.CB, dg.EV, dg.EH);
-            const int dgc = t.csw[L.srb[q] + L.J[q]];
-            c.CB = j > 0 ? m3 + dgc : HIGH;
-            code |= (dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0);
-            const int f = min3(c.EH, c.EV, c.CB);
-            const bool hh = c.EH == f, vv = c.EV == f;
-            code |= (hh ? LEAN_DO_H : 0) | (vv ? LEAN_DO_V : 0);
-            c.GM = vmax3(c.CB == f ? dg.GM : 0u, hh ? lf.GM + 1u : 0u,
-                         vv ? up.GM + 0x10000u : 0u);
-            VP[q] = c;
-            dcode[q] = code;
-        }
-        // Outside its band a row's register keeps a stale state. No in-band
-        // cell reads it: a row's first cell ignores its left neighbour (EH =
-        // HIGH, END_H masked), an up neighbour beyond the row above's band
-        // only occurs at the right border (EV = HIGH), and a diagonal one
-        // outside the band only at column 0 (CB = HIGH); the gap numbers take
-        // each neighbour only with the state it decides.
+        // Every row is computed every step, in its band or not. Outside its
+        // band a row's state is never read by an in-band cell: a row's first
+        // cell ignores its left neighbour (EH = HIGH, its H flags unread), an
+        // up neighbour beyond the row above's band only occurs at the right
+        // border (EV = HIGH), a diagonal one outside the band only at column
+        // 0 (CB = HIGH), and the gap numbers take each neighbour only with
+        // the state it decides; the codes of cells outside the band are
+        // never read either. All lookups stay in range for any row.
+        // Flags a traceback can never read are left unmasked: a row's first
+        // cell is never in the H state, a right-border cell (EV = HIGH) never
+        // in the V state, a column-0 cell (CB = HIGH) never in the D state;
+        // H_EQ_V is DO_H and DO_V together (lean_flags).
+        const int j = T - (L.itop + q);
+        const int jgr = L.JG[q];
+        LeanCell c;
+        bool endh, endv;
+        // EH: extend (left EH) vs open (left CB); END_H when open <= extend
+        const int eh = bmin_le(lf.CB + go + jgr, lf.EH + jgr, &endh);
+        const bool left = (T == L.Ts[q]);
+        c.EH = left ? HIGH : eh;
+        int code = endh ? LEAN_END_H : 0;
+        const int ev = bmin_le(up.CB + L.sgo[q], up.EV + L.sg[q], &endv);
+        const bool right = (T == L.Tr[q]);
+        c.EV = right ? HIGH : ev;
+        code |= endv ? LEAN_END_V : 0;
+        // column 0 has no diagonal (CB = HIGH); J = sj[0] keeps the lookup
+        // in range
+        const int m3 = min3(dg.CB, dg.EV, dg.EH);
+        const int dgc = t.csw[L.srb[q] + L.J[q]];
+        c.CB = j > 0 ? m3 + dgc : HIGH;
+        code |= (dg.EV == m3 ? LEAN_A2V : 0) | (dg.EH == m3 ? LEAN_A2H : 0);
+        const int f = min3(c.EH, c.EV, c.CB);
+        const bool hh = c.EH == f, vv = c.EV == f;
+        code |= (hh ? LEAN_DO_H : 0) | (vv ? LEAN_DO_V : 0);
+        c.GM = vmax3(c.CB == f ? dg.GM : 0u, hh ? lf.GM + 1u : 0u, vv ? up.GM + 0x10000u : 0u);
+        VP[q] = c;
+        dcode[q] = code;
     }
 }
 
