@@ -394,29 +394,28 @@ PA_HD void lin_step(LinLane<R>& L, int (&VC)[R], int (&VP)[R], uint32_t (&NC)[R]
             upV = RP; upN = RNP;
             dgV = RC; dgN = RNC;
         }
-        dcode[q] = 0;
-        if (T >= L.Ts[q] && T <= L.Te[q]) {
-            const int i = L.itop + q;
-            const bool c0 = (T == i);
-            const bool hasR = (L.hr >> q) & 1;
-            const bool lft = (T == L.Ts[q]) && !c0;
-            const bool edge = (T == L.Te[q]);
-            const int dlc = c0 ? (b.full ? L.dc[q] : L.tl[q]) : L.dc[q];
-            const int aln = c0 ? BIG : dgV + t.csw[L.rb[q] + L.J[q]];
-            const int ins = (c0 || lft) ? BIG : VC[q] + L.G[q];
-            int del = (edge && hasR) ? BIG : upV + dlc;
-            if (edge && !hasR && !c0) del = tmin(del, upV + L.tl[q]);
-            const int v = tmin(tmin(aln, ins), del);
-            const int d = (aln == v ? L_ALIGN : 0) | (ins == v ? L_INSERT : 0) |
-                          (del == v ? L_DELETE : 0);
-            // forward gap count along the path backtrace_2d_gaps follows
-            NP[q] = (d & L_ALIGN) ? dgN : (d & L_INSERT) ? NC[q] + 1u : upN + 0x10000u;
-            VP[q] = v;
-            dcode[q] = d;
-        } else {
-            VP[q] = VC[q];  // keep the row's last state (read as diag/left)
-            NP[q] = NC[q];
-        }
+        // Every row is computed every step, in its band or not: an in-band
+        // cell reads an out-of-band neighbour only where the neighbour's
+        // candidate is masked (left border: no INSERT; column 0: no ALIGN;
+        // right border with a border bit: no DELETE), and no code outside
+        // the band is ever read. All lookups stay in range for any row.
+        const int i = L.itop + q;
+        const bool c0 = (T == i);
+        const bool hasR = (L.hr >> q) & 1;
+        const bool lft = (T == L.Ts[q]) && !c0;
+        const bool edge = (T == L.Te[q]);
+        const int dlc = c0 ? (b.full ? L.dc[q] : L.tl[q]) : L.dc[q];
+        const int aln = c0 ? BIG : dgV + t.csw[L.rb[q] + L.J[q]];
+        const int ins = (c0 || lft) ? BIG : VC[q] + L.G[q];
+        int del = (edge && hasR) ? BIG : upV + dlc;
+        if (edge && !hasR && !c0) del = tmin(del, upV + L.tl[q]);
+        const int v = tmin(tmin(aln, ins), del);
+        const int d = (aln == v ? L_ALIGN : 0) | (ins == v ? L_INSERT : 0) |
+                      (del == v ? L_DELETE : 0);
+        // forward gap count along the path backtrace_2d_gaps follows
+        NP[q] = (d & L_ALIGN) ? dgN : (d & L_INSERT) ? NC[q] + 1u : upN + 0x10000u;
+        VP[q] = v;
+        dcode[q] = d;
     }
 }
 
