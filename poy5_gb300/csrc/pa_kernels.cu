@@ -1302,9 +1302,11 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
 // pair (after all class kernels, so no fill waits on a traceback).
 __global__ void deferred_traceback_kernel(BatchArgs A)
 {
+    __shared__ Tables t;  // median and cost lookups from shared memory
+    load_tables(t, A.tables);
+    __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
-    const Tables& t = *A.tables;
     const int la = A.lena[k], lb = A.lenb[k];
     const int swaped = la <= lb ? 0 : 1;
     const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
