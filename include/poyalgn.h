@@ -315,6 +315,39 @@ int poyalgn_downpass(poyalgn_store *s, const poyalgn_cm *cm, int nleaves,
                      int32_t *internal_node, int32_t *internal_cost,
                      int64_t *total_cost, int32_t *levels);
 
+/*
+ * SeqCS.DOS.median_3_no_union (src/seqCS.ml:1123-1147) for n resident
+ * triples: node k's parent state parent[k] is aligned with each child
+ * (child1[k], child2[k]) by Sequence.Align.align_2 (parent first); the
+ * alignment of lower cost is kept (the second child's on a tie) and the
+ * no-gap median of its aligned pair (Sequence.median_2 ->
+ * seq_get_median_2d_no_gaps, src/seq.c:259-272, leading gap included)
+ * becomes a new node (node[k]). cost and maxcost are the kept alignment's
+ * cost and worst cost (Align.max_cost_2), the cost2 and cost2_max fields of
+ * the reference's result; status is per triple. Returns POYALGN_EPAIR if
+ * any triple failed. The 2 n alignments run as one batch.
+ */
+int poyalgn_store_median3_batch(poyalgn_store *s, const poyalgn_cm *cm, int n,
+                                const int32_t *parent, const int32_t *child1,
+                                const int32_t *child2, int32_t *node,
+                                int32_t *cost, int32_t *maxcost,
+                                int32_t *status);
+
+/*
+ * Uppass of the tree of poyalgn_downpass (same encoding): final states top
+ * down, one batch per depth. The root keeps its downpass state
+ * (root_final = internal_node[ninternal - 1]); every other internal node k
+ * gets median_3_no_union(final state of its parent, states of its two
+ * children), where a child's state is its leaf sequence or its downpass
+ * median (internal_node). Writes final_node[k] and final_cost[k] (cost2 of
+ * the kept alignment; 0 for the root) for every internal node.
+ */
+int poyalgn_uppass(poyalgn_store *s, const poyalgn_cm *cm, int nleaves,
+                   const int32_t *leaf_node, int ninternal,
+                   const int32_t *left, const int32_t *right,
+                   const int32_t *internal_node, int32_t *final_node,
+                   int32_t *final_cost, int32_t *levels);
+
 /* ---- serving: continuous batching of scoring requests ------------------------ */
 
 /*

@@ -101,6 +101,130 @@ int store_batch(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* na
     return 0;
 }
 
+// median_3_no_union's choice and median (src/seqCS.ml:1123-1147): of the
+// alignments 2k (parent, child1) and 2k + 1 (parent, child2), keep the one
+// of lower cost (the second on a tie) and write seq_get_median_2d_no_gaps
+// (src/seq.c:259-272) of its aligned pair back to front into node k's
+// region. res[4k..4k+3] = cost, worst cost, median length, status.
+__global__ void median3_pick_kernel(const Tables* tg, int n, const long long* out_off,
+                                    const int* lena, const int* lenb, const int* I,
+                                    const uint8_t* ea, const uint8_t* eb, uint8_t* dst,
+                                    const long long* dst_end, int* res)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const Tables& t = *tg;
+    const int n2 = 2 * n, a = 2 * k, b = 2 * k + 1;
+    const int *cost = I, *maxcost = I + n2, *alen = I + 2 * n2, *status = I + 5 * n2;
+    const int st = status[a] != 0 ? status[a] : status[b];
+    if (st != 0) {
+        res[4 * k + 3] = st;
+        return;
+    }
+    const int j = cost[a] < cost[b] ? a : b;
+    const long long start = out_off[j] + lena[j] + lenb[j] + 2 - alen[j];
+    const uint8_t* x = ea + start;  // aligned parent
+    const uint8_t* y = eb + start;  // aligned child
+    uint8_t* o = dst + dst_end[k];
+    int w = 0;
+    for (int i = alen[j] - 1; i >= 0; i--) {
+        const int m = t.median[(x[i] << t.lcm) + y[i]];
+        if (m != t.gap) o[-(++w)] = (uint8_t)m;
+    }
+    o[-(++w)] = (uint8_t)t.gap;
+    res[4 * k] = cost[j];
+    res[4 * k + 1] = maxcost[j];
+    res[4 * k + 2] = w;
+    res[4 * k + 3] = 0;
+}
+
+int store_median3(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* parent,
+                  const int32_t* child1, const int32_t* child2, int32_t* node, int32_t* cost,
+                  int32_t* maxcost, int32_t* status)
+{
+    poyalgn_ctx* c = s->ctx;
+    int rc;
+    if ((rc = ensure_device(c))) return rc;
+    const size_t n2 = 2 * (size_t)n, ni = (size_t)n;
+    // metadata: offa | offb | out_off (int64, 2n each) | lena | lenb (int32,
+    // 2n each) | node region ends (int64, n)
+    s->hmeta.resize(n2 * 32 + ni * 8);
+    long long* offa = reinterpret_cast<long long*>(s->hmeta.data());
+    long long* offb = offa + n2;
+    long long* oo = offb + n2;
+    int* lena = reinterpret_cast<int*>(oo + n2);
+    int* lenb = lena + n2;
+    long long* dend = reinterpret_cast<long long*>(lenb + n2);
+    long long total = 0, ntotal = 0;
+    int maxmn = 2;
+    for (int k = 0; k < n; k++) {
+        const int32_t nb2[2] = {child1[k], child2[k]};
+        if (!valid_node(s, parent[k]) || !valid_node(s, child1[k]) || !valid_node(s, child2[k]))
+            return set_err(POYALGN_EINVAL, "triple %d: unknown node (%d, %d, %d)", k, parent[k],
+                           child1[k], child2[k]);
+        for (int h = 0; h < 2; h++) {
+            const size_t q = 2 * (size_t)k + h;
+            offa[q] = s->off[parent[k]];
+            offb[q] = s->off[nb2[h]];
+            lena[q] = s->len[parent[k]];
+            lenb[q] = s->len[nb2[h]];
+            oo[q] = total;
+            total += align_up((long long)lena[q] + lenb[q] + 2);
+            maxmn = std::max(maxmn, lena[q] + lenb[q]);
+        }
+        // the median has at most one entry per aligned column plus the gap
+        ntotal += align_up((long long)s->len[parent[k]] +
+                           std::max(s->len[child1[k]], s->len[child2[k]]) + 2);
+        dend[k] = ntotal;
+    }
+    const long long base = align_up(s->used);
+    if (base + ntotal > s->cap)
+        return set_err(POYALGN_ENOMEM, "store full: %lld of %lld bytes used, batch needs %lld",
+                       s->used, s->cap, ntotal);
+    if ((rc = reserve(s->meta, n2 * 32 + ni * 8))) return rc;
+    if ((rc = reserve(s->ints, n2 * 4 * 7 + ni * 4 * 4))) return rc;
+    if ((rc = reserve(s->bytes, (size_t)total * 4))) return rc;
+    cudaStream_t st = c->stream;
+    CU(cudaMemcpyAsync(s->meta.p, s->hmeta.data(), n2 * 32 + ni * 8, cudaMemcpyHostToDevice, st));
+    const long long* d_offa = as<long long>(s->meta);
+    const int* d_lena = reinterpret_cast<const int*>(d_offa + 3 * n2);
+    const long long* d_dend = reinterpret_cast<const long long*>(d_lena + 2 * n2);
+    int* I = as<int>(s->ints);
+    int* res = I + 7 * n2;
+    uint8_t* B = as<uint8_t>(s->bytes);
+    uint8_t* arena = as<uint8_t>(s->arena);
+    if ((rc = run_batch(c, cm, cm->h.cost_model == 1, (int)n2, maxmn, total, arena, d_offa,
+                        d_lena, d_offa + n2, d_lena + n2, d_offa + 2 * n2, I, I + n2,
+                        I + 2 * n2, I + 3 * n2, I + 4 * n2, I + 5 * n2, B, B + total,
+                        B + 2 * total, B + 3 * total, I + 6 * n2, nullptr, nullptr, 1, st)))
+        return rc;
+    median3_pick_kernel<<<(n + 127) / 128, 128, 0, st>>>(cm->d, n, d_offa + 2 * n2, d_lena,
+                                                         d_lena + n2, I, B, B + total,
+                                                         arena + base, d_dend, res);
+    CU(cudaGetLastError());
+    s->hints.resize(ni * 4);
+    CU(cudaMemcpyAsync(s->hints.data(), res, ni * 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    const int* h = s->hints.data();
+    int failed = -1;
+    for (int k = 0; k < n; k++) {
+        const int ok = h[4 * k + 3] == 0;
+        if (cost) cost[k] = h[4 * k];
+        if (maxcost) maxcost[k] = h[4 * k + 1];
+        if (status) status[k] = h[4 * k + 3];
+        if (!ok && failed < 0) failed = k;
+        if (node) node[k] = ok ? (int)s->len.size() : -1;
+        if (!ok) continue;
+        s->off.push_back(base + dend[k] - h[4 * k + 2]);
+        s->len.push_back(h[4 * k + 2]);
+    }
+    s->used = base + ntotal;
+    if (failed >= 0)
+        return set_err(POYALGN_EPAIR, "triple %d failed with status %d", failed,
+                       h[4 * failed + 3]);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -248,6 +372,78 @@ int poyalgn_downpass(poyalgn_store* s, const poyalgn_cm* cm, int nleaves,
     }
     *total_cost = total;
     if (levels) *levels = depth;
+    return 0;
+}
+
+int poyalgn_store_median3_batch(poyalgn_store* s, const poyalgn_cm* cm, int n,
+                                const int32_t* parent, const int32_t* child1,
+                                const int32_t* child2, int32_t* node, int32_t* cost,
+                                int32_t* maxcost, int32_t* status)
+{
+    if (!s || !cm || n < 0 || (n > 0 && (!parent || !child1 || !child2)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (n == 0) return 0;
+    return store_median3(s, cm, n, parent, child1, child2, node, cost, maxcost, status);
+}
+
+int poyalgn_uppass(poyalgn_store* s, const poyalgn_cm* cm, int nleaves,
+                   const int32_t* leaf_node, int ninternal, const int32_t* left,
+                   const int32_t* right, const int32_t* internal_node, int32_t* final_node,
+                   int32_t* final_cost, int32_t* levels)
+{
+    if (!s || !cm || nleaves < 1 || ninternal < 1 || !leaf_node || !left || !right ||
+        !internal_node || !final_node || !final_cost)
+        return set_err(POYALGN_EINVAL, "null argument");
+    // parent of every internal node (children come before their parent)
+    std::vector<int> up(ninternal, -1), depth(ninternal, 0);
+    for (int k = 0; k < ninternal; k++)
+        for (int ch : {left[k], right[k]}) {
+            if (ch < 0 || ch >= nleaves + k)
+                return set_err(POYALGN_EINVAL, "internal node %d: child %d is not an earlier node",
+                               k, ch);
+            if (ch >= nleaves) {
+                if (up[ch - nleaves] >= 0)
+                    return set_err(POYALGN_EINVAL, "internal node %d has two parents",
+                                   ch - nleaves);
+                up[ch - nleaves] = k;
+            }
+        }
+    const int root = ninternal - 1;
+    if (up[root] >= 0) return set_err(POYALGN_EINVAL, "the last internal node is not the root");
+    int maxd = 0;
+    for (int k = root - 1; k >= 0; k--) {  // parents come after their children
+        if (up[k] < 0) return set_err(POYALGN_EINVAL, "internal node %d has no parent", k);
+        depth[k] = depth[up[k]] + 1;
+        maxd = std::max(maxd, depth[k]);
+    }
+    auto state = [&](int ch) { return ch < nleaves ? leaf_node[ch] : internal_node[ch - nleaves]; };
+    final_node[root] = internal_node[root];
+    final_cost[root] = 0;
+    std::vector<int32_t> idx, pa, c1, c2, nd, cs;
+    for (int d = 1; d <= maxd; d++) {
+        idx.clear();
+        pa.clear();
+        c1.clear();
+        c2.clear();
+        for (int k = 0; k < ninternal; k++) {
+            if (k == root || depth[k] != d) continue;
+            idx.push_back(k);
+            pa.push_back(final_node[up[k]]);
+            c1.push_back(state(left[k]));
+            c2.push_back(state(right[k]));
+        }
+        const int n = (int)idx.size();
+        nd.assign(n, -1);
+        cs.assign(n, 0);
+        const int rc = store_median3(s, cm, n, pa.data(), c1.data(), c2.data(), nd.data(),
+                                     cs.data(), nullptr, nullptr);
+        if (rc) return rc;
+        for (int t = 0; t < n; t++) {
+            final_node[idx[t]] = nd[t];
+            final_cost[idx[t]] = cs[t];
+        }
+    }
+    if (levels) *levels = maxd + 1;
     return 0;
 }
 

@@ -61,6 +61,22 @@ class Store:
             check(rc)
         return med, cost, mx, st
 
+    def median3_batch(self, cm: CostMatrix, parent, child1, child2):
+        """SeqCS.DOS.median_3_no_union of resident triples (parent state, two
+        children); returns (new nodes, costs, maxcosts, status)."""
+        p = np.ascontiguousarray(parent, np.int32)
+        a = np.ascontiguousarray(child1, np.int32)
+        b = np.ascontiguousarray(child2, np.int32)
+        n = len(p)
+        node = np.full(n, -1, np.int32)
+        cost, mx, st = (np.zeros(n, np.int32) for _ in range(3))
+        rc = _lib.load().poyalgn_store_median3_batch(self._h, cm.handle, n, _ptr(p), _ptr(a),
+                                                     _ptr(b), _ptr(node), _ptr(cost), _ptr(mx),
+                                                     _ptr(st))
+        if rc not in (0, _lib.EPAIR):
+            check(rc)
+        return node, cost, mx, st
+
     def close(self):
         if self._h:
             _lib.load().poyalgn_store_free(self._h)
@@ -95,6 +111,29 @@ def downpass(store: Store, cm: CostMatrix, leaf_nodes, left, right) -> DownpassR
                                        _ptr(lt), _ptr(rt), _ptr(node), _ptr(cost),
                                        C.byref(total), C.byref(levels)))
     return DownpassResult(node, cost, int(total.value), int(levels.value))
+
+
+@dataclass
+class UppassResult:
+    final_node: np.ndarray   # store node of each internal node's final state
+    final_cost: np.ndarray   # cost2 of the alignment median_3 kept (0 at the root)
+    levels: int
+
+
+def uppass(store: Store, cm: CostMatrix, leaf_nodes, left, right, internal_node) -> UppassResult:
+    """Final states top down from a downpass; see poyalgn_uppass."""
+    leaf = np.ascontiguousarray(leaf_nodes, np.int32)
+    lt = np.ascontiguousarray(left, np.int32)
+    rt = np.ascontiguousarray(right, np.int32)
+    inode = np.ascontiguousarray(internal_node, np.int32)
+    ni = len(lt)
+    node = np.full(ni, -1, np.int32)
+    cost = np.zeros(ni, np.int32)
+    levels = C.c_int32()
+    check(_lib.load().poyalgn_uppass(store.handle, cm.handle, len(leaf), _ptr(leaf), ni,
+                                     _ptr(lt), _ptr(rt), _ptr(inode), _ptr(node), _ptr(cost),
+                                     C.byref(levels)))
+    return UppassResult(node, cost, int(levels.value))
 
 
 def tree_levels(nleaves: int, left, right) -> np.ndarray:

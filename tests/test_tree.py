@@ -79,3 +79,92 @@ def test_store_batch_matches_host_batch(ctx):
         assert np.array_equal(store.read(int(med[k])), ref.pair(k).median), k
     store.truncate(n0)
     assert len(store) == n0
+
+
+# ---- uppass: SeqCS.DOS.median_3_no_union, top down -----------------------------
+
+def _median2_no_gaps(tab, ea, eb):
+    """seq_get_median_2d_no_gaps (src/seq.c:259-272) on an aligned pair."""
+    med, lcm, gap = tab["median"], tab["lcm"], tab["gap"]
+    out = [int(med[(int(x) << lcm) + int(y)]) for x, y in zip(ea, eb)]
+    return np.array([gap] + [v for v in out if v != gap], np.uint8)
+
+
+def _oracle_median3(oracle, ocm, tab, p, c1, c2, affine):
+    """SeqCS.DOS.median_3_no_union (src/seqCS.ml:1123-1147) over the oracle's
+    Align.align_2 (parent first): the cheaper alignment, the second on a tie."""
+    r1 = oracle.median(ocm, p, c1, affine)
+    r2 = oracle.median(ocm, p, c2, affine)
+    r = r1 if r1.cost < r2.cost else r2
+    return _median2_no_gaps(tab, r.ea, r.eb), r.cost, r.maxcost
+
+
+def _oracle_uppass(oracle, ocm, t, prelim):
+    """Root keeps its downpass state; every other internal node takes
+    median_3_no_union(parent final, children states)."""
+    tab = oracle.tables(ocm)
+    nl, ni = len(t.leaves), len(t.left)
+    state = lambda ch: t.leaves[ch] if ch < nl else prelim[ch - nl]
+    parent = {}
+    for k in range(ni):
+        for ch in (t.left[k], t.right[k]):
+            if ch >= nl:
+                parent[ch - nl] = k
+    final, cost = [None] * ni, [0] * ni
+    final[ni - 1] = prelim[ni - 1]
+    for k in range(ni - 2, -1, -1):  # parents come after their children
+        final[k], cost[k], _ = _oracle_median3(oracle, ocm, tab, final[parent[k]],
+                                               state(t.left[k]), state(t.right[k]), t.affine)
+    return final, np.array(cost)
+
+
+def test_oracle_uppass_small(oracle):
+    t = wl.yule_tree(n_taxa=8, root_len=60)
+    ocm = oracle.cm(subs=t.subs, indel=t.indel)
+    meds, _ = _oracle_downpass(oracle, ocm, t)
+    final, cost = _oracle_uppass(oracle, ocm, t, meds)
+    assert len(final) == 7 and all(f[0] == wl.GAP for f in final) and cost[-1] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_taxa,root_len", [(16, 120), (64, 600)])
+def test_uppass_matches_oracle(ctx, oracle, n_taxa, root_len):
+    import poy5_gb300 as pg
+    t = wl.yule_tree(n_taxa=n_taxa, root_len=root_len)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, t.subs, t.indel, t.gap_open)
+    ocm = oracle.cm(subs=t.subs, indel=t.indel)
+    store = pg.Store(ctx, 64 << 20)
+    leaf_nodes = [store.add(s) for s in t.leaves]
+    down = pg.downpass(store, cm, leaf_nodes, t.left, t.right)
+    up = pg.uppass(store, cm, leaf_nodes, t.left, t.right, down.internal_node)
+    meds, _ = _oracle_downpass(oracle, ocm, t)
+    final, cost = _oracle_uppass(oracle, ocm, t, meds)
+    assert np.array_equal(up.final_cost, cost)
+    assert up.final_node[-1] == down.internal_node[-1]
+    for k, f in enumerate(final):
+        assert np.array_equal(store.read(int(up.final_node[k])), f), k
+
+
+@pytest.mark.gpu
+def test_median3_batch_affine_matches_oracle(ctx, oracle):
+    """Affine triples: the no-gap median of the kept aligned pair differs from
+    DOS.median's own median, so this checks the separate median path."""
+    import poy5_gb300 as pg
+    w = wl.affine_pairs(n_pairs=48, seed=wl.SEED_BASE + 70)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    ocm = oracle.cm(subs=w.subs, indel=w.indel, gap_open=w.gap_open)
+    tab = oracle.tables(ocm)
+    store = pg.Store(ctx, 32 << 20)
+    rng = np.random.default_rng(71)
+    # related triples: a parent, its workload partner, and a third variant
+    seqs = []
+    for a, b in w.pairs[:40]:
+        c = wl.with_gap(wl.mutate(rng, a[1:], 0.1, 0.02))
+        seqs.append((a, b, c if len(c) > 1 else b))
+    ids = np.array([[store.add(s) for s in t] for t in seqs], np.int32)
+    node, cost, mx, st = store.median3_batch(cm, ids[:, 0], ids[:, 1], ids[:, 2])
+    assert np.all(st == 0), st
+    for k, (p, a, b) in enumerate(seqs):
+        m, c, x = _oracle_median3(oracle, ocm, tab, p, a, b, True)
+        assert (cost[k], mx[k]) == (c, x), k
+        assert np.array_equal(store.read(int(node[k])), m), k
