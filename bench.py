@@ -378,13 +378,67 @@ def run_downpass(local: int, reps: int = 5) -> dict:
             seqs[nl + k] = out["med"][o:o + out["mlen"][j]]
         tot += int(out["cost"].sum())
     cpu_s = time.perf_counter() - c0
+    up = run_uppass(store, cm, t, leaves, res, seqs, orc, ocm, reps)
     store.close()
     return {"workload": t.name, "internal_nodes": len(t.left), "levels": res.levels,
             "ms": round(dt * 1e3, 3), "total_cost": res.total_cost,
             "gcups": round(cells / dt / 1e9, 3), "medians_per_s": round(len(t.left) / dt, 1),
             "cpu_baseline": {"ms": round(cpu_s * 1e3, 1), "kind": kind,
                              "cores": os.cpu_count() or 1, "total_cost": tot},
-            "total_cost_matches_cpu": tot == res.total_cost}
+            "total_cost_matches_cpu": tot == res.total_cost, "uppass": up}
+
+
+def run_uppass(store, cm, t, leaves, down, seqs, orc, ocm, reps: int) -> dict:
+    """Uppass of the same tree after its downpass (SeqCS.DOS.median_3_no_union
+    top down, one batch of 2 alignments per node per depth), and the host
+    implementation depth by depth on all cores beside it (the same
+    alignments, the cheaper one kept, its no-gap median)."""
+    import poy5_gb300 as pg
+    n1 = len(store)
+    for _ in range(2):
+        pg.uppass(store, cm, leaves, t.left, t.right, down.internal_node)
+        store.truncate(n1)
+    t0 = time.perf_counter()
+    for k in range(reps):
+        up = pg.uppass(store, cm, leaves, t.left, t.right, down.internal_node)
+        if k < reps - 1:
+            store.truncate(n1)
+    dt = (time.perf_counter() - t0) / reps
+    nl, ni = len(t.leaves), len(t.left)
+    parent = np.full(ni, -1)
+    for k in range(ni):
+        for ch in (t.left[k], t.right[k]):
+            if ch >= nl:
+                parent[ch - nl] = k
+    depth = np.zeros(ni, int)
+    for k in range(ni - 2, -1, -1):
+        depth[k] = depth[parent[k]] + 1
+    tab = orc.tables(ocm)
+    med_t, lcm, gap = tab["median"], tab["lcm"], tab["gap"]
+    final = [None] * ni
+    final[ni - 1] = seqs[nl + ni - 1]
+    fcost = np.zeros(ni, np.int64)
+    c0 = time.perf_counter()
+    for d in range(1, int(depth.max()) + 1):
+        ks = np.flatnonzero(depth == d)
+        pa = [final[parent[k]] for k in ks for _ in (0, 1)]
+        ch = [seqs[c] for k in ks for c in (t.left[k], t.right[k])]
+        out = orc.median_batch(ocm, pa, ch, t.affine)
+        for j, k in enumerate(ks):
+            a, b = 2 * j, 2 * j + 1
+            q = a if out["cost"][a] < out["cost"][b] else b
+            o, n = int(out["out_off"][q]), int(out["alen"][q])
+            m = med_t[(out["ea"][o:o + n].astype(np.int64) << lcm) + out["eb"][o:o + n]]
+            final[k] = np.concatenate([[gap], m[m != gap]]).astype(np.uint8)
+            fcost[k] = out["cost"][q]
+    cpu_s = time.perf_counter() - c0
+    same = np.array_equal(fcost, up.final_cost) and all(
+        np.array_equal(store.read(int(up.final_node[k])), final[k]) for k in range(ni))
+    return {"ms": round(dt * 1e3, 3), "levels": up.levels,
+            "final_cost_sum": int(up.final_cost.sum()),
+            "cpu_baseline": {"ms": round(cpu_s * 1e3, 1), "kind": "port",
+                             "cores": os.cpu_count() or 1},
+            "final_states_match_cpu": bool(same)}
 
 
 def run_long(local: int, cpu_pairs: int = 1) -> dict:
