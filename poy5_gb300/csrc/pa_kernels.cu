@@ -599,6 +599,15 @@ __device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t*
     L.V1[R - 1] = LeanCell{0, 0, 0, 0u};
     if (active) aff_lean_init(L, b, st, x, p.gl, p.P);
     const int Tlast = active ? (b.m - 1) + (b.n - 1) : 0;
+    // Pipelines that share a warp run their own pairs, and a lane's change
+    // of block (aff_lean_enter) is a divergent branch for the whole warp.
+    // Past its first rows a pipeline's lanes change blocks at steps 2 i - newk
+    // (i = first row of the block), i.e. at steps = 2 - newk (mod 2 R); each
+    // pipeline's item is delayed by `delta` steps so that these fall on
+    // multiples of 2 R for every pipeline of the warp, and the warp takes
+    // the branch once per 2 R steps instead of once per pipeline.
+    const int delta = (active && p.P < 32) ? (((b.newk - 2) % (2 * R)) + 2 * R) % (2 * R) : 0;
+    Tmax = group_max(p, active ? Tlast + delta : 0);
     auto exchange = [&](const LeanCell& sv, int T) {
         LeanCell rc;
         rc.EH = rot_prev(p, sv.EH);
@@ -618,33 +627,37 @@ __device__ void aff_fill_lean(const AffBand& b, const Tables& st, const uint8_t*
         for (int T = T0; T <= T1; T += 2) {
             {
                 const LeanCell rc = exchange(L.V0[R - 1], T);
-                if (active && T <= Tlast) {
+                const int Ti = T - delta;  // the pipeline's own step
+                if (active && Ti >= 1 && Ti <= Tlast) {
                     int dc[R];
                     aff_lean_step<R, GEN>(L, L.V0, L.V1, L.R0, L.R1, L.G0, L.G1, b, st, x, y,
-                                          p.P, T, rc, shadowEH0, dc);
-                    store_u8<R>(dm + (long long)T * (p.P * R) + p.gl * R, dc);
+                                          p.P, Ti, rc, shadowEH0, dc);
+                    store_u8<R>(dm + (long long)Ti * (p.P * R) + p.gl * R, dc);
                 }
             }
             if (T + 1 <= Tmax) {
                 const LeanCell rc = exchange(L.V1[R - 1], T + 1);
-                if (active && T + 1 <= Tlast) {
+                const int Ti = T + 1 - delta;
+                if (active && Ti >= 1 && Ti <= Tlast) {
                     int dc[R];
                     aff_lean_step<R, GEN>(L, L.V1, L.V0, L.R1, L.R0, L.G1, L.G0, b, st, x, y,
-                                          p.P, T + 1, rc, shadowEH0, dc);
-                    store_u8<R>(dm + (long long)(T + 1) * (p.P * R) + p.gl * R, dc);
+                                          p.P, Ti, rc, shadowEH0, dc);
+                    store_u8<R>(dm + (long long)Ti * (p.P * R) + p.gl * R, dc);
                 }
             }
         }
     };
-    // lane 0 generates row 0 only while in its first block (both bounds even)
-    const int tg = group_max(p, active ? lean_gen_steps(b, p.P, R) : 0);
+    // lane 0 generates row 0 only while in its first block (both bounds even;
+    // the register sets alternate with every step, so a pipeline may start on
+    // either of them: both hold the initial state)
+    const int tg = group_max(p, active ? ((lean_gen_steps(b, p.P, R) + delta + 1) & ~1) : 0);
     const int Tg = tmin((Tmax + 1) & ~1, tg);
     steps(std::true_type{}, 1, Tg - 1);
     steps(std::false_type{}, (Tg & ~1) + 1, Tmax);
     const int i = active ? b.m - 1 : 1;
     const int blk = (i - 1) / R, og = blk % p.P, oq = (i - 1) - blk * R;
     LeanCell c = L.V0[0];
-    const bool odd = (Tlast & 1) != 0;  // odd last step wrote V1
+    const bool odd = ((Tlast + delta) & 1) != 0;  // an odd last warp step wrote V1
 #pragma unroll
     for (int r = 0; r < R; r++)
         if (r == oq) c = odd ? L.V1[r] : L.V0[r];
