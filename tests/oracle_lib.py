@@ -1,7 +1,8 @@
 """ctypes bindings to the oracle libraries (test infrastructure only).
 
-``Oracle("port")`` loads ``oracle/libpoyoracle.so`` (the C restatement that
-travels to the GPU box); ``Oracle("ref")`` / ``Oracle("ref_long")`` load the
+``Oracle("port")`` loads ``oracle/libpoyoracle.so`` (the C restatement, built
+from the repository's own sources on any machine); ``Oracle("ref")`` /
+``Oracle("ref_long")`` load the
 reference POY ``algn.c`` unit compiled in ``oracle/_ref`` (present only where
 the POY sources were available). Both expose the same calls.
 """
