@@ -45,6 +45,8 @@ extern "C" {
 #define POYALGN_PAIR_TOO_LONG -6   /* sequence longer than 65535 */
 #define POYALGN_PAIR_BAD_STATE -7  /* a state outside the cost matrix's alphabet */
 #define POYALGN_PAIR_NO_CONVERGE -8 /* band doubling did not stop (e.g. all costs 0) */
+#define POYALGN_PAIR_INTERNAL -9   /* a speculative band pass was queued but did not run */
+#define POYALGN_PAIR_EMPTY_STATE -11 /* closest: a position with no state (POY asserts) */
 
 typedef struct poyalgn_ctx poyalgn_ctx;
 typedef struct poyalgn_cm poyalgn_cm;
@@ -331,6 +333,25 @@ int poyalgn_store_median3_batch(poyalgn_store *s, const poyalgn_cm *cm, int n,
                                 const int32_t *parent, const int32_t *child1,
                                 const int32_t *child2, int32_t *node,
                                 int32_t *cost, int32_t *maxcost,
+                                int32_t *status);
+
+/*
+ * Sequence.Align.closest (src/sequence.ml:1180-1237; cost matrices with
+ * combinations, no levels) for n resident pairs: node2's sequence resolved
+ * towards node1's. An all-gap node2 is returned as it is (cost 0). Equal
+ * sequences are resolved position by position with the gap bit cleared past
+ * the leading gap (cost 0); otherwise the pair is aligned (Align.align_2,
+ * node1 first), each aligned position of node2 becomes
+ * Cost_matrix.Two_D.get_closest of the two (src/cost_matrix.ml:1387-1426:
+ * the cheapest state against node1's, the first on a tie), gaps are removed
+ * (remove_gaps2) and the cost is Align.cost_2 of node1 and the result.
+ * out_node[k] is a new node (node2 itself when it was all gaps); status is
+ * per pair. Returns POYALGN_EPAIR if any pair failed, POYALGN_EUNSUPPORTED
+ * for a matrix without combinations.
+ */
+int poyalgn_store_closest_batch(poyalgn_store *s, const poyalgn_cm *cm, int n,
+                                const int32_t *node1, const int32_t *node2,
+                                int32_t *out_node, int32_t *cost,
                                 int32_t *status);
 
 /*

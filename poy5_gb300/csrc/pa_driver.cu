@@ -7,6 +7,7 @@
 #include <new>
 #include <vector>
 
+#include "pa_cost.h"
 #include "pa_runtime.h"
 
 using namespace pa;
@@ -225,6 +226,250 @@ int store_median3(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* 
     return 0;
 }
 
+// Cost_matrix.Two_D.get_closest (src/cost_matrix.ml:1387-1426) for a matrix
+// with combinations and no levels: b without the gap bit unless a or b is
+// the gap (both carrying it: the gap), then the first of its states
+// (BitSet.Int.list_of_packed_max reversed: increasing codes) of lowest cost
+// against a. 0 when b has no state (the reference fails there).
+__device__ int closest_state(const Tables& t, int a, int b)
+{
+    const int gap = t.gap;
+    const int bb = (a == gap || b == gap) ? b : ((a & gap) && (b & gap)) ? gap : (b & ~gap);
+    int best = 0, bc = 0x7fffffff;
+    for (int bit = 0; bit < t.lcm; bit++) {
+        const int x = 1 << bit;
+        if (!(bb & x)) continue;
+        const int c = tcost(t, a, x);
+        if (c < bc) {
+            best = x;
+            bc = c;
+        }
+    }
+    return best;
+}
+
+// Align.closest's resolution of pair k (src/sequence.ml:1180-1237): node2
+// all gaps -> itself (kind 0); equal sequences -> position by position with
+// the gap bit cleared past position 0 (kind 1); otherwise the aligned pair of
+// the batch (kind 2). The resolved sequence, gaps removed and the leading
+// gap prepended (remove_gaps2), is written back to front into the node's
+// region. res[3k..3k+2] = length, kind, status.
+__global__ void closest_map_kernel(const Tables* tg, int n, const uint8_t* arena,
+                                   const long long* offa, const int* lena, const long long* offb,
+                                   const int* lenb, const long long* out_off, const int* I,
+                                   const uint8_t* ea, const uint8_t* eb, uint8_t* dst,
+                                   const long long* dst_end, int* res)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const Tables& t = *tg;
+    const int gap = t.gap;
+    const uint8_t* s1 = arena + offa[k];
+    const uint8_t* s2 = arena + offb[k];
+    const int l1 = lena[k], l2 = lenb[k];
+    bool empty = true;
+    for (int i = 0; i < l2 && empty; i++) empty = s2[i] == gap;
+    if (empty) {
+        res[3 * k] = l2;
+        res[3 * k + 1] = 0;
+        res[3 * k + 2] = 0;
+        return;
+    }
+    bool equal = l1 == l2;
+    for (int i = 0; i < l1 && equal; i++) equal = s1[i] == s2[i];
+    const uint8_t *x = s1, *y = s2;
+    int len = l1;
+    if (!equal) {
+        const int st = I[5 * n + k];
+        if (st != 0) {
+            res[3 * k + 2] = st;
+            return;
+        }
+        len = I[2 * n + k];
+        const long long start = out_off[k] + l1 + l2 + 2 - len;
+        x = ea + start;
+        y = eb + start;
+    }
+    uint8_t* o = dst + dst_end[k];
+    int w = 0;
+    for (int i = len - 1; i >= 0; i--) {
+        int a = x[i], b = y[i];
+        if (equal && i > 0) {
+            a &= ~gap;
+            b &= ~gap;
+        }
+        const int c = (a > 0 && b > 0) ? closest_state(t, a, b) : 0;
+        if (c == 0) {
+            res[3 * k + 2] = POYALGN_PAIR_EMPTY_STATE;
+            return;
+        }
+        if (c != gap) o[-(++w)] = (uint8_t)c;
+    }
+    o[-(++w)] = (uint8_t)gap;
+    res[3 * k] = w;
+    res[3 * k + 1] = equal ? 1 : 2;
+    res[3 * k + 2] = 0;
+}
+
+// Metadata of n resident pairs for a batch: offa | offb | out_off (int64) |
+// lena | lenb (int32); returns the output bytes (cap la + lb + 2 per pair).
+long long pair_meta(const poyalgn_store* s, int n, const int32_t* na, const int32_t* nb,
+                    std::vector<uint8_t>& hmeta, int* maxmn)
+{
+    const size_t ni = (size_t)n;
+    hmeta.resize(ni * 32);
+    long long* offa = reinterpret_cast<long long*>(hmeta.data());
+    long long* offb = offa + ni;
+    long long* oo = offb + ni;
+    int* lena = reinterpret_cast<int*>(oo + ni);
+    int* lenb = lena + ni;
+    long long total = 0;
+    *maxmn = 2;
+    for (int k = 0; k < n; k++) {
+        offa[k] = s->off[na[k]];
+        offb[k] = s->off[nb[k]];
+        lena[k] = s->len[na[k]];
+        lenb[k] = s->len[nb[k]];
+        oo[k] = total;
+        total += align_up((long long)lena[k] + lenb[k] + 2);
+        *maxmn = std::max(*maxmn, lena[k] + lenb[k]);
+    }
+    return total;
+}
+
+// Align.cost_2 of n resident pairs (a first): the linear band doubling's
+// cost (Align.cost_2 without deltaw) or algn_CAML_cost_affine_3.
+int store_cost2(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* na,
+                const int32_t* nb, int32_t* cost, int32_t* status)
+{
+    poyalgn_ctx* c = s->ctx;
+    int rc, maxmn;
+    const size_t ni = (size_t)n;
+    const long long total = pair_meta(s, n, na, nb, s->hmeta, &maxmn);
+    if ((rc = reserve(s->meta, ni * 32))) return rc;
+    if ((rc = reserve(s->ints, ni * 4 * 7))) return rc;
+    if ((rc = reserve(s->bytes, (size_t)total * 4))) return rc;
+    cudaStream_t st = c->stream;
+    CU(cudaMemcpyAsync(s->meta.p, s->hmeta.data(), ni * 32, cudaMemcpyHostToDevice, st));
+    const long long* d_offa = as<long long>(s->meta);
+    const int* d_lena = reinterpret_cast<const int*>(d_offa + 3 * ni);
+    int* I = as<int>(s->ints);
+    uint8_t* B = as<uint8_t>(s->bytes);
+    uint8_t* arena = as<uint8_t>(s->arena);
+    if (cm->h.cost_model == 1)
+        rc = run_nobt(c, cm, n, maxmn, arena, d_offa, d_lena, d_offa + ni, d_lena + ni,
+                      NOBT_NO_MISSING, I, I + 5 * ni, st);
+    else
+        rc = run_batch(c, cm, 0, n, maxmn, total, arena, d_offa, d_lena, d_offa + ni,
+                       d_lena + ni, d_offa + 2 * ni, I, I + ni, I + 2 * ni, I + 3 * ni,
+                       I + 4 * ni, I + 5 * ni, B, B + total, B + 2 * total, B + 3 * total,
+                       I + 6 * ni, nullptr, nullptr, 0, st);
+    if (rc) return rc;
+    s->hints.resize(ni * 6);
+    CU(cudaMemcpyAsync(s->hints.data(), I, ni * 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    for (int k = 0; k < n; k++) {
+        cost[k] = s->hints[k];
+        status[k] = s->hints[5 * ni + k];
+    }
+    return 0;
+}
+
+int store_closest(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* node1,
+                  const int32_t* node2, int32_t* out_node, int32_t* cost, int32_t* status)
+{
+    poyalgn_ctx* c = s->ctx;
+    int rc, maxmn;
+    if ((rc = ensure_device(c))) return rc;
+    if (!cm->t.comb) return set_err(POYALGN_EUNSUPPORTED, "closest needs a matrix with combinations");
+    const size_t ni = (size_t)n;
+    for (int k = 0; k < n; k++)
+        if (!valid_node(s, node1[k]) || !valid_node(s, node2[k]))
+            return set_err(POYALGN_EINVAL, "pair %d: unknown node (%d, %d)", k, node1[k], node2[k]);
+    const long long total = pair_meta(s, n, node1, node2, s->hmeta, &maxmn);
+    // node regions: at most one entry per aligned column plus the gap
+    s->hmeta.resize(ni * 40);
+    long long* dend = reinterpret_cast<long long*>(s->hmeta.data() + ni * 32);
+    const int* lena = reinterpret_cast<const int*>(s->hmeta.data() + ni * 24);
+    const int* lenb = lena + ni;
+    long long ntotal = 0;
+    for (int k = 0; k < n; k++) {
+        ntotal += align_up((long long)lena[k] + lenb[k] + 2);
+        dend[k] = ntotal;
+    }
+    const long long base = align_up(s->used);
+    if (base + ntotal > s->cap)
+        return set_err(POYALGN_ENOMEM, "store full: %lld of %lld bytes used, batch needs %lld",
+                       s->used, s->cap, ntotal);
+    if ((rc = reserve(s->meta, ni * 40))) return rc;
+    if ((rc = reserve(s->ints, ni * 4 * 10))) return rc;
+    if ((rc = reserve(s->bytes, (size_t)total * 4))) return rc;
+    cudaStream_t st = c->stream;
+    CU(cudaMemcpyAsync(s->meta.p, s->hmeta.data(), ni * 40, cudaMemcpyHostToDevice, st));
+    const long long* d_offa = as<long long>(s->meta);
+    const int* d_lena = reinterpret_cast<const int*>(d_offa + 3 * ni);
+    const long long* d_dend = d_offa + 4 * ni;
+    int* I = as<int>(s->ints);
+    int* res = I + 7 * ni;
+    uint8_t* B = as<uint8_t>(s->bytes);
+    uint8_t* arena = as<uint8_t>(s->arena);
+    if ((rc = run_batch(c, cm, cm->h.cost_model == 1, n, maxmn, total, arena, d_offa, d_lena,
+                        d_offa + ni, d_lena + ni, d_offa + 2 * ni, I, I + ni, I + 2 * ni,
+                        I + 3 * ni, I + 4 * ni, I + 5 * ni, B, B + total, B + 2 * total,
+                        B + 3 * total, I + 6 * ni, nullptr, nullptr, 1, st)))
+        return rc;
+    closest_map_kernel<<<(n + 127) / 128, 128, 0, st>>>(cm->d, n, arena, d_offa, d_lena,
+                                                        d_offa + ni, d_lena + ni, d_offa + 2 * ni,
+                                                        I, B, B + total, arena + base, d_dend,
+                                                        res);
+    CU(cudaGetLastError());
+    std::vector<int> h(ni * 3);
+    CU(cudaMemcpyAsync(h.data(), res, ni * 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    std::vector<int32_t> ca, cb, cc(ni, 0), cs(ni, 0);
+    std::vector<int> which;
+    const long long dend_last = ntotal;
+    int failed = -1;
+    for (int k = 0; k < n; k++) {
+        const int st_k = h[3 * k + 2], kind = h[3 * k + 1];
+        status[k] = st_k;
+        cost[k] = 0;
+        out_node[k] = -1;
+        if (st_k != 0) {
+            if (failed < 0) failed = k;
+            continue;
+        }
+        if (kind == 0) {
+            out_node[k] = node2[k];
+            continue;
+        }
+        out_node[k] = (int)s->len.size();
+        s->off.push_back(base + dend[k] - h[3 * k]);
+        s->len.push_back(h[3 * k]);
+        if (kind == 2) {  // Align.cost_2 of node1 and the resolved sequence
+            which.push_back(k);
+            ca.push_back(node1[k]);
+            cb.push_back(out_node[k]);
+        }
+    }
+    s->used = base + dend_last;
+    if (!which.empty()) {
+        if ((rc = store_cost2(s, cm, (int)which.size(), ca.data(), cb.data(), cc.data(),
+                              cs.data())))
+            return rc;
+        for (size_t q = 0; q < which.size(); q++) {
+            cost[which[q]] = cc[q];
+            if (cs[q] != 0) {
+                status[which[q]] = cs[q];
+                if (failed < 0 || which[q] < failed) failed = which[q];
+            }
+        }
+    }
+    if (failed >= 0)
+        return set_err(POYALGN_EPAIR, "pair %d failed with status %d", failed, status[failed]);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -384,6 +629,16 @@ int poyalgn_store_median3_batch(poyalgn_store* s, const poyalgn_cm* cm, int n,
         return set_err(POYALGN_EINVAL, "null argument");
     if (n == 0) return 0;
     return store_median3(s, cm, n, parent, child1, child2, node, cost, maxcost, status);
+}
+
+int poyalgn_store_closest_batch(poyalgn_store* s, const poyalgn_cm* cm, int n,
+                                const int32_t* node1, const int32_t* node2, int32_t* out_node,
+                                int32_t* cost, int32_t* status)
+{
+    if (!s || !cm || n < 0 || (n > 0 && (!node1 || !node2 || !out_node || !cost || !status)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (n == 0) return 0;
+    return store_closest(s, cm, n, node1, node2, out_node, cost, status);
 }
 
 int poyalgn_uppass(poyalgn_store* s, const poyalgn_cm* cm, int nleaves,

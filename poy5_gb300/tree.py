@@ -77,6 +77,20 @@ class Store:
             check(rc)
         return node, cost, mx, st
 
+    def closest_batch(self, cm: CostMatrix, node1, node2):
+        """Sequence.Align.closest of resident pairs: node2 resolved towards
+        node1; returns (new nodes, costs, status)."""
+        a = np.ascontiguousarray(node1, np.int32)
+        b = np.ascontiguousarray(node2, np.int32)
+        n = len(a)
+        node = np.full(n, -1, np.int32)
+        cost, st = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        rc = _lib.load().poyalgn_store_closest_batch(self._h, cm.handle, n, _ptr(a), _ptr(b),
+                                                     _ptr(node), _ptr(cost), _ptr(st))
+        if rc not in (0, _lib.EPAIR):
+            check(rc)
+        return node, cost, st
+
     def close(self):
         if self._h:
             _lib.load().poyalgn_store_free(self._h)

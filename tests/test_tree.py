@@ -168,3 +168,68 @@ def test_median3_batch_affine_matches_oracle(ctx, oracle):
         m, c, x = _oracle_median3(oracle, ocm, tab, p, a, b, True)
         assert (cost[k], mx[k]) == (c, x), k
         assert np.array_equal(store.read(int(node[k])), m), k
+
+
+# ---- Align.closest --------------------------------------------------------------
+
+def _closest_state(tab, a, b):
+    """Cost_matrix.Two_D.get_closest (src/cost_matrix.ml:1387-1426), with
+    combinations and no levels."""
+    gap, lcm = tab["gap"], tab["lcm"]
+    bb = b if (a == gap or b == gap) else (gap if (a & gap and b & gap) else b & ~gap)
+    best, bc = 0, None
+    for bit in range(lcm):
+        x = 1 << bit
+        if bb & x:
+            c = int(tab["cost"][(a << lcm) + x])
+            if bc is None or c < bc:
+                best, bc = x, c
+    return best
+
+
+def _oracle_closest(oracle, ocm, tab, s1, s2, affine):
+    """Sequence.Align.closest (src/sequence.ml:1180-1237) over the oracle."""
+    gap = tab["gap"]
+    if np.all(s2 == gap):
+        return s2, 0
+    if len(s1) == len(s2) and np.array_equal(s1, s2):
+        a, b = s1.astype(int), s2.astype(int)
+        a[1:] &= ~gap
+        b[1:] &= ~gap
+        comp = True
+    else:
+        r = oracle.median(ocm, s1, s2, affine)
+        a, b, comp = r.ea.astype(int), r.eb.astype(int), False
+    out = [_closest_state(tab, int(x), int(y)) for x, y in zip(a, b)]
+    res = np.array([gap] + [v for v in out if v != gap], np.uint8)
+    if comp:
+        return res, 0
+    return res, (oracle.cost_affine(ocm, s1, res) if affine else oracle.cost_linear(ocm, s1, res))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("affine", [False, True])
+def test_closest_batch_matches_oracle(ctx, oracle, affine):
+    import poy5_gb300 as pg
+    from cases import AFF_TCM, STD_TCM, random_pairs, rseq
+    tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
+    cm = pg.CostMatrix.of_list(ctx, tcm, go)
+    ocm = oracle.cm(tcm=tcm, gap_open=go)
+    tab = oracle.tables(ocm)
+    rng = np.random.default_rng(81 + affine)
+    # ambiguous and gap-bearing states, an all-gap second sequence, equal pairs
+    pairs = [(a, b) for a, b in random_pairs(rng, 60, maxlen=500, kinds=3)]
+    s = rseq(rng, 50, amb=0.2)
+    pairs += [(s, s.copy()), (rseq(rng, 30), np.full(4, wl.GAP, np.uint8))]
+    store = pg.Store(ctx, 16 << 20)
+    n1 = [store.add(a) for a, _ in pairs]
+    n2 = [store.add(b) for _, b in pairs]
+    node, cost, st = store.closest_batch(cm, n1, n2)
+    for k, (a, b) in enumerate(pairs):
+        try:
+            want, c = _oracle_closest(oracle, ocm, tab, a, b, affine)
+        except Exception:
+            continue  # the reference fails (empty state); the status says so
+        assert st[k] == 0, (k, st[k])
+        assert cost[k] == c, k
+        assert np.array_equal(store.read(int(node[k])), want), k
