@@ -355,6 +355,22 @@ int poyalgn_store_closest_batch(poyalgn_store *s, const poyalgn_cm *cm, int n,
                                 int32_t *status);
 
 /*
+ * Sequence.readjust (src/sequence.ml:2097-2158, without Ukkonen) for n
+ * resident triples (child a, child b, parent): the three pairwise medians
+ * (DOS.median's cost and median: Align.align_2 + median_2 for the linear
+ * model, align_affine_3's median for the affine one), the three medians
+ * of a median with the third sequence, the centre of the cheapest
+ * two-step route resolved with Align.closest (the reference's choice and
+ * tie order), and the costs of the centre against the two children (cost2)
+ * and the parent (cost3 = cost2 + that cost). Writes the centre's node and
+ * both costs; status is per triple. Four rounds of batches.
+ */
+int poyalgn_store_readjust_batch(poyalgn_store *s, const poyalgn_cm *cm, int n,
+                                 const int32_t *child_a, const int32_t *child_b,
+                                 const int32_t *parent, int32_t *node,
+                                 int32_t *cost3, int32_t *cost2, int32_t *status);
+
+/*
  * Uppass of the tree of poyalgn_downpass (same encoding): final states top
  * down, one batch per depth. The root keeps its downpass state
  * (root_final = internal_node[ninternal - 1]); every other internal node k

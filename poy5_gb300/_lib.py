@@ -62,6 +62,7 @@ _SIGS = {
     "poyalgn_store_median3_batch": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _P, _P]),
     "poyalgn_uppass": (_I, [_P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P]),
     "poyalgn_store_closest_batch": (_I, [_P, _P, _I, _P, _P, _P, _P, _P]),
+    "poyalgn_store_readjust_batch": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _P, _P]),
     "poyalgn_server_create": (_I, [_P, _P, _I, _I, _I, _I, _I, _I64, C.POINTER(_P)]),
     "poyalgn_server_free": (None, [_P]),
     "poyalgn_server_submit": (_I, [_P, _I, _P, _P, _P]),

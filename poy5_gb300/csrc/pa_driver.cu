@@ -470,6 +470,96 @@ int store_closest(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* 
     return 0;
 }
 
+// Sequence.readjust (src/sequence.ml:2097-2158) for n triples, in rounds of
+// batches: algn = DOS.median's (cost, median) for both cost models.
+int store_readjust(poyalgn_store* s, const poyalgn_cm* cm, int n, const int32_t* ca,
+                   const int32_t* cb, const int32_t* cp, int32_t* node, int32_t* cost3,
+                   int32_t* cost2, int32_t* status)
+{
+    const size_t ni = (size_t)n;
+    for (size_t k = 0; k < ni; k++) {
+        status[k] = 0;
+        node[k] = -1;
+        cost3[k] = cost2[k] = 0;
+    }
+    std::vector<int32_t> na(3 * ni), nb(3 * ni), med(3 * ni), cst(3 * ni), st(3 * ni);
+    std::vector<char> bad(ni, 0);
+    auto round = [&](int keep) -> int {  // 3 n alignments, per-triple failures recorded
+        const int rc = store_batch(s, cm, (int)(3 * ni), na.data(), nb.data(), keep, med.data(),
+                                   cst.data(), nullptr, st.data());
+        if (rc && rc != POYALGN_EPAIR) return rc;
+        for (size_t q = 0; q < 3 * ni; q++)
+            if (st[q] != 0 && !bad[q / 3]) {
+                bad[q / 3] = 1;
+                status[q / 3] = st[q];
+            }
+        return 0;
+    };
+    int rc;
+    // make_center a b c (c = parent): ab, bc, ac
+    for (size_t k = 0; k < ni; k++) {
+        na[3 * k] = ca[k], nb[3 * k] = cb[k];
+        na[3 * k + 1] = cb[k], nb[3 * k + 1] = cp[k];
+        na[3 * k + 2] = ca[k], nb[3 * k + 2] = cp[k];
+    }
+    if ((rc = round(1))) return rc;
+    std::vector<int32_t> m1 = med, c1 = cst;
+    // abc = algn ab c, bca = algn bc a, acb = algn ac b
+    for (size_t k = 0; k < ni; k++) {
+        const bool ok = !bad[k];
+        na[3 * k] = ok ? m1[3 * k] : ca[k], nb[3 * k] = cp[k];
+        na[3 * k + 1] = ok ? m1[3 * k + 1] : ca[k], nb[3 * k + 1] = ca[k];
+        na[3 * k + 2] = ok ? m1[3 * k + 2] : ca[k], nb[3 * k + 2] = cb[k];
+    }
+    if ((rc = round(0))) return rc;
+    // the cheapest route's centre, resolved with Align.closest
+    std::vector<int32_t> x1(ni), x2(ni), cn(ni), cc(ni), cs(ni);
+    for (size_t k = 0; k < ni; k++) {
+        const long long cabc = (long long)cst[3 * k] + c1[3 * k];
+        const long long cbca = (long long)cst[3 * k + 1] + c1[3 * k + 1];
+        const long long cacb = (long long)cst[3 * k + 2] + c1[3 * k + 2];
+        int32_t p, q;  // closest p q: q resolved towards p
+        if (cabc <= cbca) {
+            if (cabc <= cacb) p = cp[k], q = m1[3 * k];  // closest c ab
+            else p = cb[k], q = m1[3 * k + 2];           // closest b ac
+        } else if (cbca < cacb) {
+            p = ca[k], q = m1[3 * k + 1];  // closest a bc
+        } else {
+            p = cb[k], q = m1[3 * k + 2];  // closest b ac
+        }
+        x1[k] = bad[k] ? ca[k] : p;
+        x2[k] = bad[k] ? cb[k] : q;
+    }
+    rc = store_closest(s, cm, n, x1.data(), x2.data(), cn.data(), cc.data(), cs.data());
+    if (rc && rc != POYALGN_EPAIR) return rc;
+    for (size_t k = 0; k < ni; k++)
+        if (cs[k] != 0 && !bad[k]) {
+            bad[k] = 1;
+            status[k] = cs[k];
+        }
+    // the centre against both children and the parent
+    for (size_t k = 0; k < ni; k++) {
+        const int32_t m = bad[k] ? ca[k] : cn[k];
+        na[3 * k] = ca[k], nb[3 * k] = m;
+        na[3 * k + 1] = cb[k], nb[3 * k + 1] = m;
+        na[3 * k + 2] = cp[k], nb[3 * k + 2] = m;
+    }
+    if ((rc = round(0))) return rc;
+    int failed = -1;
+    for (size_t k = 0; k < ni; k++) {
+        if (bad[k]) {
+            if (failed < 0) failed = (int)k;
+            continue;
+        }
+        node[k] = cn[k];
+        cost2[k] = cst[3 * k] + cst[3 * k + 1];
+        cost3[k] = cost2[k] + cst[3 * k + 2];
+    }
+    if (failed >= 0)
+        return set_err(POYALGN_EPAIR, "triple %d failed with status %d", failed, status[failed]);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -639,6 +729,21 @@ int poyalgn_store_closest_batch(poyalgn_store* s, const poyalgn_cm* cm, int n,
         return set_err(POYALGN_EINVAL, "null argument");
     if (n == 0) return 0;
     return store_closest(s, cm, n, node1, node2, out_node, cost, status);
+}
+
+int poyalgn_store_readjust_batch(poyalgn_store* s, const poyalgn_cm* cm, int n,
+                                 const int32_t* child_a, const int32_t* child_b,
+                                 const int32_t* parent, int32_t* node, int32_t* cost3,
+                                 int32_t* cost2, int32_t* status)
+{
+    if (!s || !cm || n < 0 ||
+        (n > 0 && (!child_a || !child_b || !parent || !node || !cost3 || !cost2 || !status)))
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (n == 0) return 0;
+    for (int k = 0; k < n; k++)
+        if (!valid_node(s, child_a[k]) || !valid_node(s, child_b[k]) || !valid_node(s, parent[k]))
+            return set_err(POYALGN_EINVAL, "triple %d: unknown node", k);
+    return store_readjust(s, cm, n, child_a, child_b, parent, node, cost3, cost2, status);
 }
 
 int poyalgn_uppass(poyalgn_store* s, const poyalgn_cm* cm, int nleaves,

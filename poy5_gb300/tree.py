@@ -91,6 +91,22 @@ class Store:
             check(rc)
         return node, cost, st
 
+    def readjust_batch(self, cm: CostMatrix, child_a, child_b, parent):
+        """Sequence.readjust of resident triples; returns (centre nodes,
+        cost3, cost2, status). The intermediate medians stay in the store."""
+        a = np.ascontiguousarray(child_a, np.int32)
+        b = np.ascontiguousarray(child_b, np.int32)
+        p = np.ascontiguousarray(parent, np.int32)
+        n = len(a)
+        node = np.full(n, -1, np.int32)
+        c3, c2, st = (np.zeros(n, np.int32) for _ in range(3))
+        rc = _lib.load().poyalgn_store_readjust_batch(self._h, cm.handle, n, _ptr(a), _ptr(b),
+                                                      _ptr(p), _ptr(node), _ptr(c3), _ptr(c2),
+                                                      _ptr(st))
+        if rc not in (0, _lib.EPAIR):
+            check(rc)
+        return node, c3, c2, st
+
     def close(self):
         if self._h:
             _lib.load().poyalgn_store_free(self._h)

@@ -233,3 +233,52 @@ def test_closest_batch_matches_oracle(ctx, oracle, affine):
         assert st[k] == 0, (k, st[k])
         assert cost[k] == c, k
         assert np.array_equal(store.read(int(node[k])), want), k
+
+
+# ---- Sequence.readjust ----------------------------------------------------------
+
+def _oracle_readjust(oracle, ocm, tab, a, b, c, affine):
+    """Sequence.readjust (src/sequence.ml:2097-2158) over the oracle: algn is
+    DOS.median's (cost, median)."""
+    def algn(x, y):
+        r = oracle.median(ocm, x, y, affine)
+        return r.cost, r.median
+    cab, ab = algn(a, b)
+    cbc, bc = algn(b, c)
+    cac, ac = algn(a, c)
+    cabc = algn(ab, c)[0] + cab
+    cbca = algn(bc, a)[0] + cbc
+    cacb = algn(ac, b)[0] + cac
+    if cabc <= cbca:
+        p, q = (c, ab) if cabc <= cacb else (b, ac)
+    elif cbca < cacb:
+        p, q = a, bc
+    else:
+        p, q = b, ac
+    m, _ = _oracle_closest(oracle, ocm, tab, p, q, affine)
+    cost2 = algn(a, m)[0] + algn(b, m)[0]
+    return m, cost2 + algn(c, m)[0], cost2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("affine", [False, True])
+def test_readjust_batch_matches_oracle(ctx, oracle, affine):
+    import poy5_gb300 as pg
+    from cases import AFF_TCM, STD_TCM
+    tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
+    cm = pg.CostMatrix.of_list(ctx, tcm, go)
+    ocm = oracle.cm(tcm=tcm, gap_open=go)
+    tab = oracle.tables(ocm)
+    rng = np.random.default_rng(91 + affine)
+    trip = []
+    for _ in range(24):  # a node's two children and its parent, related
+        root = wl.random_bases(rng, int(rng.integers(40, 400)))
+        trip.append(tuple(wl.with_gap(wl.mutate(rng, root, 0.1, 0.03)) for _ in range(3)))
+    store = pg.Store(ctx, 16 << 20)
+    ids = np.array([[store.add(s) for s in t] for t in trip], np.int32)
+    node, c3, c2, st = store.readjust_batch(cm, ids[:, 0], ids[:, 1], ids[:, 2])
+    assert np.all(st == 0), st
+    for k, (a, b, c) in enumerate(trip):
+        m, w3, w2 = _oracle_readjust(oracle, ocm, tab, a, b, c, affine)
+        assert (c3[k], c2[k]) == (w3, w2), k
+        assert np.array_equal(store.read(int(node[k])), m), k
