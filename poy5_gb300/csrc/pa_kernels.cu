@@ -1189,11 +1189,20 @@ __global__ void prep_kernel(BatchArgs A)
         // one that covers the plane), each as its own item
         const int S = (!A.affine && pl.full) ? 1 : A.spec_S;
         int T = pl.T0, nq = 0;
+        bool wide = false;
         for (;;) {
             const int cj = class_of(T);
             if (cj < 0) {
                 nq |= SPEC_NOCLASS;
                 break;
+            }
+            // bands that need a multi-warp pipeline (a barrier per step) are
+            // slow per step: at most the first of them is speculated, so that
+            // the widest, slowest passes do not sit on every pair's
+            // critical path; later ones go to the sequential sweep
+            if (A.lad.P[cj] > 32) {
+                if (wide && nq > 0) break;
+                wide = true;
             }
             push_item(A, 2 * cj + (lean ? 1 : 0), k, T);
             nq++;
