@@ -4,7 +4,8 @@
   (``poy_oracle.c`` + ``poy_tables.c``). Built on every machine; it is the
   checker the GPU tests, ``smoke()`` and the CPU baseline use.
 * ``oracle/_ref/libpoyref.so`` (+ ``libpoyref_long.so`` with
-  ``USE_LONG_SEQUENCES``) — the reference POY ``src/algn.c`` unit compiled
+  ``USE_LONG_SEQUENCES``) — the reference POY ``src/algn.c`` unit and
+  ``src/newkkonen.c`` (+ its queue) compiled
   unmodified from the POY source tree, plus ``ref_harness.c`` and the caml
   header shim. Built only where the POY sources are present; it validates the
   restatement and generates the golden fixtures.
@@ -49,7 +50,11 @@ def build_ref(ref_src: str = DEFAULT_REF_SRC, force: bool = False):
         return []
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
-    srcs = [os.path.join(ref_src, f) for f in ("algn.c", "avl.c", "zarr.c")]
+    # newkkonen.c (Algn_Newkk) and its queue; algn.c and newkkonen.c both
+    # define the tentative global `backtrace_mode`, hence -fcommon.
+    srcs = [os.path.join(ref_src, f) for f in ("algn.c", "avl.c", "zarr.c",
+                                               "newkkonen.c",
+                                               "queue_with_linkedlist.c")]
     mine = [os.path.join(HERE, f) for f in ("ref_harness.c", "poy_tables.c")]
     built = []
     for name, extra in (("libpoyref.so", []),
@@ -57,7 +62,7 @@ def build_ref(ref_src: str = DEFAULT_REF_SRC, force: bool = False):
         out = os.path.join(outdir, name)
         if force or _stale(out, mine + [os.path.join(HERE, "shim", "caml",
                                                       "poy_caml_shim.h")]):
-            _run(["gcc", "-O2", "-fgnu89-inline", "-fPIC", "-shared", "-w",
+            _run(["gcc", "-O2", "-fgnu89-inline", "-fcommon", "-fPIC", "-shared", "-w",
                   *extra, "-I", os.path.join(HERE, "shim"), "-I", ref_src,
                   "-I", HERE, "-o", out, *srcs, *mine])
         built.append(out)

@@ -1118,3 +1118,377 @@ int orc_schedule(void *cm, int affine, const uint8_t *a, int la,
     orc_ws_free(ws);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Algn_Newkk: POY's own Ukkonen-style banded aligner (src/newkkonen.c),    */
+/* affine cost model (newkkonen_CAML_algn_affine / _backtrace_affine).      */
+/*                                                                          */
+/* The reference grows the band in place and re-evaluates only cells whose  */
+/* neighbours changed (update_a_row, src/newkkonen.c:964-1074); every cell  */
+/* is a function of its three neighbours and the band borders alone, so the */
+/* band of each iteration is filled afresh here. tests/test_newkk.py checks */
+/* costs and alignments against the reference compiled unmodified.          */
+
+#define NK_INF (INT_MAX / 2)
+/* direction flags, src/newkkonen.c:44-61 */
+enum {
+    NK_START = 0, NK_ALIGN = 1, NK_DEL = 16, NK_INS = 32, NK_END_INS = 64,
+    NK_END_DEL = 128, NK_END_DIAG = 256, NK_DIAG = 512, NK_INS_EQ_DEL = 1024
+};
+#define NK_GAP 16  /* GAPCODE, src/newkkonen.c:37 */
+#define NK_NOGAP 15 /* NOGAP, src/newkkonen.c:41 */
+#define NK_MUCH_LONGER 100 /* src/newkkonen.c:34 */
+
+typedef struct nkcell {
+    int cost, P, Q, ED, CD;
+    uint16_t dir, g1, g2;
+} nkcell;
+
+/* my_add, src/newkkonen.c:65-71 */
+static inline int nk_add(int a, int b)
+{
+    if (a >= NK_INF) return NK_INF;
+    if (b >= NK_INF) return NK_INF;
+    return a + b;
+}
+/* get_go, src/newkkonen.c:179-184 */
+static inline int nk_go(int base, int prev, int idx, int go)
+{
+    if (idx == 1 && (base & NK_GAP)) return 0;
+    if (idx > 1 && !(prev & NK_GAP) && (base & NK_GAP)) return 0;
+    return go;
+}
+/* get_extgo, src/newkkonen.c:194-198 */
+static inline int nk_extgo(int base, int prev, int go)
+{
+    return ((prev & NK_GAP) && !(base & NK_GAP)) ? go : 0;
+}
+#define NK_MIN(a, b) ((a) < (b) ? (a) : (b))
+#define NK_MAX(a, b) ((a) > (b) ? (a) : (b))
+
+/* One band cell: update_internal_cell + assign_best_cost_and_direction
+ * (src/newkkonen.c:600-873). lb / rb: the cell lies on the band's left
+ * (i - j == k) / right (j - i == lenY - lenX + k) border. L, U, D: the
+ * cells (i, j-1), (i-1, j), (i-1, j-1), read only where the reference
+ * reads them. */
+static void nk_cell(const ocm *c, const uint8_t *s1, const uint8_t *s2, int i,
+                    int j, int lb, int rb, const nkcell *L, const nkcell *U,
+                    const nkcell *D, int go, nkcell *out)
+{
+    const int gap = c->t.gap;
+    const int b1 = s1[i], b2 = s2[j];
+    /* seq_get(s, -1) is never needed: at i == 0 (j == 0) every candidate
+     * that uses the previous base is out of the matrix */
+    const int pb1 = i > 0 ? s1[i - 1] : 0, pb2 = j > 0 ? s2[j - 1] : 0;
+    const int go1 = nk_go(b1, pb1, i, go), go2 = nk_go(b2, pb2, j, go);
+    const int eg1 = nk_extgo(b1, pb1, go), eg2 = nk_extgo(b2, pb2, go);
+    int thisP = NK_INF, thisQ = NK_INF, thisED = NK_INF, thisCD = NK_INF;
+    int costL, extL, openL, gL1 = 0, gL2 = 0;
+    if (lb || j == 0) {
+        costL = extL = openL = NK_INF;
+    } else {
+        int add = C(c, b2, gap);
+        extL = nk_add(L->Q, add + eg2);
+        openL = nk_add(L->CD, add + go2);
+        costL = thisQ = NK_MIN(openL, extL);
+        gL1 = L->g1;
+        gL2 = L->g2;
+    }
+    int costR, extR, openR, gR1 = 0, gR2 = 0;
+    if (rb || i == 0) {
+        costR = extR = openR = NK_INF;
+    } else {
+        int add = C(c, b1, gap);
+        extR = nk_add(U->P, add + eg1);
+        openR = nk_add(U->CD, add + go1);
+        costR = thisP = NK_MIN(openR, extR);
+        gR1 = U->g1;
+        gR2 = U->g2;
+    }
+    int costM, costDiag, extD, openD, gM1 = 0, gM2 = 0;
+    if (i == 0 || j == 0) {
+        costM = costDiag = extD = openD = NK_INF;
+    } else {
+        const int n1 = b1 & NK_NOGAP, n2 = b2 & NK_NOGAP;
+        const int add = C(c, n1, n2);
+        thisCD = nk_add(D->CD, add);
+        int fromR = D->P + C(c, n1, b2) + (n1 == b1 ? 0 : go);
+        int fromL = D->Q + C(c, b1, n2) + (n2 == b2 ? 0 : go);
+        thisCD = NK_MIN(thisCD, fromR);
+        thisCD = NK_MIN(thisCD, fromL);
+        thisCD = NK_MIN(thisCD, nk_add(D->ED, go1 + go2 + add));
+        int diag = ((b1 & NK_GAP) && (b2 & NK_GAP)) ? 0 : NK_INF;
+        openD = nk_add(D->CD, go1 + go2);
+        extD = nk_add(D->ED, diag);
+        thisED = NK_MIN(extD, openD);
+        costM = thisCD;
+        costDiag = thisED;
+        gM1 = D->g1;
+        gM2 = D->g2;
+    }
+    int dir = NK_INS, best = costL, g1 = gL1 + 1, g2 = gL2;
+    if (costR <= best) {
+        if (costR < best) { best = costR; dir = NK_DEL; g1 = gR1; g2 = gR2 + 1; }
+        else { dir |= NK_DEL; g1 = NK_MAX(g1, gR1); g2 = NK_MAX(g2, gR2 + 1); }
+    }
+    if (costM <= best) {
+        if (costM < best) { best = thisCD; dir = NK_ALIGN; g1 = gM1; g2 = gM2; }
+        else { dir |= NK_ALIGN; g1 = NK_MAX(g1, gM1); g2 = NK_MAX(g2, gM2); }
+    }
+    if (costDiag <= best) {
+        if (costDiag < best) { best = costDiag; dir = NK_DIAG; g1 = gM1; g2 = gM2; }
+        else { dir |= NK_DIAG; g1 = NK_MAX(g1, gM1); g2 = NK_MAX(g2, gM2); }
+    }
+    if (extR >= openR) dir |= NK_END_DEL;
+    if (extL >= openL) dir |= NK_END_INS;
+    if (extD >= openD) dir |= NK_END_DIAG;
+    if (extR == extL && extR == best) dir |= NK_INS_EQ_DEL;
+    out->cost = best;
+    out->dir = (uint16_t)dir;
+    out->g1 = (uint16_t)g1;
+    out->g2 = (uint16_t)g2;
+    out->P = thisP;
+    out->Q = thisQ;
+    out->ED = thisED;
+    out->CD = thisCD;
+}
+
+typedef struct nkband {
+    nkcell *cell;
+    size_t cap;
+    int lenX, lenY, k, W; /* row i holds columns i-k .. i+lenY-lenX+k */
+} nkband;
+
+static inline nkcell *nk_at(nkband *b, int i, int j)
+{
+    return b->cell + (size_t)i * b->W + (j - (i - b->k));
+}
+
+/* Row 0 of the matrix, columns 0 .. lenY-lenX (newkk_algn's first row,
+ * src/newkkonen.c:1380-1428). */
+static void nk_first_row(const ocm *c, nkband *b, const uint8_t *s2, int go)
+{
+    const int gap = c->t.gap, bb = b->lenY - b->lenX + 1;
+    nkcell *z = nk_at(b, 0, 0);
+    z->cost = 0;
+    z->dir = NK_START;
+    z->g1 = z->g2 = 0;
+    z->P = z->Q = go;
+    z->ED = NK_INF;
+    z->CD = 0;
+    for (int j = 1; j < bb; j++) {
+        const nkcell *l = nk_at(b, 0, j - 1);
+        nkcell *o = nk_at(b, 0, j);
+        int add = C(c, s2[j], gap);
+        int flag = gap & s2[j - 1], flag2 = gap & s2[j], gocost;
+        if (j == 1) gocost = flag2 ? 0 : go;
+        else gocost = (!flag && flag2) ? 0 : go;
+        int ext = l->Q + add + ((flag && !flag2) ? go : 0);
+        int open = l->cost + add + gocost;
+        o->cost = o->Q = NK_MIN(open, ext);
+        o->dir = NK_INS | NK_END_INS | NK_END_DEL | NK_END_DIAG;
+        o->g1 = (uint16_t)(l->g1 + 1);
+        o->g2 = l->g2;
+        o->P = o->ED = o->CD = NK_INF;
+    }
+}
+
+/* One ukktest pass at band half-width k (src/newkkonen.c:1077-1153);
+ * returns the last cell. */
+static const nkcell *nk_fill(const ocm *c, nkband *b, const uint8_t *s1,
+                             const uint8_t *s2, int k, int go)
+{
+    const int X = b->lenX, Y = b->lenY, d = Y - X;
+    b->k = k;
+    b->W = d + 2 * k + 1;
+    size_t need = (size_t)X * b->W;
+    if (need > b->cap) {
+        free(b->cell);
+        b->cell = (nkcell *)malloc(need * sizeof(nkcell));
+        b->cap = need;
+    }
+    nk_first_row(c, b, s2, go);
+    for (int i = 0; i < X; i++) {
+        int js = i - k > 0 ? i - k : 0;
+        int je = i + d + k < Y - 1 ? i + d + k : Y - 1;
+        if (i == 0) js = d + 1; /* columns 0..d hold the first row */
+        for (int j = js; j <= je; j++) {
+            int lb = (i - j == k), rb = (j - i == d + k);
+            nk_cell(c, s1, s2, i, j, lb, rb,
+                    (!lb && j > 0) ? nk_at(b, i, j - 1) : NULL,
+                    (!rb && i > 0) ? nk_at(b, i - 1, j) : NULL,
+                    (i > 0 && j > 0) ? nk_at(b, i - 1, j - 1) : NULL, go,
+                    nk_at(b, i, j));
+        }
+    }
+    return nk_at(b, X - 1, Y - 1);
+}
+
+/* trivial_algn, src/newkkonen.c:1334-1357 */
+static int nk_trivial_cost(const ocm *c, const uint8_t *s1, int l1,
+                           const uint8_t *s2, int l2)
+{
+    int r = 0;
+    for (int i = 0; i < l1; i++) r += C(c, s1[i] & NK_NOGAP, c->t.gap);
+    for (int j = 0; j < l2; j++) r += C(c, s2[j] & NK_NOGAP, c->t.gap);
+    return r;
+}
+
+/* newkk_algn + increaseT (src/newkkonen.c:1155-1172, 1361-1446) with the
+ * affine gap opening `go`; s1 is the shorter. Leaves the last band in b
+ * (b->lenX == 0 for the trivial case). */
+static int nk_align_cost(const ocm *c, nkband *b, const uint8_t *s1, int l1,
+                         const uint8_t *s2, int l2, int *iters, int64_t *cells)
+{
+    const int go = c->t.gap_open > 0 ? c->t.gap_open : 0;
+    if (iters) *iters = 0;
+    if ((int64_t)l1 * NK_MUCH_LONGER < l2) {
+        b->lenX = 0;
+        return nk_trivial_cost(c, s1, l1, s2, l2);
+    }
+    b->lenX = l1;
+    b->lenY = l2;
+    const int d = l2 - l1;
+    int T = (d + 1) * c->mnz;
+    for (;;) {
+        int p = (T - d) / 2;
+        int k = p < l1 - 1 ? p : l1 - 1;
+        const nkcell *last = nk_fill(c, b, s1, s2, k, go);
+        if (iters) (*iters)++;
+        if (cells)
+            for (int i = 0; i < l1; i++) {
+                int js = i - k > 0 ? i - k : 0;
+                int je = i + d + k < l2 - 1 ? i + d + k : l2 - 1;
+                *cells += je - js + 1;
+            }
+        int gn = last->g1 > last->g2 ? last->g1 : last->g2;
+        int newp = (T * 2 - d) / 2;
+        if (p > gn || newp - l2 + 1 >= 0) return last->cost;
+        T *= 2;
+    }
+}
+
+/* backtrace_affine (src/newkkonen.c:1666-1766) and trivial_backtrace
+ * (:1498-1520); writes back to front into r1/r2 of capacity l1 + l2 and
+ * returns the aligned length. */
+static int nk_backtrace(const ocm *c, nkband *b, const uint8_t *s1, int l1,
+                        const uint8_t *s2, int l2, int swaped, uint8_t *r1,
+                        uint8_t *r2)
+{
+    const int gap = c->t.gap, cap = l1 + l2;
+    int n = 0;
+#define NK_PUT(x, y)                                                        \
+    do {                                                                    \
+        if (n >= cap) return fail("newkk backtrace: output full");          \
+        n++;                                                                \
+        r1[cap - n] = (uint8_t)(x);                                         \
+        r2[cap - n] = (uint8_t)(y);                                         \
+    } while (0)
+    if (b->lenX == 0) {
+        for (int i = 0; i < l1; i++) NK_PUT(s1[i], gap);
+        for (int j = 0; j < l2; j++) NK_PUT(gap, s2[j]);
+        return n;
+    }
+    enum { M_TODO, M_DEL, M_INS, M_DIAG, M_ALIGN } mode = M_TODO;
+    const int d = l2 - l1;
+    int i = l1 - 1, j = l2 - 1;
+    while (i >= 0 && j >= 0) {
+        if (i - j > b->k || j - i > d + b->k)
+            return fail("newkk backtrace left the band");
+        int dir = nk_at(b, i, j)->dir;
+        if (dir == NK_START) {
+            if (i != 0 || j != 0) return fail("newkk backtrace: START off (0,0)");
+            NK_PUT(gap, gap);
+            i--;
+            j--;
+        } else if (mode == M_TODO) {
+            int ins = dir & NK_INS, del = dir & NK_DEL;
+            if (!swaped) mode = del ? M_DEL : ins ? M_INS : 0;
+            else mode = ins ? M_INS : del ? M_DEL : 0;
+            if (!mode) mode = (dir & NK_DIAG) ? M_DIAG : (dir & NK_ALIGN) ? M_ALIGN : 0;
+            if (!mode) return fail("newkk backtrace: invalid direction");
+        } else if (mode == M_DEL || mode == M_INS) {
+            int same = dir & NK_INS_EQ_DEL;
+            if (mode == M_DEL) {
+                NK_PUT(s1[i], gap);
+                i--;
+                if ((dir & NK_END_DEL) || same) mode = M_TODO;
+            } else {
+                NK_PUT(gap, s2[j]);
+                j--;
+                if ((dir & NK_END_INS) || same) mode = M_TODO;
+            }
+        } else if (mode == M_DIAG) {
+            if (dir & NK_END_DIAG) mode = M_TODO;
+            NK_PUT(s1[i], s2[j]);
+            i--;
+            j--;
+        } else {
+            NK_PUT(s1[i] & NK_NOGAP, s2[j] & NK_NOGAP);
+            i--;
+            j--;
+            mode = M_TODO;
+        }
+    }
+#undef NK_PUT
+    return n;
+}
+
+static int nk_check_affine(const ocm *c)
+{
+    if (c->t.cost_model != 1)
+        return fail("Algn_Newkk is built for the affine cost model only");
+    return 0;
+}
+
+/* newkkonen_CAML_algn_affine + newkkonen_CAML_backtrace_affine
+ * (src/newkkonen.c:1473-1496, 1788-1805) on s1 (the shorter) and s2. The
+ * aligned pair lands in r1/r2[0, *len); capacity l1 + l2 each. */
+int orc_newkk_align(void *cm, const uint8_t *s1, int l1, const uint8_t *s2,
+                    int l2, int swaped, int *cost, uint8_t *r1, uint8_t *r2,
+                    int *len, int *iters, int64_t *cells)
+{
+    const ocm *c = (const ocm *)cm;
+    if (nk_check_affine(c)) return -1;
+    if (l1 > l2) return fail("ERROR: newkkonen.newkk_algn, s1 len > s2 len");
+    if (l1 < 1) return fail("empty sequence");
+    nkband b = {0};
+    if (cells) *cells = 0;
+    *cost = nk_align_cost(c, &b, s1, l1, s2, l2, iters, cells);
+    int cap = l1 + l2, rc = 0;
+    uint8_t *t1 = (uint8_t *)malloc((size_t)cap), *t2 = (uint8_t *)malloc((size_t)cap);
+    int n = nk_backtrace(c, &b, s1, l1, s2, l2, swaped, t1, t2);
+    if (n < 0) rc = -1;
+    else {
+        memcpy(r1, t1 + cap - n, (size_t)n);
+        memcpy(r2, t2 + cap - n, (size_t)n);
+        *len = n;
+    }
+    free(t1);
+    free(t2);
+    free(b.cell);
+    return rc;
+}
+
+/* SeqCS.DOS.median with use_ukk under an affine model (src/seqCS.ml:
+ * 1043-1051): NewkkAlign.align_2 (shorter first, src/sequence.ml:
+ * 1879-1901), then Align.ancestor_2, median_2_with_gaps and max_cost_2 on
+ * the aligned pair. Output capacities as orc_median_linear. */
+int orc_newkk_median(void *cm, const uint8_t *a, int la, const uint8_t *b,
+                     int lb, int *cost, uint8_t *ea, uint8_t *eb, int *elen,
+                     uint8_t *anc, int *anclen, uint8_t *mwg, int *mwglen,
+                     int *maxcost)
+{
+    const ocm *c = (const ocm *)cm;
+    int L, rc;
+    if (la <= lb) rc = orc_newkk_align(cm, a, la, b, lb, 0, cost, ea, eb, &L, NULL, NULL);
+    else rc = orc_newkk_align(cm, b, lb, a, la, 1, cost, eb, ea, &L, NULL, NULL);
+    if (rc) return rc;
+    *elen = L;
+    if (ancestor_2(c, ea, eb, L, anc, anclen)) return -1;
+    for (int i = 0; i < L; i++) mwg[i] = c->t.median[(ea[i] << c->t.lcm) + eb[i]];
+    *mwglen = L;
+    int gap = c->t.gap;
+    *maxcost = (all_gaps(ea, L, gap) || all_gaps(eb, L, gap)) ? 0 : worst_2(c, ea, eb, L);
+    return 0;
+}

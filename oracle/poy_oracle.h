@@ -50,4 +50,17 @@ int orc_median_batch(void *cm, int affine, int npairs, const uint8_t *seqs,
 int orc_schedule(void *cm, int affine, const uint8_t *a, int la,
                  const uint8_t *b, int lb, int *iters, int64_t *cells);
 
+/* Algn_Newkk, affine (src/newkkonen.c): newkkonen_CAML_algn_affine +
+ * newkkonen_CAML_backtrace_affine on s1 (shorter, l1 <= l2) and s2; the
+ * aligned pair in r1/r2[0, *len) (capacity l1 + l2). iters/cells (optional)
+ * receive the band passes run and the cells they filled. */
+int orc_newkk_align(void *cm, const uint8_t *s1, int l1, const uint8_t *s2,
+                    int l2, int swaped, int *cost, uint8_t *r1, uint8_t *r2,
+                    int *len, int *iters, int64_t *cells);
+/* SeqCS.DOS.median with use_ukk (affine): capacities as orc_median_linear. */
+int orc_newkk_median(void *cm, const uint8_t *a, int la, const uint8_t *b,
+                     int lb, int *cost, uint8_t *ea, uint8_t *eb, int *elen,
+                     uint8_t *anc, int *anclen, uint8_t *mwg, int *mwglen,
+                     int *maxcost);
+
 #endif

@@ -461,3 +461,85 @@ int ref_median_affine(void *cm, void *ws, const uint8_t *a, int la,
     freeblk(vwg);
     return rc;
 }
+
+/* ---- Algn_Newkk (src/newkkonen.c, compiled unmodified alongside) --------- */
+
+value newkkonen_CAML_create_general(value);
+value newkkonen_CAML_algn_affine(value, value, value, value, value);
+value newkkonen_CAML_backtrace_affine(value, value, value, value, value, value, value);
+void newkkmat_CAML_free(value);
+
+/*
+ * Sequence.NewkkAlign.align_2 (sequence.ml:1879-1901) under an affine cm, on a
+ * fresh newkk matrix: shorter sequence first (swaped = 1 when b is shorter),
+ * newkkonen_CAML_algn_affine then newkkonen_CAML_backtrace_affine; the aligned
+ * pair comes back in the caller's (a, b) order (capacity la + lb each).
+ */
+int ref_newkk_align2(void *cm, const uint8_t *a, int la, const uint8_t *b,
+                     int lb, int *cost, uint8_t *ea, uint8_t *eb, int *elen)
+{
+    ref_cm *r = (ref_cm *)cm;
+    jmp_buf jb;
+    ref_jmp = &jb;
+    int swaped = la <= lb ? 0 : 1;
+    value sa = mkseq(la, a, la), sb = mkseq(lb, b, lb);
+    value pa = mkseq(la + lb, NULL, 0), pb = mkseq(la + lb, NULL, 0);
+    value mat = newkkonen_CAML_create_general(Val_unit);
+    int rc = 0;
+    if (setjmp(jb)) {
+        rc = -1;
+    } else {
+        value s1 = swaped ? sb : sa, s2 = swaped ? sa : sb;
+        value p1 = swaped ? pb : pa, p2 = swaped ? pa : pb;
+        *cost = Int_val(newkkonen_CAML_algn_affine(s1, s2, r->blk, mat, Val_int(swaped)));
+        newkkonen_CAML_backtrace_affine(s1, s2, p1, p2, r->blk, mat, Val_int(swaped));
+        *elen = getseq(pa, ea, la + lb);
+        getseq(pb, eb, la + lb);
+    }
+    ref_jmp = NULL;
+    newkkmat_CAML_free(mat);
+    freeblk(mat);
+    freeblk(sa);
+    freeblk(sb);
+    freeblk(pa);
+    freeblk(pb);
+    return rc;
+}
+
+/*
+ * SeqCS.DOS.median with use_ukk, affine (seqCS.ml:1043-1051): align_2 as
+ * above, then ancestor_2, median_2_with_gaps and max_cost_2 in caller order.
+ * Capacities: ea, eb, mwg la+lb; anc la+lb+1.
+ */
+int ref_newkk_median(void *cm, const uint8_t *a, int la, const uint8_t *b,
+                     int lb, int *cost, uint8_t *ea, uint8_t *eb, int *elen,
+                     uint8_t *anc, int *anclen, uint8_t *mwg, int *mwglen,
+                     int *maxcost)
+{
+    ref_cm *r = (ref_cm *)cm;
+    if (ref_newkk_align2(cm, a, la, b, lb, cost, ea, eb, elen)) return -1;
+    int L = *elen;
+    jmp_buf jb;
+    ref_jmp = &jb;
+    value pa = mkseq(L, ea, L), pb = mkseq(L, eb, L);
+    value sm = mkseq(L + 1, NULL, 0), swg = mkseq(L, NULL, 0);
+    int rc = 0;
+    if (setjmp(jb)) {
+        rc = -1;
+    } else {
+        algn_CAML_ancestor_2(pa, pb, r->blk, sm);
+        seq_CAML_median_2_with_gaps(pa, pb, r->blk, swg);
+        *anclen = getseq(sm, anc, la + lb + 1);
+        *mwglen = getseq(swg, mwg, la + lb);
+        if (seq_is_empty(ea, L, r->gap) || seq_is_empty(eb, L, r->gap))
+            *maxcost = 0;
+        else
+            *maxcost = Int_val(algn_CAML_worst_2(pa, pb, r->blk));
+    }
+    ref_jmp = NULL;
+    freeblk(pa);
+    freeblk(pb);
+    freeblk(sm);
+    freeblk(swg);
+    return rc;
+}

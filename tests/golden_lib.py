@@ -8,6 +8,8 @@ import numpy as np
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 NAMES = ["golden_linear", "golden_affine", "golden_plain_pairs", "golden_affine_pairs"]
+# DOS.median with use_ukk (Algn_Newkk), affine
+NEWKK_NAMES = ["golden_newkk"]
 
 
 @dataclass

@@ -175,6 +175,23 @@ class Oracle:
             raise OracleError(self.error())
         return r1[:n.value].copy(), r2[:n.value].copy()
 
+    def newkk_median(self, cm, a, b) -> Median:
+        """DOS.median with use_ukk under an affine model (Algn_Newkk)."""
+        a = np.ascontiguousarray(a, np.uint8)
+        b = np.ascontiguousarray(b, np.uint8)
+        cap = len(a) + len(b) + 2
+        ea, eb, anc, mwg = (np.zeros(cap, np.uint8) for _ in range(4))
+        cost, elen, alen, wlen, mx = (_I() for _ in range(5))
+        rc = self._f("newkk_median")(
+            cm, _ptr(a), len(a), _ptr(b), len(b), C.byref(cost), _ptr(ea),
+            _ptr(eb), C.byref(elen), _ptr(anc), C.byref(alen), _ptr(mwg),
+            C.byref(wlen), C.byref(mx))
+        if rc:
+            raise OracleError(self.error())
+        n = elen.value
+        return Median(cost.value, ea[:n].copy(), eb[:n].copy(),
+                      anc[:alen.value].copy(), mwg[:wlen.value].copy(), mx.value)
+
     # ---- port-only helpers ------------------------------------------------
     def set_check(self, on: bool):
         self.lib.orc_set_check(int(on))
@@ -187,6 +204,23 @@ class Oracle:
         self.lib.orc_schedule(cm, int(affine), _ptr(a), len(a), _ptr(b),
                               len(b), C.byref(it), C.byref(cells))
         return it.value, cells.value
+
+    def newkk_align(self, cm, s1, s2, swaped: int):
+        """newkkonen_CAML_algn_affine + _backtrace_affine on (s1 shorter, s2):
+        (cost, r1, r2, band passes, cells filled)."""
+        s1 = np.ascontiguousarray(s1, np.uint8)
+        s2 = np.ascontiguousarray(s2, np.uint8)
+        cap = len(s1) + len(s2)
+        r1 = np.zeros(cap, np.uint8)
+        r2 = np.zeros(cap, np.uint8)
+        cost, n, it = _I(), _I(), _I()
+        cells = C.c_int64()
+        if self.lib.orc_newkk_align(cm, _ptr(s1), len(s1), _ptr(s2), len(s2),
+                                    swaped, C.byref(cost), _ptr(r1), _ptr(r2),
+                                    C.byref(n), C.byref(it), C.byref(cells)):
+            raise OracleError(self.error())
+        return (cost.value, r1[:n.value].copy(), r2[:n.value].copy(), it.value,
+                cells.value)
 
     def median_batch(self, cm, seqs_a, seqs_b, affine: bool, nthreads: int = 0):
         """DOS.median over many pairs on the host cores (OpenMP)."""
