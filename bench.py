@@ -61,7 +61,7 @@ def parse_args(argv=None):
                     help="skip the downpass and serving measurements")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="arrival window of each serving rate")
-    ap.add_argument("--leg", choices=["main", "downpass", "long", "serving", "distance"],
+    ap.add_argument("--leg", choices=["main", "downpass", "long", "serving", "distance", "newkk"],
                     default="main", help="run one measurement alone and print its object")
     return ap.parse_args(argv)
 
@@ -546,6 +546,97 @@ def run_distance(local: int, n_pairs: int = 8192, reps: int = 3) -> dict:
             "alignments_per_s": round(pk.npairs / ms * 1e3, 1)}
 
 
+def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.0) -> dict:
+    """DOS.median with use_ukk (Algn_Newkk, src/newkkonen.c) on the affine
+    pair workload: device-resident inputs (value) and the host-pointer API
+    with the copies inside the timed region (e2e); the oracle's restatement
+    on the host cores on a bounded sample beside it, and a parity sample."""
+    import ctypes as C
+    import concurrent.futures as cf
+    import torch
+    import poy5_gb300 as pg
+    from poy5_gb300 import _lib
+    from poy5_gb300 import workloads as wl
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    w = wl.affine_pairs(n_pairs=n_pairs)
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    lib = _lib.load()
+    pk = pg.pack_pairs(w.pairs)
+    dev = torch.device("cuda", local)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_in = [t(pk.seqs), t(pk.offa), t(pk.lena), t(pk.offb), t(pk.lenb), t(pk.out_off)]
+    ints = [torch.zeros(pk.npairs, dtype=torch.int32, device=dev) for _ in range(7)]
+    outs = [torch.zeros(max(pk.out_bytes, 1), dtype=torch.uint8, device=dev) for _ in range(4)]
+    P = lambda x: C.c_void_p(x.data_ptr())
+    st = torch.cuda.current_stream(dev)
+    max_len = int(max(pk.lena.max(), pk.lenb.max()))
+
+    def step():
+        _lib.check(lib.poyalgn_newkk_median_batch_device(
+            ctx.handle, cm.handle, pk.npairs, *(P(x) for x in d_in), max_len,
+            *(P(x) for x in ints[:6]), *(P(x) for x in outs), P(ints[6]),
+            C.c_void_p(st.cuda_stream)))
+
+    step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    launches = ctx.last_launches()
+    status = ints[5].cpu().numpy()
+    passes = ints[6].cpu().numpy()
+    # e2e: the host-pointer entry point (copies in and out inside the call)
+    t0 = time.perf_counter()
+    res = pg.newkk_median_batch(ctx, cm, pk)
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    cells = cells_full(w)
+    # parity sample and CPU baseline: the oracle's restatement
+    orc = oracle_lib.Oracle("port")
+    ocm = orc.cm(subs=w.subs, indel=w.indel, gap_open=w.gap_open)
+    par_bad = 0
+    for k in range(64):
+        a, b = w.pairs[k]
+        r = orc.newkk_median(ocm, a, b)
+        d = res.pair(k)
+        if not (d.cost == r.cost and np.array_equal(d.aligned_a, r.ea)
+                and np.array_equal(d.aligned_b, r.eb) and np.array_equal(d.median, r.median)):
+            par_bad += 1
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    n_cpu, ccells = 0, 0
+
+    def one(k):
+        a, b = w.pairs[k]
+        orc.newkk_median(ocm, a, b)
+        return len(a) * len(b)
+
+    with cf.ThreadPoolExecutor(threads) as ex:
+        while time.perf_counter() - t0 < cpu_s and n_cpu < len(w.pairs):
+            chunk = range(n_cpu, min(n_cpu + 4 * threads, len(w.pairs)))
+            ccells += sum(ex.map(one, chunk))
+            n_cpu += len(chunk)
+    cpu_dt = time.perf_counter() - t0
+    return {"workload": f"affine_pairs_{n_pairs}_newkk", "pairs": pk.npairs,
+            "status_ok": int((status == 0).sum()), "ms": round(ms, 2),
+            "gcups": round(cells / ms / 1e6, 2),
+            "alignments_per_s": round(pk.npairs / ms * 1e3, 1),
+            "e2e": {"ms": round(e2e_ms, 2), "gcups": round(cells / e2e_ms / 1e6, 2),
+                    "h2d_bytes": int(pk.seqs.nbytes + 5 * 8 * pk.npairs),
+                    "d2h_bytes": int(4 * pk.out_bytes + 28 * pk.npairs)},
+            "passes_mean": round(float(passes.mean()), 2), "gpu_launches": launches,
+            "parity_sample": {"pairs": 64, "mismatches": par_bad, "against": "oracle port"},
+            "cpu_baseline": {"gcups": round(ccells / cpu_dt / 1e9, 4), "kind": "port",
+                             "cores": threads,
+                             "sample": f"first {n_cpu} pairs ({cpu_dt:.1f} s)",
+                             "alignments_per_s": round(n_cpu / cpu_dt, 2)}}
+
+
 def run_serving(local: int, seconds: float = 1.0) -> dict:
     """Open-loop Poisson replay against the continuous-batching server: each
     request has U{1..64} pairs of a resident pool (lognormal lengths, median
@@ -700,6 +791,8 @@ def main(argv=None):
             out = run_long(local)
         elif args.leg == "serving":
             out = run_serving(local, args.serve_seconds)
+        elif args.leg == "newkk":
+            out = run_newkk(local, args.pairs or 65536)
         else:
             out = run_distance(local, args.pairs or 8192)
         print(json.dumps({"leg": args.leg, **out}))
@@ -744,6 +837,10 @@ def main(argv=None):
             line["downpass"] = run_downpass(local)
             line["long_pairs"] = run_long(local)
             line["distance"] = run_distance(local)
+            try:
+                line["newkk"] = run_newkk(local)
+            except Exception as e:  # keep the headline line if this leg fails
+                line["newkk"] = {"error": f"{type(e).__name__}: {e}"[:300]}
             line["serving"] = run_serving(local, args.serve_seconds)
         print(json.dumps(line))
     if world > 1:

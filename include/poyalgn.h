@@ -47,6 +47,9 @@ extern "C" {
 #define POYALGN_PAIR_NO_CONVERGE -8 /* band doubling did not stop (e.g. all costs 0) */
 #define POYALGN_PAIR_INTERNAL -9   /* a speculative band pass was queued but did not run */
 #define POYALGN_PAIR_EMPTY_STATE -11 /* closest: a position with no state (POY asserts) */
+#define POYALGN_PAIR_RETRY -12     /* internal: direction arena full, the pair is rerun */
+#define POYALGN_PAIR_OFF_BAND -13  /* Newkk traceback leaves the band (POY reads
+                                      memory outside it) */
 
 typedef struct poyalgn_ctx poyalgn_ctx;
 typedef struct poyalgn_cm poyalgn_cm;
@@ -258,6 +261,75 @@ int poyalgn_distance_batch_device(poyalgn_ctx *ctx, const poyalgn_cm *cm,
                                   const int32_t *lena, const int64_t *offb,
                                   const int32_t *lenb, int32_t missing_distance,
                                   int32_t *cost, int32_t *status, void *stream);
+
+/* ---- Algn_Newkk: POY's own banded aligner (src/newkkonen.c), affine ---------- */
+
+/*
+ * newkkonen_CAML_algn_affine (src/newkkonen.c:1473-1496, external
+ * Sequence.NewkkAlign.newkk_cost2_affine, src/sequence.ml:1840): cost of
+ * aligning s1 (the shorter, l1 <= l2) with s2 under the affine model of cm,
+ * band passes doubled as newkk_algn does (src/newkkonen.c:1361-1446). The
+ * context keeps the alignment for the following backtrace, as the reference
+ * keeps it in its ukkm matrix. The linear variant (newkkonen_CAML_algn) is
+ * not provided: in the reference it leaves a zero-cost diagonal candidate in
+ * every inner cell and its backtrace fails an assertion
+ * (src/newkkonen.c:786-790, 1554); cm must be affine.
+ */
+int poyalgn_newkk_algn_affine(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                              const uint8_t *s1, int l1, const uint8_t *s2,
+                              int l2, int swaped, int32_t *cost);
+
+/*
+ * newkkonen_CAML_backtrace_affine (src/newkkonen.c:1788-1805, external
+ * newkk_backtrace_affine, src/sequence.ml:1844): the aligned pair of the
+ * last poyalgn_newkk_algn_affine call on the same (s1, s2, swaped), written
+ * back to front like seq_prepend: s1p/s2p[cap - len, cap).
+ */
+int poyalgn_newkk_backtrace_affine(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                                   const uint8_t *s1, int l1, const uint8_t *s2,
+                                   int l2, uint8_t *s1p, uint8_t *s2p, int cap,
+                                   int32_t *len, int swaped);
+
+/* Bound the Newkk direction-code arena to `words` u16 words (0: a third of
+ * the free device memory, at most 16 G words). Pairs whose band does not fit
+ * beside the others are finished in further launches. */
+int poyalgn_newkk_set_arena_words(poyalgn_ctx *ctx, int64_t words);
+
+/* newkkonen_CAML_get_k (src/newkkonen.c:247-252): band half-width of the
+ * last pass of the last poyalgn_newkk_algn_affine call. */
+int poyalgn_newkk_get_k(const poyalgn_ctx *ctx, int32_t *k);
+
+/*
+ * SeqCS.DOS.median with use_ukk under an affine model (src/seqCS.ml:
+ * 1043-1051): Sequence.NewkkAlign.align_2 (shorter first, swaped when b is
+ * the shorter, src/sequence.ml:1879-1901), then Align.ancestor_2,
+ * median_2_with_gaps and max_cost_2 on the aligned pair. Inputs and output
+ * layout as poyalgn_median_batch: ea/eb = the aligned pair, med = the
+ * ancestor, mwg = the median with gaps, each ending at the last byte of the
+ * pair's slot [out_off[k], out_off[k] + lena[k] + lenb[k] + 2). passes
+ * (optional) receives the band passes run per pair.
+ *
+ * poyalgn_newkk_median_batch takes host pointers; the _device variant takes
+ * device pointers, max_len >= every sequence length and a cudaStream_t (as
+ * void *), and returns once the batch is done (a batch whose direction codes
+ * do not fit the context's arena at once is finished in further launches).
+ */
+int poyalgn_newkk_median_batch(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                               int npairs, const uint8_t *seqs,
+                               const int64_t *offa, const int32_t *lena,
+                               const int64_t *offb, const int32_t *lenb,
+                               const int64_t *out_off, int32_t *cost,
+                               int32_t *maxcost, int32_t *alen, int32_t *mlen,
+                               int32_t *wlen, int32_t *status, uint8_t *ea,
+                               uint8_t *eb, uint8_t *med, uint8_t *mwg,
+                               int32_t *passes);
+int poyalgn_newkk_median_batch_device(
+    poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs, const uint8_t *seqs,
+    const int64_t *offa, const int32_t *lena, const int64_t *offb,
+    const int32_t *lenb, const int64_t *out_off, int max_len, int32_t *cost,
+    int32_t *maxcost, int32_t *alen, int32_t *mlen, int32_t *wlen,
+    int32_t *status, uint8_t *ea, uint8_t *eb, uint8_t *med, uint8_t *mwg,
+    int32_t *passes, void *stream);
 
 /* ---- device-resident sequences and the tree downpass ------------------------ */
 

@@ -48,6 +48,12 @@ _SIGS = {
     "poyalgn_align_affine_3": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _I, _P, _I, _P]),
     "poyalgn_aligned_medians": (_I, [_P, _P, _P, _P, _I, _P, _I, _P, _P, _P]),
     "poyalgn_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
+    "poyalgn_newkk_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
+    "poyalgn_newkk_median_batch_device": (_I, [_P, _P, _I] + [_P] * 6 + [_I] + [_P] * 12),
+    "poyalgn_newkk_algn_affine": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
+    "poyalgn_newkk_backtrace_affine": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _I, _P, _I]),
+    "poyalgn_newkk_get_k": (_I, [_P, _P]),
+    "poyalgn_newkk_set_arena_words": (_I, [_P, _I64]),
     "poyalgn_median_batch_device": (_I, [_P, _P, _I, _I, _I64] + [_P] * 18),
     "poyalgn_median_batch_device_noalloc": (_I, [_P, _I, _I, _I64] + [_P] * 18),
     "poyalgn_store_create": (_I, [_P, _I64, C.POINTER(_P)]),

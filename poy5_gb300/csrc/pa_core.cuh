@@ -1486,6 +1486,58 @@ PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int
     return res;
 }
 
+// algn_ancestor_2 (src/algn.c:3602-3626) on an aligned pair of length len:
+// writes the ancestor to anc[0, n) (anc holds len + 1 bytes) and returns n.
+// Linear models drop the gap columns and keep a leading gap; an affine
+// model over a bitset alphabet keeps them for algn_correct_blocks_affine
+// and algn_remove_gaps (src/algn.c:3530-3600).
+PA_HD int ancestor_2(const Tables& t, const uint8_t* x, const uint8_t* y, int len, uint8_t* anc)
+{
+    const int gap = t.gap;
+    const int drop = !t.comb || t.model != 1;
+    int ka = len + 1;
+    for (int i = len - 1; i >= 0; i--) {
+        const int med = t.median[(x[i] << t.lcm) + y[i]];
+        if (!drop || med != gap) anc[--ka] = (uint8_t)med;
+    }
+    int n = len + 1 - ka;
+    for (int i = 0; i < n; i++) anc[i] = anc[ka + i];
+    if (!t.comb || (t.model != 1 && (n == 0 || anc[0] != gap))) {
+        for (int i = n; i > 0; i--) anc[i] = anc[i - 1];
+        anc[0] = (uint8_t)gap;
+        n++;
+    } else if (t.comb) {
+        int inside = 0, prev = 0, ext = 0;
+        for (int i = 0; i < n; i++) {
+            const int ab = x[i], bb = y[i];
+            int sb = anc[i];
+            if (!inside && (!(ab & gap) || !(bb & gap))) inside = 0;
+            else if (inside && ((!(ab & gap)) || (!(bb & gap)))) inside = 0;
+            else if (((ab & gap) || (bb & gap)) && ((ab != gap) || (bb != gap))) inside = 1;
+            else inside = 0;
+            if (((gap & ab) || (gap & bb)) && (!(sb & gap)) && !ext) {
+                prev = inside;
+                ext = 1;
+            } else if ((gap & ab) && (gap & bb) && (sb & gap) && (sb != gap) && ext && inside &&
+                       !prev) {
+                sb = (~gap) & sb;
+                prev = 0;
+            } else if ((gap & ab) && (gap & bb) && (1 == ext)) {
+                prev = inside;
+                ext = 0;
+            }
+            anc[i] = (uint8_t)sb;
+        }
+        int w = 0;
+        for (int i = 0; i < n; i++)
+            if (anc[i] != gap) anc[w++] = anc[i];
+        for (int i = w; i > 0; i--) anc[i] = anc[i - 1];
+        anc[0] = (uint8_t)gap;
+        n = w + 1;
+    }
+    return n;
+}
+
 // backtrace_aff (src/algn.c:1714-1819) in internal order (x shorter), then
 // the caller-order aligned pair and max_cost_2 on it.
 template <class DM>

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "pa_core.cuh"
+#include "pa_newkk.cuh"
 #include "pa_tables.h"
 
 using namespace pa;
@@ -426,6 +427,75 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     return r.status;
 }
 
+// Algn_Newkk: the kernel's pass (pa_newkk.cu fill_pass) replayed with the
+// 32 lanes of the warp in arrays: every step, all lanes take their inputs,
+// then all compute, then lane r receives lane r-1's cell (shuffle up).
+struct NkEmul {
+    std::vector<uint16_t> arena;
+    std::vector<nk::Quad> bnd;
+    std::vector<uint32_t> bndg;
+    std::vector<long long> tb;
+};
+
+int nk_fill(NkEmul& E, const Tables& t, const uint8_t* s1, int l1, const uint8_t* s2, int l2,
+            int k, int go, uint32_t& glast)
+{
+    const nk::Band B{l1, l2, k};
+    E.arena.assign((size_t)nk::band_words(B), 0xffff);
+    E.bnd.assign((size_t)l2, nk::Quad{0, 0, 0, 0});
+    E.bndg.assign((size_t)l2, 0u);
+    E.tb.assign((size_t)B.tiles(), 0);
+    long long base = 0;
+    int lastc = 0;
+    for (int q = 0; q < B.tiles(); q++) {
+        const int jlo = B.jlo(q), ns = B.steps(q);
+        nk::Lane L[32];
+        int b1[32], p1[32];
+        for (int r = 0; r < 32; r++) {
+            nk::lane_reset(L[r]);
+            const int i = 32 * q + r;
+            b1[r] = i < l1 ? s1[i] : 0;
+            p1[r] = (i < l1 && i > 0) ? s1[i - 1] : 0;
+        }
+        E.tb[q] = base;
+        for (int s = 0; s < ns; s++) {
+            for (int r = 0; r < 32; r++)
+                nk::lane_inputs(L[r], r, q, s, jlo + s - r, l2, E.bnd.data(), E.bndg.data());
+            for (int r = 0; r < 32; r++) {
+                const int j = jlo + s - r;
+                const int dir = nk::lane_cell(L[r], t, s2, l1, l2, k, 32 * q + r, j, b1[r], p1[r], go);
+                if (dir >= 0) {
+                    E.arena[(size_t)(base + (long long)s * 32 + r)] = (uint16_t)dir;
+                    if (r == 31) {
+                        E.bnd[(size_t)j] = {L[r].left.P, L[r].left.Q, L[r].left.ED, L[r].left.CD};
+                        E.bndg[(size_t)j] = L[r].left.g;
+                    }
+                }
+            }
+            for (int r = 31; r >= 1; r--) L[r].nu = L[r - 1].left;
+            L[0].nu = L[0].left;
+        }
+        base += (long long)ns * 32;
+        if (q == B.tiles() - 1) {
+            const int rl = (l1 - 1) & 31;
+            lastc = L[rl].lcost;
+            glast = L[rl].left.g;
+        }
+    }
+    return lastc;
+}
+
+struct NkDir {
+    const NkEmul* E;
+    nk::Band b;
+    int operator()(int i, int j) const
+    {
+        const int q = i >> 5, r = i & 31;
+        const int s = j - b.jlo(q) + r;
+        return E->arena[(size_t)(E->tb[q] + (long long)s * 32 + r)];
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -478,6 +548,45 @@ int pa_emul_median(void* h, int affine, const uint8_t* a, int la,
     if (affine)
         return run_affine(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
     return run_linear(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
+}
+
+// DOS.median with use_ukk (affine) of one pair through the replayed Newkk
+// warp, as newkk_kernel runs it. Outputs end at index cap-1 of each buffer
+// (cap = la + lb + 2); res = {alen, mlen, wlen, maxcost}; returns the status.
+int pa_emul_newkk_median(void* h, const uint8_t* a, int la, const uint8_t* b, int lb, int* cost,
+                         uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg, int* res,
+                         int* passes)
+{
+    const Emul& Em = *(Emul*)h;
+    const Tables& t = Em.t;
+    if (t.model != 1 || la < 1 || lb < 1) return -4;
+    const int swaped = la <= lb ? 0 : 1;
+    const uint8_t* s1 = swaped ? b : a;
+    const uint8_t* s2 = swaped ? a : b;
+    const int l1 = swaped ? lb : la, l2 = swaped ? la : lb;
+    const int go = t.go > 0 ? t.go : 0;
+    PairOut o{ea, eb, med, mwg, la + lb + 2};
+    NkEmul E;
+    const bool trivial = (long long)l1 * nk::MUCH_LONGER < l2;
+    int kk = 0, npass = 0, status = 0;
+    if (trivial) {
+        *cost = nk::trivial_cost(t, s1, l1, s2, l2);
+    } else {
+        auto fill = [&](int kp, int& c, uint32_t& g) -> bool {
+            c = nk_fill(E, t, s1, l1, s2, l2, kp, go, g);
+            return true;
+        };
+        *cost = nk::drive(t, l1, l2, fill, kk, npass, status);
+    }
+    *passes = npass;
+    if (status) return status;
+    NkDir dir{&E, nk::Band{l1, l2, kk}};
+    PairRes r = nk::traceback(t, dir, trivial, kk, s1, l1, s2, l2, swaped, o);
+    res[0] = r.alen;
+    res[1] = r.mlen;
+    res[2] = r.wlen;
+    res[3] = r.maxcost;
+    return r.status;
 }
 
 }  // extern "C"

@@ -1365,49 +1365,10 @@ __global__ void aligned_medians_kernel(const Tables* tg, const uint8_t* x, const
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const Tables& t = *tg;
     const int gap = t.gap;
-    const int drop = !t.comb || t.model != 1;
-    int ka = len + 1, status = 0;
-    for (int i = len - 1; i >= 0; i--) {
-        const int med = t.median[(x[i] << t.lcm) + y[i]];
-        mwg[i] = (uint8_t)med;
-        if (med == 0) status = -3;
-        if (!drop || med != gap) anc[--ka] = (uint8_t)med;
-    }
-    int n = len + 1 - ka;
-    for (int i = 0; i < n; i++) anc[i] = anc[ka + i];
-    if (!t.comb || (t.model != 1 && (n == 0 || anc[0] != gap))) {
-        for (int i = n; i > 0; i--) anc[i] = anc[i - 1];
-        anc[0] = (uint8_t)gap;
-        n++;
-    } else if (t.comb) {
-        // algn_correct_blocks_affine + algn_remove_gaps (src/algn.c:3530-3600)
-        int inside = 0, prev = 0, ext = 0;
-        for (int i = 0; i < n; i++) {
-            const int ab = x[i], bb = y[i];
-            int sb = anc[i];
-            if (!inside && (!(ab & gap) || !(bb & gap))) inside = 0;
-            else if (inside && ((!(ab & gap)) || (!(bb & gap)))) inside = 0;
-            else if (((ab & gap) || (bb & gap)) && ((ab != gap) || (bb != gap))) inside = 1;
-            else inside = 0;
-            if (((gap & ab) || (gap & bb)) && (!(sb & gap)) && !ext) {
-                prev = inside;
-                ext = 1;
-            } else if ((gap & ab) && (gap & bb) && (sb & gap) && (sb != gap) && ext && inside && !prev) {
-                sb = (~gap) & sb;
-                prev = 0;
-            } else if ((gap & ab) && (gap & bb) && (1 == ext)) {
-                prev = inside;
-                ext = 0;
-            }
-            anc[i] = (uint8_t)sb;
-        }
-        int w = 0;
-        for (int i = 0; i < n; i++)
-            if (anc[i] != gap) anc[w++] = anc[i];
-        for (int i = w; i > 0; i--) anc[i] = anc[i - 1];
-        anc[0] = (uint8_t)gap;
-        n = w + 1;
-    }
+    int status = 0;
+    for (int i = 0; i < len; i++)
+        if ((mwg[i] = (uint8_t)t.median[(x[i] << t.lcm) + y[i]]) == 0) status = -3;
+    const int n = ancestor_2(t, x, y, len, anc);
     int nga = 0, ngb = 0;
     for (int i = 0; i < len; i++) {
         nga |= x[i] != gap;

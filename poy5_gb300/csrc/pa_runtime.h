@@ -58,6 +58,10 @@ struct poyalgn_ctx {
     pa::DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
     pa::DevBuf dwh, swp, order, order_scratch;
     pa::DevBuf nobt_bnd, nobt_ctr, nobt_coop;  // cost-only affine fill scratch
+    // Algn_Newkk (pa_newkk.cu): per-warp boundary rows and tile offsets, the
+    // direction-code arena, counters, visiting order
+    pa::DevBuf nk_bnd, nk_bndg, nk_tb, nk_arena, nk_ctr, nk_order;
+    long long nk_arena_words = 0;  // 0: sized from the free device memory
     pa::DevBuf dmarena, dmoff, dmctr;          // deferred tracebacks
     int defer_traceback = 1;                   // 0: trace back inside the class kernels
     pa::DevBuf spec_t0, spec_n, spec_res, spec_off;  // speculative band passes
@@ -83,6 +87,11 @@ struct poyalgn_ctx {
     const poyalgn_cm* call_cm = nullptr;
     std::vector<uint8_t> call_s1, call_s2;
     long long call_strides[pa::NCLASS] = {0};
+    // per-call Newkk stubs: the alignment of the last newkk_algn_affine
+    bool nk_valid = false;
+    int nk_l1 = 0, nk_l2 = 0, nk_swaped = 0, nk_k = 0;
+    const poyalgn_cm* nk_cm = nullptr;
+    std::vector<uint8_t> nk_s1, nk_s2, nk_r1, nk_r2;
 };
 
 // Device-resident node sequences (poyalgn_store_*, pa_driver.cu).
@@ -123,6 +132,18 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
 // Reserve run_nobt's scratch for up to max_pairs pairs of lengths up to
 // max_len.
 int prereserve_nobt(poyalgn_ctx* c, int max_pairs, int max_len);
+
+// Enqueue Algn_Newkk DOS.median (use_ukk, affine) for npairs pairs and wait
+// for it (the direction arena may need a rerun of some pairs); max_len
+// bounds every sequence length. swp (optional): pair k is already in
+// internal order (lena <= lenb) and swp[k] is its swaped flag. kmax
+// (optional): receives the last pass's band half-width of each pair.
+int run_newkk(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_len,
+              const uint8_t* seqs, const long long* offa, const int* lena,
+              const long long* offb, const int* lenb, const long long* out_off, int* cost,
+              int* maxcost, int* alen, int* mlen, int* wlen, int* status, uint8_t* ea,
+              uint8_t* eb, uint8_t* med, uint8_t* mwg, int* passes, const int* order,
+              const int* swp, int* kmax, cudaStream_t st);
 
 // Reserve the per-batch scratch of run_batch for batches of up to max_pairs
 // pairs, out_total output bytes and a slab arena of slab_bytes, so that such

@@ -77,3 +77,173 @@ def test_oracle_newkk_rejects_linear(oracle):
     cm = oracle.cm(subs=1, indel=2)
     with pytest.raises(OracleError):
         oracle.newkk_median(cm, np.array([16, 1], np.uint8), np.array([16, 2], np.uint8))
+
+
+# ---- the kernel's warp schedule replayed on the host (no GPU) -------------
+
+def _emul_newkk(lib, h, a, b):
+    import ctypes as C
+    a = np.ascontiguousarray(a, np.uint8)
+    b = np.ascontiguousarray(b, np.uint8)
+    cap = len(a) + len(b) + 2
+    bufs = [np.zeros(cap, np.uint8) for _ in range(4)]
+    res = np.zeros(4, np.int32)
+    cost, ps = C.c_int(), C.c_int()
+    p = lambda x: x.ctypes.data_as(C.c_void_p)
+    rc = lib.pa_emul_newkk_median(h, p(a), len(a), p(b), len(b), C.byref(cost),
+                                  *(p(x) for x in bufs), p(res), C.byref(ps))
+    al, ml, wl, mx = (int(x) for x in res)
+    return rc, cost.value, bufs[0][cap - al:], bufs[1][cap - al:], bufs[2][cap - ml:], \
+        bufs[3][cap - wl:], mx
+
+
+@pytest.fixture(scope="module")
+def nk_emul():
+    import ctypes as C
+    from conftest import build_emulator
+    lib = C.CDLL(build_emulator())
+    lib.pa_emul_new.restype = C.c_void_p
+    lib.pa_emul_new.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.pa_emul_free.argtypes = [C.c_void_p]
+    return lib
+
+
+def _emul_handle(lib, tcm, go):
+    import ctypes as C
+    flat = np.ascontiguousarray(np.asarray(tcm, np.int32).reshape(-1))
+    return C.c_void_p(lib.pa_emul_new(flat.ctypes.data_as(C.c_void_p), 5, go))
+
+
+def test_replay_newkk_matches_golden(nk_emul):
+    g = golden_lib.load("golden_newkk")
+    h = _emul_handle(nk_emul, g.tcm, g.gap_open)
+    bad = []
+    for k, (a, b) in enumerate(g.pairs):
+        rc, cost, ea, eb, med, mwg, mx = _emul_newkk(nk_emul, h, a, b)
+        m = golden_lib.mismatches(g, k, cost, ea, eb, med, mwg, mx) if rc == 0 else ["rc%d" % rc]
+        if m:
+            bad.append((k, m))
+    nk_emul.pa_emul_free(h)
+    assert not bad, bad[:5]
+
+
+@pytest.mark.parametrize("model", [(1, 1, 3), (2, 1, 1), (3, 2, 5)])
+def test_replay_newkk_matches_oracle(oracle, nk_emul, model):
+    subs, indel, go = model
+    tcm = [[0 if r == c else (indel if 4 in (r, c) else subs) for c in range(5)]
+           for r in range(5)]
+    cm = oracle.cm(tcm=tcm, gap_open=go)
+    h = _emul_handle(nk_emul, tcm, go)
+    rng = np.random.default_rng(7 + go)
+    # lengths across tile boundaries (multiples of 32 +- 1) and wide bands
+    pairs = random_pairs(rng, 60, maxlen=300)
+    for L in (31, 32, 33, 63, 64, 65, 97):
+        a = np.array([16] + list(rng.choice([1, 2, 4, 8], L - 1)), np.uint8)
+        b = np.array([16] + list(rng.choice([1, 2, 4, 8], L + int(rng.integers(0, 40)))), np.uint8)
+        pairs += [(a, b), (b, a)]
+    for k, (a, b) in enumerate(pairs):
+        try:
+            r = oracle.newkk_median(cm, a, b)
+        except OracleError:
+            continue
+        rc, cost, ea, eb, med, mwg, mx = _emul_newkk(nk_emul, h, a, b)
+        assert rc == 0, (k, rc)
+        assert cost == r.cost and mx == r.maxcost, k
+        assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb), k
+        assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg), k
+    nk_emul.pa_emul_free(h)
+
+
+# ---- the CUDA library (C ABI) against the reference and the oracle ---------
+
+def _check_batch(res, want, tag):
+    bad = []
+    for k, r in enumerate(want):
+        d = res.pair(k)
+        if res.status[k] != 0:
+            bad.append((k, "status", int(res.status[k])))
+            continue
+        if (d.cost, d.maxcost) != (r.cost, r.maxcost):
+            bad.append((k, "cost", d.cost, r.cost))
+        elif not (np.array_equal(d.aligned_a, r.ea) and np.array_equal(d.aligned_b, r.eb)):
+            bad.append((k, "alignment"))
+        elif not (np.array_equal(d.median, r.median) and np.array_equal(d.median_wg, r.medianwg)):
+            bad.append((k, "median"))
+    assert not bad, (tag, bad[:5])
+
+
+@pytest.mark.gpu
+def test_gpu_newkk_batch_matches_golden(ctx):
+    import poy5_gb300 as pg
+    g = golden_lib.load("golden_newkk")
+    cm = pg.CostMatrix.of_list(ctx, g.tcm, g.gap_open)
+    res = pg.newkk_median_batch(ctx, cm, g.pairs)
+    bad = []
+    for k in range(len(g.pairs)):
+        d = res.pair(k)
+        m = golden_lib.mismatches(g, k, d.cost, d.aligned_a, d.aligned_b, d.median,
+                                  d.median_wg, d.maxcost)
+        if res.status[k] != 0 or m:
+            bad.append((k, int(res.status[k]), m))
+    assert not bad, bad[:5]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model", [(1, 1, 3), (2, 1, 1)])
+def test_gpu_newkk_batch_matches_oracle(ctx, oracle, model):
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    subs, indel, go = model
+    tcm = [[0 if r == c else (indel if 4 in (r, c) else subs) for c in range(5)]
+           for r in range(5)]
+    cm = pg.CostMatrix.of_list(ctx, tcm, go)
+    ocm = oracle.cm(tcm=tcm, gap_open=go)
+    rng = np.random.default_rng(11 + go)
+    pairs = random_pairs(rng, 150, maxlen=400) + wl.affine_pairs(n_pairs=300).pairs
+    want = [oracle.newkk_median(ocm, a, b) for a, b in pairs]
+    _check_batch(pg.newkk_median_batch(ctx, cm, pairs), want, model)
+
+
+@pytest.mark.gpu
+def test_gpu_newkk_arena_reruns(ctx, oracle):
+    """A direction arena far smaller than the batch's bands: the pairs that
+    do not fit are finished by further launches, with the same results."""
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    c2 = pg.Context(0)
+    nk = pg.NewkkAlign(c2)
+    nk.set_arena_words(1 << 21)
+    cm = pg.CostMatrix.of_list(c2, AFF_TCM, 3)
+    ocm = oracle.cm(tcm=AFF_TCM, gap_open=3)
+    pairs = wl.affine_pairs(n_pairs=400).pairs
+    want = [oracle.newkk_median(ocm, a, b) for a, b in pairs]
+    res = pg.newkk_median_batch(c2, cm, pairs)
+    assert c2.last_launches() > 1
+    _check_batch(res, want, "small arena")
+
+
+@pytest.mark.gpu
+def test_gpu_newkk_per_call_stubs(ctx, oracle):
+    """newkkonen_CAML_algn_affine + _backtrace_affine through NewkkAlign.align_2
+    (both argument orders), get_k, and the misuse errors."""
+    import poy5_gb300 as pg
+    cm = pg.CostMatrix.of_list(ctx, AFF_TCM, 3)
+    ocm = oracle.cm(tcm=AFF_TCM, gap_open=3)
+    nk = pg.NewkkAlign(ctx)
+    rng = np.random.default_rng(3)
+    for a, b in edge_pairs()[:12] + random_pairs(rng, 20, maxlen=200):
+        if len(a) == 1 and len(b) == 1:
+            continue
+        try:
+            r = oracle.newkk_median(ocm, a, b)
+        except OracleError:
+            continue
+        pa, pb, cost = nk.align_2(a, b, cm)
+        assert cost == r.cost
+        assert np.array_equal(pa, r.ea) and np.array_equal(pb, r.eb)
+        assert 0 <= nk.get_k() < max(len(a), len(b))
+    with pytest.raises(pg.PoyAlgnError):
+        nk.cost2_affine(np.array([16, 1, 2, 4], np.uint8), np.array([16, 1], np.uint8), cm, 0)
+    lin = pg.CostMatrix.of_list(ctx, [[0 if r == c else 1 for c in range(5)] for r in range(5)], 0)
+    with pytest.raises(pg.PoyAlgnError):
+        pg.newkk_median_batch(ctx, lin, [(np.array([16, 1], np.uint8), np.array([16, 2], np.uint8))])
