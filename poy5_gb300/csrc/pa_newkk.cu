@@ -38,10 +38,9 @@ struct NewkkArgs {
     const int* order;  // optional visiting order
     const int* swp;    // optional: pairs already in internal order, their swaped flag
     const Tables* tables;
-    int* ctr;          // [0] next pair, [1] pairs to rerun (arena full)
-    unsigned long long* arena_used;
+    int* ctr;          // [0] next pair, [1] pairs to rerun (band too large for a slice)
     uint16_t* arena;
-    long long arena_words;
+    long long slice_words;  // each warp's slice of the arena
     nk::Quad* bnd;     // per warp: P, Q, ED, CD of the tile's upper row
     uint32_t* bndg;    // per warp: gap counters of that row
     int bnd_stride;    // >= the longer length of every pair
@@ -139,7 +138,7 @@ __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
     uint32_t* bndg = A.bndg + gw * A.bnd_stride;
     long long* tb = A.tb + gw * A.tb_stride;
     const int go = t.go > 0 ? t.go : 0;
-    long long rbase = 0, rwords = 0;  // this warp's arena region, reused across pairs
+    const long long slice = gw * A.slice_words;  // this warp's arena slice
     for (;;) {
         int idx = 0;
         if (lane == 0) idx = atomicAdd(A.ctr, 1);
@@ -179,24 +178,11 @@ __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
             cost = nk::trivial_cost(t, s1, l1, s2, l2);
         } else {
             auto fill = [&](int kp, int& c, uint32_t& g) -> bool {
-                const long long words = nk::band_words(nk::Band{l1, l2, kp});
-                if (words > rwords) {
-                    long long off = -1;
-                    if (lane == 0) {
-                        const unsigned long long w = ((unsigned long long)words + 127ull) & ~127ull;
-                        const unsigned long long at = atomicAdd(A.arena_used, w);
-                        if (at + w <= (unsigned long long)A.arena_words) off = (long long)at;
-                    }
-                    off = __shfl_sync(FULL, off, 0);
-                    if (off < 0) {
-                        status = POYALGN_PAIR_RETRY;
-                        rwords = 0;
-                        return false;
-                    }
-                    rbase = off;
-                    rwords = words;
+                if (nk::band_words(nk::Band{l1, l2, kp}) > A.slice_words) {
+                    status = POYALGN_PAIR_RETRY;  // rerun with fewer, larger slices
+                    return false;
                 }
-                c = fill_pass(t, s1, l1, s2, l2, kp, go, A.arena, rbase, bnd, bndg, tb, g);
+                c = fill_pass(t, s1, l1, s2, l2, kp, go, A.arena, slice, bnd, bndg, tb, g);
                 return true;
             };
             cost = nk::drive(t, l1, l2, fill, kk, npass, status);
@@ -268,9 +254,7 @@ int run_newkk(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_len,
     A.swp = swp;
     A.tables = cm->d;
     A.ctr = as<int>(c->nk_ctr);
-    A.arena_used = reinterpret_cast<unsigned long long*>(as<int>(c->nk_ctr) + 2);
     A.arena = as<uint16_t>(c->nk_arena);
-    A.arena_words = words;
     A.bnd = as<nk::Quad>(c->nk_bnd);
     A.bndg = as<uint32_t>(c->nk_bndg);
     A.bnd_stride = stride;
@@ -289,20 +273,28 @@ int run_newkk(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_len,
     A.eb = eb;
     A.med = med;
     A.mwg = mwg;
-    int left = -1, launches = 0;
+    // Every warp owns an equal slice of the arena. A pair whose band does
+    // not fit its warp's slice is marked for a rerun, which launches fewer
+    // warps (larger slices) over the marked pairs only, down to one warp
+    // holding the whole arena.
+    int w = (int)std::min<long long>(nwarps, npairs), launches = 0;
     for (A.rerun = 0;; A.rerun = 1) {
-        CU(cudaMemsetAsync(c->nk_ctr.p, 0, 16, st));
-        newkk_kernel<<<grid, NK_WARPS * 32, 0, st>>>(A);
+        const int threads = std::min(w, NK_WARPS) * 32;
+        const int blocks = (w * 32 + threads - 1) / threads;
+        const long long launched = (long long)blocks * threads / 32;
+        A.slice_words = (words / launched) & ~31LL;
+        CU(cudaMemsetAsync(c->nk_ctr.p, 0, 8, st));
+        newkk_kernel<<<blocks, threads, 0, st>>>(A);
         CU(cudaGetLastError());
         launches++;
         int h = 0;
         CU(cudaMemcpyAsync(&h, A.ctr + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
         CU(cudaStreamSynchronize(st));
         if (h == 0) break;
-        if (left >= 0 && h >= left)
-            return set_err(POYALGN_ENOMEM, "Newkk: %d pairs do not fit the direction arena "
-                           "(%lld words)", h, words);
-        left = h;
+        if (launched == 1)
+            return set_err(POYALGN_ENOMEM, "Newkk: %d pairs have bands larger than the "
+                           "direction arena (%lld words)", h, words);
+        w = std::max(1, std::min(w / 2, h));
     }
     c->last_launches = launches;
     return 0;
