@@ -212,7 +212,7 @@ def test_gpu_newkk_arena_reruns(ctx, oracle):
     from poy5_gb300 import workloads as wl
     c2 = pg.Context(0)
     nk = pg.NewkkAlign(c2)
-    nk.set_arena_words(1 << 21)
+    nk.set_arena_words(1 << 23)  # the largest band here is ~3 M words
     cm = pg.CostMatrix.of_list(c2, AFF_TCM, 3)
     ocm = oracle.cm(tcm=AFF_TCM, gap_open=3)
     pairs = wl.affine_pairs(n_pairs=400).pairs
