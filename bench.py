@@ -61,6 +61,8 @@ def parse_args(argv=None):
                     help="skip the downpass and serving measurements")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="arrival window of each serving rate")
+    ap.add_argument("--newkk-arena-mb", type=int, default=0,
+                    help="bound the Newkk direction arena (MB; 0: library default)")
     ap.add_argument("--leg", choices=["main", "downpass", "long", "serving", "distance", "newkk"],
                     default="main", help="run one measurement alone and print its object")
     return ap.parse_args(argv)
@@ -546,7 +548,8 @@ def run_distance(local: int, n_pairs: int = 8192, reps: int = 3) -> dict:
             "alignments_per_s": round(pk.npairs / ms * 1e3, 1)}
 
 
-def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.0) -> dict:
+def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.0,
+              arena_mb: int = 0) -> dict:
     """DOS.median with use_ukk (Algn_Newkk, src/newkkonen.c) on the affine
     pair workload: device-resident inputs (value) and the host-pointer API
     with the copies inside the timed region (e2e); the oracle's restatement
@@ -562,6 +565,8 @@ def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.
     w = wl.affine_pairs(n_pairs=n_pairs)
     ctx = pg.Context(local)
     cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    if arena_mb:
+        pg.NewkkAlign(ctx).set_arena_words(arena_mb << 19)
     lib = _lib.load()
     pk = pg.pack_pairs(w.pairs)
     dev = torch.device("cuda", local)
@@ -792,7 +797,7 @@ def main(argv=None):
         elif args.leg == "serving":
             out = run_serving(local, args.serve_seconds)
         elif args.leg == "newkk":
-            out = run_newkk(local, args.pairs or 65536)
+            out = run_newkk(local, args.pairs or 65536, arena_mb=args.newkk_arena_mb)
         else:
             out = run_distance(local, args.pairs or 8192)
         print(json.dumps({"leg": args.leg, **out}))
