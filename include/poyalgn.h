@@ -273,7 +273,7 @@ int poyalgn_distance_batch_device(poyalgn_ctx *ctx, const poyalgn_cm *cm,
  * keeps it in its ukkm matrix. The linear variant (newkkonen_CAML_algn) is
  * not provided: in the reference it leaves a zero-cost diagonal candidate in
  * every inner cell and its backtrace fails an assertion
- * (src/newkkonen.c:786-790, 1554); cm must be affine.
+ * (src/newkkonen.c:796, 1554); cm must be affine.
  */
 int poyalgn_newkk_algn_affine(poyalgn_ctx *ctx, const poyalgn_cm *cm,
                               const uint8_t *s1, int l1, const uint8_t *s2,

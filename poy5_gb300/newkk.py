@@ -3,7 +3,7 @@
 POY's own banded aligner (src/newkkonen.c) that ``SeqCS.DOS.median`` uses
 when ``use_ukk`` is set. Only the affine cost model is provided: the
 reference's linear variant leaves a zero-cost diagonal candidate in every
-inner cell and its backtrace fails an assertion (src/newkkonen.c:786-790,
+inner cell and its backtrace fails an assertion (src/newkkonen.c:796,
 1554).
 
 * :class:`NewkkAlign` -- ``align_2`` (shorter sequence first, ``swaped``)

@@ -73,7 +73,7 @@ def test_oracle_newkk_trivial_path(oracle):
 
 def test_oracle_newkk_rejects_linear(oracle):
     """The reference's linear Newkk keeps a zero-cost diagonal candidate and
-    its backtrace asserts (src/newkkonen.c:786-790, 1554): only affine."""
+    its backtrace asserts (src/newkkonen.c:796, 1554): only affine."""
     cm = oracle.cm(subs=1, indel=2)
     with pytest.raises(OracleError):
         oracle.newkk_median(cm, np.array([16, 1], np.uint8), np.array([16, 2], np.uint8))
