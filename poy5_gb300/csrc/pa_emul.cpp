@@ -428,71 +428,54 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
 }
 
 // Algn_Newkk: the kernel's pass (pa_newkk.cu fill_pass) replayed with the
-// 32 lanes of the warp in arrays: every step, all lanes take their inputs,
-// then all compute, then lane r receives lane r-1's cell (shuffle up).
+// 32 lanes of the warp in arrays: every step, lanes 0..31 run lane_step in
+// turn (lane 0's boundary-row reads never meet lane 31's write of the same
+// step: they are at least one column apart), then lane r receives lane
+// r-1's last cell (shuffle up).
 struct NkEmul {
     std::vector<uint16_t> arena;
     std::vector<nk::Quad> bnd;
     std::vector<uint32_t> bndg;
-    std::vector<long long> tb;
+    std::vector<int> c0;
 };
 
 int nk_fill(NkEmul& E, const Tables& t, const uint8_t* s1, int l1, const uint8_t* s2, int l2,
             int k, int go, uint32_t& glast)
 {
     const nk::Band B{l1, l2, k};
-    E.arena.assign((size_t)nk::band_words(B), 0xffff);
+    E.c0.assign((size_t)B.rounds(), 0);
+    const long long steps = nk::rounds_table(B, E.c0.data());
+    E.arena.assign((size_t)steps * 32, 0xffff);
     E.bnd.assign((size_t)l2, nk::Quad{0, 0, 0, 0});
     E.bndg.assign((size_t)l2, 0u);
-    E.tb.assign((size_t)B.tiles(), 0);
-    long long base = 0;
-    int lastc = 0;
-    for (int q = 0; q < B.tiles(); q++) {
-        const int jlo = B.jlo(q), ns = B.steps(q);
-        nk::Lane L[32];
-        int b1[32], p1[32];
+    nk::Lane L[32];
+    for (int r = 0; r < 32; r++) nk::lane_start(L[r], B, s1, r);
+    for (long long st = 0; st < steps; st++) {
         for (int r = 0; r < 32; r++) {
-            nk::lane_reset(L[r]);
-            const int i = 32 * q + r;
-            b1[r] = i < l1 ? s1[i] : 0;
-            p1[r] = (i < l1 && i > 0) ? s1[i - 1] : 0;
-        }
-        E.tb[q] = base;
-        for (int s = 0; s < ns; s++) {
-            for (int r = 0; r < 32; r++)
-                nk::lane_inputs(L[r], r, q, s, jlo + s - r, l2, E.bnd.data(), E.bndg.data());
-            for (int r = 0; r < 32; r++) {
-                const int j = jlo + s - r;
-                const int dir = nk::lane_cell(L[r], t, s2, l1, l2, k, 32 * q + r, j, b1[r], p1[r], go);
-                if (dir >= 0) {
-                    E.arena[(size_t)(base + (long long)s * 32 + r)] = (uint16_t)dir;
-                    if (r == 31) {
-                        E.bnd[(size_t)j] = {L[r].left.P, L[r].left.Q, L[r].left.ED, L[r].left.CD};
-                        E.bndg[(size_t)j] = L[r].left.g;
-                    }
+            int j = 0;
+            const int dir = nk::lane_step(L[r], t, s1, s2, B, E.c0.data(), r, st, E.bnd.data(),
+                                          E.bndg.data(), go, j);
+            if (dir >= 0) {
+                E.arena[(size_t)(st * 32 + r)] = (uint16_t)dir;
+                if (r == 31) {
+                    E.bnd[(size_t)j] = {L[r].left.P, L[r].left.Q, L[r].left.ED, L[r].left.CD};
+                    E.bndg[(size_t)j] = L[r].left.g;
                 }
             }
-            for (int r = 31; r >= 1; r--) L[r].nu = L[r - 1].left;
-            L[0].nu = L[0].left;
         }
-        base += (long long)ns * 32;
-        if (q == B.tiles() - 1) {
-            const int rl = (l1 - 1) & 31;
-            lastc = L[rl].lcost;
-            glast = L[rl].left.g;
-        }
+        for (int r = 31; r >= 1; r--) L[r].nu = L[r - 1].left;
+        L[0].nu = L[0].left;
     }
-    return lastc;
+    const int rl = (l1 - 1) & 31;
+    glast = L[rl].left.g;
+    return L[rl].lcost;
 }
 
 struct NkDir {
     const NkEmul* E;
-    nk::Band b;
     int operator()(int i, int j) const
     {
-        const int q = i >> 5, r = i & 31;
-        const int s = j - b.jlo(q) + r;
-        return E->arena[(size_t)(E->tb[q] + (long long)s * 32 + r)];
+        return E->arena[(size_t)nk::dir_word(E->c0.data(), i, j)];
     }
 };
 
@@ -580,7 +563,7 @@ int pa_emul_newkk_median(void* h, const uint8_t* a, int la, const uint8_t* b, in
     }
     *passes = npass;
     if (status) return status;
-    NkDir dir{&E, nk::Band{l1, l2, kk}};
+    NkDir dir{&E};
     PairRes r = nk::traceback(t, dir, trivial, kk, s1, l1, s2, l2, swaped, o);
     res[0] = r.alen;
     res[1] = r.mlen;

@@ -1,12 +1,13 @@
 // Algn_Newkk (src/newkkonen.c), affine cost model, on the GPU: one warp per
-// pair. Each band pass (ukktest, src/newkkonen.c:1077-1153) is filled by the
-// warp in tiles of 32 rows, lane r holding row 32q + r and sweeping the
-// band's columns one step behind lane r-1: the cell above comes from lane
-// r-1's previous step by shuffle, the diagonal one from the step before,
-// and lane 0 reads the tile above from a per-warp boundary row written by
-// lane 31. A step's 32 direction codes are one contiguous 64-byte store.
-// After the last pass lane 0 walks the codes back (backtrace_affine) and
-// derives DOS.median's ancestor, median with gaps and worst cost.
+// pair. Each band pass (ukktest, src/newkkonen.c:1077-1153) is filled on a
+// rolling schedule: lane r takes rows r, r + 32, r + 64, ..., one column
+// per step and one column behind lane r - 1, so the cells above and
+// above-left come from lane r - 1 by shuffle; a lane moves on to its next
+// row as soon as its row ends, and lane 0 reads the previous round's last
+// row from a per-warp boundary row that lane 31 writes. A step's 32
+// direction codes are one contiguous 64-byte store. After the last pass
+// lane 0 walks the codes back (backtrace_affine) and derives DOS.median's
+// ancestor, median with gaps and worst cost.
 //
 // C ABI (include/poyalgn.h): poyalgn_newkk_median_batch[_device] (DOS.median
 // with use_ukk, src/seqCS.ml:1043-1051), and the per-call stubs
@@ -44,8 +45,8 @@ struct NewkkArgs {
     nk::Quad* bnd;     // per warp: P, Q, ED, CD of the tile's upper row
     uint32_t* bndg;    // per warp: gap counters of that row
     int bnd_stride;    // >= the longer length of every pair
-    long long* tb;     // per warp: arena word offset of each tile
-    int tb_stride;     // >= tiles of every pair
+    int* tb;           // per warp: the rounds table of its pass
+    int tb_stride;     // >= rounds of every pair
     int rerun;         // 1: only pairs whose status is POYALGN_PAIR_RETRY
     const long long* out_off;
     int *cost, *maxcost, *alen, *mlen, *wlen, *status, *passes, *kmax;
@@ -72,58 +73,60 @@ __device__ __forceinline__ nk::State shfl_up_state(const nk::State& v)
 }
 
 struct ArenaDir {
-    const uint16_t* a;
-    const long long* tb;
-    nk::Band b;
-    __device__ int operator()(int i, int j) const
-    {
-        const int q = i >> 5, r = i & 31;
-        const int s = j - b.jlo(q) + r;
-        return a[tb[q] + (long long)s * 32 + r];
-    }
+    const uint16_t* a;  // the pass's first word
+    const int* c0;
+    __device__ int operator()(int i, int j) const { return a[nk::dir_word(c0, i, j)]; }
 };
 
-// One band pass of the warp at half-width k into the arena words from
-// `base`; returns the last cell's cost (all lanes) and its gap counters.
+// The rounds table of a pass (C0 of every round, nk::rounds_table) built by
+// the warp with a scan over 32 rounds at a time; returns the pass's steps.
+__device__ long long build_rounds(const nk::Band& B, int* c0)
+{
+    const int lane = threadIdx.x & 31;
+    const int Q = B.rounds();
+    int carry = 0;
+    for (int q0 = 0; q0 < Q; q0 += 32) {
+        const int q = q0 + lane;
+        const int dl = q < Q - 1 ? B.delta(q) : 0;
+        int incl = dl;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (q < Q) c0[q] = carry + incl - dl;
+        carry += __shfl_sync(FULL, incl, 31);
+    }
+    __syncwarp();
+    return B.steps(c0[Q - 1]);
+}
+
+// One band pass of the warp at half-width k on the rolling schedule into
+// the arena words from `dm`; returns the last cell's cost (all lanes) and
+// its gap counters.
 __device__ int fill_pass(const Tables& t, const uint8_t* s1, int l1, const uint8_t* s2, int l2,
-                         int k, int go, uint16_t* arena, long long base, nk::Quad* bnd,
-                         uint32_t* bndg, long long* tb, uint32_t& glast)
+                         int k, int go, uint16_t* dm, long long steps, nk::Quad* bnd,
+                         uint32_t* bndg, const int* c0, uint32_t& glast)
 {
     const int lane = threadIdx.x & 31;
     const nk::Band B{l1, l2, k};
-    const int tiles = B.tiles();
-    int lastc = 0;
-    uint32_t lastg = 0;
-    for (int q = 0; q < tiles; q++) {
-        const int i = 32 * q + lane;
-        const int jlo = B.jlo(q), ns = B.steps(q);
-        const int b1 = i < l1 ? s1[i] : 0, p1 = (i < l1 && i > 0) ? s1[i - 1] : 0;
-        if (lane == 0) tb[q] = base;
-        nk::Lane L;
-        nk::lane_reset(L);
-        for (int s = 0; s < ns; s++) {
-            const int j = jlo + s - lane;
-            nk::lane_inputs(L, lane, q, s, j, l2, bnd, bndg);
-            const int dir = nk::lane_cell(L, t, s2, l1, l2, k, i, j, b1, p1, go);
-            if (dir >= 0) {
-                arena[base + (long long)s * 32 + lane] = (uint16_t)dir;
-                if (lane == 31) {
-                    bnd[j] = {L.left.P, L.left.Q, L.left.ED, L.left.CD};
-                    bndg[j] = L.left.g;
-                }
+    nk::Lane L;
+    nk::lane_start(L, B, s1, lane);
+    for (long long st = 0; st < steps; st++) {
+        int j = 0;
+        const int dir = nk::lane_step(L, t, s1, s2, B, c0, lane, st, bnd, bndg, go, j);
+        if (dir >= 0) {
+            dm[st * 32 + lane] = (uint16_t)dir;
+            if (lane == 31) {
+                bnd[j] = {L.left.P, L.left.Q, L.left.ED, L.left.CD};
+                bndg[j] = L.left.g;
             }
-            L.nu = shfl_up_state(L.left);
         }
-        __syncwarp();
-        base += (long long)ns * 32;
-        if (q == tiles - 1) {
-            const int rl = (l1 - 1) & 31;
-            lastc = __shfl_sync(FULL, L.lcost, rl);
-            lastg = __shfl_sync(FULL, L.left.g, rl);
-        }
+        L.nu = shfl_up_state(L.left);
+        __syncwarp();  // lane 31's boundary-row writes before lane 0's later reads
     }
-    glast = lastg;
-    return lastc;
+    const int rl = (l1 - 1) & 31;
+    glast = __shfl_sync(FULL, L.left.g, rl);
+    return __shfl_sync(FULL, L.lcost, rl);
 }
 
 __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     nk::Quad* bnd = A.bnd + gw * A.bnd_stride;
     uint32_t* bndg = A.bndg + gw * A.bnd_stride;
-    long long* tb = A.tb + gw * A.tb_stride;
+    int* tb = A.tb + gw * A.tb_stride;
     const int go = t.go > 0 ? t.go : 0;
     const long long slice = gw * A.slice_words;  // this warp's arena slice
     for (;;) {
@@ -178,11 +181,13 @@ __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
             cost = nk::trivial_cost(t, s1, l1, s2, l2);
         } else {
             auto fill = [&](int kp, int& c, uint32_t& g) -> bool {
-                if (nk::band_words(nk::Band{l1, l2, kp}) > A.slice_words) {
+                const nk::Band B{l1, l2, kp};
+                const long long steps = build_rounds(B, tb);
+                if (steps * 32 > A.slice_words) {
                     status = POYALGN_PAIR_RETRY;  // rerun with fewer, larger slices
                     return false;
                 }
-                c = fill_pass(t, s1, l1, s2, l2, kp, go, A.arena, slice, bnd, bndg, tb, g);
+                c = fill_pass(t, s1, l1, s2, l2, kp, go, A.arena + slice, steps, bnd, bndg, tb, g);
                 return true;
             };
             cost = nk::drive(t, l1, l2, fill, kk, npass, status);
@@ -190,7 +195,7 @@ __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
         if (lane == 0) {
             PairRes r = {0, 0, 0, 0, status};
             if (status == 0) {
-                ArenaDir dir{A.arena, tb, nk::Band{l1, l2, kk}};
+                ArenaDir dir{A.arena + slice, tb};
                 r = nk::traceback(t, dir, trivial, kk, s1, l1, s2, l2, swaped, o);
             } else if (status == POYALGN_PAIR_RETRY) {
                 atomicAdd(A.ctr + 1, 1);
@@ -233,7 +238,7 @@ int run_newkk(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_len,
     const int tstride = (stride + 31) / 32;
     if ((rc = reserve(c->nk_bnd, (size_t)nwarps * stride * sizeof(nk::Quad)))) return rc;
     if ((rc = reserve(c->nk_bndg, (size_t)nwarps * stride * sizeof(uint32_t)))) return rc;
-    if ((rc = reserve(c->nk_tb, (size_t)nwarps * tstride * sizeof(long long)))) return rc;
+    if ((rc = reserve(c->nk_tb, (size_t)nwarps * tstride * sizeof(int)))) return rc;
     if ((rc = reserve(c->nk_ctr, 16))) return rc;
     long long words = c->nk_arena_words;
     if (words <= 0) {
@@ -258,7 +263,7 @@ int run_newkk(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_len,
     A.bnd = as<nk::Quad>(c->nk_bnd);
     A.bndg = as<uint32_t>(c->nk_bndg);
     A.bnd_stride = stride;
-    A.tb = as<long long>(c->nk_tb);
+    A.tb = as<int>(c->nk_tb);
     A.tb_stride = tstride;
     A.out_off = out_off;
     A.cost = cost;

@@ -173,57 +173,118 @@ PA_HD int first_row(const Tables& t, int b2, int p2, int j, int lcost, const Sta
     return c;
 }
 
-// Band geometry of a pass: rows are processed in tiles of 32, lane r of a
-// tile holding row 32q + r; step s of tile q covers columns jlo(q) + s - r.
-// The direction codes of a step are 32 consecutive u16 words (one per lane),
-// so tile q occupies steps(q) * 32 words from its base.
+// Band geometry of a pass at half-width k: row i holds columns js(i) ..
+// je(i). The warp fills a pass on a rolling schedule: lane r takes rows r,
+// r + 32, r + 64, ... (round q holds rows 32q .. 32q + 31), and cell (i, j)
+// is computed at step j + C(i), C(32q + r) = C0(q) + r. Within a round,
+// lane r is one column behind lane r - 1, so the cells above and above-left
+// are lane r - 1's last two cells. Round q + 1 starts Delta(q) steps after
+// round q: late enough for each lane to have finished its row, and at least
+// 32 so that lane 0 trails lane 31's row (handed over through the boundary
+// row). The direction codes of step t are 32 consecutive u16 words, lane
+// r's at word 32t + r.
 struct Band {
     int X, Y, k;
     PA_HDM int d() const { return Y - X; }
-    PA_HDM int jlo(int q) const { return tmax(0, 32 * q - k); }
-    PA_HDM int jhi(int q) const { return tmin(Y - 1, tmin(X - 1, 32 * q + 31) + (Y - X) + k); }
-    PA_HDM int steps(int q) const { return jhi(q) - jlo(q) + 32; }
-    PA_HDM int tiles() const { return (X + 31) >> 5; }
+    PA_HDM int js(int i) const { return tmax(0, i - k); }
+    PA_HDM int je(int i) const { return tmin(Y - 1, i + (Y - X) + k); }
+    PA_HDM int rounds() const { return (X + 31) >> 5; }
     PA_HDM bool in_band(int i, int j) const
     {
         return i >= 0 && j >= 0 && i < X && j < Y && i - j <= k && j - i <= (Y - X) + k;
     }
+    // Delta(q) = max(32, 1 + max over lanes r of je(32q + r) - js(32q + 32 + r))
+    PA_HDM int delta(int q) const
+    {
+        int dl = 32;
+        for (int r = 0; r < 32 && 32 * q + 32 + r < X; r++)
+            dl = tmax(dl, je(32 * q + r) - js(32 * q + 32 + r) + 1);
+        return dl;
+    }
+    // steps of a pass whose last round starts at c0last
+    PA_HDM long long steps(int c0last) const
+    {
+        const int q = rounds() - 1;
+        return (long long)c0last + (X - 1 - 32 * q) + (Y - 1) + 1;
+    }
 };
 
-// One column of a tile's upper row (the states lane 31 leaves for lane 0
-// of the next tile); the gap counters travel in a separate u32 array.
+// C0 of every round of a pass, sequentially (the kernel builds the same
+// table with a warp scan); returns the steps of the pass.
+PA_HD long long rounds_table(const Band& b, int* c0)
+{
+    int c = 0;
+    for (int q = 0; q < b.rounds(); q++) {
+        c0[q] = c;
+        c += b.delta(q);
+    }
+    return b.steps(c0[b.rounds() - 1]);
+}
+
+// One column of a round's last row (the states lane 31 leaves for lane 0
+// of the next round); the gap counters travel in a separate u32 array.
 struct alignas(16) Quad {
     int P, Q, ED, CD;
 };
 
-// A lane's registers during a pass: its last cell (left), the cells above
-// and above-left of the next one, what lane-1 produced last step (nu), and
-// the cost of its last cell.
+// A lane's registers during a pass: its current row i (C(i), its columns,
+// s1[i], s1[i-1]), its last cell (left), the cells above and above-left of
+// its next one, what lane r - 1 produced last step (nu), and the cost of
+// its last cell.
 struct Lane {
     State left, up, diag, nu;
     int lcost;
+    int i, C, js, je, b1, p1;
 };
 
-PA_HD void lane_reset(Lane& L)
+PA_HD void lane_row(Lane& L, const Band& b, const uint8_t* s1, int i, int C)
+{
+    L.i = i;
+    L.C = C;
+    if (i < b.X) {
+        L.js = b.js(i);
+        L.je = b.je(i);
+        L.b1 = s1[i];
+        L.p1 = i > 0 ? s1[i - 1] : 0;
+    } else {  // no row: the lane idles
+        L.js = 1;
+        L.je = 0;
+        L.b1 = L.p1 = 0;
+    }
+}
+
+PA_HD void lane_start(Lane& L, const Band& b, const uint8_t* s1, int lane)
 {
     const State z = {0, 0, 0, 0, 0u};
     L.left = L.up = L.diag = L.nu = z;
     L.lcost = 0;
+    lane_row(L, b, s1, lane, lane);
 }
 
-// Inputs of the lane's cell at step s of tile q (column j): lane 0 reads
-// the tile's upper row (kept for the l2 columns of the pair; the steps past
-// the row's end only drain the tile), every other lane takes what lane-1
-// produced at the previous step, the previous upper cell becoming the
-// diagonal one.
-PA_HD void lane_inputs(Lane& L, int lane, int q, int s, int j, int l2, const Quad* bnd,
-                       const uint32_t* bndg)
+// Step `step` of a pass for lane `lane`: moves the lane to its next row
+// when its row has ended (c0: the rounds table), takes the inputs (lane 0
+// reads the previous round's last row from the boundary row, the others
+// take lane - 1's last cells) and computes the cell. Returns its direction
+// code with its column in jout, or -1 when the lane idles this step (its
+// registers are then never read by a neighbour).
+PA_HD int lane_step(Lane& L, const Tables& t, const uint8_t* s1, const uint8_t* s2,
+                    const Band& b, const int* c0, int lane, long long step, const Quad* bnd,
+                    const uint32_t* bndg, int go, int& jout)
 {
+    int j = (int)(step - L.C);
+    if (j > L.je && L.i + 32 < b.X) {
+        const int q = (L.i >> 5) + 1;
+        lane_row(L, b, s1, L.i + 32, c0[q] + lane);
+        j = (int)(step - L.C);
+    }
+    const bool valid = L.i < b.X && j >= L.js && j <= L.je;
     if (lane == 0) {
-        if (q > 0 && j < l2) {
-            if (s == 0 && j > 0) {
-                const Quad v = bnd[j - 1];
-                L.diag = {v.P, v.Q, v.ED, v.CD, bndg[j - 1]};
+        if (valid && L.i > 0) {
+            if (j == L.js) {
+                if (j > 0) {
+                    const Quad v = bnd[j - 1];
+                    L.diag = {v.P, v.Q, v.ED, v.CD, bndg[j - 1]};
+                }
             } else {
                 L.diag = L.up;
             }
@@ -234,34 +295,26 @@ PA_HD void lane_inputs(Lane& L, int lane, int q, int s, int j, int l2, const Qua
         L.diag = L.up;
         L.up = L.nu;
     }
-}
-
-// The lane's cell (i, j) of a pass at half-width k, b1 = s1[i], p1 =
-// s1[i-1]; returns its direction code, or -1 when (i, j) is outside the
-// band (the lane idles; its registers are then never read by a neighbour).
-PA_HD int lane_cell(Lane& L, const Tables& t, const uint8_t* s2, int l1, int l2, int k, int i,
-                    int j, int b1, int p1, int go)
-{
-    const int d = l2 - l1;
-    if (i >= l1 || j < tmax(0, i - k) || j > tmin(l2 - 1, i + d + k)) return -1;
+    if (!valid) return -1;
+    const int i = L.i, d = b.d();
     const int b2 = s2[j], p2 = j > 0 ? s2[j - 1] : 0;
     State o;
     int dir;
     if (i == 0 && j <= d)
         L.lcost = first_row(t, b2, p2, j, L.lcost, L.left, go, o, dir);
     else
-        L.lcost = cell(t, b1, p1, b2, p2, i, j, i - j == k, j - i == d + k, L.left, L.up, L.diag,
-                       go, o, dir);
+        L.lcost = cell(t, L.b1, L.p1, b2, p2, i, j, i - j == b.k, j - i == d + b.k, L.left, L.up,
+                       L.diag, go, o, dir);
     L.left = o;
+    jout = j;
     return dir;
 }
 
-// u16 words of one pass's direction codes
-PA_HD long long band_words(const Band& b)
+// Word of cell (i, j) in its pass's direction codes.
+PA_HD long long dir_word(const int* c0, int i, int j)
 {
-    long long w = 0;
-    for (int q = 0; q < b.tiles(); q++) w += (long long)b.steps(q) * 32;
-    return w;
+    const int r = i & 31;
+    return ((long long)j + c0[i >> 5] + r) * 32 + r;
 }
 
 // trivial_algn (src/newkkonen.c:1334-1357)
