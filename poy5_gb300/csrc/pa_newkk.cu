@@ -418,7 +418,6 @@ int poyalgn_newkk_algn_affine(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint
     if ((rc = ensure_device(ctx))) return rc;
     ctx->nk_valid = false;
     const size_t cap = (size_t)l1 + l2 + 2;
-    const size_t ni = 1;
     if ((rc = reserve(ctx->seqs, (size_t)l1 + l2))) return rc;
     if ((rc = reserve(ctx->offa, 16))) return rc;
     if ((rc = reserve(ctx->ints, 4 * 10))) return rc;
@@ -444,7 +443,6 @@ int poyalgn_newkk_algn_affine(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint
     std::vector<uint8_t> r(2 * cap);
     CU(cudaMemcpyAsync(r.data(), B, 2 * cap, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    (void)ni;
     if (h[5] != 0) return set_err(POYALGN_EPAIR, "Newkk alignment failed with status %d", h[5]);
     const int L = h[2];
     // swaped: the traceback wrote s1's aligned states to the second slot
