@@ -310,7 +310,8 @@ int poyalgn_newkk_get_k(const poyalgn_ctx *ctx, int32_t *k);
  * (optional) receives the band passes run per pair.
  *
  * poyalgn_newkk_median_batch takes host pointers; the _device variant takes
- * device pointers, max_len >= every sequence length and a cudaStream_t (as
+ * device pointers, max_len >= every sequence length (a longer pair gets
+ * POYALGN_PAIR_TOO_LONG) and a cudaStream_t (as
  * void *), and returns once the batch is done (a batch whose direction codes
  * do not fit the context's arena at once is finished in further launches).
  */

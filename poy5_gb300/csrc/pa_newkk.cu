@@ -163,13 +163,17 @@ __global__ void __launch_bounds__(NK_WARPS * 32) newkk_kernel(NewkkArgs A)
         o.med = A.med + A.out_off[k];
         o.mwg = A.mwg + A.out_off[k];
         o.cap = la + lb + 2;
+        // the boundary row and the rounds table hold max_len columns / rows;
         // the cost matrix covers states below 1 << lcm
-        bool bad = l1 < 1 || l1 > l2;
+        const bool shape = l1 < 1 || l1 > l2;
+        const bool too_long = l2 > A.bnd_stride;
+        bool bad = shape || too_long;
         for (int x = lane; x < l1 + l2 && !bad; x += 32)
             bad = (x < l1 ? s1[x] : s2[x - l1]) >= (1 << t.lcm);
         if (__any_sync(FULL, bad)) {
             if (lane == 0) {
-                A.status[k] = (l1 < 1 || l1 > l2) ? POYALGN_PAIR_EMPTY : POYALGN_PAIR_BAD_STATE;
+                A.status[k] = shape ? POYALGN_PAIR_EMPTY
+                              : too_long ? POYALGN_PAIR_TOO_LONG : POYALGN_PAIR_BAD_STATE;
                 A.cost[k] = A.maxcost[k] = A.alen[k] = A.mlen[k] = A.wlen[k] = 0;
                 if (A.passes) A.passes[k] = 0;
             }
