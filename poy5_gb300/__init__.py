@@ -7,12 +7,12 @@ host-side interface.
 from .align import (Align, BatchResult, Context, CostMatrix, DOSMedian, PackedPairs,
                     PoyAlgnError, count_gaps, deltaw_calc, distance_batch, dos_median,
                     encode, median_batch, pack_pairs)
-from .newkk import NewkkAlign, newkk_median_batch
+from .newkk import NewkkAlign, newkk_distance_batch, newkk_median_batch
 from .serve import ReplayResult, Reply, Server, Trace, poisson_trace
 from .tree import DownpassResult, Store, UppassResult, downpass, tree_levels, uppass
 
 __all__ = ["Align", "BatchResult", "Context", "CostMatrix", "DOSMedian", "PackedPairs",
            "PoyAlgnError", "count_gaps", "deltaw_calc", "dos_median", "encode",
            "median_batch", "pack_pairs", "distance_batch", "DownpassResult", "Store", "downpass", "UppassResult", "uppass",
-           "tree_levels", "NewkkAlign", "newkk_median_batch", "ReplayResult", "Reply", "Server", "Trace", "poisson_trace"]
+           "tree_levels", "NewkkAlign", "newkk_median_batch", "newkk_distance_batch", "ReplayResult", "Reply", "Server", "Trace", "poisson_trace"]
 __version__ = "0.1.0"

@@ -23,8 +23,10 @@ _I64 = C.c_int64
 EINVAL, ENOMEM, ECUDA, EUNSUPPORTED, EPAIR, EBUSY = -1, -2, -3, -4, -5, -6
 PAIR_STATUS = {0: "ok", -2: "output capacity exceeded", -3: "median should not be 0",
                -4: "empty sequence or empty median", -5: "band wider than the largest pipeline",
-               -6: "sequence longer than 65535", -7: "state outside the alphabet",
-               -8: "band doubling did not stop", 1: "not processed"}
+               -6: "sequence too long", -7: "state outside the alphabet",
+               -8: "band doubling did not stop", -9: "speculative pass not run",
+               -11: "closest: a position with no state", -12: "rerun (arena full)",
+               -13: "traceback leaves the band", 1: "not processed"}
 
 
 class PoyAlgnError(RuntimeError):

@@ -76,7 +76,8 @@ class NewkkAlign:
         is the shorter), src/sequence.ml:1879-1901."""
         s1, s2 = _u8(s1), _u8(s2)
         if not cm.affine:
-            raise PoyAlgnError("Algn_Newkk is built for the affine cost model only")
+            raise PoyAlgnError(_lib.EUNSUPPORTED,
+                               "Algn_Newkk is built for the affine cost model only")
         exchange = len(s1) > len(s2)
         a, b = (s2, s1) if exchange else (s1, s2)
         sw = 1 if exchange else 0
@@ -101,3 +102,26 @@ def newkk_median_batch(ctx: Context, cm: CostMatrix, pairs) -> BatchResult:
     return BatchResult(cost=ints[0], maxcost=ints[1], alen=ints[2], mlen=ints[3],
                        wlen=ints[4], status=ints[5], passes=ints[6], out_off=pk.out_off,
                        cap=pk.cap, ea=bufs[0], eb=bufs[1], med=bufs[2], mwg=bufs[3])
+
+
+def newkk_distance_batch(ctx: Context, cm: CostMatrix, pairs, missing_distance: int = 0):
+    """SeqCS.DOS.distance with use_ukk under an affine model (src/seqCS.ml:
+    701-705, 745-747): ``missing_distance`` when either sequence is empty
+    (every position the gap, ``Sequence.is_empty``), otherwise
+    ``NewkkAlign.cost_2`` (src/sequence.ml:1938-1975), the Newkk cost of the
+    pair with the shorter sequence first. Returns an int32 array."""
+    gap = 16
+    pairs = [(_u8(a), _u8(b)) for a, b in pairs]
+    out = np.full(len(pairs), missing_distance, np.int32)
+    live = [k for k, (a, b) in enumerate(pairs)
+            if not (np.all(a == gap) or np.all(b == gap))]
+    if live:
+        res = newkk_median_batch(ctx, cm, [pairs[k] for k in live])
+        # the cost needs the fill only: statuses the traceback or the medians
+        # set (capacity, zero median, off band) leave it valid
+        bad = np.nonzero(~np.isin(res.status, (0, -2, -3, -13)))[0]
+        if len(bad):
+            raise PoyAlgnError(_lib.EPAIR, "pair %d failed with status %d"
+                               % (live[int(bad[0])], int(res.status[bad[0]])))
+        out[live] = res.cost
+    return out

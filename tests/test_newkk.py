@@ -247,3 +247,23 @@ def test_gpu_newkk_per_call_stubs(ctx, oracle):
     lin = pg.CostMatrix.of_list(ctx, [[0 if r == c else 1 for c in range(5)] for r in range(5)], 0)
     with pytest.raises(pg.PoyAlgnError):
         pg.newkk_median_batch(ctx, lin, [(np.array([16, 1], np.uint8), np.array([16, 2], np.uint8))])
+
+
+@pytest.mark.gpu
+def test_gpu_newkk_distance(ctx, oracle):
+    """DOS.distance with use_ukk: missing_distance for an all-gap sequence,
+    otherwise the Newkk cost of the pair (shorter first)."""
+    import poy5_gb300 as pg
+    cm = pg.CostMatrix.of_list(ctx, AFF_TCM, 3)
+    ocm = oracle.cm(tcm=AFF_TCM, gap_open=3)
+    rng = np.random.default_rng(21)
+    pairs = random_pairs(rng, 60, maxlen=300)
+    pairs += [(np.array([16, 16, 16], np.uint8), pairs[0][1]),
+              (pairs[1][0], np.array([16], np.uint8))]
+    got = pg.newkk_distance_batch(ctx, cm, pairs, missing_distance=7)
+    for k, (a, b) in enumerate(pairs):
+        if np.all(a == 16) or np.all(b == 16):
+            assert got[k] == 7, k
+            continue
+        s1, s2 = (a, b) if len(a) <= len(b) else (b, a)
+        assert got[k] == oracle.newkk_align(ocm, s1, s2, 0)[0], k
