@@ -28,6 +28,11 @@
  *   affine entry           src/algn.c:2358-2447
  *   facade                 src/sequence.ml:633-649, 854-925, 1019-1082
  *   DOS.median             src/seqCS.ml:1053-1071
+ *   Algn_Newkk (affine)    src/newkkonen.c:65-873 (cells), 1155-1172 and
+ *                          1334-1446 (passes, trivial case), 1498-1766
+ *                          (tracebacks); NewkkAlign.align_2 and DOS.median
+ *                          with use_ukk, src/sequence.ml:1879-1901,
+ *                          src/seqCS.ml:1043-1051
  */
 #include <limits.h>
 #include <stdint.h>

@@ -47,6 +47,12 @@ def test_oracle_newkk_matches_reference(oracle, model):
     cr, cp = ref.cm(tcm=tcm, gap_open=go), oracle.cm(tcm=tcm, gap_open=go)
     rng = np.random.default_rng(sum(model))
     pairs = edge_pairs() + random_pairs(rng, 80, maxlen=300)
+    # a few long pairs: several 32-row rounds and band passes
+    for L in (900, 1500):
+        a = np.array([16] + list(rng.choice([1, 2, 4, 8], L)), np.uint8)
+        b = a.copy()
+        b[1:][rng.random(L) < 0.12] = 2
+        pairs += [(a, np.concatenate([b[:L // 2], b[L // 2 + 9:]])), (b[:L - 40], a)]
     for k, (a, b) in enumerate(pairs):
         try:
             r = ref.newkk_median(cr, a, b)
