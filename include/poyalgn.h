@@ -145,6 +145,47 @@ int poyalgn_aligned_medians(poyalgn_ctx *ctx, const poyalgn_cm *cm,
                             uint8_t *ancestor, int cap, int32_t *anc_len,
                             uint8_t *median_wg, int32_t *worst);
 
+/*
+ * algn_CAML_verify_2 (src/algn.c:3120-3131 -> algn_verify_2, :3099-3105): the
+ * cost of an aligned pair of length len under cm's cost table, one gap
+ * opening per gap block (algn_calculate_from_2_aligned).
+ */
+int poyalgn_verify_2(poyalgn_ctx *ctx, const poyalgn_cm *cm, const uint8_t *a,
+                     const uint8_t *b, int len, int32_t *cost);
+
+/*
+ * seq_CAML_median_2_no_gaps (src/seq.c:274-285 -> seq_get_median_2d_no_gaps,
+ * :259-272): the median of every column of an aligned pair that is not the
+ * gap, after a leading gap; written back to front into median[cap - n, cap).
+ */
+int poyalgn_median_2_no_gaps(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                             const uint8_t *a, const uint8_t *b, int len,
+                             uint8_t *median, int cap, int32_t *median_len);
+
+/*
+ * algn_CAML_limit_2 (src/algn.c:3160-3185 -> algn_nw_limit, :2954-2964), same
+ * argument order: the whole plane of (s1, s2) is filled; the window arguments
+ * only enter the plane choice, whose height is (s1_len - s2_len) + 50 + w
+ * (h, s1_st and s2_st are unused, as in the reference). The fill is kept for
+ * poyalgn_backtrace_2d / poyalgn_backtrace_2d_limit.
+ */
+int poyalgn_limit_2(poyalgn_ctx *ctx, const poyalgn_cm *cm, const uint8_t *s1,
+                    int l1, const uint8_t *s2, int l2, int w, int h, int s1_st,
+                    int s2_st, int s1_len, int s2_len, int32_t *cost);
+
+/*
+ * algn_CAML_backtrace_2d_limit (src/algn.c:3448-3469): backtrace_2d from cell
+ * (st_s1 + algn_s1, st_s2 + algn_s2). Provided for the call that starts at
+ * the last cell (st_s1 = st_s2 = 0, algn_s1 = l1, algn_s2 = l2), where it is
+ * poyalgn_backtrace_2d; other starts walk the reference's full direction
+ * matrix outside the band and return POYALGN_EUNSUPPORTED.
+ */
+int poyalgn_backtrace_2d_limit(poyalgn_ctx *ctx, const poyalgn_cm *cm,
+                               const uint8_t *s1, int l1, const uint8_t *s2,
+                               int l2, uint8_t *s1p, uint8_t *s2p, int cap,
+                               int32_t *len, int st_s1, int st_s2, int algn_s1,
+                               int algn_s2, int swaped);
+
 /* ---- batched SeqCS.DOS.median ---------------------------------------------- */
 
 /*

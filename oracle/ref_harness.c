@@ -543,3 +543,57 @@ int ref_newkk_median(void *cm, const uint8_t *a, int la, const uint8_t *b,
     freeblk(swg);
     return rc;
 }
+
+/* ---- the remaining per-call externals ------------------------------------ */
+
+value algn_CAML_limit_2(value, value, value, value, value, value, value, value,
+                        value, value);
+value algn_CAML_verify_2(value, value, value);
+value seq_CAML_median_2_no_gaps(value, value, value, value);
+
+/* algn_CAML_limit_2 (src/algn.c:3160), the reference's argument order. */
+int ref_limit_2(void *cm, void *ws, const uint8_t *s1, int l1, const uint8_t *s2,
+                int l2, int w, int h, int s1_st, int s2_st, int s1_len,
+                int s2_len, int *cost)
+{
+    ref_cm *r = (ref_cm *)cm;
+    jmp_buf jb;
+    ref_jmp = &jb;
+    value v1 = mkseq(l1, s1, l1), v2 = mkseq(l2, s2, l2);
+    int rc = 0;
+    if (setjmp(jb))
+        rc = -1;
+    else
+        *cost = Int_val(algn_CAML_limit_2(v1, v2, r->blk, (value)ws, Val_int(w),
+                                          Val_int(h), Val_int(s1_st), Val_int(s2_st),
+                                          Val_int(s1_len), Val_int(s2_len)));
+    ref_jmp = NULL;
+    freeblk(v1);
+    freeblk(v2);
+    return rc;
+}
+
+/* algn_CAML_verify_2 and seq_CAML_median_2_no_gaps on an aligned pair;
+ * out holds len + 1 bytes (front-aligned on return). */
+int ref_verify_and_nogap(void *cm, const uint8_t *a, const uint8_t *b, int len,
+                         int *cost, uint8_t *out, int *outlen)
+{
+    ref_cm *r = (ref_cm *)cm;
+    jmp_buf jb;
+    ref_jmp = &jb;
+    value va = mkseq(len, a, len), vb = mkseq(len, b, len);
+    value vm = mkseq(len + 1, NULL, 0);
+    int rc = 0;
+    if (setjmp(jb)) {
+        rc = -1;
+    } else {
+        *cost = Int_val(algn_CAML_verify_2(va, vb, r->blk));
+        seq_CAML_median_2_no_gaps(va, vb, r->blk, vm);
+        *outlen = getseq(vm, out, len + 1);
+    }
+    ref_jmp = NULL;
+    freeblk(va);
+    freeblk(vb);
+    freeblk(vm);
+    return rc;
+}

@@ -50,6 +50,10 @@ _SIGS = {
     "poyalgn_align_affine_3": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P, _P, _I, _P, _I, _P]),
     "poyalgn_aligned_medians": (_I, [_P, _P, _P, _P, _I, _P, _I, _P, _P, _P]),
     "poyalgn_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
+    "poyalgn_verify_2": (_I, [_P, _P, _P, _P, _I, _P]),
+    "poyalgn_median_2_no_gaps": (_I, [_P, _P, _P, _P, _I, _P, _I, _P]),
+    "poyalgn_limit_2": (_I, [_P, _P, _P, _I, _P, _I] + [_I] * 6 + [_P]),
+    "poyalgn_backtrace_2d_limit": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _I, _P] + [_I] * 5),
     "poyalgn_newkk_median_batch": (_I, [_P, _P, _I] + [_P] * 17),
     "poyalgn_newkk_median_batch_device": (_I, [_P, _P, _I] + [_P] * 6 + [_I] + [_P] * 12),
     "poyalgn_newkk_algn_affine": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),

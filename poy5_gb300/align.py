@@ -237,6 +237,47 @@ class Align:
         p2, p1 = self.extract_edited_2(s2, s1, cm, 1)
         return p1, p2
 
+    def limit_2(self, s1, s2, cm: CostMatrix, w: int, h: int, s1_st: int, s2_st: int,
+                s1_len: int, s2_len: int) -> int:
+        """The ``c_cost_2_limit`` external: algn_CAML_limit_2 (s1 shorter)."""
+        s1, s2 = _u8(s1), _u8(s2)
+        out = C.c_int32()
+        check(self.lib.poyalgn_limit_2(self.ctx.handle, cm.handle, _ptr(s1), len(s1),
+                                       _ptr(s2), len(s2), int(w), int(h), int(s1_st),
+                                       int(s2_st), int(s1_len), int(s2_len), C.byref(out)))
+        return out.value
+
+    def backtrace_2d_limit(self, s1, s2, cm: CostMatrix, st_s1: int, st_s2: int,
+                           algn_s1: int, algn_s2: int, swap: int):
+        """The ``extract_edited_2_limit`` external on the last fill."""
+        s1, s2 = _u8(s1), _u8(s2)
+        cap = len(s1) + len(s2)
+        p1, p2 = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
+        n = C.c_int32()
+        check(self.lib.poyalgn_backtrace_2d_limit(
+            self.ctx.handle, cm.handle, _ptr(s1), len(s1), _ptr(s2), len(s2), _ptr(p1),
+            _ptr(p2), cap, C.byref(n), int(st_s1), int(st_s2), int(algn_s1), int(algn_s2),
+            int(swap)))
+        return p1[cap - n.value:], p2[cap - n.value:]
+
+    def verify_2(self, a, b, cm: CostMatrix) -> int:
+        """algn_CAML_verify_2: cost of an aligned pair under cm's cost table."""
+        a, b = _u8(a), _u8(b)
+        out = C.c_int32()
+        check(self.lib.poyalgn_verify_2(self.ctx.handle, cm.handle, _ptr(a), _ptr(b), len(a),
+                                        C.byref(out)))
+        return out.value
+
+    def median_2_no_gaps(self, a, b, cm: CostMatrix) -> np.ndarray:
+        """seq_CAML_median_2_no_gaps: the non-gap column medians after a gap."""
+        a, b = _u8(a), _u8(b)
+        cap = len(a) + 1
+        out = np.zeros(cap, np.uint8)
+        n = C.c_int32()
+        check(self.lib.poyalgn_median_2_no_gaps(self.ctx.handle, cm.handle, _ptr(a), _ptr(b),
+                                                len(a), _ptr(out), cap, C.byref(n)))
+        return out[cap - n.value:]
+
     # -- affine ----------------------------------------------------------
     def c_align_affine_3(self, si, sj, cm: CostMatrix, swaped: int):
         si, sj = _u8(si), _u8(sj)

@@ -742,6 +742,17 @@ int poyalgn_align_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t
     return 0;
 }
 
+// every state of an aligned pair indexes the cost matrix's tables
+static int check_aligned_states(const poyalgn_cm* cm, const uint8_t* a, const uint8_t* b, int len)
+{
+    const int ns = 1 << cm->h.lcm;
+    for (int i = 0; i < len; i++)
+        if (a[i] >= ns || b[i] >= ns)
+            return set_err(POYALGN_EINVAL, "state %d at position %d outside the alphabet",
+                           a[i] >= ns ? a[i] : b[i], i);
+    return 0;
+}
+
 int poyalgn_aligned_medians(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* a,
                             const uint8_t* b, int len, uint8_t* ancestor, int cap,
                             int32_t* anc_len, uint8_t* median_wg, int32_t* worst)
@@ -750,6 +761,7 @@ int poyalgn_aligned_medians(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_
         return set_err(POYALGN_EINVAL, "null argument");
     if (len < 1) return set_err(POYALGN_EINVAL, "empty alignment");
     int rc;
+    if ((rc = check_aligned_states(cm, a, b, len))) return rc;
     if ((rc = ensure_device(ctx))) return rc;
     if ((rc = reserve(ctx->seqs, (size_t)2 * len))) return rc;
     if ((rc = reserve(ctx->bytes, (size_t)2 * len + 2))) return rc;
@@ -770,6 +782,79 @@ int poyalgn_aligned_medians(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_
     *anc_len = h[0];
     *worst = h[1];
     return 0;
+}
+
+// algn_verify_2 / seq_get_median_2d_no_gaps of an aligned pair on the
+// device: res = {verify cost, no-gap median length}; the median is left in
+// ctx->bytes[0, res[1]).
+static int aligned_extra(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* a,
+                         const uint8_t* b, int len, int res[2])
+{
+    if (!ctx || !cm || !a || !b) return set_err(POYALGN_EINVAL, "null argument");
+    if (len < 1) return set_err(POYALGN_EINVAL, "empty alignment");
+    int rc;
+    if ((rc = check_aligned_states(cm, a, b, len))) return rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    if ((rc = reserve(ctx->seqs, (size_t)2 * len))) return rc;
+    if ((rc = reserve(ctx->bytes, (size_t)len + 1))) return rc;
+    if ((rc = reserve(ctx->ints, 16 * sizeof(int)))) return rc;
+    uint8_t* d = as<uint8_t>(ctx->seqs);
+    CU(cudaMemcpyAsync(d, a, len, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d + len, b, len, cudaMemcpyHostToDevice, ctx->stream));
+    launch_aligned_extra(cm->d, d, d + len, len, as<uint8_t>(ctx->bytes), as<int>(ctx->ints),
+                         ctx->stream);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(res, ctx->ints.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int poyalgn_verify_2(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* a, const uint8_t* b,
+                     int len, int32_t* cost)
+{
+    if (!cost) return set_err(POYALGN_EINVAL, "null argument");
+    int res[2], rc;
+    if ((rc = aligned_extra(ctx, cm, a, b, len, res))) return rc;
+    *cost = res[0];
+    return 0;
+}
+
+int poyalgn_median_2_no_gaps(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* a,
+                             const uint8_t* b, int len, uint8_t* median, int cap,
+                             int32_t* median_len)
+{
+    if (!median || !median_len) return set_err(POYALGN_EINVAL, "null argument");
+    int res[2], rc;
+    if ((rc = aligned_extra(ctx, cm, a, b, len, res))) return rc;
+    if (res[1] > cap) return set_err(POYALGN_EINVAL, "median capacity %d < %d", cap, res[1]);
+    CU(cudaMemcpy(median + cap - res[1], ctx->bytes.p, res[1], cudaMemcpyDeviceToHost));
+    *median_len = res[1];
+    return 0;
+}
+
+int poyalgn_limit_2(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, int l1,
+                    const uint8_t* s2, int l2, int w, int h, int s1_st, int s2_st, int s1_len,
+                    int s2_len, int32_t* cost)
+{
+    (void)h;
+    (void)s1_st;
+    (void)s2_st;
+    // algn_nw_limit fills the whole plane of (s1, s2); the window lengths
+    // only replace the full lengths in the plane choice's height, which
+    // simple_2 computes as (l1 - l2) + 50 + deltawh
+    return poyalgn_simple_2(ctx, cm, s1, l1, s2, l2, w + (s1_len - s2_len) - (l1 - l2), cost);
+}
+
+int poyalgn_backtrace_2d_limit(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, int l1,
+                               const uint8_t* s2, int l2, uint8_t* s1p, uint8_t* s2p, int cap,
+                               int32_t* len, int st_s1, int st_s2, int algn_s1, int algn_s2,
+                               int swaped)
+{
+    if (st_s1 != 0 || st_s2 != 0 || algn_s1 != l1 || algn_s2 != l2)
+        return set_err(POYALGN_EUNSUPPORTED,
+                       "backtrace_2d_limit from a cell other than (len1, len2) walks the "
+                       "reference's full direction matrix outside the band");
+    return poyalgn_backtrace_2d(ctx, cm, s1, l1, s2, l2, s1p, s2p, cap, len, swaped);
 }
 
 int poyalgn_median_batch_device(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,

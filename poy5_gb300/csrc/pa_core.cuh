@@ -1460,8 +1460,12 @@ struct AffDmRow {
     }
 };
 
-// algn_calculate_from_2_aligned on the worst table, bitset alphabet
-PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int L)
+// algn_calculate_from_2_aligned (src/algn.c:3003-3089), bitset alphabet:
+// the cost of an aligned pair under table `cost` (a functor of two
+// states), one gap opening per gap block of either sequence.
+template <class COST>
+PA_HD int aligned_cost_tbl(const Tables& t, const uint8_t* x, const uint8_t* y, int L,
+                           const COST& cost)
 {
     const int gap = t.gap, go = t.go;
     int i = ((gap & x[0]) && (gap & y[0])) ? 1 : 0, res = 0, st = 0;
@@ -1481,9 +1485,44 @@ PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int
                 else st = 0;
             }
         }
-        res += t.worst[(a << t.lcm) + b];
+        res += cost(a, b);
     }
     return res;
+}
+
+struct WorstTbl {
+    const Tables& t;
+    PA_HDM int operator()(int a, int b) const { return t.worst[(a << t.lcm) + b]; }
+};
+struct CostTbl {
+    const Tables& t;
+    PA_HDM int operator()(int a, int b) const { return tcost(t, a, b); }
+};
+
+// algn_worst_2 (src/algn.c:3092-3097): the worst table
+PA_HD int worst_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int L)
+{
+    return aligned_cost_tbl(t, x, y, L, WorstTbl{t});
+}
+
+// algn_verify_2 (src/algn.c:3099-3105): the cost table
+PA_HD int verify_aligned(const Tables& t, const uint8_t* x, const uint8_t* y, int L)
+{
+    return aligned_cost_tbl(t, x, y, L, CostTbl{t});
+}
+
+// seq_get_median_2d_no_gaps (src/seq.c:259-272): the median of every
+// column that is not the gap, after a leading gap; writes out[0, n) (out
+// holds L + 1 bytes) and returns n.
+PA_HD int median_no_gaps(const Tables& t, const uint8_t* x, const uint8_t* y, int L, uint8_t* out)
+{
+    int n = 0;
+    out[n++] = (uint8_t)t.gap;
+    for (int i = 0; i < L; i++) {
+        const int m = t.median[(x[i] << t.lcm) + y[i]];
+        if (m != t.gap) out[n++] = (uint8_t)m;
+    }
+    return n;
 }
 
 // algn_ancestor_2 (src/algn.c:3602-3626) on an aligned pair of length len:

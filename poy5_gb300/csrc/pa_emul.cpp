@@ -533,6 +533,18 @@ int pa_emul_median(void* h, int affine, const uint8_t* a, int la,
     return run_linear(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
 }
 
+// verify_aligned / median_no_gaps / worst_aligned (pa_core.cuh) on an
+// aligned pair, as the per-call kernels run them; out holds len + 1 bytes.
+int pa_emul_aligned_extra(void* h, const uint8_t* a, const uint8_t* b, int len, int* res,
+                          uint8_t* out)
+{
+    const Tables& t = ((Emul*)h)->t;
+    res[0] = verify_aligned(t, a, b, len);
+    res[1] = median_no_gaps(t, a, b, len, out);
+    res[2] = worst_aligned(t, a, b, len);
+    return 0;
+}
+
 // DOS.median with use_ukk (affine) of one pair through the replayed Newkk
 // warp, as newkk_kernel runs it. Outputs end at index cap-1 of each buffer
 // (cap = la + lb + 2); res = {alen, mlen, wlen, maxcost}; returns the status.

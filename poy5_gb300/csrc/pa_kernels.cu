@@ -1379,6 +1379,16 @@ __global__ void aligned_medians_kernel(const Tables* tg, const uint8_t* x, const
     out3[2] = status;
 }
 
+// algn_verify_2 and seq_get_median_2d_no_gaps on an aligned pair (single
+// thread; the per-call stubs of algn_CAML_verify_2 / seq_CAML_median_2_no_gaps).
+__global__ void aligned_extra_kernel(const Tables* tg, const uint8_t* x, const uint8_t* y,
+                                     int len, uint8_t* nogap, int* out2)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    out2[0] = verify_aligned(*tg, x, y, len);
+    out2[1] = median_no_gaps(*tg, x, y, len, nogap);
+}
+
 }  // namespace
 
 using ClassKernel = void (*)(BatchArgs, int);
@@ -1543,6 +1553,12 @@ void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
                             cudaStream_t s)
 {
     aligned_medians_kernel<<<1, 32, 0, s>>>(t, x, y, len, anc, mwg, out3);
+}
+
+void launch_aligned_extra(const Tables* t, const uint8_t* x, const uint8_t* y, int len,
+                          uint8_t* nogap, int* out2, cudaStream_t s)
+{
+    aligned_extra_kernel<<<1, 32, 0, s>>>(t, x, y, len, nogap, out2);
 }
 
 }  // namespace pa

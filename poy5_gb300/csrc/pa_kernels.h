@@ -121,5 +121,8 @@ int class_pipes_per_cta(const Ladder& lad, int affine, int cls, int variant, int
 void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
                             int len, uint8_t* anc, uint8_t* mwg, int* out3,
                             cudaStream_t s);
+// out2 = {verify cost, no-gap median length}; nogap holds len + 1 bytes
+void launch_aligned_extra(const Tables* t, const uint8_t* x, const uint8_t* y, int len,
+                          uint8_t* nogap, int* out2, cudaStream_t s);
 
 }  // namespace pa
