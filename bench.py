@@ -53,6 +53,8 @@ def parse_args(argv=None):
                     default="affine_pairs")
     ap.add_argument("--pairs", type=int, default=0, help="override the pair count")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the untimed check of every pair against the oracle")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the host baseline sample")
     ap.add_argument("--no-autotune", action="store_true",
@@ -63,7 +65,8 @@ def parse_args(argv=None):
                     help="arrival window of each serving rate")
     ap.add_argument("--newkk-arena-mb", type=int, default=0,
                     help="bound the Newkk direction arena (MB; 0: library default)")
-    ap.add_argument("--leg", choices=["main", "downpass", "long", "serving", "distance", "newkk"],
+    ap.add_argument("--leg", choices=["main", "peak", "plain", "downpass", "long", "serving",
+                                      "distance", "newkk"],
                     default="main", help="run one measurement alone and print its object")
     return ap.parse_args(argv)
 
@@ -250,6 +253,12 @@ def run_gpu(args):
         raise RuntimeError(f"{int((status != 0).sum())} pairs failed: {np.unique(status)}")
     passes = d_int[6].cpu().numpy()
     launches_per_step = ctx.last_launches()
+    # the integer issue rates of this GPU (the roofline's measured peak),
+    # measured before the timed region with its own clock sample
+    pclk = ClockSampler(local)
+    pclk.start()
+    peak = pg.int32_rates(local)
+    peak["clocks"] = pclk.stop()
 
     def barrier():
         if world > 1:
@@ -303,6 +312,12 @@ def run_gpu(args):
         d2h = int(7 * 4 * n + 4 * pk.out_bytes)
         e2e = {"seconds": e2e_s, "h2d": h2d, "d2h": d2h}
 
+    # every pair of the timed batch against the oracle (untimed; rank 0)
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = batch_parity(w, pk, [x.cpu().numpy() for x in d_int[:6]],
+                              [x.cpu().numpy() for x in d_out])
+
     # the plain per-call path: one drop-in stub call per pair (sample)
     plain = plain_per_call(ctx, cm, w, seconds=3.0)
 
@@ -317,7 +332,25 @@ def run_gpu(args):
     lib.poyalgn_batch_graph_free(graph)
     return dict(w=w, model=model, n=n, ms=ms, cells=cells, computed=computed, prof=prof,
                 clocks=clk, e2e=e2e, launches=launches_per_step, passes=passes,
-                world=world, rank=rank, pk=pk, plain=plain, tuned=tuned)
+                world=world, rank=rank, pk=pk, plain=plain, tuned=tuned, peak=peak,
+                parity=parity)
+
+
+def batch_parity(w, pk, ints, bufs) -> dict:
+    """Every pair of a GPU batch against the oracle's C restatement run over
+    the same pairs on all host cores: cost, worst cost, aligned pair, median
+    and median with gaps, byte for byte."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    orc = oracle_lib.Oracle("port")
+    ocm = orc.cm(subs=w.subs, indel=w.indel, gap_open=w.gap_open)
+    t0 = time.perf_counter()
+    ref = orc.median_batch(ocm, [a for a, _ in w.pairs], [b for _, b in w.pairs], w.affine,
+                           os.cpu_count() or 1)
+    out = oracle_lib.compare_batch(ref, ints, bufs, pk.out_off, pk.cap)
+    out["against"] = "oracle port, every pair of the timed batch"
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def plain_per_call(ctx, cm, w, seconds: float = 3.0) -> dict:
@@ -443,7 +476,7 @@ def run_uppass(store, cm, t, leaves, down, seqs, orc, ocm, reps: int) -> dict:
             "final_states_match_cpu": bool(same)}
 
 
-def run_long(local: int, cpu_pairs: int = 1) -> dict:
+def run_long(local: int, cpu_pairs: int = 1, parity_pairs: int = 4, n_pairs: int = 512) -> dict:
     """The long-pair stress workload (512 pairs of 20-50 kb, 15% substitutions,
     2% indels, linear 1/2): one timed batch with inputs resident on the
     device, direction bytes written per filled cell as the HBM figure, and
@@ -453,7 +486,7 @@ def run_long(local: int, cpu_pairs: int = 1) -> dict:
     import poy5_gb300 as pg
     from poy5_gb300 import _lib, schedule
     from poy5_gb300 import workloads as wl
-    w = wl.long_pairs()
+    w = wl.long_pairs(n_pairs=n_pairs)
     ctx = pg.Context(local)
     cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
     lib = _lib.load()
@@ -481,6 +514,10 @@ def run_long(local: int, cpu_pairs: int = 1) -> dict:
     e1.record(st)
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1)
+    ctx.profile_begin(1)
+    step()
+    torch.cuda.synchronize(dev)
+    prof = ctx.profile_end()
     status = d_int[5].cpu().numpy()
     passes = d_int[6].cpu().numpy()
     cells = cells_full(w)
@@ -489,6 +526,29 @@ def run_long(local: int, cpu_pairs: int = 1) -> dict:
                                       [gaps(b) for _, b in w.pairs])
     mnz = cm.tables()["min_non0_cost"]
     computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, False, full).sum())
+    # full-length parity: the longest pairs (both sequences past 40 kb)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    longest = [int(k) for k in np.argsort(-(pk.lena.astype(np.int64) + pk.lenb))[:parity_pairs]]
+    sub = [w.pairs[k] for k in longest]
+    spk = pg.pack_pairs(sub)
+    ints = [x.cpu().numpy()[longest] for x in d_int[:6]]
+    host = [x.cpu().numpy() for x in d_out]
+    bufs = []
+    for h, ln in zip(host, (ints[2], ints[2], ints[3], ints[4])):
+        g = np.zeros(spk.out_bytes, np.uint8)
+        for j, k in enumerate(longest):
+            e = int(pk.out_off[k] + pk.cap[k])
+            f = int(spk.out_off[j] + spk.cap[j])
+            g[f - ln[j]:f] = h[e - ln[j]:e]
+        bufs.append(g)
+    porc = oracle_lib.Oracle("port")
+    pcm = porc.cm(subs=w.subs, indel=w.indel)
+    t0 = time.perf_counter()
+    ref = porc.median_batch(pcm, [a for a, _ in sub], [b for _, b in sub], False, len(sub))
+    par = oracle_lib.compare_batch(ref, ints, bufs, spk.out_off, spk.cap)
+    par.update({"against": "oracle port (64-bit indices)", "seconds": round(time.perf_counter() - t0, 1),
+                "min_len": int(min(min(len(a), len(b)) for a, b in sub))})
     # host implementation on the first pair(s), single pair at a time
     orc, kind = host_oracle()
     ocm = orc.cm(subs=w.subs, indel=w.indel)
@@ -502,8 +562,75 @@ def run_long(local: int, cpu_pairs: int = 1) -> dict:
             "status_ok": int((status == 0).sum()), "gcups": round(cells / ms / 1e6, 2),
             "gcups_computed_cells": round(computed / ms / 1e6, 2),
             "dm_write_gbs": round(computed / ms / 1e6, 2), "passes_mean": round(float(passes.mean()), 2),
+            "launch_ms": {k: round(v, 3) for k, v in prof.items() if k != "batches"},
+            "parity": par,
             "cpu_baseline": {"gcups": round(ccells / cpu_s / 1e9, 4), "kind": kind, "cores": 1,
                              "sample": f"first {cpu_pairs} pair(s), one thread"}}
+
+
+def run_plain(local: int, steps: int = 10, warmup: int = 3) -> dict:
+    """The plain pairwise workload (4,096 linear pairs, lengths 200-600, 1 %
+    ambiguity codes; subs 1, indel 2): the batch on device-resident inputs
+    (CUDA graph replay, CUDA events), end to end through
+    poyalgn_median_batch with pinned host buffers, every pair against the
+    oracle, and the oracle on all host cores over the whole batch."""
+    import ctypes as C
+    import torch
+    import poy5_gb300 as pg
+    from poy5_gb300 import _lib
+    from poy5_gb300 import workloads as wl
+    w = wl.plain_pairs()
+    ctx = pg.Context(local)
+    cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+    lib = _lib.load()
+    pk = pg.pack_pairs(w.pairs)
+    n = pk.npairs
+    dev = torch.device("cuda", local)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_in = [t(pk.seqs), t(pk.offa), t(pk.lena), t(pk.offb), t(pk.lenb), t(pk.out_off)]
+    d_int = [torch.zeros(n, dtype=torch.int32, device=dev) for _ in range(7)]
+    d_out = [torch.zeros(pk.out_bytes, dtype=torch.uint8, device=dev) for _ in range(4)]
+    P = lambda x: C.c_void_p(x.data_ptr())
+    st = torch.cuda.current_stream(dev)
+    graph = C.c_void_p()
+    _lib.check(lib.poyalgn_batch_graph_create(
+        ctx.handle, cm.handle, n, pk.max_pair_len, pk.out_bytes, *(P(x) for x in d_in),
+        *(P(x) for x in d_int[:6]), *(P(x) for x in d_out), P(d_int[6]), C.byref(graph)))
+    step = lambda: _lib.check(lib.poyalgn_batch_graph_launch(graph, C.c_void_p(st.cuda_stream)))
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    launches = ctx.last_launches()
+    lib.poyalgn_batch_graph_free(graph)
+    ints = [x.cpu().numpy() for x in d_int[:6]]
+    bufs = [x.cpu().numpy() for x in d_out]
+    # end to end: host buffers, copies inside the call
+    pg.median_batch(ctx, cm, pk)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pg.median_batch(ctx, cm, pk)
+    e2e_s = (time.perf_counter() - t0) / steps
+    cells = cells_full(w)
+    par = batch_parity(w, pk, ints, bufs)
+    cpu = cpu_rate(w, 1e9, os.cpu_count() or 1)  # the whole batch
+    return {"workload": w.name, "pairs": n, "ms": round(ms, 3),
+            "gcups": round(cells / ms / 1e6, 2), "alignments_per_s": round(n / ms * 1e3, 1),
+            "gpu_launches_per_step": launches,
+            "e2e": {"ms": round(e2e_s * 1e3, 3), "gcups": round(cells / e2e_s / 1e9, 2),
+                    "h2d_bytes_per_step": int(pk.seqs.nbytes + 5 * 8 * n),
+                    "d2h_bytes_per_step": int(4 * pk.out_bytes + 28 * n)},
+            "parity": par,
+            "cpu_baseline": {"gcups": round(cpu["cells_per_s"] / 1e9, 4), "kind": cpu["kind"],
+                             "cores": cpu["threads"], "ms": round(cpu["seconds"] * 1e3, 1),
+                             "sample": f"all {cpu['pairs']} pairs",
+                             "alignments_per_s": round(cpu["pairs_per_s"], 1)}}
 
 
 def run_distance(local: int, n_pairs: int = 8192, reps: int = 3) -> dict:
@@ -735,8 +862,13 @@ def gpu_line(args, r) -> dict:
         nsm = torch.cuda.get_device_properties(0).multi_processor_count
     except Exception:
         pass
-    int_peak = nsm * 128 * sm_mhz * 1e6 / 1e12  # Tops: 128 int32 lanes per SM
+    # measured integer issue rate, scaled from the microbenchmark's clock to
+    # the clock sampled during the timed steps
+    pk_ = r["peak"]
+    pmhz = pk_["clocks"].get("sm_mhz") or sm_mhz
+    int_peak = pk_["peak_tops"] * (sm_mhz / pmhz)
     int_ach = r["computed"] * OPS_PER_CELL[model] / (fill_ms * 1e-3) / 1e12
+    nominal = nsm * 128 * sm_mhz * 1e6 / 1e12
     line = {
         "metric": METRIC, "value": round(gcups, 3), "unit": "GCUPS",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -754,18 +886,27 @@ def gpu_line(args, r) -> dict:
         "alignments_per_s": round(pairs / (ms * 1e-3), 1),
         "gcups_computed_cells": round(computed / (ms * 1e-3) / 1e9, 3),
         "gpu_launches": r["launches"] * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "class kernels (fill+traceback), dominant "
-                     + dom, "achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
-                     "frac": round(gbs / hbm_peak, 4) if hbm_peak else None,
+        "roofline": {"bound": "int32", "kernel": "class kernels (band fill), dominant " + dom,
+                     "ops_per_cell": OPS_PER_CELL[model],
+                     "achieved": round(int_ach, 2), "peak": round(int_peak, 2),
+                     "unit": "Tops", "frac": round(int_ach / int_peak, 4),
                      "traffic": (round(r["computed"] * DRAM_BYTES_PER_CELL[model])
                                  if model in DRAM_BYTES_PER_CELL else None),
-                     "traffic_source": "ncu dram bytes per computed cell, 8,192-pair batch, "
-                                       "scaled by computed cells",
-                     "peak_source": "measured" if hbm_peak else None},
-        "roofline_int32": {"bound": "int32 ALU", "ops_per_cell": OPS_PER_CELL[model],
-                           "achieved": round(int_ach, 2), "peak": round(int_peak, 2),
-                           "unit": "Tops", "frac": round(int_ach / int_peak, 4),
-                           "peak_source": "nominal 128 int32 lanes/SM x sampled SM clock"},
+                     "traffic_source": "ncu dram bytes per computed cell (class kernels), "
+                                       "scaled by computed cells; per step",
+                     "peak_source": (f"measured: poyalgn_int32_peak, fastest single-op kind "
+                                     f"({pk_['peak_kind']}) {pk_['peak_tops']:.2f} "
+                                     f"T thread-inst/s at {pmhz:.0f} MHz, scaled to "
+                                     f"{sm_mhz:.0f} MHz"),
+                     "achieved_source": "computed cells x ops per cell / summed class-kernel "
+                                        "event time per step (launch_ms)",
+                     "frac_of_nominal_128_lanes": round(int_ach / nominal, 4)},
+        "int32_rates_tinst_s": {k: round(v["tinst_per_s"], 2)
+                                for k, v in pk_["kinds"].items()},
+        "roofline_hbm": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(gbs / hbm_peak, 4) if hbm_peak else None,
+                         "bytes": "direction bytes per computed cell + sequences + outputs",
+                         "peak_source": "measured" if hbm_peak else None},
         "launch_ms": {k: round(v / nb, 3) for k, v in prof.items() if k != "batches"},
         "clocks": {"sm_mhz": clk.get("sm_mhz"), "sm_max_mhz": clk.get("sm_max_mhz"),
                    "reasons": clk.get("reasons")},
@@ -775,6 +916,8 @@ def gpu_line(args, r) -> dict:
                            "sample": f"first {r['plain']['pairs']} pairs, one stub call each"},
         "batched_over_plain": round(gcups / max(r["plain"]["gcups"], 1e-9), 1),
     }
+    if r["parity"]:
+        line["parity"] = r["parity"]
     if r["e2e"]:
         e = r["e2e"]
         e_s = reduce_max(e["seconds"], world)
@@ -790,10 +933,18 @@ def main(argv=None):
     if args.leg != "main" and args.impl == "gpu":
         import torch
         torch.cuda.set_device(local)
-        if args.leg == "downpass":
+        if args.leg == "peak":
+            import poy5_gb300 as pg
+            clk = ClockSampler(local)
+            clk.start()
+            out = pg.int32_rates(local)
+            out["clocks"] = clk.stop()
+        elif args.leg == "plain":
+            out = run_plain(local)
+        elif args.leg == "downpass":
             out = run_downpass(local)
         elif args.leg == "long":
-            out = run_long(local)
+            out = run_long(local, n_pairs=args.pairs or 512)
         elif args.leg == "serving":
             out = run_serving(local, args.serve_seconds)
         elif args.leg == "newkk":
@@ -839,6 +990,7 @@ def main(argv=None):
             "sample": f"first {cpu['pairs']} pairs of {r['w'].name} ({cpu['seconds']:.1f} s)",
             "alignments_per_s": round(cpu["pairs_per_s"], 2)}
         if world == 1 and not args.no_extras:
+            line["plain_pairs"] = run_plain(local)
             line["downpass"] = run_downpass(local)
             line["long_pairs"] = run_long(local)
             line["distance"] = run_distance(local)

@@ -38,11 +38,13 @@ extern "C" {
 
 /* Per-pair status codes written by the batched entry points. */
 #define POYALGN_PAIR_OK 0
-#define POYALGN_PAIR_CAPACITY -2   /* output capacity exceeded */
+#define POYALGN_PAIR_CAPACITY -2   /* output capacity exceeded (a device batch pair
+                                      whose slot ends past out_bytes) */
 #define POYALGN_PAIR_ZERO_MEDIAN -3 /* "median should not be 0" (src/algn.c:3619) */
 #define POYALGN_PAIR_EMPTY -4      /* empty sequence / empty median (POY UB) */
 #define POYALGN_PAIR_TOO_WIDE -5   /* band wider than the largest pipeline */
-#define POYALGN_PAIR_TOO_LONG -6   /* sequence longer than 65535 */
+#define POYALGN_PAIR_TOO_LONG -6   /* sequence longer than 65535, or a device batch
+                                      pair with lena + lenb > max_pair_len */
 #define POYALGN_PAIR_BAD_STATE -7  /* a state outside the cost matrix's alphabet */
 #define POYALGN_PAIR_NO_CONVERGE -8 /* band doubling did not stop (e.g. all costs 0) */
 #define POYALGN_PAIR_INTERNAL -9   /* a speculative band pass was queued but did not run */
@@ -201,6 +203,10 @@ int poyalgn_backtrace_2d_limit(poyalgn_ctx *ctx, const poyalgn_cm *cm,
  * call); poyalgn_median_batch_device takes device pointers and a cudaStream_t
  * (as void *) and only enqueues work; max_pair_len bounds lena + lenb and
  * out_bytes bounds out_off[k] + cap_k (the size of each output buffer).
+ * Both size device scratch, so they are checked on the device per pair: a
+ * pair with lena + lenb > max_pair_len gets POYALGN_PAIR_TOO_LONG, one whose
+ * slot ends past out_bytes POYALGN_PAIR_CAPACITY; such a pair reads and
+ * writes nothing, and the other pairs of the batch are unaffected.
  * passes (optional) receives the band iterations run per pair.
  */
 int poyalgn_median_batch(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
@@ -289,7 +295,8 @@ int poyalgn_cost_affine_3(poyalgn_ctx *ctx, const poyalgn_cm *cm,
  * and the linear model Align.cost_2 ~deltaw:(max 8 |la - lb|)
  * (src/sequence.ml:868-925) -> algn_CAML_simple_2's band doubling, without
  * traceback. Layout as poyalgn_median_batch; per-pair cost and status.
- * The _device form takes device pointers and a stream and only enqueues.
+ * The _device form takes device pointers and a stream and only enqueues; a
+ * pair with lena + lenb > max_pair_len gets POYALGN_PAIR_TOO_LONG.
  */
 int poyalgn_distance_batch(poyalgn_ctx *ctx, const poyalgn_cm *cm, int npairs,
                            const uint8_t *seqs, const int64_t *offa,
@@ -660,11 +667,30 @@ int poyalgn_last_launches(const poyalgn_ctx *ctx);
  * the next max_batches batches records CUDA events on its own stream around
  * its prep launch and each pipeline-class launch. poyalgn_profile_end waits
  * for them and writes, per launch slot (prep, class 0 .. class N-1, N =
- * poyalgn_num_classes()), the summed milliseconds into ms[N + 1].
+ * poyalgn_num_classes()), the summed milliseconds into ms[N + 1]; the prep
+ * slot of a batch that runs speculative band passes also holds that sweep.
  */
 int poyalgn_profile_begin(poyalgn_ctx *ctx, int max_batches);
 int poyalgn_profile_end(poyalgn_ctx *ctx, float *ms, int *batches);
 int poyalgn_num_classes(void);
+
+/*
+ * Integer issue-rate microbenchmark (no POY counterpart): the measured peak
+ * against which the fill kernels' int32 roofline is reported. Runs one
+ * instruction kind back to back at full occupancy on `device` (iters loop
+ * trips of 128 instructions per thread; 2048 threads per SM) and writes the
+ * thread-instructions per second of the timed launch (CUDA events, after one
+ * untimed launch), its duration and its instruction count. Kinds: 32-bit
+ * add, two-way signed min, bitwise logic, DPX three-way signed min
+ * (__vimin3_s32) and DPX packed u16 three-way max (__vimax3_u16x2).
+ */
+#define POYALGN_PEAK_ADD 0
+#define POYALGN_PEAK_MIN 1
+#define POYALGN_PEAK_LOGIC 2
+#define POYALGN_PEAK_MIN3 3
+#define POYALGN_PEAK_MAX3_U16X2 4
+int poyalgn_int32_peak(int device, int kind, int iters, double *inst_per_s,
+                       float *ms, int64_t *thread_inst);
 
 #ifdef __cplusplus
 }

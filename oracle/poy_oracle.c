@@ -6,7 +6,7 @@
  * CPU checker of the CUDA library. Only tests/, __graft_entry__.smoke() and
  * bench.py's CPU-baseline arm load it; the product never links it.
  *
- * Parity pin: tests/test_oracle_vs_ref.py compares every function here with
+ * Parity pin: tests/test_oracle.py compares every function here with
  * the reference algn.c compiled unmodified (oracle/_ref), and the committed
  * golden fixtures in tests/golden/ were generated from that build.
  *

@@ -8,11 +8,13 @@ from .align import (Align, BatchResult, Context, CostMatrix, DOSMedian, PackedPa
                     PoyAlgnError, count_gaps, deltaw_calc, distance_batch, dos_median,
                     encode, median_batch, pack_pairs)
 from .newkk import NewkkAlign, newkk_distance_batch, newkk_median_batch
+from .peak import int32_rates
 from .serve import ReplayResult, Reply, Server, Trace, poisson_trace
 from .tree import DownpassResult, Store, UppassResult, downpass, tree_levels, uppass
 
 __all__ = ["Align", "BatchResult", "Context", "CostMatrix", "DOSMedian", "PackedPairs",
            "PoyAlgnError", "count_gaps", "deltaw_calc", "dos_median", "encode",
            "median_batch", "pack_pairs", "distance_batch", "DownpassResult", "Store", "downpass", "UppassResult", "uppass",
-           "tree_levels", "NewkkAlign", "newkk_median_batch", "newkk_distance_batch", "ReplayResult", "Reply", "Server", "Trace", "poisson_trace"]
+           "tree_levels", "NewkkAlign", "newkk_median_batch", "newkk_distance_batch", "ReplayResult", "Reply", "Server", "Trace", "poisson_trace",
+           "int32_rates"]
 __version__ = "0.1.0"

@@ -96,6 +96,7 @@ _SIGS = {
     "poyalgn_profile_begin": (_I, [_P, _I]),
     "poyalgn_profile_end": (_I, [_P, _P, _P]),
     "poyalgn_num_classes": (_I, []),
+    "poyalgn_int32_peak": (_I, [_I, _I, _I, _P, _P, _P]),
 }
 
 _lib = None

@@ -191,6 +191,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     A.offb = offb;
     A.lenb = lenb;
     A.npairs = npairs;
+    A.max_pair_len = maxmn;
+    A.out_bytes = out_total;
     A.affine = affine;
     A.do_traceback = do_traceback;
     A.distance = distance;
@@ -250,14 +252,15 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
 
     int launches = 0;
     cudaEvent_t* ev = nullptr;
-    if (!capturing && !spec_S && c->prof_used < c->prof_cap) {
+    if (!capturing && c->prof_used < c->prof_cap) {
         ev = &c->prof_ev[(size_t)c->prof_used * (NCLASS + 2)];
         c->prof_used++;
         CU(cudaEventRecord(ev[0], st));
     }
     launch_prep(A, st);
     launches++;
-    if (ev) CU(cudaEventRecord(ev[1], st));
+    // the prep slot of a speculative batch also holds its speculative sweep
+    if (ev && !spec_S) CU(cudaEventRecord(ev[1], st));
     const int sort_grid = std::max(1, std::min(2 * c->nsm, (items + 255) / 256));
     auto sweep = [&]() -> int {
         for (int k = 0; k < NCLASS; k++) {
@@ -300,6 +303,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         A.spec = 0;
         launch_spec_resolve(A, st);
         launches++;
+        if (ev) CU(cudaEventRecord(ev[1], st));
     }
     if ((rc = sweep())) return rc;
     if (A.dm_cap > 0) {
@@ -1446,6 +1450,8 @@ extern "C" int poyalgn_median_batch_device_noalloc(
     A.offb = reinterpret_cast<const long long*>(offb);
     A.lenb = lenb;
     A.npairs = npairs;
+    A.max_pair_len = max_pair_len;
+    A.out_bytes = out_bytes;
     A.affine = affine;
     A.do_traceback = 1;
     A.lad = lad;

@@ -4,7 +4,7 @@
 // Everything in this header is plain arithmetic on registers and pointers so
 // that the same code is compiled into the CUDA kernels (pa_kernels.cu) and,
 // for testing only, into a host build that replays the lane pipeline one lane
-// at a time (pa_emul.cpp).
+// at a time (tests/pa_emul.cpp).
 //
 // Fill layout ("lane pipeline"): a pipeline of P lanes (one CTA of P/32
 // warps) aligns one pair. Lane g owns blocks of R consecutive rows; block b of
@@ -1252,6 +1252,21 @@ PA_HD int count_gap_states(const uint8_t* s, int len, int gap)
     int n = 0;
     for (int i = 0; i < len; i++) n += (s[i] >= gap && (s[i] & gap)) ? 1 : 0;
     return n;
+}
+
+// Per-pair bounds of a batch, checked before a pair touches any buffer
+// sized by the caller's declared shape: every direction slab holds a fill of
+// m + n <= max_pair_len, and pair k's outputs and its affine row-0 shadow
+// occupy [out_off, out_off + la + lb + 2) of buffers of out_bytes bytes
+// (has_out = 0: the batch writes no per-pair outputs). Returns 0 when the
+// pair fits, else the pair's status: -6 (longer than declared) or -2 (its
+// output slot leaves the buffers).
+PA_HD int pair_bounds_status(int la, int lb, int max_pair_len, long long out_off,
+                             long long out_bytes, int has_out)
+{
+    if (la < 0 || lb < 0 || (long long)la + lb > (long long)max_pair_len) return -6;
+    if (has_out && (out_off < 0 || out_off + la + lb + 2 > out_bytes)) return -2;
+    return 0;
 }
 
 struct PairPlan {

@@ -1102,6 +1102,19 @@ __global__ void prep_kernel(BatchArgs A)
     const int k = A.order ? A.order[wk] : wk;
     const Tables& t = *A.tables;
     const int la = A.lena[k], lb = A.lenb[k];
+    // a pair outside the caller's declared shape would overrun a direction
+    // slab or its output slot: it fails before any read or write of its own
+    const int oob = pair_bounds_status(la, lb, A.max_pair_len, A.out_off ? A.out_off[k] : 0,
+                                       A.out_bytes, A.out_off != nullptr);
+    if (oob) {
+        if (lane == 0) {
+            A.passes[k] = 0;
+            A.lastcls[k] = -1;
+            if (A.dm_off) A.dm_off[k] = -1;
+            A.status[k] = oob;
+        }
+        return;
+    }
     const uint8_t* a = A.seqs + A.offa[k];
     const uint8_t* b = A.seqs + A.offb[k];
     // every state must index the 1 << lcm tables

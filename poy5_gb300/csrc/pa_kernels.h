@@ -21,6 +21,11 @@ struct BatchArgs {
     const long long* offb;
     const int* lenb;
     int npairs;
+    // the caller's declared shape: lena + lenb <= max_pair_len sizes every
+    // direction slab, out_off[k] + lena + lenb + 2 <= out_bytes every output
+    // slot and the affine row-0 shadow; prep fails a pair outside either
+    int max_pair_len;
+    long long out_bytes;
     int affine;
     int do_traceback;          // 0: keep the last fill in the slab (per-call stubs)
     int distance;              // DOS.distance: deltaw = max 8 |la - lb|, all-gap -> missing

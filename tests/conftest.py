@@ -27,12 +27,12 @@ def gpu_available() -> bool:
 def build_emulator() -> str:
     """Host replay of the kernels' lane pipeline (test-only library)."""
     csrc = os.path.join(ROOT, "poy5_gb300", "csrc")
-    srcs = [os.path.join(csrc, f) for f in ("pa_emul.cpp", "pa_tables.cpp")]
+    srcs = [os.path.join(ROOT, "tests", "pa_emul.cpp"), os.path.join(csrc, "pa_tables.cpp")]
     deps = srcs + [os.path.join(csrc, f) for f in ("pa_core.cuh", "pa_tables.h", "pa_newkk.cuh")]
     if (not os.path.exists(EMUL_SO) or
             any(os.path.getmtime(d) > os.path.getmtime(EMUL_SO) for d in deps)):
         os.makedirs(os.path.dirname(EMUL_SO), exist_ok=True)
-        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared",
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", csrc,
                         "-Wno-unknown-pragmas", "-o", EMUL_SO, *srcs], check=True)
     return EMUL_SO
 

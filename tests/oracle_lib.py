@@ -246,3 +246,40 @@ class Oracle:
         return dict(cost=ints[0], maxcost=ints[1], alen=ints[2], mlen=ints[3],
                     wlen=ints[4], status=ints[5], ea=bufs[0], eb=bufs[1],
                     med=bufs[2], mwg=bufs[3], out_off=out_off)
+
+
+def compare_batch(ref: dict, ints, bufs, out_off, cap, chunk: int = 4096) -> dict:
+    """Pairs of a GPU batch that differ from the oracle's median_batch on the
+    same pairs. ints = (cost, maxcost, alen, mlen, wlen, status) and bufs =
+    (ea, eb, med, mwg) as the batched entry points return them (each output
+    ending at out_off + cap - 1); the oracle writes each from out_off on.
+    Returns the count of differing pairs and the first few indices."""
+    out_off = np.asarray(out_off, np.int64)
+    cap = np.asarray(cap, np.int64)
+    names = ("cost", "maxcost", "alen", "mlen", "wlen")
+    bad = np.asarray(ref["status"]) != 0
+    bad |= np.asarray(ints[5]) != 0
+    for name, g in zip(names, ints[:5]):
+        bad |= np.asarray(ref[name]) != np.asarray(g)
+    lens = {"ea": ref["alen"], "eb": ref["alen"], "med": ref["mlen"], "mwg": ref["wlen"]}
+    for lo in range(0, len(cap), chunk):
+        hi = min(lo + chunk, len(cap))
+        ok = ~bad[lo:hi]
+        ks = np.arange(lo, hi)[ok]
+        if len(ks) == 0:
+            continue
+        for name, g in zip(("ea", "eb", "med", "mwg"), bufs):
+            n = np.asarray(lens[name])[ks].astype(np.int64)
+            if n.sum() == 0:
+                continue
+            pair = np.repeat(np.arange(len(ks)), n)
+            start = np.repeat(np.cumsum(n) - n, n)
+            pos = np.arange(int(n.sum())) - start
+            o = out_off[ks][pair] + pos
+            gi = (out_off[ks] + cap[ks] - n)[pair] + pos
+            diff = np.asarray(ref[name])[o] != np.asarray(g)[gi]
+            if diff.any():
+                bad[ks[np.unique(pair[diff])]] = True
+    idx = np.flatnonzero(bad)
+    return {"pairs": int(len(cap)), "mismatches": int(len(idx)),
+            "first": [int(i) for i in idx[:8]]}

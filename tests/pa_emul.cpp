@@ -584,4 +584,12 @@ int pa_emul_newkk_median(void* h, const uint8_t* a, int la, const uint8_t* b, in
     return r.status;
 }
 
+// The per-pair bounds check prep_kernel runs before a pair touches any
+// buffer (pair_bounds_status): 0, -6 or -2.
+int pa_emul_pair_bounds(int la, int lb, int max_pair_len, long long out_off,
+                        long long out_bytes, int has_out)
+{
+    return pair_bounds_status(la, lb, max_pair_len, out_off, out_bytes, has_out);
+}
+
 }  // extern "C"

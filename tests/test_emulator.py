@@ -117,3 +117,24 @@ def test_pipeline_random_tables(emul, oracle):
             r = oracle.median(cm, a, b, go > 0)
             assert (cost, mx) == (r.cost, r.maxcost)
             assert np.array_equal(med, r.median) and np.array_equal(ea, r.ea)
+
+
+def test_pair_bounds_status(emul):
+    """prep_kernel's per-pair guard (pair_bounds_status): a pair longer than
+    the batch's declared max_pair_len (-6) or whose output slot runs past
+    out_bytes (-2) fails before it touches a slab, an output or the shadow."""
+    f = emul.pa_emul_pair_bounds
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int]
+    cases = [
+        ((100, 200, 300, 0, 302, 1), 0),        # exactly fits both bounds
+        ((100, 201, 300, 0, 10_000, 1), -6),    # one position past max_pair_len
+        ((100, 200, 300, 0, 301, 1), -2),       # slot one byte past out_bytes
+        ((100, 200, 300, 500, 801, 1), -2),
+        ((100, 200, 300, 499, 801, 1), 0),
+        ((100, 200, 300, -1, 10_000, 1), -2),   # negative offset
+        ((100, 200, 300, 1 << 40, 0, 0), 0),    # no outputs: out_off unused
+        ((-1, 5, 300, 0, 100, 1), -6),          # negative length
+        ((2_000_000_000, 2_000_000_000, 2_147_483_647, 0, 1 << 40, 1), -6),  # no int overflow
+    ]
+    for args, want in cases:
+        assert f(*args) == want, (args, want)
