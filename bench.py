@@ -65,6 +65,9 @@ def parse_args(argv=None):
                     help="arrival window of each serving rate")
     ap.add_argument("--newkk-arena-mb", type=int, default=0,
                     help="bound the Newkk direction arena (MB; 0: library default)")
+    ap.add_argument("--mem-gb", type=float, default=0.0,
+                    help="cap each context's direction slabs and traceback arena (GB; 0: "
+                         "library defaults), e.g. to keep a profiled case small")
     ap.add_argument("--leg", choices=["main", "peak", "plain", "downpass", "long", "serving",
                                       "distance", "newkk"],
                     default="main", help="run one measurement alone and print its object")
@@ -210,6 +213,8 @@ def run_gpu(args):
     w = make_workload(args.workload, args.pairs, rank)
     model = "affine" if w.affine else "linear"
     ctx = pg.Context(local)
+    if args.mem_gb:
+        ctx.set_memory_budget(int(args.mem_gb * 2**30), int(args.mem_gb * 2**30))
     cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
     lib = _lib.load()
     pk = pg.pack_pairs(w.pairs)
@@ -476,7 +481,8 @@ def run_uppass(store, cm, t, leaves, down, seqs, orc, ocm, reps: int) -> dict:
             "final_states_match_cpu": bool(same)}
 
 
-def run_long(local: int, cpu_pairs: int = 1, parity_pairs: int = 4, n_pairs: int = 512) -> dict:
+def run_long(local: int, cpu_pairs: int = 1, parity_pairs: int = 4, n_pairs: int = 512,
+             mem_gb: float = 0.0) -> dict:
     """The long-pair stress workload (512 pairs of 20-50 kb, 15% substitutions,
     2% indels, linear 1/2): one timed batch with inputs resident on the
     device, direction bytes written per filled cell as the HBM figure, and
@@ -488,6 +494,8 @@ def run_long(local: int, cpu_pairs: int = 1, parity_pairs: int = 4, n_pairs: int
     from poy5_gb300 import workloads as wl
     w = wl.long_pairs(n_pairs=n_pairs)
     ctx = pg.Context(local)
+    if mem_gb:
+        ctx.set_memory_budget(int(mem_gb * 2**30), int(mem_gb * 2**30))
     cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
     lib = _lib.load()
     pk = pg.pack_pairs(w.pairs)
@@ -944,7 +952,7 @@ def main(argv=None):
         elif args.leg == "downpass":
             out = run_downpass(local)
         elif args.leg == "long":
-            out = run_long(local, n_pairs=args.pairs or 512)
+            out = run_long(local, n_pairs=args.pairs or 512, mem_gb=args.mem_gb)
         elif args.leg == "serving":
             out = run_serving(local, args.serve_seconds)
         elif args.leg == "newkk":

@@ -102,7 +102,10 @@ void poyalgn_cm_free(poyalgn_cm *cm);
  * algn_CAML_simple_2 (src/algn.c:3133-3158): cost of aligning s1 (the
  * shorter, l1 <= l2) with s2 under a linear cost matrix, band doubling seeded
  * with deltawh (algn_nw, src/algn.c:2954-2975). The fill stays in the
- * context for poyalgn_backtrace_2d.
+ * context for poyalgn_backtrace_2d. l1 > l2 returns POYALGN_EUNSUPPORTED: the
+ * reference compiles out its assertion that s1 is the shorter
+ * (src/algn.c:25, 1139) and runs its band arithmetic with a negative length
+ * difference; Sequence.cost_2 never passes that order.
  */
 int poyalgn_simple_2(poyalgn_ctx *ctx, const poyalgn_cm *cm, const uint8_t *s1,
                      int l1, const uint8_t *s2, int l2, int deltawh,
@@ -176,11 +179,16 @@ int poyalgn_limit_2(poyalgn_ctx *ctx, const poyalgn_cm *cm, const uint8_t *s1,
                     int s2_st, int s1_len, int s2_len, int32_t *cost);
 
 /*
- * algn_CAML_backtrace_2d_limit (src/algn.c:3448-3469): backtrace_2d from cell
- * (st_s1 + algn_s1, st_s2 + algn_s2). Provided for the call that starts at
- * the last cell (st_s1 = st_s2 = 0, algn_s1 = l1, algn_s2 = l2), where it is
- * poyalgn_backtrace_2d; other starts walk the reference's full direction
- * matrix outside the band and return POYALGN_EUNSUPPORTED.
+ * algn_CAML_backtrace_2d_limit (src/algn.c:3448-3469): backtrace_2d from a
+ * start given by (st_s1, st_s2, algn_s1, algn_s2), over the fill of the last
+ * simple_2 / limit_2 call on the same pair, with the reference's arithmetic:
+ * the walk starts at cell (algn_s1 - 1, st_s2 + algn_s2 - 1) of the row-major
+ * matrix of row stride l2, takes s1 / s2 at counters that start at
+ * st_s1 + algn_s1 and st_s2 + algn_s2, and ends when its linear index drops
+ * below st_s2. From the last cell (0, 0, l1, l2) it is poyalgn_backtrace_2d.
+ * A walk that reaches a cell the last fill never wrote returns
+ * POYALGN_EUNSUPPORTED (the reference reads what earlier alignments left in
+ * its workspace there); one whose counters leave the sequences POYALGN_EINVAL.
  */
 int poyalgn_backtrace_2d_limit(poyalgn_ctx *ctx, const poyalgn_cm *cm,
                                const uint8_t *s1, int l1, const uint8_t *s2,
@@ -638,6 +646,17 @@ int poyalgn_set_row_tile(poyalgn_ctx *ctx, int mode);
  */
 #define POYALGN_SPEC_MAX_PASSES 16
 int poyalgn_set_speculation(poyalgn_ctx *ctx, int mode, int passes);
+
+/*
+ * Caps on the device scratch a context's batches reserve (no counterpart in
+ * the reference): slab_bytes bounds the direction slabs (default: half of
+ * the free memory at the batch, at most 128 GB; a smaller cap runs a wide
+ * class in more rounds), arena_bytes the deferred-traceback arena (default:
+ * the free memory less 16 GB, at most 64 GB; fills that do not fit trace
+ * back in their slab). 0 keeps a default. Results never depend on either.
+ */
+int poyalgn_set_memory_budget(poyalgn_ctx *ctx, int64_t slab_bytes,
+                              int64_t arena_bytes);
 
 /*
  * A CUDA graph of poyalgn_median_batch_device's launch sequence for fixed

@@ -20,7 +20,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF_SRC = "/root/reference/src"
+# where the POY 5.1.1 sources are (POY_REF_SRC, or --ref-src): this recipe
+# compiles the reference unit from them in place; without them only the port
+# is built
+DEFAULT_REF_SRC = os.environ.get("POY_REF_SRC", "/root/reference/src")
 
 
 def _run(cmd):

@@ -367,6 +367,38 @@ int ref_backtrace_2d(void *cm, void *ws, const uint8_t *s1, int l1,
     return rc;
 }
 
+/* algn_CAML_backtrace_2d_limit (src/algn.c:3448) from (st_s1, st_s2,
+ * algn_s1, algn_s2) on the workspace left by the last simple_2 / limit_2. */
+value algn_CAML_backtrace_2d_limit(value, value, value, value, value, value, value,
+                                   value, value, value, value);
+int ref_backtrace_2d_limit(void *cm, void *ws, const uint8_t *s1, int l1,
+                           const uint8_t *s2, int l2, int st_s1, int st_s2,
+                           int algn_s1, int algn_s2, int swaped, uint8_t *r1,
+                           uint8_t *r2, int cap, int *len)
+{
+    ref_cm *r = (ref_cm *)cm;
+    jmp_buf jb;
+    ref_jmp = &jb;
+    value v1 = mkseq(l1, s1, l1), v2 = mkseq(l2, s2, l2);
+    value p1 = mkseq(cap, NULL, 0), p2 = mkseq(cap, NULL, 0);
+    int rc = 0;
+    if (setjmp(jb)) {
+        rc = -1;
+    } else {
+        algn_CAML_backtrace_2d_limit(v1, v2, p1, p2, (value)ws, r->blk, Val_int(st_s1),
+                                     Val_int(st_s2), Val_int(algn_s1), Val_int(algn_s2),
+                                     Val_bool(swaped));
+        *len = getseq(p1, r1, cap);
+        getseq(p2, r2, cap);
+    }
+    ref_jmp = NULL;
+    freeblk(v1);
+    freeblk(v2);
+    freeblk(p1);
+    freeblk(p2);
+    return rc;
+}
+
 /*
  * SeqCS.DOS.median, linear cost model, Algn_Normal (seqCS.ml:1059-1071):
  * align_2 (cost_2 + create_edited_2), ancestor_2, median_2_with_gaps and

@@ -89,6 +89,7 @@ _SIGS = {
     "poyalgn_distance_batch_device": (_I, [_P, _P, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "poyalgn_set_row_tile": (_I, [_P, _I]),
     "poyalgn_set_speculation": (_I, [_P, _I, _I]),
+    "poyalgn_set_memory_budget": (_I, [_P, _I64, _I64]),
     "poyalgn_batch_graph_create": (_I, [_P, _P, _I, _I, _I64] + [_P] * 17 + [C.POINTER(_P)]),
     "poyalgn_batch_graph_launch": (_I, [_P, _P]),
     "poyalgn_batch_graph_free": (None, [_P]),

@@ -82,6 +82,10 @@ class Context:
         (default); `passes` bands of each pair run at once."""
         check(_lib.load().poyalgn_set_speculation(self._h, int(mode), int(passes)))
 
+    def set_memory_budget(self, slab_bytes: int = 0, arena_bytes: int = 0):
+        """Cap the direction slabs and the deferred-traceback arena (0: default)."""
+        check(_lib.load().poyalgn_set_memory_budget(self._h, int(slab_bytes), int(arena_bytes)))
+
     def profile_begin(self, max_batches: int):
         """Record per-launch CUDA events for the next `max_batches` batches."""
         check(_lib.load().poyalgn_profile_begin(self._h, int(max_batches)))

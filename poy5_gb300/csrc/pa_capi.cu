@@ -136,8 +136,11 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if (!capturing) {
         size_t free_b = 0, total_b = 0;
         CU(cudaMemGetInfo(&free_b, &total_b));
-        total_budget = std::min<long long>((long long)(free_b / 2), 64LL << 30);
+        // half of the free memory, at most 128 GB: the widest long-pair
+        // classes (512 pairs of 50 kb on 256-lane pipelines) fit in one round
+        total_budget = std::min<long long>((long long)(free_b / 2), 128LL << 30);
         if (c->slab_budget > 0) total_budget = std::min(total_budget, c->slab_budget);
+        if (c->slab_cap > 0) total_budget = std::min(total_budget, c->slab_cap);
         c->last_budget = total_budget;
     }
     const long long budget = total_budget;
@@ -173,6 +176,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         dm_cap = std::max<long long>(0, std::min({free_now - (16LL << 30), 64LL << 30, want}));
         if (capturing) dm_cap = std::min<long long>(dm_cap, (long long)c->dmarena.n);
         if (c->dm_fixed > 0) dm_cap = std::min(dm_cap, c->dm_fixed);
+        if (c->arena_cap > 0) dm_cap = std::min(dm_cap, c->arena_cap);
         if ((rc = reserve(c->dmarena, (size_t)std::max<long long>(dm_cap, 256)))) return rc;
         if ((rc = reserve(c->dmoff, (size_t)npairs * 8))) return rc;
         if ((rc = reserve(c->dmctr, 8))) return rc;
@@ -667,7 +671,10 @@ int poyalgn_simple_2(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, 
 {
     if (!ctx || !cm || !s1 || !s2 || !cost) return set_err(POYALGN_EINVAL, "null argument");
     if (l1 < 1 || l2 < 1) return set_err(POYALGN_EINVAL, "empty sequence");
-    if (l1 > l2) return set_err(POYALGN_EINVAL, "pass the shorter sequence first");
+    if (l1 > l2)  // the reference's assert (src/algn.c:1139) is compiled out there
+        return set_err(POYALGN_EUNSUPPORTED,
+                       "s1 (%d) longer than s2 (%d): the band arithmetic of algn_fill_plane_2 "
+                       "assumes the shorter sequence first", l1, l2);
     int rc;
     ctx->call_valid = false;
     if ((rc = ensure_device(ctx))) return rc;
@@ -675,6 +682,7 @@ int poyalgn_simple_2(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, 
     if ((rc = fill_pair(ctx, cm, 0, l1, l2, &deltawh, cost))) return rc;
     ctx->call_valid = true;
     ctx->call_affine = 0;
+    ctx->call_dwh = deltawh;
     ctx->call_cm = cm;
     ctx->call_l1 = l1;
     ctx->call_l2 = l2;
@@ -854,11 +862,63 @@ int poyalgn_backtrace_2d_limit(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uin
                                int32_t* len, int st_s1, int st_s2, int algn_s1, int algn_s2,
                                int swaped)
 {
-    if (st_s1 != 0 || st_s2 != 0 || algn_s1 != l1 || algn_s2 != l2)
+    if (st_s1 == 0 && st_s2 == 0 && algn_s1 == l1 && algn_s2 == l2)
+        return poyalgn_backtrace_2d(ctx, cm, s1, l1, s2, l2, s1p, s2p, cap, len, swaped);
+    if (!ctx || !cm || !s1 || !s2 || !s1p || !s2p || !len)
+        return set_err(POYALGN_EINVAL, "null argument");
+    if (!ctx->call_valid || ctx->call_affine || ctx->call_l1 != l1 || ctx->call_l2 != l2 ||
+        memcmp(ctx->call_s1.data(), s1, l1) || memcmp(ctx->call_s2.data(), s2, l2))
+        return set_err(POYALGN_EINVAL,
+                       "backtrace_2d_limit needs the fill of simple_2 / limit_2 on the same pair");
+    int rc;
+    if ((rc = ensure_device(ctx))) return rc;
+    // the walk writes at most one column per counter step: l1 + l2 columns
+    const int wcap = l1 + l2 + 2;
+    uint8_t* bytes = as<uint8_t>(ctx->bytes);  // staged with 4 (l1 + l2 + 2) bytes
+    int* out2 = as<int>(ctx->ints) + 8;
+    LimitWalk w;
+    w.t = cm->d;
+    w.slab = as<uint8_t>(ctx->slab);
+    w.strides = as<long long>(ctx->strides);
+    w.lastcls = as<int>(ctx->lastcls);
+    w.slab_cta = as<int>(ctx->slabcta);
+    w.passes = as<int>(ctx->ints) + 6;  // written by the kept fill
+    w.pfull = as<int>(ctx->pfull);
+    w.lad = ctx->lad[0];
+    w.s1 = as<uint8_t>(ctx->seqs);
+    w.s2 = as<uint8_t>(ctx->seqs) + l1;
+    w.l1 = l1;
+    w.l2 = l2;
+    w.deltawh = ctx->call_dwh;
+    w.st_s1 = st_s1;
+    w.st_s2 = st_s2;
+    w.algn_s1 = algn_s1;
+    w.algn_s2 = algn_s2;
+    w.swaped = swaped ? 1 : 0;
+    w.cap = wcap;
+    w.r1 = bytes;
+    w.r2 = bytes + wcap;
+    w.out2 = out2;
+    launch_limit_walk(w, ctx->stream);
+    CU(cudaGetLastError());
+    int h[2];
+    CU(cudaMemcpyAsync(h, out2, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (h[0] == -14)
         return set_err(POYALGN_EUNSUPPORTED,
-                       "backtrace_2d_limit from a cell other than (len1, len2) walks the "
-                       "reference's full direction matrix outside the band");
-    return poyalgn_backtrace_2d(ctx, cm, s1, l1, s2, l2, s1p, s2p, cap, len, swaped);
+                       "backtrace_2d_limit from (%d, %d, %d, %d) reaches a cell the last fill "
+                       "never wrote (the reference reads what earlier alignments left there)",
+                       st_s1, st_s2, algn_s1, algn_s2);
+    if (h[0] == -15)
+        return set_err(POYALGN_EINVAL, "backtrace_2d_limit start (%d, %d, %d, %d) leaves the "
+                       "sequences", st_s1, st_s2, algn_s1, algn_s2);
+    if (h[0] != 0) return set_err(POYALGN_EINVAL, "backtrace_2d_limit walk failed (%d)", h[0]);
+    const int L = h[1];
+    if (L > cap) return set_err(POYALGN_EINVAL, "capacity %d < aligned length %d", cap, L);
+    CU(cudaMemcpy(s1p + cap - L, bytes + wcap - L, L, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(s2p + cap - L, bytes + 2 * wcap - L, L, cudaMemcpyDeviceToHost));
+    *len = L;
+    return 0;
 }
 
 int poyalgn_median_batch_device(poyalgn_ctx* ctx, const poyalgn_cm* cm, int npairs,
@@ -979,6 +1039,14 @@ int poyalgn_profile_end(poyalgn_ctx* ctx, float* ms, int* batches)
 }
 
 int poyalgn_num_classes(void) { return NCLASS; }
+
+int poyalgn_set_memory_budget(poyalgn_ctx* ctx, int64_t slab_bytes, int64_t arena_bytes)
+{
+    if (!ctx || slab_bytes < 0 || arena_bytes < 0) return set_err(POYALGN_EINVAL, "bad budget");
+    ctx->slab_cap = slab_bytes;
+    ctx->arena_cap = arena_bytes;
+    return 0;
+}
 
 struct poyalgn_graph {
     cudaGraph_t graph = nullptr;

@@ -1453,6 +1453,68 @@ PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
     return lin_traceback_dm(rd, t, x, m, y, n, swaped, o);
 }
 
+// algn_CAML_backtrace_2d_limit from any start: backtrace_2d with st_s1,
+// st_s2, algn_s1, algn_s2 (src/algn.c:3277-3327, 3448-3469) over the kept
+// linear fill of s1 (m rows) against s2 (n columns) with band b. The walk
+// keeps the reference's own arithmetic on a row-major matrix of row stride
+// n: it starts at linear index st_s2 + n (algn_s1 - 1) + algn_s2 - 1, moves
+// by -(n + 1) on ALIGN, -1 on an insertion and -n on a deletion (insertion
+// before deletion when swaped, deletion first otherwise), takes s1 / s2 at
+// counters that start at st_s1 + algn_s1 and st_s2 + algn_s2, and ends when
+// the index drops below st_s2. Row 0 holds ALIGN at column 0 and INSERT up
+// to its filled length. The pair is written back to front into
+// r1 / r2[cap - len, cap). Returns 0; -2 when cap is exceeded; -14 when the
+// walk reaches a cell the last fill never wrote (the reference reads what
+// earlier alignments left in its workspace there); -15 when a counter
+// leaves its sequence.
+template <class DM>
+PA_HD int lin_limit_walk(DM& rd, const LinBand& b, const uint8_t* s1, const uint8_t* s2,
+                         int gap, int st_s1, int st_s2, int algn_s1, int algn_s2,
+                         int swaped, uint8_t* r1, uint8_t* r2, int cap, int* len)
+{
+    const long long l = b.n;
+    long long idx = (long long)st_s2 + l * (algn_s1 - 1) + algn_s2 - 1;
+    long long a1 = (long long)algn_s1 + st_s1, a2 = (long long)algn_s2 + st_s2;
+    int k = cap;
+    *len = 0;
+    while (idx >= st_s2) {
+        if (idx < 0) return -14;
+        const long long i = idx / l, j = idx - i * l;
+        int d;
+        if (i >= b.m) return -14;
+        if (i == 0) {
+            if (j >= b.first) return -14;
+            d = j == 0 ? L_ALIGN : L_INSERT;
+        } else {
+            if (j < lin_s(b, (int)i) || j > lin_e(b, (int)i)) return -14;
+            d = rd((int)i, (int)j);
+        }
+        if (k <= 0) return -2;
+        int x, y;
+        if (d & L_ALIGN) {
+            if (a1 < 1 || a1 > b.m || a2 < 1 || a2 > b.n) return -15;
+            x = s1[--a1];
+            y = s2[--a2];
+            idx -= l + 1;
+        } else if (swaped ? (d & L_INSERT) != 0 : !(d & L_DELETE)) {
+            if (a2 < 1 || a2 > b.n) return -15;
+            x = gap;
+            y = s2[--a2];
+            idx -= 1;
+        } else {
+            if (a1 < 1 || a1 > b.m) return -15;
+            x = s1[--a1];
+            y = gap;
+            idx -= l;
+        }
+        k--;
+        r1[k] = (uint8_t)x;
+        r2[k] = (uint8_t)y;
+    }
+    *len = cap - k;
+    return 0;
+}
+
 // Direction flags of cell (i, j) from a slab of aff_step words or of lean
 // bytes.
 struct AffDmWords {

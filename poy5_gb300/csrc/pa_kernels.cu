@@ -1574,4 +1574,30 @@ void launch_aligned_extra(const Tables* t, const uint8_t* x, const uint8_t* y, i
     aligned_extra_kernel<<<1, 32, 0, s>>>(t, x, y, len, nogap, out2);
 }
 
+namespace {
+
+__global__ void limit_walk_kernel(LimitWalk a)
+{
+    const Tables& t = *a.t;
+    const int cls = a.lastcls[0] & LASTCLS_MASK;
+    // the final pass's band: T doubled once per pass after the first
+    const PairPlan pl = plan_linear_deltawh(t, a.l1, a.l2, a.deltawh);
+    const int full = a.pfull[0] & 1;
+    const long long T = (long long)pl.T0 << tmax(a.passes[0] - 1, 0);
+    const LinBand b = lin_band(pl.m, pl.n, full, full ? 0 : band_p((int)T, pl.m, pl.n));
+    LinDmBytes rd{a.slab + (long long)a.slab_cta[0] * a.strides[cls], a.lad.P[cls],
+                  a.lad.R[cls]};
+    int len = 0;
+    a.out2[0] = lin_limit_walk(rd, b, a.s1, a.s2, t.gap, a.st_s1, a.st_s2, a.algn_s1,
+                               a.algn_s2, a.swaped, a.r1, a.r2, a.cap, &len);
+    a.out2[1] = len;
+}
+
+}  // namespace
+
+void launch_limit_walk(const LimitWalk& a, cudaStream_t s)
+{
+    limit_walk_kernel<<<1, 1, 0, s>>>(a);
+}
+
 }  // namespace pa

@@ -130,4 +130,26 @@ void launch_aligned_medians(const Tables* t, const uint8_t* x, const uint8_t* y,
 void launch_aligned_extra(const Tables* t, const uint8_t* x, const uint8_t* y, int len,
                           uint8_t* nogap, int* out2, cudaStream_t s);
 
+// backtrace_2d_limit from any start (lin_limit_walk) over the fill the
+// per-call path kept in its slab: s1 = l1 rows, s2 = l2 columns, planned with
+// the caller's deltawh. One thread; out2 = {walk status, length}; r1 / r2
+// end at index cap - 1.
+struct LimitWalk {
+    const Tables* t;
+    const uint8_t* slab;
+    const long long* strides;  // slab bytes per pipeline of each class
+    const int* lastcls;
+    const int* slab_cta;
+    const int* passes;
+    const int* pfull;
+    Ladder lad;
+    const uint8_t* s1;
+    const uint8_t* s2;
+    int l1, l2, deltawh, st_s1, st_s2, algn_s1, algn_s2, swaped, cap;
+    uint8_t* r1;
+    uint8_t* r2;
+    int* out2;
+};
+void launch_limit_walk(const LimitWalk& a, cudaStream_t s);
+
 }  // namespace pa

@@ -75,6 +75,8 @@ struct poyalgn_ctx {
     // upper bound on the direction-slab arena of one batch (0: half the free
     // device memory, at most 64 GB)
     long long slab_budget = 0;
+    // caller's caps (poyalgn_set_memory_budget; 0: the defaults below)
+    long long slab_cap = 0, arena_cap = 0;
     long long last_budget = 1LL << 30;  // slab budget of the last uncaptured batch
     long long last_free = 0;            // free memory seen by it (arena included)
     // optional per-launch timing: one event before the prep launch and one
@@ -84,6 +86,7 @@ struct poyalgn_ctx {
     // per-call stub state: the fill of the last simple_2 / align_affine_3
     bool call_valid = false;
     int call_affine = 0, call_l1 = 0, call_l2 = 0;
+    int call_dwh = 0;  // deltawh of the kept linear fill (its plane choice)
     const poyalgn_cm* call_cm = nullptr;
     std::vector<uint8_t> call_s1, call_s2;
     long long call_strides[pa::NCLASS] = {0};

@@ -287,22 +287,21 @@ struct Emul {
     int row_tile = 1;  // lean bands up to 512 wide on the row tile (0: lane pipeline)
 };
 
-int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb,
-               int* cost, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
-               int cap, int* res, int* passes, int* last_class)
+// The band doubling of plan pl (x = rows, y = columns), as the class
+// kernels run it: the final fill stays in dm (P lanes x R rows) with band bd.
+int lin_fill_doubling(const Emul& E, const PairPlan& pl, const uint8_t* x, const uint8_t* y,
+                      std::vector<uint8_t>& dm, int& P, int& R, LinBand& bd, int* cost,
+                      int* passes, int* last_class)
 {
     const Tables& t = E.t;
-    PairPlan pl = plan_linear(t, count_gap_states(a, la, t.gap), la,
-                              count_gap_states(b, lb, t.gap), lb);
-    const uint8_t* x = pl.swaped ? b : a;
-    const uint8_t* y = pl.swaped ? a : b;
     const int m = pl.m, n = pl.n;
-    std::vector<uint8_t> dm;
-    int P = 32, R = 1, T = pl.T0, g = 0;
+    int T = pl.T0, g = 0;
+    P = 32;
+    R = 1;
     *passes = 0;
     *last_class = -1;
     for (;;) {
-        LinBand bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
+        bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
         int c = pick_class(E.lad[0], lin_wu(bd), n);
         if (c < 0) return -5;
         P = E.lad[0].P[c];
@@ -323,9 +322,26 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
                 default: lin_pass<8>(bd, P, t, x, y, dm.data(), cost, &g); break;
             }
         }
-        if (pl.full || lin_done(T, m, n, g)) break;
+        if (pl.full || lin_done(T, m, n, g)) return 0;
         T *= 2;
     }
+}
+
+int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb,
+               int* cost, uint8_t* ea, uint8_t* eb, uint8_t* med, uint8_t* mwg,
+               int cap, int* res, int* passes, int* last_class)
+{
+    const Tables& t = E.t;
+    PairPlan pl = plan_linear(t, count_gap_states(a, la, t.gap), la,
+                              count_gap_states(b, lb, t.gap), lb);
+    const uint8_t* x = pl.swaped ? b : a;
+    const uint8_t* y = pl.swaped ? a : b;
+    const int m = pl.m, n = pl.n;
+    std::vector<uint8_t> dm;
+    int P, R;
+    LinBand bd;
+    const int st = lin_fill_doubling(E, pl, x, y, dm, P, R, bd, cost, passes, last_class);
+    if (st) return st;
     PairOut o = {ea, eb, med, mwg, cap};
     PairRes r = lin_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
     res[0] = r.alen;
@@ -582,6 +598,26 @@ int pa_emul_newkk_median(void* h, const uint8_t* a, int la, const uint8_t* b, in
     res[2] = r.wlen;
     res[3] = r.maxcost;
     return r.status;
+}
+
+// algn_CAML_simple_2 (caller's deltawh, s1 down the rows) followed by
+// algn_CAML_backtrace_2d_limit from (st_s1, st_s2, algn_s1, algn_s2), as the
+// per-call path runs them: the walk of lin_limit_walk over the kept fill.
+// r1 / r2 end at index cap - 1; returns the walk's status.
+int pa_emul_limit_walk(void* h, const uint8_t* s1, int l1, const uint8_t* s2, int l2,
+                       int deltawh, int st_s1, int st_s2, int algn_s1, int algn_s2,
+                       int swaped, uint8_t* r1, uint8_t* r2, int cap, int* len, int* cost)
+{
+    const Emul& E = *(Emul*)h;
+    const PairPlan pl = plan_linear_deltawh(E.t, l1, l2, deltawh);
+    std::vector<uint8_t> dm;
+    int P, R, passes, cls;
+    LinBand bd;
+    const int st = lin_fill_doubling(E, pl, s1, s2, dm, P, R, bd, cost, &passes, &cls);
+    if (st) return st;
+    LinDmBytes rd{dm.data(), P, R};
+    return lin_limit_walk(rd, bd, s1, s2, E.t.gap, st_s1, st_s2, algn_s1, algn_s2, swaped, r1,
+                          r2, cap, len);
 }
 
 // The per-pair bounds check prep_kernel runs before a pair touches any

@@ -110,3 +110,26 @@ def test_errors_are_loud(ctx):
         al.c_align_affine_3(long_, short, cm, 0)  # "pass the shorter one as first"
     with pytest.raises(pg.PoyAlgnError):
         al.extract_edited_2(pg.encode("AC"), pg.encode("ACGA"), _cm(ctx, STD_TCM, 0), 0)
+
+
+@pytest.mark.parametrize("name", golden_lib.NAMES)
+def test_adopted_reference_tables_match_golden(ctx, name):
+    """poyalgn_cm_adopt, the route the POY stub library takes a struct cm by:
+    the reference's own tables from the golden file (as cm_CAML_create and
+    the OCaml setters left them: lcm 5, gap 16, 31 states with combinations)
+    give the golden results."""
+    import poy5_gb300 as pg
+    g = golden_lib.load(name)
+    t = g.tables
+    cm = pg.CostMatrix.adopt(ctx, 5, 16, 31, 1, 1 if g.affine else 0, g.gap_open,
+                             t["cost"], t["median"], t["worst"], t["tail"], t["prepend"])
+    back = cm.tables()
+    for key, want in t.items():
+        assert np.array_equal(back[key], want), key
+    res = pg.median_batch(ctx, cm, g.pairs)
+    assert np.all(res.status == 0), res.status
+    for k in range(len(g.pairs)):
+        d = res.pair(k)
+        bad = golden_lib.mismatches(g, k, d.cost, d.aligned_a, d.aligned_b, d.median,
+                                    d.median_wg, d.maxcost)
+        assert not bad, (name, k, bad)
