@@ -1453,6 +1453,61 @@ PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
     return lin_traceback_dm(rd, t, x, m, y, n, swaped, o);
 }
 
+// A window of a linear slab for a traceback that one warp runs together
+// (every lane walks the same path over the same data): the codes of rows
+// [ilo, itop] on anti-diagonals (Ttop - LW_DIAG, Ttop], refilled by all
+// lanes at once whenever the walk leaves it, so that a refill costs one
+// round of independent loads instead of one dependent load per step. A path
+// that enters at (itop, Ttop) stays inside for LW_DIAG - 1 anti-diagonals:
+// each step lowers T by 1 or 2 and the row by at most 1. Row i of
+// anti-diagonal T is byte (i - 1) mod (P R) of the step's P R bytes
+// (dm_index), so the window's rows are LW_WORDS consecutive words (modulo
+// the step) of every anti-diagonal. Needs P R a power of two of at least
+// LW_ROWS and a 4-byte aligned slab (linear pipelines of 32 lanes or more).
+constexpr int LW_DIAG = 64;
+constexpr int LW_ROWS = 64;
+constexpr int LW_WORDS = LW_ROWS / 4 + 1;
+constexpr int LW_SMEM_WORDS = LW_DIAG * LW_WORDS;
+
+struct LinDmWindow {
+    const uint8_t* dm;
+    uint32_t* win;   // LW_SMEM_WORDS words (shared memory on the device)
+    int prm;         // P R - 1
+    int prw;         // words per anti-diagonal, P R / 4
+    int lane, nl;    // this lane, and the lanes that refill together
+    int Ttop = -1, ilo = 0, itop = -1, w0 = 0;
+
+    PA_HDM void refill(int i, int T)
+    {
+#if defined(__CUDA_ARCH__)
+        __syncwarp();  // every lane is done with the old window
+#endif
+        Ttop = T;
+        itop = i;
+        ilo = i - LW_ROWS + 1 > 1 ? i - LW_ROWS + 1 : 1;
+        w0 = ((ilo - 1) & prm) >> 2;
+        const uint32_t* d32 = reinterpret_cast<const uint32_t*>(dm);
+        for (int e = lane; e < LW_SMEM_WORDS; e += nl) {
+            const int dd = e / LW_WORDS, c = e - dd * LW_WORDS;
+            const int t = Ttop - dd;
+            win[e] = t >= 1 ? d32[(long long)t * prw + ((w0 + c) & (prw - 1))] : 0u;
+        }
+#if defined(__CUDA_ARCH__)
+        __syncwarp();
+#endif
+    }
+    PA_HDM int operator()(int i, int j)
+    {
+        const int T = i + j;
+        if (T > Ttop || T <= Ttop - LW_DIAG || i < ilo || i > itop) refill(i, T);
+        const int off = (i - 1) & prm;
+        const int w = ((off >> 2) - w0) & (prw - 1);
+        return (int)((win[(Ttop - T) * LW_WORDS + w] >> ((off & 3) * 8)) & 0xFFu);
+    }
+};
+
+PA_HD bool lin_window_ok(int P, int R) { return P * R >= LW_ROWS && P >= 32; }
+
 // algn_CAML_backtrace_2d_limit from any start: backtrace_2d with st_s1,
 // st_s2, algn_s1, algn_s2 (src/algn.c:3277-3327, 3448-3469) over the kept
 // linear fill of s1 (m rows) against s2 (n columns) with band b. The walk

@@ -510,6 +510,17 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                     A.cost[w.k] = cost;
                     A.status[w.k] = 0;
                 }
+            } else if (lin_window_ok(p.P, R)) {
+                // the pipeline's first warp walks the path through a shared
+                // window of the slab (one round of loads per LW_DIAG steps)
+                if (p.gl < 32) {
+                    extern __shared__ uint32_t lin_win[];
+                    LinDmWindow rd{dm, lin_win + (p.K == 1 ? (threadIdx.x >> 5) : 0) * LW_SMEM_WORDS,
+                                   p.P * R - 1, p.P * R / 4, p.lane, 32};
+                    const PairRes r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.swaped,
+                                                       pair_out(A, w.k));
+                    if (p.gl == 0) finish_pair(A, w.k, cost, r);
+                }
             } else if (p.gl == 0) {
                 const PairRes r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
                                                 pair_out(A, w.k));
@@ -518,6 +529,15 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
         }
         pipe_sync(p);
     }
+}
+
+// Dynamic shared memory of a class launch: the traceback windows of linear
+// pipelines of 32 lanes or more (one per pipeline of the CTA).
+int class_dyn_smem(const Ladder& lad, int affine, int cls)
+{
+    if (affine || !lin_window_ok(lad.P[cls], lad.R[cls])) return 0;
+    const int pipes = ladder_K(lad, cls) == 1 ? NARROW_WARPS : 1;
+    return pipes * LW_SMEM_WORDS * (int)sizeof(uint32_t);
 }
 
 // ---------------------------------------------------------------------------
@@ -1451,7 +1471,7 @@ int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant, int
     const int K = ladder_K(lad, cls), R = lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, class_kernel(affine, R, variant, K == 1),
-                                                  threads, 0);
+                                                  threads, class_dyn_smem(lad, affine, cls));
     return n;
 }
 
@@ -1515,7 +1535,9 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
     }
     const int K = ladder_K(a.lad, cls), R = a.lad.R[cls];
     const int threads = K == 1 ? 32 * NARROW_WARPS : 32 * K;
-    class_kernel(a.affine, R, a.affine ? variant : 0, K == 1)<<<grid, threads, 0, s>>>(a, cls);
+    class_kernel(a.affine, R, a.affine ? variant : 0, K == 1)<<<grid, threads,
+                                                               class_dyn_smem(a.lad, a.affine, cls),
+                                                               s>>>(a, cls);
 }
 
 void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s)

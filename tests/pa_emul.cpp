@@ -343,7 +343,14 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     const int st = lin_fill_doubling(E, pl, x, y, dm, P, R, bd, cost, passes, last_class);
     if (st) return st;
     PairOut o = {ea, eb, med, mwg, cap};
-    PairRes r = lin_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    PairRes r;
+    if (lin_window_ok(P, R)) {  // as the class kernel does: through the shared window
+        std::vector<uint32_t> win(LW_SMEM_WORDS);
+        LinDmWindow rd{dm.data(), win.data(), P * R - 1, P * R / 4, 0, 1};
+        r = lin_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
+    } else {
+        r = lin_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    }
     res[0] = r.alen;
     res[1] = r.mlen;
     res[2] = r.wlen;
@@ -618,6 +625,44 @@ int pa_emul_limit_walk(void* h, const uint8_t* s1, int l1, const uint8_t* s2, in
     LinDmBytes rd{dm.data(), P, R};
     return lin_limit_walk(rd, bd, s1, s2, E.t.gap, st_s1, st_s2, algn_s1, algn_s2, swaped, r1,
                           r2, cap, len);
+}
+
+// The band doubling of one linear pair (DOS.median's plan) pass by pass:
+// T, the gap count of the pass's fill and its pipeline class, for at most
+// maxp passes; returns the number of passes (or a negative status).
+int pa_emul_lin_passes(void* h, const uint8_t* a, int la, const uint8_t* b, int lb, int* Ts,
+                       int* gaps, int* classes, int maxp)
+{
+    const Emul& E = *(Emul*)h;
+    const Tables& t = E.t;
+    PairPlan pl = plan_linear(t, count_gap_states(a, la, t.gap), la,
+                              count_gap_states(b, lb, t.gap), lb);
+    const uint8_t* x = pl.swaped ? b : a;
+    const uint8_t* y = pl.swaped ? a : b;
+    const int m = pl.m, n = pl.n;
+    std::vector<uint8_t> dm;
+    int T = pl.T0, np = 0;
+    for (;;) {
+        LinBand bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
+        int c = pick_class(E.lad[0], lin_wu(bd), n);
+        if (c < 0) return -5;
+        const int P = E.lad[0].P[c], R = E.lad[0].R[c];
+        dm.assign((size_t)(m + n + 1) * P * R, 0);
+        int cost = 0, g = 0;
+        switch (R) {
+            case 2: lin_pass<2>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+            case 4: lin_pass<4>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+            default: lin_pass<8>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+        }
+        if (np < maxp) {
+            Ts[np] = T;
+            gaps[np] = g;
+            classes[np] = c;
+        }
+        np++;
+        if (pl.full || lin_done(T, m, n, g)) return np;
+        T *= 2;
+    }
 }
 
 // The per-pair bounds check prep_kernel runs before a pair touches any

@@ -138,3 +138,26 @@ def test_pair_bounds_status(emul):
     ]
     for args, want in cases:
         assert f(*args) == want, (args, want)
+
+
+def test_window_traceback_on_wide_classes(emul, oracle):
+    """Longer, more divergent linear pairs, whose final bands need pipelines
+    of 64-256 lanes: their tracebacks run through the shared-memory window
+    (LinDmWindow, refilled every LW_DIAG anti-diagonals) and must match the
+    oracle byte for byte."""
+    from poy5_gb300 import workloads as wl
+    rng = np.random.default_rng(77)
+    e = Emu(emul, STD_TCM, 0)
+    cm = oracle.cm(tcm=STD_TCM)
+    classes = set()
+    for L, sub, ind in ((1500, 0.15, 0.03), (2500, 0.2, 0.05), (3000, 0.1, 0.08)):
+        core = wl.random_bases(rng, L)
+        a = wl.with_gap(core)
+        b = wl.with_gap(wl.mutate(rng, core, sub, ind))
+        cost, ea, eb, med, mwg, mx, cls = e.median(a, b)
+        classes.add(cls)
+        r = oracle.median(cm, a, b, False)
+        assert (cost, mx) == (r.cost, r.maxcost)
+        assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb)
+        assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
+    assert max(classes) >= 6, classes
