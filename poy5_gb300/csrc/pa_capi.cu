@@ -70,6 +70,14 @@ constexpr int SPEC_MAX_PAIRS = 32;
 // Largest arena region one pair's fills in one class may take; wider fills
 // (long pairs) keep the pipeline's slab and trace back in the class kernel.
 constexpr long long DM_MAX_REGION = 64LL << 20;
+// The second speculative sweep (linear batches with pairs of at least
+// SPEC2_MIN_LEN positions together): the traced final pass of each pair
+// takes a region of up to DM_MAX_REGION2, from an arena of up to
+// ARENA_MAX_SPEC2 (64 GB otherwise).
+constexpr int SPEC2_MIN_LEN = 8192;
+constexpr long long DM_MAX_REGION2 = 512LL << 20;
+constexpr long long ARENA_MAX = 64LL << 30;
+constexpr long long ARENA_MAX_SPEC2 = 192LL << 30;
 
 // Enqueue one batch on `st`. All pointers are device pointers. `out_total`
 // bounds out_off[k] + cap_k (sizes the affine row-0 scratch).
@@ -101,7 +109,12 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     const int row_tile = affine && !spec_S &&
                          (c->row_tile_mode == 1 ||
                           (c->row_tile_mode == 2 && npairs <= ROW_TILE_MAX_PAIRS * c->nsm));
-    const int items = npairs * std::max(1, spec_S);  // queue capacity
+    // long linear pairs: every pass after the first sweep up to the predicted
+    // final one runs at once in a second speculative sweep
+    const bool spec2 = spec_S > 0 && !affine && maxmn >= SPEC2_MIN_LEN;
+    // queue capacity: a sweep queues at most spec_S passes of a pair, the
+    // second one at most SPEC_STRIDE
+    const int items = npairs * std::max(spec2 ? SPEC_STRIDE : 1, spec_S);
     if ((rc = reserve(c->pfull, (size_t)npairs * 4))) return rc;
     if ((rc = reserve(c->eh0, (size_t)npairs * 4))) return rc;
     if ((rc = reserve(c->lastcls, (size_t)npairs * 4))) return rc;
@@ -114,13 +127,15 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * items * sizeof(int2)))) return rc;
     if ((rc = reserve(c->qctr, QCTR_INTS * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
+    const size_t spec_items = (size_t)npairs * SPEC_STRIDE;  // every pass by its index
     if (spec_S) {
-        DevBuf* per_pair[] = {&c->spec_t0, &c->spec_n};
+        DevBuf* per_pair[] = {&c->spec_t0, &c->spec_n, &c->spec_tstar};
         for (DevBuf* b : per_pair)
             if ((rc = reserve(*b, (size_t)npairs * 4))) return rc;
-        if ((rc = reserve(c->spec_res, (size_t)items * sizeof(int4)))) return rc;
-        if ((rc = reserve(c->spec_off, (size_t)items * 8))) return rc;
-        CU(cudaMemsetAsync(c->spec_res.p, 0, (size_t)items * sizeof(int4), st));
+        if ((rc = reserve(c->spec_p2, (size_t)npairs * sizeof(int2)))) return rc;
+        if ((rc = reserve(c->spec_res, spec_items * sizeof(int4)))) return rc;
+        if ((rc = reserve(c->spec_off, spec_items * 8))) return rc;
+        CU(cudaMemsetAsync(c->spec_res.p, 0, spec_items * sizeof(int4), st));
     }
 
     // a capture (poyalgn_batch_graph_create) records the launches only: the
@@ -172,8 +187,10 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
             free_now = (long long)fr + (long long)c->dmarena.n;  // the arena may be re-reserved
             c->last_free = free_now;
         }
-        const long long want = (long long)items * DM_MAX_REGION;
-        dm_cap = std::max<long long>(0, std::min({free_now - (16LL << 30), 64LL << 30, want}));
+        const long long want = (long long)items * DM_MAX_REGION +
+                               (spec2 ? (long long)npairs * DM_MAX_REGION2 : 0);
+        dm_cap = std::max<long long>(0, std::min({free_now - (16LL << 30),
+                                                  spec2 ? ARENA_MAX_SPEC2 : ARENA_MAX, want}));
         if (capturing) dm_cap = std::min<long long>(dm_cap, (long long)c->dmarena.n);
         if (c->dm_fixed > 0) dm_cap = std::min(dm_cap, c->dm_fixed);
         if (c->arena_cap > 0) dm_cap = std::min(dm_cap, c->arena_cap);
@@ -235,6 +252,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         A.dm_arena = as<uint8_t>(c->dmarena);
         A.dm_cap = dm_cap;
         A.dm_max_region = DM_MAX_REGION;
+        A.dm_max_region2 = DM_MAX_REGION2;
         A.dm_used = as<unsigned long long>(c->dmctr);
         A.dm_off = as<long long>(c->dmoff);
     }
@@ -252,6 +270,9 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         A.spec_n = as<int>(c->spec_n);
         A.spec_res = as<int4>(c->spec_res);
         A.spec_off = as<long long>(c->spec_off);
+        A.spec2 = spec2 ? 1 : 0;
+        A.spec_Tstar = as<int>(c->spec_tstar);
+        A.spec_p2 = as<int2>(c->spec_p2);
     }
 
     int launches = 0;
@@ -280,9 +301,8 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         return 0;
     };
     if (spec_S) {
-        // speculative sweep: only linear / lean items, which never move
+        // speculative sweeps: only linear / lean items, which never move
         // between classes, so the classes run concurrently (fork / join)
-        A.spec = 1;
         if (!c->spec_fork) {
             CU(cudaEventCreateWithFlags(&c->spec_fork, cudaEventDisableTiming));
             for (int k = 0; k < NCLASS; k++) {
@@ -290,23 +310,33 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
                 CU(cudaEventCreateWithFlags(&c->spec_join[k], cudaEventDisableTiming));
             }
         }
-        CU(cudaEventRecord(c->spec_fork, st));
-        const int v = affine ? 1 : 0;
-        for (int k = 0; k < NCLASS; k++) {
-            cudaStream_t sk = c->spec_st[k];
-            CU(cudaStreamWaitEvent(sk, c->spec_fork, 0));
-            A.slab_stride = strides[k];
-            launch_sort_queues(A, k, sort_grid, sk);
-            launch_class(A, k, v, grid[k][v], sk);
-            launches += 3;
-            CU(cudaEventRecord(c->spec_join[k], sk));
-            CU(cudaStreamWaitEvent(st, c->spec_join[k], 0));
-        }
-        // fresh queues for the sequential sweep, which the resolve fills
-        CU(cudaMemsetAsync(c->qctr.p, 0, QCTR_INTS * sizeof(int), st));
-        A.spec = 0;
+        auto spec_sweep = [&](int phase) -> int {
+            A.spec = phase;
+            CU(cudaEventRecord(c->spec_fork, st));
+            const int v = affine ? 1 : 0;
+            for (int k = 0; k < NCLASS; k++) {
+                cudaStream_t sk = c->spec_st[k];
+                CU(cudaStreamWaitEvent(sk, c->spec_fork, 0));
+                A.slab_stride = strides[k];
+                launch_sort_queues(A, k, sort_grid, sk);
+                launch_class(A, k, v, grid[k][v], sk);
+                launches += 3;
+                CU(cudaEventRecord(c->spec_join[k], sk));
+                CU(cudaStreamWaitEvent(st, c->spec_join[k], 0));
+            }
+            // fresh queues for the next sweep, which the resolve fills
+            CU(cudaMemsetAsync(c->qctr.p, 0, QCTR_INTS * sizeof(int), st));
+            A.spec = 0;
+            return 0;
+        };
+        if ((rc = spec_sweep(1))) return rc;
         launch_spec_resolve(A, st);
         launches++;
+        if (spec2) {
+            if ((rc = spec_sweep(2))) return rc;
+            launch_spec_resolve2(A, st);
+            launches++;
+        }
         if (ev) CU(cudaEventRecord(ev[1], st));
     }
     if ((rc = sweep())) return rc;
@@ -328,8 +358,10 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     for (DevBuf* b : per_pair)
         if ((rc = reserve(*b, n * 4))) return rc;
     if ((rc = reserve(c->shadow, (size_t)(affine ? out_total : 1) * 4))) return rc;
-    // speculative batches queue up to spec_passes items per pair
-    const size_t items = n * (size_t)(c->spec_mode ? std::max(1, c->spec_passes) : 1);
+    // speculative batches queue up to spec_passes items per pair, and linear
+    // ones up to SPEC_STRIDE in the second sweep
+    const size_t items =
+        n * (size_t)(c->spec_mode ? std::max(affine ? 1 : SPEC_STRIDE, c->spec_passes) : 1);
     if ((rc = reserve(c->qitems, 2 * (size_t)NQUEUE * items * sizeof(int2)))) return rc;
     if ((rc = reserve(c->qctr, QCTR_INTS * sizeof(int)))) return rc;
     if ((rc = reserve(c->strides, NCLASS * sizeof(long long)))) return rc;
@@ -337,8 +369,10 @@ int prereserve(poyalgn_ctx* c, int affine, int max_pairs, long long out_total,
     if (c->spec_mode) {
         if ((rc = reserve(c->spec_t0, n * 4))) return rc;
         if ((rc = reserve(c->spec_n, n * 4))) return rc;
-        if ((rc = reserve(c->spec_res, items * sizeof(int4)))) return rc;
-        if ((rc = reserve(c->spec_off, items * 8))) return rc;
+        if ((rc = reserve(c->spec_tstar, n * 4))) return rc;
+        if ((rc = reserve(c->spec_p2, n * sizeof(int2)))) return rc;
+        if ((rc = reserve(c->spec_res, n * SPEC_STRIDE * sizeof(int4)))) return rc;
+        if ((rc = reserve(c->spec_off, n * SPEC_STRIDE * 8))) return rc;
     }
     if ((rc = reserve(c->slab, (size_t)slab_bytes))) return rc;
     if (c->dm_fixed > 0) {
@@ -578,7 +612,8 @@ void poyalgn_free(poyalgn_ctx* c)
                       &c->passes, &c->shadow, &c->qitems, &c->qctr, &c->slab, &c->strides,
                       &c->dwh, &c->swp, &c->order, &c->order_scratch, &c->nobt_bnd,
                       &c->nobt_ctr, &c->nobt_coop, &c->dmarena, &c->dmoff, &c->dmctr,
-                      &c->spec_t0, &c->spec_n, &c->spec_res, &c->spec_off};
+                      &c->spec_t0, &c->spec_n, &c->spec_res, &c->spec_off,
+                      &c->spec_tstar, &c->spec_p2};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);

@@ -219,7 +219,7 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& A, int k, int cost,
 // traceback runs in the class kernel).
 __device__ __forceinline__ long long arena_take(const BatchArgs& A, long long bytes)
 {
-    if (A.dm_cap <= 0 || bytes > A.dm_max_region) return -1;
+    if (A.dm_cap <= 0 || bytes > (A.spec == 2 ? A.dm_max_region2 : A.dm_max_region)) return -1;
     const unsigned long long b = ((unsigned long long)bytes + 255ull) & ~255ull;
     const unsigned long long off = atomicAdd(A.dm_used, b);
     return off + b <= (unsigned long long)A.dm_cap ? (long long)off : -1;
@@ -301,9 +301,23 @@ __device__ __forceinline__ int spec_eh0(const BatchArgs& A, const Item& w, int j
 __device__ __forceinline__ void spec_record(const BatchArgs& A, const Item& w, int j, int cost,
                                             int gapnum, int cls_flags, long long off)
 {
-    const long long si = (long long)w.k * A.spec_S + j;
+    const long long si = (long long)w.k * SPEC_STRIDE + j;
     A.spec_res[si] = make_int4(cost, gapnum, cls_flags, 1);
     A.spec_off[si] = off;
+}
+
+// A pass of the second sweep that traced back at once: its outputs and
+// results are written, the status waits for spec_resolve2_kernel.
+__device__ __forceinline__ void spec_traced(const BatchArgs& A, const Item& w, int j, int cost,
+                                            const PairRes& r)
+{
+    A.cost[w.k] = cost;
+    A.alen[w.k] = r.alen;
+    A.mlen[w.k] = r.mlen;
+    A.wlen[w.k] = r.wlen;
+    A.maxcost[w.k] = r.maxcost;
+    const long long si = (long long)w.k * SPEC_STRIDE + j;
+    A.spec_res[si].z |= SPEC_TRACED | ((-r.status & 0xFF) << 16);
 }
 
 // ---------------------------------------------------------------------------
@@ -462,7 +476,11 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
         {  // first pass of an item in this class: its arena region (a warp-
            // or CTA-wide call: pipelines of one warp admit items at different times)
             const bool fresh = off == -2;
-            const long long o = pipe_take(A, p, fresh && live && A.do_traceback,
+            // in the second sweep only the predicted final pass keeps its
+            // fill (in a region of its own: the classes run concurrently and
+            // share the slabs); the other passes are read for their gap counts
+            const bool keepfill = A.spec != 2 || (live && w.T == A.spec_Tstar[w.k]);
+            const long long o = pipe_take(A, p, fresh && live && A.do_traceback && keepfill,
                                           (long long)(w.m + w.n + 1) * p.P * R, &soff);
             if (fresh) {
                 off = o;
@@ -474,6 +492,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
         int fc = 0, fg = 0;
         if (Tmax > 0) lin_fill<R>(b, st, w.x, w.y, dm, p, act, Tmax, xv, xn, sres, fc, fg);
         bool finished = false;
+        bool strace = false;  // second sweep: trace back the predicted final pass now
         if (live) {
             int gapnum = fg;
             cost = fc;
@@ -485,6 +504,11 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
             }
             if (spec) {  // one pass; spec_resolve_kernel decides
                 if (p.gl == 0) spec_record(A, w, sj, cost, gapnum, cls, off);
+                // second sweep: the predicted final pass traces back at once
+                // when its own test ends the doubling (kept by the resolve if
+                // no earlier pass of the sweep stopped)
+                strace = A.spec == 2 && A.do_traceback && off >= 0 &&
+                         w.T == A.spec_Tstar[w.k] && (w.full || lin_done(w.T, w.m, w.n, gapnum));
                 live = false;
             } else {
                 w.npass++;
@@ -499,33 +523,35 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
             }
         }
         pipe_sync(p);
-        if (finished) {
+        if (finished && p.gl == 0) {
+            A.lastcls[w.k] = cls;
+            A.slab_cta[w.k] = p.slot;
+        }
+        if (finished && (!A.do_traceback || off >= 0)) {  // no traceback, or after all fills
             if (p.gl == 0) {
-                A.lastcls[w.k] = cls;
-                A.slab_cta[w.k] = p.slot;
+                if (off >= 0) A.dm_off[w.k] = off;
+                A.cost[w.k] = cost;
+                A.status[w.k] = 0;
             }
-            if (!A.do_traceback || off >= 0) {  // no traceback, or after all fills
-                if (p.gl == 0) {
-                    if (off >= 0) A.dm_off[w.k] = off;
-                    A.cost[w.k] = cost;
-                    A.status[w.k] = 0;
-                }
-            } else if (lin_window_ok(p.P, R)) {
+        } else if (finished || strace) {
+            PairRes r;
+            bool lead = false;
+            if (lin_window_ok(p.P, R)) {
                 // the pipeline's first warp walks the path through a shared
                 // window of the slab (one round of loads per LW_DIAG steps)
                 if (p.gl < 32) {
                     extern __shared__ uint32_t lin_win[];
                     LinDmWindow rd{dm, lin_win + (p.K == 1 ? (threadIdx.x >> 5) : 0) * LW_SMEM_WORDS,
                                    p.P * R - 1, p.P * R / 4, p.lane, 32};
-                    const PairRes r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.swaped,
-                                                       pair_out(A, w.k));
-                    if (p.gl == 0) finish_pair(A, w.k, cost, r);
+                    r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k));
+                    lead = p.gl == 0;
                 }
             } else if (p.gl == 0) {
-                const PairRes r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
-                                                pair_out(A, w.k));
-                finish_pair(A, w.k, cost, r);
+                r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k));
+                lead = true;
             }
+            if (lead && finished) finish_pair(A, w.k, cost, r);
+            if (lead && strace) spec_traced(A, w, sj, cost, r);
         }
         pipe_sync(p);
     }
@@ -1277,6 +1303,15 @@ __device__ void spec_requeue(const BatchArgs& A, int k, int m, int n, int j, int
     push_item(A, 2 * c + (lean ? 1 : 0), k, T);
 }
 
+// The sequential sweep resumes a pair at pass j; with a second speculative
+// sweep ahead, the first resolve only notes where (the queues then belong to
+// that sweep).
+__device__ void spec_resume(const BatchArgs& A, int k, int m, int n, int j, int T, bool lean)
+{
+    if (A.spec2) A.spec_p2[k] = make_int2(j, -1);
+    else spec_requeue(A, k, m, n, j, T, lean);
+}
+
 // One thread per speculated pair: the first queued pass whose result
 // satisfies the doubling test is the pair's final pass (the sequential
 // doubling runs exactly the passes before it, in order, and stops there).
@@ -1289,20 +1324,20 @@ __global__ void spec_resolve_kernel(BatchArgs A)
     const bool lean = A.affine && (A.pfull[k] & 2);
     int T = A.spec_T0[k];
     if (A.spec_n[k] < 0) {  // not speculated (gap-bearing affine pair): sequential from pass 0
-        spec_requeue(A, k, m, n, 0, T, lean);
+        spec_resume(A, k, m, n, 0, T, lean);
         return;
     }
-    const int S = A.spec_S, nq = A.spec_n[k] & ~SPEC_NOCLASS;
+    const int nq = A.spec_n[k] & ~SPEC_NOCLASS;
     const bool full = !A.affine && (A.pfull[k] & 1);
     for (int j = 0; j < nq; j++, T *= 2) {
-        const int4 r = A.spec_res[(long long)k * S + j];
+        const int4 r = A.spec_res[(long long)k * SPEC_STRIDE + j];
         if (r.w != 1) {  // a queued pass did not run
             A.status[k] = -9;
             return;
         }
         const bool done = A.affine ? aff_done(T, m, n, r.y) : (full || lin_done(T, m, n, r.y));
         if (!done) continue;
-        const long long off = A.spec_off[(long long)k * S + j];
+        const long long off = A.spec_off[(long long)k * SPEC_STRIDE + j];
         if (off >= 0 || !A.do_traceback) {
             A.cost[k] = r.x;
             A.passes[k] = j + 1;
@@ -1310,7 +1345,7 @@ __global__ void spec_resolve_kernel(BatchArgs A)
             if (A.dm_off) A.dm_off[k] = off;
             A.status[k] = 0;
         } else {  // no arena region for its fill: the sequential sweep runs it again
-            spec_requeue(A, k, m, n, j, T, lean);
+            spec_resume(A, k, m, n, j, T, lean);
         }
         return;
     }
@@ -1318,7 +1353,71 @@ __global__ void spec_resolve_kernel(BatchArgs A)
         A.status[k] = -5;
         return;
     }
-    spec_requeue(A, k, m, n, nq, T, lean);
+    if (A.spec2 && !A.affine && !full && nq > 0) {
+        // the gap count of the last pass predicts the final one: the first
+        // whose p exceeds it by more than one (or that covers the plane);
+        // every pass up to it runs at once in the second sweep
+        const int G = A.spec_res[(long long)k * SPEC_STRIDE + nq - 1].y;
+        int last = -1;
+        for (int j = nq; j < SPEC_STRIDE; j++, T *= 2) {
+            const int c = pick_class(A.lad, lin_wu(lin_band(m, n, 0, band_p(T, m, n))), n);
+            if (c < 0) break;
+            push_item(A, 2 * c, k, T);
+            last = j;
+            if (band_p(T, m, n) > G + 1 || lin_covers(T, m, n)) break;
+        }
+        if (last >= 0) {
+            A.spec_p2[k] = make_int2(nq, last);
+            A.spec_Tstar[k] = A.spec_T0[k] << last;
+            return;
+        }
+        T = A.spec_T0[k] << nq;
+    }
+    spec_resume(A, k, m, n, nq, T, lean);
+}
+
+// One thread per pair still open after the first resolve, when the second
+// speculative sweep ran (linear batches): the first of the sweep's passes
+// whose result satisfies the doubling test ends the pair, exactly where the
+// sequential doubling stops. The predicted final pass already traced back;
+// any other stopping pass runs again in the sequential sweep with its
+// traceback, and a pair none of whose passes stopped continues there.
+__global__ void spec_resolve2_kernel(BatchArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.npairs || A.status[k] != 1) return;
+    const int la = A.lena[k], lb = A.lenb[k];
+    const int m = la <= lb ? la : lb, n = la <= lb ? lb : la;
+    const int T0 = A.spec_T0[k];
+    const int2 q = A.spec_p2[k];
+    if (q.y < 0) {
+        spec_requeue(A, k, m, n, q.x, T0 << q.x, false);
+        return;
+    }
+    const bool full = A.pfull[k] & 1;
+    for (int j = q.x; j <= q.y; j++) {
+        const int T = T0 << j;
+        const int4 r = A.spec_res[(long long)k * SPEC_STRIDE + j];
+        if (r.w != 1) {
+            A.status[k] = -9;
+            return;
+        }
+        if (!(full || lin_done(T, m, n, r.y))) continue;
+        if (j == q.y && (r.z & SPEC_TRACED)) {  // traced in the sweep: outputs are written
+            A.passes[k] = j + 1;
+            A.lastcls[k] = r.z & LASTCLS_MASK;
+            A.status[k] = -((r.z >> 16) & 0xFF);
+        } else if (!A.do_traceback) {
+            A.cost[k] = r.x;
+            A.passes[k] = j + 1;
+            A.lastcls[k] = r.z & LASTCLS_MASK;
+            A.status[k] = 0;
+        } else {
+            spec_requeue(A, k, m, n, j, T, false);
+        }
+        return;
+    }
+    spec_requeue(A, k, m, n, q.y + 1, T0 << (q.y + 1), false);
 }
 
 // Traceback of fills kept in their slabs (per-call stub path); one thread
@@ -1550,6 +1649,11 @@ void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s)
 void launch_spec_resolve(const BatchArgs& a, cudaStream_t s)
 {
     spec_resolve_kernel<<<(a.npairs + 127) / 128, 128, 0, s>>>(a);
+}
+
+void launch_spec_resolve2(const BatchArgs& a, cudaStream_t s)
+{
+    spec_resolve2_kernel<<<(a.npairs + 127) / 128, 128, 0, s>>>(a);
 }
 
 void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)

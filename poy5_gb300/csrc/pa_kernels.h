@@ -69,6 +69,7 @@ struct BatchArgs {
     uint8_t* dm_arena;
     long long dm_cap;
     long long dm_max_region;      // larger fills keep the pipeline's slab
+    long long dm_max_region2;     // the same for the traced pass of the second sweep
     unsigned long long* dm_used;  // bump counter, zero before the batch
     long long* dm_off;            // per pair: arena offset of the final fill, -1 if none
     // Speculative band passes (small batches): the first spec_S passes of
@@ -81,9 +82,26 @@ struct BatchArgs {
     int spec_S;                   // passes per pair (0: no speculation in this batch)
     int* spec_T0;                 // per pair: T of pass 0 (0: not speculated)
     int* spec_n;                  // per pair: passes queued (| SPEC_NOCLASS)
-    int4* spec_res;               // per pair x spec_S: cost, gap count, class flags, 1 = ran
-    long long* spec_off;          // per pair x spec_S: arena region of that pass (-1: none)
+    int4* spec_res;               // per pair x SPEC_STRIDE passes: cost, gap count, class flags, 1 = ran
+    long long* spec_off;          // per pair x SPEC_STRIDE passes: arena region (-1: none)
+    // Second speculative sweep (linear batches of long pairs): a pair's gap
+    // count settles once its band holds the alignment, so the first resolve
+    // predicts the pass that will end the doubling (the first whose p exceeds
+    // the last gap count + 1) and queues every pass up to it at once; the
+    // predicted final pass traces back in its class kernel when its own test
+    // stops the doubling, and spec_resolve2_kernel keeps exactly the pass the
+    // sequential doubling stops at (rerunning it when the prediction missed).
+    int spec2;                    // the first resolve queues the second sweep
+    int* spec_Tstar;              // per pair: T of the predicted final pass
+    int2* spec_p2;                // per pair: first pass after the first sweep, predicted
+                                  // final pass (-1: the sequential sweep resumes there)
 };
+
+// spec_res / spec_off hold every speculated pass of a pair at its pass index
+constexpr int SPEC_STRIDE = 16;
+// spec_res.z: the pass's traceback already ran (second sweep), with its
+// status negated in bits 16..23
+constexpr int SPEC_TRACED = 0x1000;
 
 // spec_n: the pass after the queued ones has no class (the sequential
 // doubling would fail the pair there with status -5)
@@ -100,6 +118,9 @@ void launch_sort_queues(const BatchArgs& a, int cls, int grid, cudaStream_t s);
 // After a speculative sweep: finish the pairs one of whose passes stopped,
 // queue the others for the sequential sweep.
 void launch_spec_resolve(const BatchArgs& a, cudaStream_t s);
+// After the second speculative sweep: keep each pair's stopping pass or
+// queue the sequential sweep where the doubling continues.
+void launch_spec_resolve2(const BatchArgs& a, cudaStream_t s);
 // Persistent CTAs per SM a class kernel can keep resident.
 int class_blocks_per_sm(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // The row tile width of a class's lean queue (0: lane pipeline).

@@ -65,6 +65,7 @@ struct poyalgn_ctx {
     pa::DevBuf dmarena, dmoff, dmctr;          // deferred tracebacks
     int defer_traceback = 1;                   // 0: trace back inside the class kernels
     pa::DevBuf spec_t0, spec_n, spec_res, spec_off;  // speculative band passes
+    pa::DevBuf spec_tstar, spec_p2;                  // the second speculative sweep
     int spec_mode = 2;     // 0 off, 1 every batch, 2 by batch size
     int spec_passes = 8;   // passes per pair run at once
     // the speculative sweep runs every class at once, one stream per class

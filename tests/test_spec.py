@@ -70,3 +70,37 @@ def test_speculative_distance_and_downpass():
     assert all(np.array_equal(x, y) for x, y in zip(a[2], b[2]))
     assert np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4]) and np.all(a[4] == 0)
     ctx.close()
+
+
+def test_second_sweep_matches_sequential(oracle):
+    """Linear pairs of 4-9 kb (together at least 8,192 positions: the second
+    speculative sweep runs the passes up to each pair's predicted final pass
+    at once). With a first sweep of 1 or 2 passes the prediction comes from
+    gap counts that have not settled yet, so mispredictions (a pass before
+    the predicted one stops, or none does) take the rerun paths. Results,
+    pass counts and distances must equal the sequential doubling's."""
+    import poy5_gb300 as pg
+    rng = np.random.default_rng(404)
+    pairs = []
+    for t in range(20):
+        L = int(rng.integers(4200, 9000))
+        core = wl.random_bases(rng, L)
+        sub, ind = [(0.05, 0.01), (0.15, 0.02), (0.3, 0.06), (0.1, 0.1)][t % 4]
+        pairs.append((wl.with_gap(core), wl.with_gap(wl.mutate(rng, core, sub, ind))))
+    assert min(len(a) + len(b) for a, b in pairs) >= 8192
+    ctx = pg.Context(0)
+    cm = pg.CostMatrix.of_list(ctx, STD_TCM, 0)
+    ctx.set_speculation(0)
+    ref = pg.median_batch(ctx, cm, pairs)
+    assert np.all(ref.status == 0)
+    dref = pg.distance_batch(ctx, cm, pairs)
+    ocm = oracle.cm(tcm=STD_TCM)
+    for k in (0, 7, 13):
+        r = oracle.median(ocm, *pairs[k], False)
+        assert ref.cost[k] == r.cost and np.array_equal(ref.pair(k).aligned_a, r.ea), k
+    for passes in (1, 2, 4, 8):
+        ctx.set_speculation(1, passes)
+        _same(ref, pg.median_batch(ctx, cm, pairs))
+        d = pg.distance_batch(ctx, cm, pairs)
+        assert np.array_equal(d[0], dref[0]) and np.array_equal(d[1], dref[1])
+    ctx.close()
