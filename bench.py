@@ -63,6 +63,8 @@ def parse_args(argv=None):
                     help="skip the downpass and serving measurements")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="arrival window of each serving rate")
+    ap.add_argument("--serve-slots", type=int, default=3, help="server execution slots")
+    ap.add_argument("--serve-batch", type=int, default=2048, help="server pairs per batch")
     ap.add_argument("--newkk-arena-mb", type=int, default=0,
                     help="bound the Newkk direction arena (MB; 0: library default)")
     ap.add_argument("--mem-gb", type=float, default=0.0,
@@ -777,7 +779,8 @@ def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.
                              "alignments_per_s": round(n_cpu / cpu_dt, 2)}}
 
 
-def run_serving(local: int, seconds: float = 1.0) -> dict:
+def run_serving(local: int, seconds: float = 1.0, nslots: int = 3,
+                max_batch_pairs: int = 2048) -> dict:
     """Open-loop Poisson replay against the continuous-batching server: each
     request has U{1..64} pairs of a resident pool (lognormal lengths, median
     1,000, clipped 100-5,000, ~30% divergence), affine 3/1/1."""
@@ -790,7 +793,8 @@ def run_serving(local: int, seconds: float = 1.0) -> dict:
     na = np.array([store.add(a) for a, _ in w.pairs], np.int32)
     nb = np.array([store.add(b) for _, b in w.pairs], np.int32)
     pair_cells = np.array([len(a) * len(b) for a, b in w.pairs], np.int64)
-    cfg = dict(nslots=3, max_batch_pairs=2048, max_waiting_pairs=16384)
+    cfg = dict(nslots=nslots, max_batch_pairs=max_batch_pairs,
+               max_waiting_pairs=max(16384, 2 * nslots * max_batch_pairs))
     rng = np.random.default_rng(wl.SEED_BASE + 4)
 
     def sweep(kind, rates):
@@ -815,8 +819,9 @@ def run_serving(local: int, seconds: float = 1.0) -> dict:
         return {"batches": st["batches"], "points": points}
 
     from poy5_gb300.serve import DISTANCE, MEDIAN
-    dist = sweep(DISTANCE, (250, 1000, 5000, 20000, 50000, 100000, 200000))
-    med = sweep(MEDIAN, (250, 1000, 5000))
+    rates = (250, 1000, 5000, 20000, 50000, 100000, 200000)
+    dist = sweep(DISTANCE, rates)
+    med = sweep(MEDIAN, rates)
     store.close()
     return {"workload": "serving_requests_poisson_1-64pairs_lognormal1000", **cfg,
             "distance": dist, "median": med}
@@ -954,7 +959,7 @@ def main(argv=None):
         elif args.leg == "long":
             out = run_long(local, n_pairs=args.pairs or 512, mem_gb=args.mem_gb)
         elif args.leg == "serving":
-            out = run_serving(local, args.serve_seconds)
+            out = run_serving(local, args.serve_seconds, args.serve_slots, args.serve_batch)
         elif args.leg == "newkk":
             out = run_newkk(local, args.pairs or 65536, arena_mb=args.newkk_arena_mb)
         else:
@@ -1006,7 +1011,8 @@ def main(argv=None):
                 line["newkk"] = run_newkk(local)
             except Exception as e:  # keep the headline line if this leg fails
                 line["newkk"] = {"error": f"{type(e).__name__}: {e}"[:300]}
-            line["serving"] = run_serving(local, args.serve_seconds)
+            line["serving"] = run_serving(local, args.serve_seconds, args.serve_slots,
+                                          args.serve_batch)
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -526,11 +526,14 @@ int poyalgn_uppass(poyalgn_store *s, const poyalgn_cm *cm, int nleaves,
  * arrive while others run overlaps on the device. Whenever a slot frees it
  * forms the next batch from the oldest waiting requests, up to
  * max_batch_pairs pairs and the slot's share of the device-memory budget.
- * Memory is reserved once, at creation: hbm_budget bytes (0: half of the free
- * device memory) split across the slots. A request whose pairs cannot fit
- * one slot is refused at submission (POYALGN_EINVAL), and a submission that
- * would make more than max_waiting_pairs pairs wait is refused with
- * POYALGN_EBUSY (admission control; nothing is queued).
+ * Slot memory is reserved once, at creation: hbm_budget bytes (0: half of
+ * the free device memory) split across the slots. A request whose pairs
+ * cannot fit one slot is refused at submission (POYALGN_EINVAL). Admission
+ * control refuses a submission with POYALGN_EBUSY (nothing is queued) when
+ * it would make more than max_waiting_pairs pairs wait, or when the device
+ * memory the waiting requests will take in a slot (their four output
+ * buffers and per-pair metadata) would exceed half of the device's free
+ * memory, sampled at submission (at most once a millisecond).
  *
  * Nodes are those the store holds when the server is created (later
  * additions are not visible to it); the store must outlive the server, and

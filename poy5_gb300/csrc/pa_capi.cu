@@ -314,7 +314,11 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
             A.spec = phase;
             CU(cudaEventRecord(c->spec_fork, st));
             const int v = affine ? 1 : 0;
-            for (int k = 0; k < NCLASS; k++) {
+            // the second sweep's passes are the wide ones: the widest class
+            // goes first, so its long passes start at once and the narrower
+            // classes fill the SMs it leaves
+            for (int i = 0; i < NCLASS; i++) {
+                const int k = phase == 2 ? NCLASS - 1 - i : i;
                 cudaStream_t sk = c->spec_st[k];
                 CU(cudaStreamWaitEvent(sk, c->spec_fork, 0));
                 A.slab_stride = strides[k];

@@ -1258,9 +1258,11 @@ __global__ void prep_kernel(BatchArgs A)
             // bands that need a multi-warp pipeline (a barrier per step) are
             // slow per step: at most the first of them is speculated, so that
             // the widest, slowest passes do not sit on every pair's
-            // critical path; later ones go to the sequential sweep
+            // critical path; later ones go to the sequential sweep (or, with
+            // a second sweep ahead, all of them go there: the gap count of
+            // the single-warp passes predicts the final pass)
             if (A.lad.P[cj] > 32) {
-                if (wide && nq > 0) break;
+                if ((wide || A.spec2) && nq > 0) break;
                 wide = true;
             }
             push_item(A, 2 * cj + (lean ? 1 : 0), k, T);

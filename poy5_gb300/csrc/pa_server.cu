@@ -75,6 +75,13 @@ struct poyalgn_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Req*> waiting;
     long long waiting_pairs = 0;
+    // admission by device memory: the device bytes the waiting requests will
+    // take in a slot, against the free device memory sampled at submission
+    // (at most every kFreeSampleUs)
+    long long waiting_bytes = 0;
+    long long free_bytes = 0;
+    Clock::time_point free_at;
+    int64_t n_refused_hbm = 0;
     std::unordered_map<int64_t, Req*> reqs;
     int64_t next_id = 1;
     bool stop = false;
@@ -96,11 +103,23 @@ void fail_all(poyalgn_server* s, int code, const char* msg)
     }
     s->waiting.clear();
     s->waiting_pairs = 0;
+    s->waiting_bytes = 0;
     s->cv_done.notify_all();
 }
 
 // pairs per SM up to which a batch with no backlog speculates
 constexpr int SERVE_SPEC_PAIRS = 2;
+// the waiting requests may take at most this fraction of the free device
+// memory; the free memory is sampled at most this often
+constexpr double kAdmitFrac = 0.5;
+constexpr int kFreeSampleUs = 1000;
+
+// Device bytes a request occupies in a slot: its four output buffers, the
+// per-pair metadata and result words.
+long long request_device_bytes(long long out_bytes, int npairs)
+{
+    return 4 * out_bytes + 60LL * npairs;
+}
 
 // Build and enqueue one batch on slot `sl` from the requests in `batch`.
 // Runs without the server lock; touches only the slot and the requests,
@@ -240,6 +259,7 @@ void scheduler(poyalgn_server* s)
                 s->waiting.pop_front();
             }
             s->waiting_pairs -= n;
+            s->waiting_bytes -= request_device_bytes(bytes, n);
             const bool backlog = !s->waiting.empty();
             lk.unlock();
             const int rc = launch(s, sl, batch, backlog);
@@ -278,6 +298,7 @@ int submit_at(poyalgn_server* s, int npairs, const int32_t* na, const int32_t* n
     if (npairs > s->max_batch_pairs || bytes > s->out_cap)
         return set_err(POYALGN_EINVAL, "request of %d pairs (%lld output bytes) exceeds one batch",
                        npairs, bytes);
+    const long long dev_bytes = request_device_bytes(bytes, npairs);
     Req* r = new (std::nothrow) Req;
     if (!r) return set_err(POYALGN_ENOMEM, "request allocation");
     r->npairs = npairs;
@@ -297,10 +318,28 @@ int submit_at(poyalgn_server* s, int npairs, const int32_t* na, const int32_t* n
             return set_err(POYALGN_EBUSY, "admission refused: %lld pairs waiting",
                            s->waiting_pairs);
         }
+        const Clock::time_point now = Clock::now();
+        if (now - s->free_at > std::chrono::microseconds(kFreeSampleUs)) {
+            size_t fr = 0, tot = 0;
+            if (cudaSetDevice(s->device) == cudaSuccess &&
+                cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+                s->free_bytes = (long long)fr;
+                s->free_at = now;
+            }
+        }
+        if (s->waiting_bytes + dev_bytes > (long long)(kAdmitFrac * (double)s->free_bytes)) {
+            s->n_refused++;
+            s->n_refused_hbm++;
+            delete r;
+            return set_err(POYALGN_EBUSY,
+                           "admission refused: waiting requests would take %lld of %lld free "
+                           "device bytes", s->waiting_bytes + dev_bytes, s->free_bytes);
+        }
         r->id = s->next_id++;
         s->reqs[r->id] = r;
         s->waiting.push_back(r);
         s->waiting_pairs += npairs;
+        s->waiting_bytes += dev_bytes;
         *ticket = r->id;
     }
     s->cv_work.notify_one();
