@@ -63,8 +63,8 @@ def parse_args(argv=None):
                     help="skip the downpass and serving measurements")
     ap.add_argument("--serve-seconds", type=float, default=1.0,
                     help="arrival window of each serving rate")
-    ap.add_argument("--serve-slots", type=int, default=3, help="server execution slots")
-    ap.add_argument("--serve-batch", type=int, default=2048, help="server pairs per batch")
+    ap.add_argument("--serve-slots", type=int, default=2, help="server execution slots")
+    ap.add_argument("--serve-batch", type=int, default=8192, help="server pairs per batch")
     ap.add_argument("--newkk-arena-mb", type=int, default=0,
                     help="bound the Newkk direction arena (MB; 0: library default)")
     ap.add_argument("--mem-gb", type=float, default=0.0,
@@ -779,8 +779,8 @@ def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.
                              "alignments_per_s": round(n_cpu / cpu_dt, 2)}}
 
 
-def run_serving(local: int, seconds: float = 1.0, nslots: int = 3,
-                max_batch_pairs: int = 2048) -> dict:
+def run_serving(local: int, seconds: float = 1.0, nslots: int = 2,
+                max_batch_pairs: int = 8192) -> dict:
     """Open-loop Poisson replay against the continuous-batching server: each
     request has U{1..64} pairs of a resident pool (lognormal lengths, median
     1,000, clipped 100-5,000, ~30% divergence), affine 3/1/1."""
