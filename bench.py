@@ -70,8 +70,8 @@ def parse_args(argv=None):
     ap.add_argument("--mem-gb", type=float, default=0.0,
                     help="cap each context's direction slabs and traceback arena (GB; 0: "
                          "library defaults), e.g. to keep a profiled case small")
-    ap.add_argument("--leg", choices=["main", "peak", "plain", "downpass", "long", "serving",
-                                      "distance", "newkk"],
+    ap.add_argument("--leg", choices=["main", "peak", "plain", "percall", "downpass", "long",
+                                      "serving", "distance", "newkk"],
                     default="main", help="run one measurement alone and print its object")
     return ap.parse_args(argv)
 
@@ -375,6 +375,24 @@ def plain_per_call(ctx, cm, w, seconds: float = 3.0) -> dict:
         n += 1
     dt = time.perf_counter() - t0
     return {"gcups": cells / dt / 1e9, "alignments_per_s": n / dt, "pairs": n}
+
+
+def run_percall(local: int, seconds: float = 3.0) -> dict:
+    """The drop-in per-call stubs alone, one call sequence per pair as POY's
+    OCaml makes them: algn_CAML_align_affine_3 on the affine pair workload,
+    simple_2 + backtrace_2d on the plain pairwise workload (host buffers)."""
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    ctx = pg.Context(local)
+    out = {}
+    for w in (wl.affine_pairs(n_pairs=4096), wl.plain_pairs()):
+        cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
+        plain_per_call(ctx, cm, w, seconds=0.3)  # warm-up
+        r = plain_per_call(ctx, cm, w, seconds=seconds)
+        out[w.name] = {"alignments_per_s": round(r["alignments_per_s"], 1),
+                       "gcups": round(r["gcups"], 3), "pairs": r["pairs"]}
+    ctx.close()
+    return out
 
 
 def run_downpass(local: int, reps: int = 5) -> dict:
@@ -954,6 +972,8 @@ def main(argv=None):
             out["clocks"] = clk.stop()
         elif args.leg == "plain":
             out = run_plain(local)
+        elif args.leg == "percall":
+            out = run_percall(local)
         elif args.leg == "downpass":
             out = run_downpass(local)
         elif args.leg == "long":

@@ -92,6 +92,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
 {
     int rc;
     if (npairs <= 0) return 0;
+    c->call_valid = false;  // the slabs and the arena are about to be reused
     // Batches too small to fill the GPU run their pairs' first band passes
     // at once (speculative sweep, then the sequential sweep for the pairs
     // that need more). The fills must outlive the sweep: the arena holds
@@ -499,6 +500,60 @@ int stage_pair(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int l
     return 0;
 }
 
+// A pinned host buffer that only grows.
+int pinned(unsigned char** p, size_t* n, size_t want)
+{
+    if (*n >= want) return 0;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *n = 0;
+    if (cudaHostAlloc((void**)p, want, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_err(POYALGN_ENOMEM, "pinned staging of %zu bytes", want);
+    }
+    *n = want;
+    return 0;
+}
+
+// Per-call block layout: offa, offb, out_off (3 int64), lena, lenb, tie
+// (3 int32), then both sequences from byte CALL_SEQ.
+constexpr size_t CALL_SEQ = 48;
+
+// One pair and its tie preference staged with a single copy from pinned host
+// memory; the device pointers of the block's fields.
+struct CallPair {
+    const uint8_t* seqs;
+    const long long* offa;
+    const int* lena;
+    const int* tie;
+};
+int stage_call(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int lb, int tie,
+               CallPair* cp)
+{
+    int rc;
+    const size_t n = CALL_SEQ + (size_t)la + lb;
+    if ((rc = pinned(&c->h_in, &c->h_in_n, n))) return rc;
+    if ((rc = reserve(c->callblk, n))) return rc;
+    long long* o = reinterpret_cast<long long*>(c->h_in);
+    o[0] = CALL_SEQ;
+    o[1] = CALL_SEQ + la;
+    o[2] = 0;
+    int* l = reinterpret_cast<int*>(c->h_in + 24);
+    l[0] = la;
+    l[1] = lb;
+    l[2] = tie;
+    memcpy(c->h_in + CALL_SEQ, a, (size_t)la);
+    memcpy(c->h_in + CALL_SEQ + la, b, (size_t)lb);
+    CU(cudaMemcpyAsync(c->callblk.p, c->h_in, n, cudaMemcpyHostToDevice, c->stream));
+    const uint8_t* d = as<uint8_t>(c->callblk);
+    cp->seqs = d;  // offsets are from the block's start
+    cp->offa = reinterpret_cast<const long long*>(d);
+    cp->lena = reinterpret_cast<const int*>(d + 24);
+    cp->tie = reinterpret_cast<const int*>(d + 32);
+    return 0;
+}
+
 // Run the fill of the staged pair, keeping the final fill in the slab.
 int fill_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
               const int* dwh_host, int32_t* cost)
@@ -617,9 +672,11 @@ void poyalgn_free(poyalgn_ctx* c)
                       &c->dwh, &c->swp, &c->order, &c->order_scratch, &c->nobt_bnd,
                       &c->nobt_ctr, &c->nobt_coop, &c->dmarena, &c->dmoff, &c->dmctr,
                       &c->spec_t0, &c->spec_n, &c->spec_res, &c->spec_off,
-                      &c->spec_tstar, &c->spec_p2};
+                      &c->spec_tstar, &c->spec_p2, &c->callblk};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
+    if (c->h_in) cudaFreeHost(c->h_in);
+    if (c->h_out) cudaFreeHost(c->h_out);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     for (int k = 0; k < NCLASS; k++) {
         if (c->spec_st[k]) cudaStreamDestroy(c->spec_st[k]);
@@ -772,21 +829,43 @@ int poyalgn_align_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t
         return set_err(POYALGN_EINVAL, "null argument");
     if (lj < li) return set_err(POYALGN_EINVAL, "pass the shorter one as first");
     if (li < 1 || (li == 1 && lj == 1)) return set_err(POYALGN_EINVAL, "empty sequences");
-    int rc, res[6];
+    int rc;
     ctx->call_valid = false;
     if ((rc = ensure_device(ctx))) return rc;
-    if ((rc = stage_pair(ctx, si, li, sj, lj))) return rc;
-    if ((rc = fill_pair(ctx, cm, 1, li, lj, nullptr, cost))) return rc;
-    if ((rc = trace_pair(ctx, cm, 1, li, lj, swaped ? 1 : 0, res))) return rc;
-    const int L = res[2], ML = res[3], WL = res[4], pcap = li + lj + 2;
-    if (L > cap || ML > cap || WL > cap) return set_err(POYALGN_EINVAL, "capacity %d too small", cap);
+    // one pinned copy in; the pair runs as a one-pair DOS.median batch with
+    // the caller's tie preference (its first band passes speculative, the
+    // traceback from its arena region); one pinned copy of the results out
+    CallPair cp;
+    if ((rc = stage_call(ctx, si, li, sj, lj, swaped ? 1 : 0, &cp))) return rc;
+    const int pcap = li + lj + 2;
+    if ((rc = reserve(ctx->ints, 16 * sizeof(int)))) return rc;
+    if ((rc = reserve(ctx->bytes, (size_t)4 * pcap))) return rc;
+    int* ints = as<int>(ctx->ints);
     uint8_t* bytes = as<uint8_t>(ctx->bytes);
-    const uint8_t* ea = bytes + (pcap - L);
-    const uint8_t* eb = bytes + pcap + (pcap - L);
-    CU(cudaMemcpy(resi + cap - L, swaped ? eb : ea, L, cudaMemcpyDeviceToHost));
-    CU(cudaMemcpy(resj + cap - L, swaped ? ea : eb, L, cudaMemcpyDeviceToHost));
-    CU(cudaMemcpy(median + cap - ML, bytes + 2 * pcap + (pcap - ML), ML, cudaMemcpyDeviceToHost));
-    CU(cudaMemcpy(medianwg + cap - WL, bytes + 3 * pcap + (pcap - WL), WL, cudaMemcpyDeviceToHost));
+    if ((rc = run_batch(ctx, cm, 1, 1, li + lj, pcap, cp.seqs, cp.offa, cp.lena, cp.offa + 1,
+                        cp.lena + 1, cp.offa + 2, ints + 0, ints + 1, ints + 2, ints + 3,
+                        ints + 4, ints + 5, bytes, bytes + pcap, bytes + 2 * pcap,
+                        bytes + 3 * pcap, ints + 6, nullptr, cp.tie, 1, ctx->stream)))
+        return rc;
+    const size_t nout = 32 + (size_t)4 * pcap;
+    if ((rc = pinned(&ctx->h_out, &ctx->h_out_n, nout))) return rc;
+    CU(cudaMemcpyAsync(ctx->h_out, ints, 7 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(ctx->h_out + 32, bytes, (size_t)4 * pcap, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    const int* h = reinterpret_cast<const int*>(ctx->h_out);
+    if (h[5] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[5]);
+    const int L = h[2], ML = h[3], WL = h[4];
+    if (L > cap || ML > cap || WL > cap) return set_err(POYALGN_EINVAL, "capacity %d too small", cap);
+    const uint8_t* hb = ctx->h_out + 32;
+    const uint8_t* ea = hb + (pcap - L);
+    const uint8_t* eb = hb + pcap + (pcap - L);
+    // the traceback writes caller order; with swaped the first sequence is sj's side
+    memcpy(resi + cap - L, swaped ? eb : ea, (size_t)L);
+    memcpy(resj + cap - L, swaped ? ea : eb, (size_t)L);
+    memcpy(median + cap - ML, hb + 2 * pcap + (pcap - ML), (size_t)ML);
+    memcpy(medianwg + cap - WL, hb + 3 * pcap + (pcap - WL), (size_t)WL);
+    *cost = h[0];
     lens[0] = L;
     lens[1] = ML;
     lens[2] = WL;

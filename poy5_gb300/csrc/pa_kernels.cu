@@ -246,6 +246,7 @@ __device__ __forceinline__ long long pipe_take(const BatchArgs& A, const Pipe& p
 // Work item of one pipeline: the pair in internal order and its band state.
 struct Item {
     int k, T, m, n, swaped, full, npass;
+    int tie;  // traceback tie preference: swaped, or the per-call caller's
     const uint8_t* x;
     const uint8_t* y;
 };
@@ -262,6 +263,7 @@ __device__ __forceinline__ Item load_item(const BatchArgs& A, int q, int it)
     w.y = A.seqs + (w.swaped ? A.offa[w.k] : A.offb[w.k]);
     w.m = w.swaped ? lb : la;
     w.n = w.swaped ? la : lb;
+    w.tie = A.swap_override ? A.swap_override[w.k] : w.swaped;
     w.full = A.pfull[w.k] & 1;
     w.npass = A.passes[w.k];  // passes run by smaller classes (earlier launches)
     return w;
@@ -275,6 +277,7 @@ __device__ __forceinline__ Item empty_item(const BatchArgs& A)
     w.m = 1;
     w.n = 1;
     w.swaped = 0;
+    w.tie = 0;
     w.full = 0;
     w.npass = 0;
     w.x = A.seqs;
@@ -543,11 +546,11 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                     extern __shared__ uint32_t lin_win[];
                     LinDmWindow rd{dm, lin_win + (p.K == 1 ? (threadIdx.x >> 5) : 0) * LW_SMEM_WORDS,
                                    p.P * R - 1, p.P * R / 4, p.lane, 32};
-                    r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k));
+                    r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.tie, pair_out(A, w.k));
                     lead = p.gl == 0;
                 }
             } else if (p.gl == 0) {
-                r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k));
+                r = lin_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.tie, pair_out(A, w.k));
                 lead = true;
             }
             if (lead && finished) finish_pair(A, w.k, cost, r);
@@ -851,8 +854,8 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
             } else if (p.gl == 0) {
                 const PairRes r =
                     FAST ? aff_traceback_lean(reinterpret_cast<const uint8_t*>(dm), p.P, R, st,
-                                              w.x, w.m, w.y, w.n, w.swaped, pair_out(A, w.k))
-                         : aff_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.swaped,
+                                              w.x, w.m, w.y, w.n, w.tie, pair_out(A, w.k))
+                         : aff_traceback(dm, p.P, R, st, w.x, w.m, w.y, w.n, w.tie,
                                          pair_out(A, w.k));
                 finish_pair(A, w.k, cost, r);
             }
@@ -1056,7 +1059,7 @@ __global__ void __launch_bounds__(32 * NARROW_WARPS) aff_rk_kernel(BatchArgs A, 
                     A.status[w.k] = 0;
                 } else {
                     const PairRes r = aff_traceback_rowtile(dm, 32 * K, newk, st, w.x, w.m, w.y,
-                                                            w.n, w.swaped, pair_out(A, w.k));
+                                                            w.n, w.tie, pair_out(A, w.k));
                     finish_pair(A, w.k, cost, r);
                 }
             }
@@ -1468,6 +1471,7 @@ __global__ void deferred_traceback_kernel(BatchArgs A)
     const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
     const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
     const int m = swaped ? lb : la, n = swaped ? la : lb;
+    const int tie = A.swap_override ? A.swap_override[k] : swaped;
     const int cls = A.lastcls[k] & LASTCLS_MASK;
     const bool lean = (A.lastcls[k] & LASTCLS_LEAN) != 0;
     const bool row = (A.lastcls[k] & LASTCLS_ROW) != 0;
@@ -1479,14 +1483,14 @@ __global__ void deferred_traceback_kernel(BatchArgs A)
         const long long T = (long long)pl.T0 << tmax(A.passes[k] - 1, 0);
         const AffBand b = aff_band(m, n, band_p((int)T, m, n));
         r = aff_traceback_rowtile(base, 32 * rk_k_for(ladder_cap(A.lad, cls)), b.newk, t, x, m, y,
-                                  n, swaped, pair_out(A, k));
+                                  n, tie, pair_out(A, k));
     } else if (A.affine && lean) {
-        r = aff_traceback_lean(base, P, R, t, x, m, y, n, swaped, pair_out(A, k));
+        r = aff_traceback_lean(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
     } else if (A.affine) {
-        r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, swaped,
+        r = aff_traceback(reinterpret_cast<const uint16_t*>(base), P, R, t, x, m, y, n, tie,
                           pair_out(A, k));
     } else {
-        r = lin_traceback(base, P, R, t, x, m, y, n, swaped, pair_out(A, k));
+        r = lin_traceback(base, P, R, t, x, m, y, n, tie, pair_out(A, k));
     }
     finish_pair(A, k, A.cost[k], r);
 }

@@ -57,6 +57,13 @@ struct poyalgn_ctx {
     // per-batch scratch
     pa::DevBuf pfull, eh0, lastcls, slabcta, passes, shadow, qitems, qctr, slab, strides;
     pa::DevBuf dwh, swp, order, order_scratch;
+    // per-call staging: one device block (offsets, lengths, tie, sequences)
+    // filled from one pinned host block, and a pinned block for the results
+    pa::DevBuf callblk;
+    unsigned char* h_in = nullptr;
+    size_t h_in_n = 0;
+    unsigned char* h_out = nullptr;
+    size_t h_out_n = 0;
     pa::DevBuf nobt_bnd, nobt_ctr, nobt_coop;  // cost-only affine fill scratch
     // Algn_Newkk (pa_newkk.cu): per-warp boundary rows and tile offsets, the
     // direction-code arena, counters, visiting order
