@@ -1462,8 +1462,12 @@ PA_HD PairRes lin_traceback(const uint8_t* dm, int P, int R, const Tables& t,
 // each step lowers T by 1 or 2 and the row by at most 1. Row i of
 // anti-diagonal T is byte (i - 1) mod (P R) of the step's P R bytes
 // (dm_index), so the window's rows are LW_WORDS consecutive words (modulo
-// the step) of every anti-diagonal. Needs P R a power of two of at least
-// LW_ROWS and a 4-byte aligned slab (linear pipelines of 32 lanes or more).
+// the step) of every anti-diagonal. Needs P R a power of two (8 or more) and
+// a 4-byte aligned slab. With P R < LW_ROWS the window holds whole
+// anti-diagonals and rows alias modulo P R; the walk still reads the right
+// byte because a path cell lies in the band, and at any step each of the
+// P R slots holds the one band row that owns it (a band fits its class:
+// fewer than P R rows cross one anti-diagonal).
 constexpr int LW_DIAG = 64;
 constexpr int LW_ROWS = 64;
 constexpr int LW_WORDS = LW_ROWS / 4 + 1;
@@ -1506,6 +1510,8 @@ struct LinDmWindow {
     }
 };
 
+// The class kernels' in-kernel traceback uses the window when the pipeline
+// has a warp of its own (32 lanes or more).
 PA_HD bool lin_window_ok(int P, int R) { return P * R >= LW_ROWS && P >= 32; }
 
 // algn_CAML_backtrace_2d_limit from any start: backtrace_2d with st_s1,

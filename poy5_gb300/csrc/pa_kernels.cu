@@ -1662,9 +1662,49 @@ void launch_spec_resolve2(const BatchArgs& a, cudaStream_t s)
     spec_resolve2_kernel<<<(a.npairs + 127) / 128, 128, 0, s>>>(a);
 }
 
+namespace {
+
+constexpr int LWARP_WARPS = 4;  // warps (pairs) per CTA of the linear deferred traceback
+
+// Linear deferred tracebacks, one warp per pair: every lane walks the same
+// path through a shared-memory window of the pair's arena region (whole
+// anti-diagonals for pipelines of fewer than 64 lane-rows: at any step a
+// slot holds only the row of the band that owns it), refilled by all lanes
+// at once every LW_DIAG anti-diagonals instead of one dependent load per
+// step.
+__global__ void __launch_bounds__(32 * LWARP_WARPS)
+    deferred_traceback_lin_kernel(BatchArgs A)
+{
+    __shared__ Tables t;
+    __shared__ uint32_t win[LWARP_WARPS][LW_SMEM_WORDS];
+    load_tables(t, A.tables);
+    __syncthreads();
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = blockIdx.x * LWARP_WARPS + wib;
+    if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;  // warp-uniform
+    const int la = A.lena[k], lb = A.lenb[k];
+    const int swaped = la <= lb ? 0 : 1;
+    const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
+    const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
+    const int m = swaped ? lb : la, n = swaped ? la : lb;
+    const int tie = A.swap_override ? A.swap_override[k] : swaped;
+    const int cls = A.lastcls[k] & LASTCLS_MASK;
+    const int PR = A.lad.P[cls] * A.lad.R[cls];
+    LinDmWindow rd{A.dm_arena + A.dm_off[k], win[wib], PR - 1, PR / 4, lane, 32};
+    const PairRes r = lin_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
+    if (lane == 0) finish_pair(A, k, A.cost[k], r);
+}
+
+}  // namespace
+
 void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)
 {
     if (a.npairs <= 0 || a.dm_cap <= 0) return;
+    if (!a.affine) {
+        deferred_traceback_lin_kernel<<<(a.npairs + LWARP_WARPS - 1) / LWARP_WARPS,
+                                        32 * LWARP_WARPS, 0, s>>>(a);
+        return;
+    }
     const int threads = 128;
     deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a);
 }

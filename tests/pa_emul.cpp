@@ -285,6 +285,7 @@ struct Emul {
     Tables t;
     Ladder lad[2] = {default_ladder(0), default_ladder(1)};
     int row_tile = 1;  // lean bands up to 512 wide on the row tile (0: lane pipeline)
+    int window_all = 0;  // every linear traceback through the shared-memory window
 };
 
 // The band doubling of plan pl (x = rows, y = columns), as the class
@@ -344,7 +345,10 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     if (st) return st;
     PairOut o = {ea, eb, med, mwg, cap};
     PairRes r;
-    if (lin_window_ok(P, R)) {  // as the class kernel does: through the shared window
+    // as the kernels do: the class kernel's in-kernel traceback through the
+    // window for pipelines of a warp or more; the deferred one (window_all)
+    // through the window for every class
+    if (lin_window_ok(P, R) || E.window_all) {
         std::vector<uint32_t> win(LW_SMEM_WORDS);
         LinDmWindow rd{dm.data(), win.data(), P * R - 1, P * R / 4, 0, 1};
         r = lin_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
@@ -522,6 +526,10 @@ void pa_emul_free(void* e) { delete (Emul*)e; }
 // 0: lean affine passes on the lane pipeline only; 1: on the row tile up to
 // 512 wide (the default, as in a context).
 void pa_emul_set_row_tile(void* e, int mode) { ((Emul*)e)->row_tile = mode ? 1 : 0; }
+
+// 1: every linear traceback through the shared-memory window, as the
+// deferred traceback runs it (0: only pipelines of a warp or more).
+void pa_emul_set_window(void* e, int all) { ((Emul*)e)->window_all = all ? 1 : 0; }
 
 // Copies out the product's host tables for comparison with the oracle.
 int pa_emul_tables(void* h, int* cost, uint8_t* median, int* worst, int* tail,

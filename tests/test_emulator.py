@@ -161,3 +161,32 @@ def test_window_traceback_on_wide_classes(emul, oracle):
         assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb)
         assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
     assert max(classes) >= 6, classes
+
+
+def test_window_traceback_on_every_class(emul, oracle):
+    """The deferred linear traceback runs every class's walk through the
+    shared-memory window, also for pipelines of fewer than 64 lane-rows,
+    whose window holds whole anti-diagonals with rows aliased modulo P R:
+    golden pairs and random pairs of every width against the references."""
+    emul.pa_emul_set_window.argtypes = [_P, C.c_int]
+    for name in ("golden_linear", "golden_plain_pairs"):
+        g = golden_lib.load(name)
+        e = Emu(emul, g.tcm, g.gap_open)
+        emul.pa_emul_set_window(e.h, 1)
+        for k, (a, b) in enumerate(g.pairs):
+            cost, ea, eb, med, mwg, mx, _ = e.median(a, b)
+            bad = golden_lib.mismatches(g, k, cost, ea, eb, med, mwg, mx)
+            assert not bad, (name, k, bad)
+    rng = np.random.default_rng(515)
+    e = Emu(emul, STD_TCM, 0)
+    emul.pa_emul_set_window(e.h, 1)
+    cm = oracle.cm(tcm=STD_TCM)
+    classes = set()
+    for a, b in edge_pairs() + random_pairs(rng, 300, maxlen=700):
+        cost, ea, eb, med, mwg, mx, cls = e.median(a, b)
+        classes.add(cls)
+        r = oracle.median(cm, a, b, False)
+        assert (cost, mx) == (r.cost, r.maxcost)
+        assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb)
+        assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
+    assert min(classes) == 0 and len(classes) >= 5, classes
