@@ -347,7 +347,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     if ((rc = sweep())) return rc;
     if (A.dm_cap > 0) {
         launch_deferred_traceback(A, st);
-        launches++;
+        launches += affine ? 2 : 1;
     }
     CU(cudaGetLastError());
     c->last_launches = launches;

@@ -1476,11 +1476,20 @@ constexpr int LW_SMEM_WORDS = LW_DIAG * LW_WORDS;
 struct LinDmWindow {
     const uint8_t* dm;
     uint32_t* win;   // LW_SMEM_WORDS words (shared memory on the device)
-    int prm;         // P R - 1
+    int pr;          // P R, a multiple of 4 (a power of two on the linear ladder,
+                     // 3 times one on the affine ladder's R = 3 classes)
     int prw;         // words per anti-diagonal, P R / 4
     int lane, nl;    // this lane, and the lanes that refill together
     int Ttop = -1, ilo = 0, itop = -1, w0 = 0;
 
+    PA_HDM int slot(int i) const  // byte of row i >= 1 in its step
+    {
+        return (pr & (pr - 1)) == 0 ? (i - 1) & (pr - 1) : (i - 1) % pr;
+    }
+    PA_HDM int wmod(int w) const  // w modulo the words of a step, w > -prw
+    {
+        return (prw & (prw - 1)) == 0 ? w & (prw - 1) : (w + prw) % prw;
+    }
     PA_HDM void refill(int i, int T)
     {
 #if defined(__CUDA_ARCH__)
@@ -1489,12 +1498,12 @@ struct LinDmWindow {
         Ttop = T;
         itop = i;
         ilo = i - LW_ROWS + 1 > 1 ? i - LW_ROWS + 1 : 1;
-        w0 = ((ilo - 1) & prm) >> 2;
+        w0 = slot(ilo) >> 2;
         const uint32_t* d32 = reinterpret_cast<const uint32_t*>(dm);
         for (int e = lane; e < LW_SMEM_WORDS; e += nl) {
             const int dd = e / LW_WORDS, c = e - dd * LW_WORDS;
             const int t = Ttop - dd;
-            win[e] = t >= 1 ? d32[(long long)t * prw + ((w0 + c) & (prw - 1))] : 0u;
+            win[e] = t >= 1 ? d32[(long long)t * prw + wmod(w0 + c - prw)] : 0u;
         }
 #if defined(__CUDA_ARCH__)
         __syncwarp();
@@ -1504,10 +1513,16 @@ struct LinDmWindow {
     {
         const int T = i + j;
         if (T > Ttop || T <= Ttop - LW_DIAG || i < ilo || i > itop) refill(i, T);
-        const int off = (i - 1) & prm;
-        const int w = ((off >> 2) - w0) & (prw - 1);
+        const int off = slot(i);
+        const int w = wmod((off >> 2) - w0);
         return (int)((win[(Ttop - T) * LW_WORDS + w] >> ((off & 3) * 8)) & 0xFFu);
     }
+};
+
+// Lean affine codes (one byte per cell, same slab layout) through the window.
+struct AffDmLeanWindow {
+    LinDmWindow w;
+    PA_HDM int operator()(int i, int j) { return lean_flags(w(i, j)); }
 };
 
 // The class kernels' in-kernel traceback uses the window when the pipeline

@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                 if (p.gl < 32) {
                     extern __shared__ uint32_t lin_win[];
                     LinDmWindow rd{dm, lin_win + (p.K == 1 ? (threadIdx.x >> 5) : 0) * LW_SMEM_WORDS,
-                                   p.P * R - 1, p.P * R / 4, p.lane, 32};
+                                   p.P * R, p.P * R / 4, p.lane, 32};
                     r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.tie, pair_out(A, w.k));
                     lead = p.gl == 0;
                 }
@@ -1466,6 +1466,8 @@ __global__ void deferred_traceback_kernel(BatchArgs A)
     __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
+    // lean lane-pipeline fills: deferred_traceback_win_kernel
+    if (A.affine && (A.lastcls[k] & (LASTCLS_LEAN | LASTCLS_ROW)) == LASTCLS_LEAN) return;
     const int la = A.lena[k], lb = A.lenb[k];
     const int swaped = la <= lb ? 0 : 1;
     const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
@@ -1666,14 +1668,15 @@ namespace {
 
 constexpr int LWARP_WARPS = 4;  // warps (pairs) per CTA of the linear deferred traceback
 
-// Linear deferred tracebacks, one warp per pair: every lane walks the same
-// path through a shared-memory window of the pair's arena region (whole
+// Deferred tracebacks of byte-coded lane-pipeline fills (every linear fill,
+// lean affine ones), one warp per pair: every lane walks the same path
+// through a shared-memory window of the pair's arena region (whole
 // anti-diagonals for pipelines of fewer than 64 lane-rows: at any step a
 // slot holds only the row of the band that owns it), refilled by all lanes
 // at once every LW_DIAG anti-diagonals instead of one dependent load per
-// step.
+// step. Other affine fills are left to deferred_traceback_kernel.
 __global__ void __launch_bounds__(32 * LWARP_WARPS)
-    deferred_traceback_lin_kernel(BatchArgs A)
+    deferred_traceback_win_kernel(BatchArgs A)
 {
     __shared__ Tables t;
     __shared__ uint32_t win[LWARP_WARPS][LW_SMEM_WORDS];
@@ -1681,7 +1684,9 @@ __global__ void __launch_bounds__(32 * LWARP_WARPS)
     __syncthreads();
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k = blockIdx.x * LWARP_WARPS + wib;
-    if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;  // warp-uniform
+    // warp-uniform exits
+    if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
+    if (A.affine && (A.lastcls[k] & (LASTCLS_LEAN | LASTCLS_ROW)) != LASTCLS_LEAN) return;
     const int la = A.lena[k], lb = A.lenb[k];
     const int swaped = la <= lb ? 0 : 1;
     const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
@@ -1690,8 +1695,14 @@ __global__ void __launch_bounds__(32 * LWARP_WARPS)
     const int tie = A.swap_override ? A.swap_override[k] : swaped;
     const int cls = A.lastcls[k] & LASTCLS_MASK;
     const int PR = A.lad.P[cls] * A.lad.R[cls];
-    LinDmWindow rd{A.dm_arena + A.dm_off[k], win[wib], PR - 1, PR / 4, lane, 32};
-    const PairRes r = lin_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
+    LinDmWindow w{A.dm_arena + A.dm_off[k], win[wib], PR, PR / 4, lane, 32};
+    PairRes r;
+    if (A.affine) {
+        AffDmLeanWindow rd{w};
+        r = aff_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
+    } else {
+        r = lin_traceback_dm(w, t, x, m, y, n, tie, pair_out(A, k));
+    }
     if (lane == 0) finish_pair(A, k, A.cost[k], r);
 }
 
@@ -1700,11 +1711,9 @@ __global__ void __launch_bounds__(32 * LWARP_WARPS)
 void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)
 {
     if (a.npairs <= 0 || a.dm_cap <= 0) return;
-    if (!a.affine) {
-        deferred_traceback_lin_kernel<<<(a.npairs + LWARP_WARPS - 1) / LWARP_WARPS,
-                                        32 * LWARP_WARPS, 0, s>>>(a);
-        return;
-    }
+    deferred_traceback_win_kernel<<<(a.npairs + LWARP_WARPS - 1) / LWARP_WARPS,
+                                    32 * LWARP_WARPS, 0, s>>>(a);
+    if (!a.affine) return;
     const int threads = 128;
     deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a);
 }

@@ -350,7 +350,7 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     // through the window for every class
     if (lin_window_ok(P, R) || E.window_all) {
         std::vector<uint32_t> win(LW_SMEM_WORDS);
-        LinDmWindow rd{dm.data(), win.data(), P * R - 1, P * R / 4, 0, 1};
+        LinDmWindow rd{dm.data(), win.data(), P * R, P * R / 4, 0, 1};
         r = lin_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
     } else {
         r = lin_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
@@ -443,10 +443,17 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
         T *= 2;
     }
     PairOut o = {ea, eb, med, mwg, cap};
-    PairRes r = (lean_last && rk) ? aff_traceback_rowtile(dm8.data(), 32 * rk, rk_newk, t, x, m,
-                                                          y, n, pl.swaped, o)
-                : lean_last ? aff_traceback_lean(dm8.data(), P, R, t, x, m, y, n, pl.swaped, o)
-                            : aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    PairRes r;
+    if (lean_last && !rk && E.window_all) {  // as the deferred lean traceback: the window
+        std::vector<uint32_t> win(LW_SMEM_WORDS);
+        AffDmLeanWindow rd{LinDmWindow{dm8.data(), win.data(), P * R, P * R / 4, 0, 1}};
+        r = aff_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
+    } else {
+        r = (lean_last && rk) ? aff_traceback_rowtile(dm8.data(), 32 * rk, rk_newk, t, x, m, y, n,
+                                                      pl.swaped, o)
+            : lean_last ? aff_traceback_lean(dm8.data(), P, R, t, x, m, y, n, pl.swaped, o)
+                        : aff_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
+    }
     res[0] = r.alen;
     res[1] = r.mlen;
     res[2] = r.wlen;
@@ -527,8 +534,9 @@ void pa_emul_free(void* e) { delete (Emul*)e; }
 // 512 wide (the default, as in a context).
 void pa_emul_set_row_tile(void* e, int mode) { ((Emul*)e)->row_tile = mode ? 1 : 0; }
 
-// 1: every linear traceback through the shared-memory window, as the
-// deferred traceback runs it (0: only pipelines of a warp or more).
+// 1: every linear traceback and every lean affine one (lane pipeline) through
+// the shared-memory window, as the deferred tracebacks run them (0: only
+// linear pipelines of a warp or more).
 void pa_emul_set_window(void* e, int all) { ((Emul*)e)->window_all = all ? 1 : 0; }
 
 // Copies out the product's host tables for comparison with the oracle.

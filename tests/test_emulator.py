@@ -190,3 +190,37 @@ def test_window_traceback_on_every_class(emul, oracle):
         assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb)
         assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
     assert min(classes) == 0 and len(classes) >= 5, classes
+
+
+@pytest.mark.parametrize("row_tile", [0, 1])
+def test_window_traceback_lean_affine(emul, oracle, row_tile):
+    """Lean affine tracebacks (gap-free pairs on the lane pipeline, one byte
+    per cell) through the same window as the deferred lean traceback runs
+    them, on every affine class including the R = 3 ones, whose P R is not
+    a power of two; row-tile fills keep their own layout."""
+    emul.pa_emul_set_window.argtypes = [_P, C.c_int]
+    for name in ("golden_affine", "golden_affine_pairs"):
+        g = golden_lib.load(name)
+        e = Emu(emul, g.tcm, g.gap_open, row_tile)
+        emul.pa_emul_set_window(e.h, 1)
+        for k, (a, b) in enumerate(g.pairs):
+            cost, ea, eb, med, mwg, mx, _ = e.median(a, b)
+            bad = golden_lib.mismatches(g, k, cost, ea, eb, med, mwg, mx)
+            assert not bad, (name, k, bad)
+    rng = np.random.default_rng(616 + row_tile)
+    e = Emu(emul, AFF_TCM, 3, row_tile)
+    emul.pa_emul_set_window(e.h, 1)
+    cm = oracle.cm(tcm=AFF_TCM, gap_open=3)
+    classes = set()
+    for a, b in random_pairs(rng, 300, maxlen=900, kinds=2):  # gap-free kinds: lean
+        try:
+            r = oracle.median(cm, a, b, True)
+        except Exception:
+            continue
+        cost, ea, eb, med, mwg, mx, cls = e.median(a, b)
+        classes.add(cls)
+        assert (cost, mx) == (r.cost, r.maxcost)
+        assert np.array_equal(ea, r.ea) and np.array_equal(eb, r.eb)
+        assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
+    if row_tile == 0:
+        assert {1, 3, 5} & classes and len(classes) >= 5, classes  # R = 3 classes walked
