@@ -66,6 +66,8 @@ constexpr int ROW_TILE_MAX_PAIRS = 2;  // per SM, for row_tile_mode 2
 // spec_passes passes, up to SPEC_MAX_PAIRS two fewer (measured on GB300: the
 // extra cells cost more than the latency saved beyond about 30 pairs per SM)
 constexpr int SPEC_FULL_PAIRS = 8;
+// batches of at most this many pairs per SM trace back a warp per pair
+constexpr int WIN_TB_PAIRS = 8;
 constexpr int SPEC_MAX_PAIRS = 32;
 // Largest arena region one pair's fills in one class may take; wider fills
 // (long pairs) keep the pipeline's slab and trace back in the class kernel.
@@ -200,6 +202,12 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         if ((rc = reserve(c->dmctr, 8))) return rc;
         CU(cudaMemsetAsync(c->dmctr.p, 0, 8, st));
     }
+    if (do_traceback && dm_cap <= 0) {
+        // no arena: every fill stays in its slab (a later per-call traceback
+        // reads "no region" here)
+        if ((rc = reserve(c->dmoff, (size_t)npairs * 8))) return rc;
+        CU(cudaMemsetAsync(c->dmoff.p, 0xFF, (size_t)npairs * 8, st));
+    }
     if (!capturing)  // slab strides for the per-call traceback
         CU(cudaMemcpyAsync(c->strides.p, strides, sizeof(strides), cudaMemcpyHostToDevice, st));
     memcpy(c->call_strides, strides, sizeof(strides));
@@ -272,6 +280,7 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         A.spec_res = as<int4>(c->spec_res);
         A.spec_off = as<long long>(c->spec_off);
         A.spec2 = spec2 ? 1 : 0;
+        A.keep_fill = c->skip_deferred ? 1 : 0;
         A.spec_Tstar = as<int>(c->spec_tstar);
         A.spec_p2 = as<int2>(c->spec_p2);
     }
@@ -345,9 +354,11 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         if (ev) CU(cudaEventRecord(ev[1], st));
     }
     if ((rc = sweep())) return rc;
-    if (A.dm_cap > 0) {
-        launch_deferred_traceback(A, st);
-        launches += affine ? 2 : 1;
+    if (A.dm_cap > 0 && !c->skip_deferred) {
+        // a warp per pair through the shared-memory window cuts a small
+        // batch's latency; a large batch has the parallelism to hide one
+        // thread per pair's dependent loads and less traffic that way
+        launches += launch_deferred_traceback(A, npairs <= WIN_TB_PAIRS * c->nsm, st);
     }
     CU(cudaGetLastError());
     c->last_launches = launches;
@@ -479,27 +490,6 @@ int upload_cm(poyalgn_cm* m)
     return 0;
 }
 
-// Stage a one-pair batch (a then b) into the context's buffers.
-int stage_pair(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int lb)
-{
-    int rc;
-    const int cap = la + lb + 2;
-    if ((rc = reserve(c->seqs, (size_t)la + lb))) return rc;
-    if ((rc = reserve(c->offa, 4 * sizeof(long long)))) return rc;
-    if ((rc = reserve(c->lena, 4 * sizeof(int)))) return rc;
-    if ((rc = reserve(c->ints, 16 * sizeof(int)))) return rc;
-    if ((rc = reserve(c->bytes, (size_t)4 * cap))) return rc;
-    if ((rc = reserve(c->dwh, sizeof(int)))) return rc;
-    if ((rc = reserve(c->swp, sizeof(int)))) return rc;
-    CU(cudaMemcpyAsync(as<uint8_t>(c->seqs), a, la, cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemcpyAsync(as<uint8_t>(c->seqs) + la, b, lb, cudaMemcpyHostToDevice, c->stream));
-    long long offs[3] = {0, la, 0};
-    int lens[2] = {la, lb};
-    CU(cudaMemcpyAsync(c->offa.p, offs, sizeof(offs), cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemcpyAsync(c->lena.p, lens, sizeof(lens), cudaMemcpyHostToDevice, c->stream));
-    return 0;
-}
-
 // A pinned host buffer that only grows.
 int pinned(unsigned char** p, size_t* n, size_t want)
 {
@@ -516,20 +506,22 @@ int pinned(unsigned char** p, size_t* n, size_t want)
     return 0;
 }
 
-// Per-call block layout: offa, offb, out_off (3 int64), lena, lenb, tie
-// (3 int32), then both sequences from byte CALL_SEQ.
+// Per-call block layout: offa, offb, out_off (3 int64), lena, lenb, tie,
+// deltawh (4 int32), then both sequences from byte CALL_SEQ.
 constexpr size_t CALL_SEQ = 48;
+constexpr size_t CALL_TIE = 32;
 
-// One pair and its tie preference staged with a single copy from pinned host
-// memory; the device pointers of the block's fields.
+// One pair, its tie preference and deltawh staged with a single copy from
+// pinned host memory; the device pointers of the block's fields.
 struct CallPair {
     const uint8_t* seqs;
     const long long* offa;
     const int* lena;
     const int* tie;
+    const int* dwh;
 };
 int stage_call(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int lb, int tie,
-               CallPair* cp)
+               int deltawh, CallPair* cp)
 {
     int rc;
     const size_t n = CALL_SEQ + (size_t)la + lb;
@@ -543,6 +535,7 @@ int stage_call(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int l
     l[0] = la;
     l[1] = lb;
     l[2] = tie;
+    l[3] = deltawh;
     memcpy(c->h_in + CALL_SEQ, a, (size_t)la);
     memcpy(c->h_in + CALL_SEQ + la, b, (size_t)lb);
     CU(cudaMemcpyAsync(c->callblk.p, c->h_in, n, cudaMemcpyHostToDevice, c->stream));
@@ -550,82 +543,23 @@ int stage_call(poyalgn_ctx* c, const uint8_t* a, int la, const uint8_t* b, int l
     cp->seqs = d;  // offsets are from the block's start
     cp->offa = reinterpret_cast<const long long*>(d);
     cp->lena = reinterpret_cast<const int*>(d + 24);
-    cp->tie = reinterpret_cast<const int*>(d + 32);
+    cp->tie = reinterpret_cast<const int*>(d + CALL_TIE);
+    cp->dwh = reinterpret_cast<const int*>(d + CALL_TIE + 4);
     return 0;
 }
 
-// Run the fill of the staged pair, keeping the final fill in the slab.
-int fill_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
-              const int* dwh_host, int32_t* cost)
+// Results of a staged one-pair call: the seven result ints and nbytes of
+// the output buffers, copied to the pinned result block with one
+// synchronisation. Returns the host pointer of the ints (bytes follow at 32).
+int fetch_call(poyalgn_ctx* c, size_t nbytes, const int** h)
 {
     int rc;
-    const long long* offa = as<long long>(c->offa);
-    const int* lena = as<int>(c->lena);
-    int* ints = as<int>(c->ints);
-    uint8_t* bytes = as<uint8_t>(c->bytes);
-    const int cap = la + lb + 2;
-    const int* dwh = nullptr;
-    if (dwh_host) {
-        CU(cudaMemcpyAsync(c->dwh.p, dwh_host, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-        dwh = as<int>(c->dwh);
-    }
-    // offa[2] = 0 is the output offset of the single pair
-    if ((rc = run_batch(c, cm, affine, 1, la + lb, cap, as<uint8_t>(c->seqs), offa, lena,
-                        offa + 1, lena + 1, offa + 2, ints + 0, ints + 1, ints + 2,
-                        ints + 3, ints + 4, ints + 5, bytes, bytes + cap,
-                        bytes + 2 * cap, bytes + 3 * cap, ints + 6, dwh, nullptr, 0,
-                        c->stream)))
-        return rc;
-    int h[7];
-    CU(cudaMemcpyAsync(h, ints, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    if ((rc = pinned(&c->h_out, &c->h_out_n, 32 + nbytes))) return rc;
+    CU(cudaMemcpyAsync(c->h_out, c->ints.p, 7 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (nbytes)
+        CU(cudaMemcpyAsync(c->h_out + 32, c->bytes.p, nbytes, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
-    if (h[5] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[5]);
-    *cost = h[0];
-    return 0;
-}
-
-// Trace back the staged pair's kept fill with tie preference `swap`.
-int trace_pair(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int la, int lb,
-               int swap, int* res)
-{
-    const long long* offa = as<long long>(c->offa);
-    const int* lena = as<int>(c->lena);
-    int* ints = as<int>(c->ints);
-    uint8_t* bytes = as<uint8_t>(c->bytes);
-    const int cap = la + lb + 2;
-    CU(cudaMemcpyAsync(c->swp.p, &swap, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    BatchArgs A;
-    memset(&A, 0, sizeof(A));
-    A.seqs = as<uint8_t>(c->seqs);
-    A.offa = offa;
-    A.lena = lena;
-    A.offb = offa + 1;
-    A.lenb = lena + 1;
-    A.out_off = offa + 2;
-    A.npairs = 1;
-    A.affine = affine;
-    A.lad = c->lad[affine];
-    A.tables = cm->d;
-    A.slab = as<uint8_t>(c->slab);
-    A.cost = ints + 0;
-    A.maxcost = ints + 1;
-    A.alen = ints + 2;
-    A.mlen = ints + 3;
-    A.wlen = ints + 4;
-    A.status = ints + 5;
-    A.passes = ints + 6;  // written by the fill (fill_pair): locates the final band
-    A.lastcls = as<int>(c->lastcls);
-    A.slab_cta = as<int>(c->slabcta);
-    A.swap_override = as<int>(c->swp);
-    A.ea = bytes;
-    A.eb = bytes + cap;
-    A.med = bytes + 2 * cap;
-    A.mwg = bytes + 3 * cap;
-    launch_traceback(A, as<long long>(c->strides), c->stream);
-    CU(cudaGetLastError());
-    CU(cudaMemcpyAsync(res, ints, 6 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
-    if (res[5] != 0) return set_err(POYALGN_EINVAL, "traceback failed (status %d)", res[5]);
+    *h = reinterpret_cast<const int*>(c->h_out);
     return 0;
 }
 
@@ -774,8 +708,28 @@ int poyalgn_simple_2(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* s1, 
     int rc;
     ctx->call_valid = false;
     if ((rc = ensure_device(ctx))) return rc;
-    if ((rc = stage_pair(ctx, s1, l1, s2, l2))) return rc;
-    if ((rc = fill_pair(ctx, cm, 0, l1, l2, &deltawh, cost))) return rc;
+    // one pinned copy in; a one-pair batch with the caller's deltawh and no
+    // reordering (its first band passes speculative); the final fill stays
+    // in its arena region (or its pipeline's slab) for backtrace_2d, whose
+    // tie preference is not known yet, so no traceback runs here
+    CallPair cp;
+    if ((rc = stage_call(ctx, s1, l1, s2, l2, 0, deltawh, &cp))) return rc;
+    const int pcap = l1 + l2 + 2;
+    if ((rc = reserve(ctx->ints, 16 * sizeof(int)))) return rc;
+    if ((rc = reserve(ctx->bytes, (size_t)4 * pcap))) return rc;
+    int* ints = as<int>(ctx->ints);
+    uint8_t* bytes = as<uint8_t>(ctx->bytes);
+    ctx->skip_deferred = true;
+    rc = run_batch(ctx, cm, 0, 1, l1 + l2, pcap, cp.seqs, cp.offa, cp.lena, cp.offa + 1,
+                   cp.lena + 1, cp.offa + 2, ints + 0, ints + 1, ints + 2, ints + 3, ints + 4,
+                   ints + 5, bytes, bytes + pcap, bytes + 2 * pcap, bytes + 3 * pcap, ints + 6,
+                   cp.dwh, cp.tie, 1, ctx->stream);
+    ctx->skip_deferred = false;
+    if (rc) return rc;
+    const int* h;
+    if ((rc = fetch_call(ctx, 0, &h))) return rc;
+    if (h[5] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[5]);
+    *cost = h[0];
     ctx->call_valid = true;
     ctx->call_affine = 0;
     ctx->call_dwh = deltawh;
@@ -796,17 +750,58 @@ int poyalgn_backtrace_2d(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t* 
     if (!ctx->call_valid || ctx->call_affine || ctx->call_l1 != l1 || ctx->call_l2 != l2 ||
         memcmp(ctx->call_s1.data(), s1, l1) || memcmp(ctx->call_s2.data(), s2, l2))
         return set_err(POYALGN_EINVAL, "backtrace_2d needs the fill of simple_2 on the same pair");
-    int rc, res[6];
+    int rc;
     if ((rc = ensure_device(ctx))) return rc;
-    if ((rc = trace_pair(ctx, cm, 0, l1, l2, swap ? 1 : 0, res))) return rc;
-    const int L = res[2], pcap = l1 + l2 + 2;
-    if (L > cap) return set_err(POYALGN_EINVAL, "capacity %d < aligned length %d", cap, L);
+    // the kept fill of simple_2, walked by one warp through the shared-memory
+    // window with this call's tie preference; one pinned copy of the results
+    const int pcap = l1 + l2 + 2;
+    *reinterpret_cast<int*>(ctx->h_in + CALL_TIE) = swap ? 1 : 0;
+    CU(cudaMemcpyAsync(static_cast<uint8_t*>(ctx->callblk.p) + CALL_TIE, ctx->h_in + CALL_TIE,
+                       sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    const uint8_t* blk = as<uint8_t>(ctx->callblk);
+    int* ints = as<int>(ctx->ints);
     uint8_t* bytes = as<uint8_t>(ctx->bytes);
-    const uint8_t* ea = bytes + (pcap - L);
-    const uint8_t* eb = bytes + pcap + (pcap - L);
+    BatchArgs A;
+    memset(&A, 0, sizeof(A));
+    A.seqs = blk;
+    A.offa = reinterpret_cast<const long long*>(blk);
+    A.lena = reinterpret_cast<const int*>(blk + 24);
+    A.offb = A.offa + 1;
+    A.lenb = A.lena + 1;
+    A.out_off = A.offa + 2;
+    A.npairs = 1;
+    A.lad = ctx->lad[0];
+    A.tables = cm->d;
+    A.slab = as<uint8_t>(ctx->slab);
+    A.dm_arena = as<uint8_t>(ctx->dmarena);
+    A.dm_off = as<long long>(ctx->dmoff);
+    A.cost = ints + 0;
+    A.maxcost = ints + 1;
+    A.alen = ints + 2;
+    A.mlen = ints + 3;
+    A.wlen = ints + 4;
+    A.status = ints + 5;
+    A.passes = ints + 6;
+    A.lastcls = as<int>(ctx->lastcls);
+    A.slab_cta = as<int>(ctx->slabcta);
+    A.swap_override = reinterpret_cast<const int*>(blk + CALL_TIE);
+    A.ea = bytes;
+    A.eb = bytes + pcap;
+    A.med = bytes + 2 * pcap;
+    A.mwg = bytes + 3 * pcap;
+    launch_call_traceback_lin(A, as<long long>(ctx->strides), ctx->stream);
+    CU(cudaGetLastError());
+    const int* h;
+    if ((rc = fetch_call(ctx, (size_t)2 * pcap, &h))) return rc;
+    if (h[5] != 0) return set_err(POYALGN_EINVAL, "traceback failed (status %d)", h[5]);
+    const int L = h[2];
+    if (L > cap) return set_err(POYALGN_EINVAL, "capacity %d < aligned length %d", cap, L);
+    const uint8_t* hb = ctx->h_out + 32;
+    const uint8_t* ea = hb + (pcap - L);
+    const uint8_t* eb = hb + pcap + (pcap - L);
     // the traceback writes caller order; with swap the first sequence is y
-    CU(cudaMemcpy(s1p + cap - L, swap ? eb : ea, L, cudaMemcpyDeviceToHost));
-    CU(cudaMemcpy(s2p + cap - L, swap ? ea : eb, L, cudaMemcpyDeviceToHost));
+    memcpy(s1p + cap - L, swap ? eb : ea, (size_t)L);
+    memcpy(s2p + cap - L, swap ? ea : eb, (size_t)L);
     *len = L;
     return 0;
 }
@@ -836,7 +831,7 @@ int poyalgn_align_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t
     // the caller's tie preference (its first band passes speculative, the
     // traceback from its arena region); one pinned copy of the results out
     CallPair cp;
-    if ((rc = stage_call(ctx, si, li, sj, lj, swaped ? 1 : 0, &cp))) return rc;
+    if ((rc = stage_call(ctx, si, li, sj, lj, swaped ? 1 : 0, 0, &cp))) return rc;
     const int pcap = li + lj + 2;
     if ((rc = reserve(ctx->ints, 16 * sizeof(int)))) return rc;
     if ((rc = reserve(ctx->bytes, (size_t)4 * pcap))) return rc;
@@ -847,13 +842,8 @@ int poyalgn_align_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t
                         ints + 4, ints + 5, bytes, bytes + pcap, bytes + 2 * pcap,
                         bytes + 3 * pcap, ints + 6, nullptr, cp.tie, 1, ctx->stream)))
         return rc;
-    const size_t nout = 32 + (size_t)4 * pcap;
-    if ((rc = pinned(&ctx->h_out, &ctx->h_out_n, nout))) return rc;
-    CU(cudaMemcpyAsync(ctx->h_out, ints, 7 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaMemcpyAsync(ctx->h_out + 32, bytes, (size_t)4 * pcap, cudaMemcpyDeviceToHost,
-                       ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
-    const int* h = reinterpret_cast<const int*>(ctx->h_out);
+    const int* h;
+    if ((rc = fetch_call(ctx, (size_t)4 * pcap, &h))) return rc;
     if (h[5] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[5]);
     const int L = h[2], ML = h[3], WL = h[4];
     if (L > cap || ML > cap || WL > cap) return set_err(POYALGN_EINVAL, "capacity %d too small", cap);
@@ -1002,9 +992,11 @@ int poyalgn_backtrace_2d_limit(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uin
     w.slab_cta = as<int>(ctx->slabcta);
     w.passes = as<int>(ctx->ints) + 6;  // written by the kept fill
     w.pfull = as<int>(ctx->pfull);
+    w.dm_off = as<long long>(ctx->dmoff);
+    w.dm_arena = as<uint8_t>(ctx->dmarena);
     w.lad = ctx->lad[0];
-    w.s1 = as<uint8_t>(ctx->seqs);
-    w.s2 = as<uint8_t>(ctx->seqs) + l1;
+    w.s1 = as<uint8_t>(ctx->callblk) + CALL_SEQ;
+    w.s2 = as<uint8_t>(ctx->callblk) + CALL_SEQ + l1;
     w.l1 = l1;
     w.l2 = l2;
     w.deltawh = ctx->call_dwh;
@@ -1262,15 +1254,15 @@ int poyalgn_cost_affine_3(poyalgn_ctx* ctx, const poyalgn_cm* cm, const uint8_t*
     if (cm->h.cost_model != 1) return set_err(POYALGN_EINVAL, "cost matrix is not affine");
     int rc;
     if ((rc = ensure_device(ctx))) return rc;
-    if ((rc = stage_pair(ctx, si, li, sj, lj))) return rc;
+    CallPair cp;
+    if ((rc = stage_call(ctx, si, li, sj, lj, 0, 0, &cp))) return rc;
+    if ((rc = reserve(ctx->ints, 16 * sizeof(int)))) return rc;
     int* I = as<int>(ctx->ints);
-    if ((rc = run_nobt(ctx, cm, 1, li + lj, as<uint8_t>(ctx->seqs),
-                       as<long long>(ctx->offa), as<int>(ctx->lena), as<long long>(ctx->offa) + 1,
-                       as<int>(ctx->lena) + 1, NOBT_NO_MISSING, I, I + 1, ctx->stream)))
+    if ((rc = run_nobt(ctx, cm, 1, li + lj, cp.seqs, cp.offa, cp.lena, cp.offa + 1, cp.lena + 1,
+                       NOBT_NO_MISSING, I, I + 1, ctx->stream)))
         return rc;
-    int h[2];
-    CU(cudaMemcpyAsync(h, I, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
+    const int* h;
+    if ((rc = fetch_call(ctx, 0, &h))) return rc;
     if (h[1] != 0) return set_err(POYALGN_EUNSUPPORTED, "pair rejected (status %d)", h[1]);
     *cost = h[0];
     return 0;

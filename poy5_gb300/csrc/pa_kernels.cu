@@ -1411,6 +1411,7 @@ __global__ void spec_resolve2_kernel(BatchArgs A)
         if (j == q.y && (r.z & SPEC_TRACED)) {  // traced in the sweep: outputs are written
             A.passes[k] = j + 1;
             A.lastcls[k] = r.z & LASTCLS_MASK;
+            if (A.keep_fill) A.dm_off[k] = A.spec_off[(long long)k * SPEC_STRIDE + j];
             A.status[k] = -((r.z >> 16) & 0xFF);
         } else if (!A.do_traceback) {
             A.cost[k] = r.x;
@@ -1459,15 +1460,16 @@ __global__ void traceback_kernel(BatchArgs A, const long long* strides)
 
 // Tracebacks of the pairs whose final fill sits in the arena, one thread per
 // pair (after all class kernels, so no fill waits on a traceback).
-__global__ void deferred_traceback_kernel(BatchArgs A)
+__global__ void deferred_traceback_kernel(BatchArgs A, int skip_win)
 {
     __shared__ Tables t;  // median and cost lookups from shared memory
     load_tables(t, A.tables);
     __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
-    // lean lane-pipeline fills: deferred_traceback_win_kernel
-    if (A.affine && (A.lastcls[k] & (LASTCLS_LEAN | LASTCLS_ROW)) == LASTCLS_LEAN) return;
+    // lean lane-pipeline fills when deferred_traceback_win_kernel takes them
+    if (skip_win && A.affine && (A.lastcls[k] & (LASTCLS_LEAN | LASTCLS_ROW)) == LASTCLS_LEAN)
+        return;
     const int la = A.lena[k], lb = A.lenb[k];
     const int swaped = la <= lb ? 0 : 1;
     const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
@@ -1708,14 +1710,55 @@ __global__ void __launch_bounds__(32 * LWARP_WARPS)
 
 }  // namespace
 
-void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s)
+int launch_deferred_traceback(const BatchArgs& a, bool warp_per_pair, cudaStream_t s)
 {
-    if (a.npairs <= 0 || a.dm_cap <= 0) return;
+    if (a.npairs <= 0 || a.dm_cap <= 0) return 0;
+    const int threads = 128;
+    if (!warp_per_pair) {
+        deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a, 0);
+        return 1;
+    }
     deferred_traceback_win_kernel<<<(a.npairs + LWARP_WARPS - 1) / LWARP_WARPS,
                                     32 * LWARP_WARPS, 0, s>>>(a);
-    if (!a.affine) return;
-    const int threads = 128;
-    deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a);
+    if (!a.affine) return 1;
+    deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a, 1);
+    return 2;
+}
+
+namespace {
+
+// The per-call backtrace_2d of a kept linear fill, one warp: the fill sits
+// in the pair's arena region (dm_off[0] >= 0) or, when it had none, in the
+// slab of the pipeline that ran it; every lane walks the path through the
+// shared-memory window with the caller's tie preference.
+__global__ void __launch_bounds__(32) call_traceback_lin_kernel(BatchArgs A,
+                                                                 const long long* strides)
+{
+    __shared__ Tables t;
+    __shared__ uint32_t win[LW_SMEM_WORDS];
+    load_tables(t, A.tables);
+    __syncthreads();
+    if (A.status[0] != 0) return;
+    const int la = A.lena[0], lb = A.lenb[0];
+    const int swaped = la <= lb ? 0 : 1;
+    const uint8_t* x = A.seqs + (swaped ? A.offb[0] : A.offa[0]);
+    const uint8_t* y = A.seqs + (swaped ? A.offa[0] : A.offb[0]);
+    const int m = swaped ? lb : la, n = swaped ? la : lb;
+    const int tie = A.swap_override ? A.swap_override[0] : swaped;
+    const int cls = A.lastcls[0] & LASTCLS_MASK;
+    const int PR = A.lad.P[cls] * A.lad.R[cls];
+    const uint8_t* base = A.dm_off[0] >= 0 ? A.dm_arena + A.dm_off[0]
+                                           : A.slab + (long long)A.slab_cta[0] * strides[cls];
+    LinDmWindow w{base, win, PR, PR / 4, (int)threadIdx.x, 32};
+    const PairRes r = lin_traceback_dm(w, t, x, m, y, n, tie, pair_out(A, 0));
+    if (threadIdx.x == 0) finish_pair(A, 0, A.cost[0], r);
+}
+
+}  // namespace
+
+void launch_call_traceback_lin(const BatchArgs& a, const long long* d_strides, cudaStream_t s)
+{
+    call_traceback_lin_kernel<<<1, 32, 0, s>>>(a, d_strides);
 }
 
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s)
@@ -1766,8 +1809,10 @@ __global__ void limit_walk_kernel(LimitWalk a)
     const int full = a.pfull[0] & 1;
     const long long T = (long long)pl.T0 << tmax(a.passes[0] - 1, 0);
     const LinBand b = lin_band(pl.m, pl.n, full, full ? 0 : band_p((int)T, pl.m, pl.n));
-    LinDmBytes rd{a.slab + (long long)a.slab_cta[0] * a.strides[cls], a.lad.P[cls],
-                  a.lad.R[cls]};
+    const uint8_t* base = (a.dm_off && a.dm_off[0] >= 0)
+                              ? a.dm_arena + a.dm_off[0]
+                              : a.slab + (long long)a.slab_cta[0] * a.strides[cls];
+    LinDmBytes rd{base, a.lad.P[cls], a.lad.R[cls]};
     int len = 0;
     a.out2[0] = lin_limit_walk(rd, b, a.s1, a.s2, t.gap, a.st_s1, a.st_s2, a.algn_s1,
                                a.algn_s2, a.swaped, a.r1, a.r2, a.cap, &len);

@@ -92,6 +92,8 @@ struct BatchArgs {
     // stops the doubling, and spec_resolve2_kernel keeps exactly the pass the
     // sequential doubling stops at (rerunning it when the prediction missed).
     int spec2;                    // the first resolve queues the second sweep
+    int keep_fill;                // per-call simple_2: the final fill's region is
+                                  // recorded for a later traceback (dm_off)
     int* spec_Tstar;              // per pair: T of the predicted final pass
     int2* spec_p2;                // per pair: first pass after the first sweep, predicted
                                   // final pass (-1: the sequential sweep resumes there)
@@ -139,8 +141,14 @@ void launch_class(const BatchArgs& a, int cls, int variant, int grid, cudaStream
 // Traceback + medians of pairs whose fill was left in the slab (per-call
 // path); d_strides[c] = slab bytes per pipeline of class c.
 void launch_traceback(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
-// Tracebacks + medians of the pairs whose final fill sits in the arena.
-void launch_deferred_traceback(const BatchArgs& a, cudaStream_t s);
+// The per-call backtrace_2d of the kept linear fill of a one-pair batch (in
+// its arena region, or in its pipeline's slab), one warp through the window.
+void launch_call_traceback_lin(const BatchArgs& a, const long long* d_strides, cudaStream_t s);
+// Tracebacks + medians of the pairs whose final fill sits in the arena: one
+// thread per pair, or (small batches, latency-bound) one warp per pair
+// through the shared-memory window for byte-coded fills. Returns the
+// launches made.
+int launch_deferred_traceback(const BatchArgs& a, bool warp_per_pair, cudaStream_t s);
 // Pipelines per CTA of a class launch.
 int class_pipes_per_cta(const Ladder& lad, int affine, int cls, int variant, int row_tile);
 // Column-wise medians of already aligned pairs (ancestor_2 / with-gaps / worst).
@@ -163,6 +171,8 @@ struct LimitWalk {
     const int* slab_cta;
     const int* passes;
     const int* pfull;
+    const long long* dm_off;   // the fill's arena region (-1: in the slab)
+    const uint8_t* dm_arena;
     Ladder lad;
     const uint8_t* s1;
     const uint8_t* s2;

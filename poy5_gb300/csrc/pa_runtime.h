@@ -60,6 +60,7 @@ struct poyalgn_ctx {
     // per-call staging: one device block (offsets, lengths, tie, sequences)
     // filled from one pinned host block, and a pinned block for the results
     pa::DevBuf callblk;
+    bool skip_deferred = false;  // simple_2: the traceback waits for backtrace_2d
     unsigned char* h_in = nullptr;
     size_t h_in_n = 0;
     unsigned char* h_out = nullptr;
