@@ -68,6 +68,8 @@ constexpr int ROW_TILE_MAX_PAIRS = 2;  // per SM, for row_tile_mode 2
 constexpr int SPEC_FULL_PAIRS = 8;
 // batches of at most this many pairs per SM trace back a warp per pair
 constexpr int WIN_TB_PAIRS = 8;
+// batches of at most this many pairs launch only their non-empty classes
+constexpr int HOST_PLAN_PAIRS = 4;
 constexpr int SPEC_MAX_PAIRS = 32;
 // Largest arena region one pair's fills in one class may take; wider fills
 // (long pairs) keep the pipeline's slab and trace back in the class kernel.
@@ -80,6 +82,22 @@ constexpr int SPEC2_MIN_LEN = 8192;
 constexpr long long DM_MAX_REGION2 = 512LL << 20;
 constexpr long long ARENA_MAX = 64LL << 30;
 constexpr long long ARENA_MAX_SPEC2 = 192LL << 30;
+
+// A pinned host buffer that only grows.
+int pinned(unsigned char** p, size_t* n, size_t want)
+{
+    if (*n >= want) return 0;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *n = 0;
+    if (cudaHostAlloc((void**)p, want, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_err(POYALGN_ENOMEM, "pinned staging of %zu bytes", want);
+    }
+    *n = want;
+    return 0;
+}
 
 // Enqueue one batch on `st`. All pointers are device pointers. `out_total`
 // bounds out_off[k] + cap_k (sizes the affine row-0 scratch).
@@ -297,8 +315,27 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
     // the prep slot of a speculative batch also holds its speculative sweep
     if (ev && !spec_S) CU(cudaEventRecord(ev[1], st));
     const int sort_grid = std::max(1, std::min(2 * c->nsm, (items + 255) / 256));
+    // A batch of a few pairs (the per-call stubs) reads its queue counts
+    // back before each sweep, so that a speculative sweep launches only its
+    // non-empty classes and the sequential sweep starts at the lowest
+    // non-empty class (items only move up the ladder) or is skipped: two
+    // short synchronisations instead of dozens of empty launches.
+    const bool host_plan = !capturing && !ev && npairs <= HOST_PLAN_PAIRS;
+    int qcnt[NQUEUE];
+    auto read_counts = [&]() -> int {
+        if ((rc = pinned(&c->h_q, &c->h_q_n, NQUEUE * sizeof(int)))) return rc;
+        CU(cudaMemcpyAsync(c->h_q, c->qctr.p, NQUEUE * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        memcpy(qcnt, c->h_q, sizeof(qcnt));
+        return 0;
+    };
     auto sweep = [&]() -> int {
-        for (int k = 0; k < NCLASS; k++) {
+        int k0 = 0;
+        if (host_plan) {
+            if ((rc = read_counts())) return rc;
+            while (k0 < NCLASS && qcnt[2 * k0] == 0 && qcnt[2 * k0 + 1] == 0) k0++;
+        }
+        for (int k = k0; k < NCLASS; k++) {
             A.slab_stride = strides[k];
             launch_sort_queues(A, k, sort_grid, st);
             launches += 2;
@@ -321,14 +358,16 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
             }
         }
         auto spec_sweep = [&](int phase) -> int {
+            const int v = affine ? 1 : 0;
+            if (host_plan && (rc = read_counts())) return rc;
             A.spec = phase;
             CU(cudaEventRecord(c->spec_fork, st));
-            const int v = affine ? 1 : 0;
             // the second sweep's passes are the wide ones: the widest class
             // goes first, so its long passes start at once and the narrower
             // classes fill the SMs it leaves
             for (int i = 0; i < NCLASS; i++) {
                 const int k = phase == 2 ? NCLASS - 1 - i : i;
+                if (host_plan && qcnt[2 * k + v] == 0) continue;
                 cudaStream_t sk = c->spec_st[k];
                 CU(cudaStreamWaitEvent(sk, c->spec_fork, 0));
                 A.slab_stride = strides[k];
@@ -490,21 +529,6 @@ int upload_cm(poyalgn_cm* m)
     return 0;
 }
 
-// A pinned host buffer that only grows.
-int pinned(unsigned char** p, size_t* n, size_t want)
-{
-    if (*n >= want) return 0;
-    if (*p) cudaFreeHost(*p);
-    *p = nullptr;
-    *n = 0;
-    if (cudaHostAlloc((void**)p, want, cudaHostAllocDefault) != cudaSuccess) {
-        cudaGetLastError();
-        *p = nullptr;
-        return set_err(POYALGN_ENOMEM, "pinned staging of %zu bytes", want);
-    }
-    *n = want;
-    return 0;
-}
 
 // Per-call block layout: offa, offb, out_off (3 int64), lena, lenb, tie,
 // deltawh (4 int32), then both sequences from byte CALL_SEQ.
@@ -611,6 +635,7 @@ void poyalgn_free(poyalgn_ctx* c)
         if (b->p) cudaFree(b->p);
     if (c->h_in) cudaFreeHost(c->h_in);
     if (c->h_out) cudaFreeHost(c->h_out);
+    if (c->h_q) cudaFreeHost(c->h_q);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     for (int k = 0; k < NCLASS; k++) {
         if (c->spec_st[k]) cudaStreamDestroy(c->spec_st[k]);

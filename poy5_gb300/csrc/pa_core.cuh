@@ -1473,6 +1473,7 @@ constexpr int LW_ROWS = 64;
 constexpr int LW_WORDS = LW_ROWS / 4 + 1;
 constexpr int LW_SMEM_WORDS = LW_DIAG * LW_WORDS;
 
+template <bool POW2 = true>  // P R a power of two (every linear class)
 struct LinDmWindow {
     const uint8_t* dm;
     uint32_t* win;   // LW_SMEM_WORDS words (shared memory on the device)
@@ -1484,11 +1485,13 @@ struct LinDmWindow {
 
     PA_HDM int slot(int i) const  // byte of row i >= 1 in its step
     {
-        return (pr & (pr - 1)) == 0 ? (i - 1) & (pr - 1) : (i - 1) % pr;
+        if constexpr (POW2) return (i - 1) & (pr - 1);
+        else return (i - 1) % pr;
     }
-    PA_HDM int wmod(int w) const  // w modulo the words of a step, w > -prw
+    PA_HDM int wmod(int w) const  // w modulo the words of a step, w >= -prw
     {
-        return (prw & (prw - 1)) == 0 ? w & (prw - 1) : (w + prw) % prw;
+        if constexpr (POW2) return w & (prw - 1);
+        else return (w + prw) % prw;
     }
     PA_HDM void refill(int i, int T)
     {
@@ -1520,8 +1523,9 @@ struct LinDmWindow {
 };
 
 // Lean affine codes (one byte per cell, same slab layout) through the window.
+template <bool POW2>
 struct AffDmLeanWindow {
-    LinDmWindow w;
+    LinDmWindow<POW2> w;
     PA_HDM int operator()(int i, int j) { return lean_flags(w(i, j)); }
 };
 

@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                 // window of the slab (one round of loads per LW_DIAG steps)
                 if (p.gl < 32) {
                     extern __shared__ uint32_t lin_win[];
-                    LinDmWindow rd{dm, lin_win + (p.K == 1 ? (threadIdx.x >> 5) : 0) * LW_SMEM_WORDS,
+                    LinDmWindow<> rd{dm, lin_win + (p.K == 1 ? (threadIdx.x >> 5) : 0) * LW_SMEM_WORDS,
                                    p.P * R, p.P * R / 4, p.lane, 32};
                     r = lin_traceback_dm(rd, st, w.x, w.m, w.y, w.n, w.tie, pair_out(A, w.k));
                     lead = p.gl == 0;
@@ -1697,13 +1697,17 @@ __global__ void __launch_bounds__(32 * LWARP_WARPS)
     const int tie = A.swap_override ? A.swap_override[k] : swaped;
     const int cls = A.lastcls[k] & LASTCLS_MASK;
     const int PR = A.lad.P[cls] * A.lad.R[cls];
-    LinDmWindow w{A.dm_arena + A.dm_off[k], win[wib], PR, PR / 4, lane, 32};
+    const uint8_t* base = A.dm_arena + A.dm_off[k];
     PairRes r;
-    if (A.affine) {
-        AffDmLeanWindow rd{w};
-        r = aff_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
-    } else {
+    if (!A.affine) {
+        LinDmWindow<> w{base, win[wib], PR, PR / 4, lane, 32};
         r = lin_traceback_dm(w, t, x, m, y, n, tie, pair_out(A, k));
+    } else if ((PR & (PR - 1)) == 0) {
+        AffDmLeanWindow<true> rd{LinDmWindow<true>{base, win[wib], PR, PR / 4, lane, 32}};
+        r = aff_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
+    } else {  // the R = 3 classes
+        AffDmLeanWindow<false> rd{LinDmWindow<false>{base, win[wib], PR, PR / 4, lane, 32}};
+        r = aff_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
     }
     if (lane == 0) finish_pair(A, k, A.cost[k], r);
 }
@@ -1749,7 +1753,7 @@ __global__ void __launch_bounds__(32) call_traceback_lin_kernel(BatchArgs A,
     const int PR = A.lad.P[cls] * A.lad.R[cls];
     const uint8_t* base = A.dm_off[0] >= 0 ? A.dm_arena + A.dm_off[0]
                                            : A.slab + (long long)A.slab_cta[0] * strides[cls];
-    LinDmWindow w{base, win, PR, PR / 4, (int)threadIdx.x, 32};
+    LinDmWindow<> w{base, win, PR, PR / 4, (int)threadIdx.x, 32};
     const PairRes r = lin_traceback_dm(w, t, x, m, y, n, tie, pair_out(A, 0));
     if (threadIdx.x == 0) finish_pair(A, 0, A.cost[0], r);
 }

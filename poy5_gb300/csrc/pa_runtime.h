@@ -65,6 +65,8 @@ struct poyalgn_ctx {
     size_t h_in_n = 0;
     unsigned char* h_out = nullptr;
     size_t h_out_n = 0;
+    unsigned char* h_q = nullptr;  // queue counts read back by small batches
+    size_t h_q_n = 0;
     pa::DevBuf nobt_bnd, nobt_ctr, nobt_coop;  // cost-only affine fill scratch
     // Algn_Newkk (pa_newkk.cu): per-warp boundary rows and tile offsets, the
     // direction-code arena, counters, visiting order

@@ -350,7 +350,7 @@ int run_linear(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     // through the window for every class
     if (lin_window_ok(P, R) || E.window_all) {
         std::vector<uint32_t> win(LW_SMEM_WORDS);
-        LinDmWindow rd{dm.data(), win.data(), P * R, P * R / 4, 0, 1};
+        LinDmWindow<> rd{dm.data(), win.data(), P * R, P * R / 4, 0, 1};
         r = lin_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
     } else {
         r = lin_traceback(dm.data(), P, R, t, x, m, y, n, pl.swaped, o);
@@ -446,8 +446,14 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     PairRes r;
     if (lean_last && !rk && E.window_all) {  // as the deferred lean traceback: the window
         std::vector<uint32_t> win(LW_SMEM_WORDS);
-        AffDmLeanWindow rd{LinDmWindow{dm8.data(), win.data(), P * R, P * R / 4, 0, 1}};
-        r = aff_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
+        const int PR = P * R;
+        if ((PR & (PR - 1)) == 0) {
+            AffDmLeanWindow<true> rd{LinDmWindow<true>{dm8.data(), win.data(), PR, PR / 4, 0, 1}};
+            r = aff_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
+        } else {
+            AffDmLeanWindow<false> rd{LinDmWindow<false>{dm8.data(), win.data(), PR, PR / 4, 0, 1}};
+            r = aff_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
+        }
     } else {
         r = (lean_last && rk) ? aff_traceback_rowtile(dm8.data(), 32 * rk, rk_newk, t, x, m, y, n,
                                                       pl.swaped, o)
