@@ -158,6 +158,25 @@ def host_oracle():
     return oracle_lib.Oracle("port"), "port"
 
 
+def host_cpu() -> str:
+    """Model name of this host's CPU (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
 def cpu_rate(w, target_s: float, threads: int, single_thread_ref: bool = True):
     """Cells/s and pairs/s of the host CPU implementation on a bounded
     sample of `w` (pairs taken in order until ~target_s of work)."""
@@ -1007,7 +1026,7 @@ def main(argv=None):
                 "config": {"workload": w.name, "pairs_per_step": rates[0]["pairs"]},
                 "alignments_per_s": round(aps, 2),
                 "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": rates[0]["threads"],
-                                 "kind": kind,
+                                 "kind": kind, "cpu_model": host_cpu(),
                                  "sample": f"first {rates[0]['pairs']} pairs of {w.name} per step"},
                 "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
@@ -1019,7 +1038,7 @@ def main(argv=None):
         cpu = cpu_rate(r["w"], args.cpu_seconds, os.cpu_count() or 1)
         line["cpu_baseline"] = {
             "value": round(cpu["cells_per_s"] / 1e9, 4), "unit": "GCUPS",
-            "cores": cpu["threads"], "kind": cpu["kind"],
+            "cores": cpu["threads"], "kind": cpu["kind"], "cpu_model": host_cpu(),
             "sample": f"first {cpu['pairs']} pairs of {r['w'].name} ({cpu['seconds']:.1f} s)",
             "alignments_per_s": round(cpu["pairs_per_s"], 2)}
         if world == 1 and not args.no_extras:
