@@ -505,6 +505,7 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
     A.next = as<int>(c->nobt_ctr);
     A.next_coop = as<int>(c->nobt_ctr) + 1;
     A.ncoop = nobt_ncoop(c, npairs);
+    A.long_cells = NOBT_LONG_CELLS;
     A.bnd = as<int4>(c->nobt_bnd);
     A.bnd_stride = stride;
     A.coop_cols = as<int4>(c->nobt_coop);

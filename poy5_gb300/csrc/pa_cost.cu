@@ -10,6 +10,12 @@
 // is a min-plus recurrence, solved per row by composing each lane's K maps
 // and an inclusive warp scan of the compositions.
 //
+// Long pairs take a whole CTA instead: its warps split the column blocks
+// and advance one row per barrier, each a row behind the warp to its left.
+// Small batches run every pair that way (nobt_coop_kernel); in large ones
+// the leading pairs of the longest-first order with at least 2^22 cells do
+// (nobt_kernel), so that no single warp is left with a long pair at the end.
+//
 // The reference keeps its rows in one buffer whose current and previous rows
 // overlap by a few words (the previous row starts lenj + 2 ints after the
 // current one, arrays of 2 * largest ints). For lenj >= 2 the only effect is
@@ -203,16 +209,17 @@ __device__ __forceinline__ void nobt_block_begin(NOBT_LANE_PARAMS, const Tables&
             out[0] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
 }
 
-// Row i >= 1 of the block. Reads left[i] (lane 0) before writing out[i]
-// (the last lane), so left and out may be the same column.
+// Row i >= 1 of the block: ic = si[i]; lbv = the block boundary of row i
+// (the previous block's last column; used by lane 0 when blk > 0), read by
+// the caller before this row writes out[i] (the last lane), so the boundary
+// and out may be the same column.
 template <int K>
-__device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t,
-                                               const uint8_t* si, int i, int lenj, int blk,
-                                               int lane, const int4* left, int4* out)
+__device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t, int ic,
+                                               int i, int lenj, int blk, int lane, int4 lbv,
+                                               int4* out)
 {
     const int gap = t.gap, go = t.go;
     const int ip = ic_last;
-    const int ic = si[i];
     ic_last = ic;
     const int sgext = tcost(t, ic, gap);
     const int sgop = gap_open_cost(i, ip, ic, gap, go);
@@ -230,7 +237,7 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
     int4 lb = make_int4(HIGH, HIGH, HIGH, HIGH);  // block boundary, row i
     if (lane == 0) {
         dg = dprev;
-        if (blk > 0) lb = left[i];
+        if (blk > 0) lb = lbv;
         dprev = lb;
     }
     int nEV[K], nEB[K], nCB[K];
@@ -312,10 +319,15 @@ __device__ __forceinline__ int nobt_block_result(NOBT_LANE_PARAMS, int lane)
     return __shfl_sync(FULL, r, last_lane);
 }
 
-// One warp, blocks in sequence; bnd: one column (the block boundary).
+// One warp, blocks in sequence; bnd: one column (the block boundary), read
+// and rewritten row by row. The rows arrive in groups of 32: while a group
+// runs from this warp's shared pfb / pfs (boundary words and row bases),
+// each lane already holds one row of the next group in registers, so no row
+// waits for its boundary word to come back from L2. A group's prefetch reads
+// rows this block has not yet rewritten.
 template <int K>
 __device__ __forceinline__ int nobt_warp(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
-                         int4* bnd, int lane)
+                         int4* bnd, int lane, int4* pfb, uint8_t* pfs)
 {
     const int leni = li - 1, lenj = lj - 1;
     const int nblk = (lenj + 1 + 32 * K - 1) / (32 * K);
@@ -323,45 +335,80 @@ __device__ __forceinline__ int nobt_warp(const Tables& t, const uint8_t* si, int
     int result = 0;
     for (int blk = 0; blk < nblk; blk++) {
         nobt_block_begin<K>(NOBT_LANE_ARGS, t, si, sj, lenj, blk, lane, bnd, bnd);
-        for (int i = 1; i <= leni; i++)
-            nobt_block_row<K>(NOBT_LANE_ARGS, t, si, i, lenj, blk, lane, bnd, bnd);
+        int4 rb = make_int4(HIGH, HIGH, HIGH, HIGH);
+        int rs = 0;
+        if (1 + lane <= leni) {
+            rs = si[1 + lane];
+            if (blk > 0) rb = bnd[1 + lane];
+        }
+        for (int i0 = 1; i0 <= leni; i0 += 32) {
+            __syncwarp();
+            pfb[lane] = rb;
+            pfs[lane] = (uint8_t)rs;
+            __syncwarp();
+            const int r = i0 + 32 + lane;
+            if (r <= leni) {
+                rs = si[r];
+                if (blk > 0) rb = bnd[r];
+            }
+            const int n = tmin(32, leni - i0 + 1);
+            for (int q = 0; q < n; q++)
+                nobt_block_row<K>(NOBT_LANE_ARGS, t, pfs[q], i0 + q, lenj, blk, lane, pfb[q],
+                                  bnd);
+        }
         __syncwarp();
         if (blk == nblk - 1) result = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
     }
     return result;
 }
 
+// CTA barrier that the warps may reach from different loops (non-aligned
+// barrier.sync): the cooperative schedule below has every warp execute the
+// same number of them, from a stagger, its rows and a pad loop. It orders
+// the warps' global writes before the other warps' later reads.
+__device__ __forceinline__ void cta_barrier() { asm volatile("barrier.sync 0;" ::: "memory"); }
+
 // All NW warps of the CTA on one pair: warp w takes blocks w, w + NW, ...
 // and the warps advance one row per barrier, warp w a row behind warp w - 1,
 // so block b + 1 reads block b's last column one row after it is written.
-// cols: one column (rows 0..leni) per block.
-template <int K, int NW>
+// cols: one column (rows 0..leni) per block; RING: one per warp instead,
+// rewritten block after block. Warp w - 1 rewrites row i of its column
+// rows - 1 barriers after warp w read it, and warp 0 reads warp NW - 1's
+// column rows - NW + 1 barriers after it was written, so with li >= NW
+// every read sees the previous block's row and no later one.
+template <int K, int NW, bool RING = false>
 __device__ __forceinline__ int nobt_coop(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
                          int4* cols, int col_stride, int warp, int lane, int* sres)
 {
     const int leni = li - 1, lenj = lj - 1;
     const int nblk = (lenj + 1 + 32 * K - 1) / (32 * K);
     const int rows = leni + 1;
+    // barriers of the schedule: the warp owning the last block finishes its
+    // last row at step total - 1; every warp pads to total
     const long long total = (long long)((nblk - 1) / NW) * rows + rows + (nblk - 1) % NW;
     NOBT_LANE_DECL;
-    for (long long it = 0; it < total; it++) {
-        const long long u = it - warp;
-        if (u >= 0) {
-            const int bi = (int)(u / rows), i = (int)(u % rows);
-            const int blk = warp + bi * NW;
-            if (blk < nblk) {
-                const int4* left = cols + (long long)(blk > 0 ? blk - 1 : 0) * col_stride;
-                int4* out = cols + (long long)blk * col_stride;
-                if (i == 0) nobt_block_begin<K>(NOBT_LANE_ARGS, t, si, sj, lenj, blk, lane, left, out);
-                else nobt_block_row<K>(NOBT_LANE_ARGS, t, si, i, lenj, blk, lane, left, out);
-                if (blk == nblk - 1 && i == leni) {
-                    const int r = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
-                    if (lane == 0) *sres = r;
-                }
+    long long it = 0;
+    for (; it < warp; it++) cta_barrier();
+    for (int blk = warp; blk < nblk; blk += NW) {
+        const int4* left = RING ? cols + (long long)((warp + NW - 1) % NW) * col_stride
+                                : cols + (long long)(blk > 0 ? blk - 1 : 0) * col_stride;
+        int4* out = cols + (long long)(RING ? warp : blk) * col_stride;
+        nobt_block_begin<K>(NOBT_LANE_ARGS, t, si, sj, lenj, blk, lane, left, out);
+        cta_barrier();
+        it++;
+        for (int i = 1; i <= leni; i++) {
+            nobt_block_row<K>(NOBT_LANE_ARGS, t, si[i], i, lenj, blk, lane,
+                              (lane == 0 && blk > 0) ? left[i] : make_int4(HIGH, HIGH, HIGH, HIGH),
+                              out);
+            if (blk == nblk - 1 && i == leni) {
+                const int r = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
+                if (lane == 0) *sres = r;
             }
+            cta_barrier();
+            it++;
         }
-        __syncthreads();
     }
+    for (; it < total; it++) cta_barrier();
     return *sres;
 }
 
@@ -421,33 +468,81 @@ __device__ NobtPair nobt_screen(const NobtArgs& A, const Tables& st, int k, int 
     return q;
 }
 
-// Pairs ncoop .. npairs - 1 of the visiting order, one warp each.
-__global__ void __launch_bounds__(32 * NOBT_WARPS) nobt_kernel(NobtArgs A)
+// The first position of the order in [ncoop, npairs) whose pair has fewer
+// than long_cells cells (the order is by la * lb, largest first), minus ncoop.
+__device__ int nobt_count_long(const NobtArgs& A)
+{
+    if (!A.order || A.long_cells <= 0) return 0;
+    int lo = A.ncoop, hi = A.npairs;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int k = A.order[mid];
+        if ((long long)A.lena[k] * A.lenb[k] >= A.long_cells) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo - A.ncoop;
+}
+
+// Pairs ncoop .. npairs - 1 of the visiting order. The leading ones with at
+// least long_cells cells go one per CTA, the CTA's warps splitting the
+// column blocks (nobt_coop over the warps' own boundary columns), so that no
+// single warp is left with a long pair at the end of the launch; the rest go
+// NOBT_WARPS neighbours of the order per fetch, one per warp.
+__global__ void __launch_bounds__(32 * NOBT_WARPS, 3) nobt_kernel(NobtArgs A)
 {
     __shared__ Tables st;
+    __shared__ int4 pfb[NOBT_WARPS][32];
+    __shared__ uint8_t pfs[NOBT_WARPS][32];
+    __shared__ int s_item, s_nlong, sres;
+    if (threadIdx.x == 0) s_nlong = nobt_count_long(A);
     load_tables_smem(st, A.tables);
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int4* bnd = A.bnd + (long long)gw * A.bnd_stride;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int4* cols = A.bnd + (long long)blockIdx.x * NOBT_WARPS * A.bnd_stride;
+    int4* bnd = cols + (long long)warp * A.bnd_stride;
+    const int nlong = s_nlong;
     for (;;) {
-        int w = 0;
-        if (lane == 0) w = A.ncoop + atomicAdd(A.next, 1);
-        w = __shfl_sync(FULL, w, 0);
-        if (w >= A.npairs) break;
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(A.next, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item < nlong) {
+            NobtPair q = nobt_screen(A, st, A.order[A.ncoop + item], lane);
+            if (q.run && q.lj > 2 && q.li >= NOBT_WARPS) {
+                q.cost = nobt_coop<NOBT_K, NOBT_WARPS, true>(st, q.si, q.li, q.sj, q.lj, cols,
+                                                              A.bnd_stride, warp, lane, &sres);
+            } else if (q.run && warp == 0) {
+                if (q.lj <= 2) {
+                    if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
+                    q.cost = __shfl_sync(FULL, q.cost, 0);
+                } else {
+                    q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, bnd, lane, pfb[0],
+                                               pfs[0]);
+                }
+            }
+            if (threadIdx.x == 0) {
+                A.cost[q.k] = q.cost;
+                A.status[q.k] = q.status;
+            }
+            continue;
+        }
+        const int w0 = A.ncoop + nlong + (item - nlong) * NOBT_WARPS;
+        if (w0 >= A.npairs) break;
+        const int w = w0 + warp;
+        if (w >= A.npairs) continue;
         NobtPair q = nobt_screen(A, st, A.order ? A.order[w] : w, lane);
         if (q.run) {
             if (q.lj <= 2) {
                 if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
                 q.cost = __shfl_sync(FULL, q.cost, 0);
             } else {
-                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, bnd, lane);
+                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, bnd, lane, pfb[warp],
+                                           pfs[warp]);
             }
         }
         if (lane == 0) {
             A.cost[q.k] = q.cost;
             A.status[q.k] = q.status;
         }
-        __syncwarp();
     }
 }
 
@@ -457,6 +552,8 @@ __global__ void __launch_bounds__(32 * COOP_WARPS) nobt_coop_kernel(NobtArgs A)
 {
     __shared__ Tables st;
     __shared__ int sw, sres;
+    __shared__ int4 pfb[32];
+    __shared__ uint8_t pfs[32];
     load_tables_smem(st, A.tables);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int4* cols = A.coop_cols + (long long)blockIdx.x * A.coop_stride;
@@ -477,7 +574,7 @@ __global__ void __launch_bounds__(32 * COOP_WARPS) nobt_coop_kernel(NobtArgs A)
                 if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
                 q.cost = __shfl_sync(FULL, q.cost, 0);
             } else {
-                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, cols, lane);
+                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, cols, lane, pfb, pfs);
             }
         }
         if (threadIdx.x == 0) {

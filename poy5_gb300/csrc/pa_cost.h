@@ -23,6 +23,9 @@ struct NobtArgs {
     int* next;                // work counters (one pair per warp; one per CTA), zero
     int* next_coop;           // before the launch
     int ncoop;                // the first ncoop pairs of the order go one per CTA
+                              // (nobt_coop_kernel); the rest to nobt_kernel, which
+    long long long_cells;     // gives its leading pairs of >= long_cells cells a
+                              // CTA each (0: none)
     int4* bnd;                // per warp: block boundary column, bnd_stride rows
     int bnd_stride;           // >= the shorter length of every pair
     int4* coop_cols;          // per CTA of the cooperative kernel: one column per
@@ -30,6 +33,9 @@ struct NobtArgs {
     int* cost;
     int* status;              // 0 ok, -4 empty, -6 too long, -7 bad state
 };
+
+// nobt_kernel: pairs of at least this many cells run one per CTA
+constexpr long long NOBT_LONG_CELLS = 1LL << 22;
 
 int nobt_warps_per_cta();
 int nobt_blocks_per_sm();

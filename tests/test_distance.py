@@ -4,7 +4,7 @@ against the oracle (itself pinned to the reference build)."""
 import numpy as np
 import pytest
 
-from cases import AFF_TCM, STD_TCM, edge_pairs, random_pairs, rseq
+from cases import AFF_TCM, STD_TCM, edge_pairs, mutate, random_pairs, rseq
 from poy5_gb300 import workloads as wl
 
 GAP = 16
@@ -87,3 +87,29 @@ def test_distance_batch_serving_sample(ctx, oracle):
     assert np.all(status == 0)
     for k, (a, b) in enumerate(w.pairs):
         assert cost[k] == oracle.cost_affine(ocm, a, b), k
+
+
+@pytest.mark.gpu
+def test_distance_batch_long_prefix_matches_oracle(ctx, oracle):
+    """A batch large enough for one pair per warp whose longest pairs (at
+    least 2^22 cells) go one per CTA: column-block counts of every residue
+    modulo the CTA's warps, unequal lengths, a long all-gap sequence."""
+    import poy5_gb300 as pg
+    cm = pg.CostMatrix.of_list(ctx, AFF_TCM, 3)
+    ocm = oracle.cm(tcm=AFF_TCM, gap_open=3)
+    rng = np.random.default_rng(47)
+    pairs = random_pairs(rng, 420, maxlen=300)
+    for la, lb in ((2100, 2100), (2400, 2050), (2050, 2600), (2900, 2300), (3300, 2100),
+                   (2200, 4000)):
+        a = rseq(rng, la - 1)
+        b = np.asarray(mutate(rng, a, 0.2, 0.03), np.uint8)
+        b = b[:lb] if len(b) >= lb else np.concatenate([b, rseq(rng, lb - len(b))[1:]])
+        pairs.append((a, b))
+    pairs.append((np.full(2100, GAP, np.uint8), rseq(rng, 2100)))
+    order = rng.permutation(len(pairs))
+    pairs = [pairs[k] for k in order]
+    assert len(pairs) > 2 * 152
+    cost, status = pg.distance_batch(ctx, cm, pairs, missing_distance=999)
+    for k, (a, b) in enumerate(pairs):
+        assert status[k] == 0, (k, status[k])
+        assert cost[k] == oracle_distance(oracle, ocm, a, b, True, 999), (k, len(a), len(b))
