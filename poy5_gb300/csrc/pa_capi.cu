@@ -463,7 +463,8 @@ static int nobt_reserve(poyalgn_ctx* c, int npairs, int max_pair_len, int* grid,
     if ((rc = reserve(c->nobt_coop, ncoop > 0 ? (size_t)*cgrid * (size_t)*cstride * sizeof(int4)
                                               : sizeof(int4))))
         return rc;
-    if ((rc = reserve(c->nobt_ctr, 2 * sizeof(int)))) return rc;
+    // work counters (2 ints) and the batch's cell total (u64 at byte 8)
+    if ((rc = reserve(c->nobt_ctr, 16))) return rc;
     if ((rc = reserve(c->order, (size_t)std::max(npairs, 1) * 4))) return rc;
     return reserve(c->order_scratch, order_scratch_bytes(std::max(npairs, 1)));
 }
@@ -488,7 +489,7 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
     int grid, cgrid, stride;
     long long cstride;
     if ((rc = nobt_reserve(c, npairs, max_pair_len, &grid, &cgrid, &stride, &cstride))) return rc;
-    CU(cudaMemsetAsync(c->nobt_ctr.p, 0, 2 * sizeof(int), st));
+    CU(cudaMemsetAsync(c->nobt_ctr.p, 0, 16, st));
     if (launch_order(lena, lenb, npairs, as<int>(c->order), c->order_scratch.p, st) != 0)
         return set_err(POYALGN_ECUDA, "ordering pairs failed");
     NobtArgs A;
@@ -506,6 +507,7 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
     A.next_coop = as<int>(c->nobt_ctr) + 1;
     A.ncoop = nobt_ncoop(c, npairs);
     A.long_cells = NOBT_LONG_CELLS;
+    A.total = reinterpret_cast<const unsigned long long*>(as<uint8_t>(c->nobt_ctr) + 8);
     A.bnd = as<int4>(c->nobt_bnd);
     A.bnd_stride = stride;
     A.coop_cols = as<int4>(c->nobt_coop);
@@ -514,7 +516,7 @@ int run_nobt(poyalgn_ctx* c, const poyalgn_cm* cm, int npairs, int max_pair_len,
     A.status = status;
     launch_nobt(A, grid, cgrid, st);
     CU(cudaGetLastError());
-    c->last_launches = 3 + (A.ncoop > 0 && A.ncoop < npairs ? 1 : 0);
+    c->last_launches = 2 + (A.ncoop > 0 ? 1 : 0) + (A.ncoop < npairs ? 2 : 0);
     return 0;
 }
 

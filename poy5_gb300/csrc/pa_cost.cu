@@ -13,8 +13,9 @@
 // Long pairs take a whole CTA instead: its warps split the column blocks
 // and advance one row per barrier, each a row behind the warp to its left.
 // Small batches run every pair that way (nobt_coop_kernel); in large ones
-// the leading pairs of the longest-first order with at least 2^22 cells do
-// (nobt_kernel), so that no single warp is left with a long pair at the end.
+// the leading pairs of the longest-first order with more cells than the
+// batch has per launched warp do (nobt_kernel), so that no single warp is
+// left with a long pair at the end.
 //
 // The reference keeps its rows in one buffer whose current and previous rows
 // overlap by a few words (the previous row starts lenj + 2 ints after the
@@ -136,22 +137,23 @@ __device__ __forceinline__ MinPlus warp_scan(MinPlus f, int lane)
     return f;
 }
 
-// One lane's K columns of a column block: column constants (jc, jgr, gop,
-// shx, jpgap), the previous row of every state (pEH, pEV, pEB, pCB), the
+// One lane's K columns of a column block: column constants (jc, gj = gop +
+// prepend, gop, shx, jpgap, lastm = the bit of column lenj if this lane has
+// it and lenj >= 2), the previous row of every state (pEH, pEV, pEB, pCB), the
 // block geometry and, in lane 0, the previous row's value of column c0 - 1.
 // Kept as separate arrays in the caller so that they stay in registers.
 #define NOBT_LANE_PARAMS                                                                   \
-    int (&jc)[K], int (&jgr)[K], int (&gop)[K], int (&shx)[K], unsigned& jpgap,            \
+    int (&jc)[K], int (&gj)[K], int (&gop)[K], int (&shx)[K], unsigned& jpgap, unsigned& lastm, \
         int (&pEH)[K], int (&pEV)[K], int (&pEB)[K], int (&pCB)[K], int &c0, int &last_lane, \
         int &last_q, int4 &dprev, int &ic_last
 #define NOBT_LANE_DECL                                                                     \
-    int jc[K], jgr[K], gop[K], shx[K];                                                     \
-    unsigned jpgap;                                                                        \
+    int jc[K], gj[K], gop[K], shx[K];                                                      \
+    unsigned jpgap, lastm;                                                                 \
     int pEH[K], pEV[K], pEB[K], pCB[K];                                                    \
     int c0, last_lane, last_q;                                                             \
     int4 dprev;                                                                            \
     int ic_last
-#define NOBT_LANE_ARGS jc, jgr, gop, shx, jpgap, pEH, pEV, pEB, pCB, c0, last_lane, last_q, dprev, ic_last
+#define NOBT_LANE_ARGS jc, gj, gop, shx, jpgap, lastm, pEH, pEV, pEB, pCB, c0, last_lane, last_q, dprev, ic_last
 
 // Start column block `blk`: constants and row 0. left: the previous block's
 // last column (row 0 read here; unused for blk 0); out: this block's last
@@ -165,6 +167,8 @@ __device__ __forceinline__ void nobt_block_begin(NOBT_LANE_PARAMS, const Tables&
     constexpr int W = 32 * K;
     c0 = blk * W + lane * K;
     jpgap = 0;
+    lastm = 0;
+    int jgr[K];
 #pragma unroll
     for (int q = 0; q < K; q++) {
         const int j = c0 + q;
@@ -174,8 +178,10 @@ __device__ __forceinline__ void nobt_block_begin(NOBT_LANE_PARAMS, const Tables&
         jc[q] = c;
         jgr[q] = t.prepend[c];
         gop[q] = (real && j > 0) ? gap_open_cost(j, cp, c, gap, go) : 0;
+        gj[q] = gop[q] + jgr[q];
         shx[q] = (j > 1 && (cp & gap) && !(c & gap)) ? gop[q] + jgr[q] : jgr[q];
         jpgap |= (cp & TMPGAP) ? 1u << q : 0u;
+        lastm |= (j == lenj && lenj >= 2) ? 1u << q : 0u;
     }
     MinPlus f{0, BIG};
 #pragma unroll
@@ -209,6 +215,23 @@ __device__ __forceinline__ void nobt_block_begin(NOBT_LANE_PARAMS, const Tables&
             out[0] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
 }
 
+// The reference's even rows read HIGH for the previous row's EV and CB at
+// column lenj (its overlapping row buffers). Applied to the lane state
+// before the row's cells: the changed words feed no other column of the row
+// (column lenj + 1 does not exist) and the row then overwrites them.
+template <int K>
+__device__ __forceinline__ void even_row_last_column(NOBT_LANE_PARAMS, int i)
+{
+    if ((i & 1) == 0 && lastm) {
+#pragma unroll
+        for (int q = 0; q < K; q++)
+            if ((lastm >> q) & 1) {
+                pEV[q] = HIGH;
+                pCB[q] = HIGH;
+            }
+    }
+}
+
 // Row i >= 1 of the block: ic = si[i]; lbv = the block boundary of row i
 // (the previous block's last column; used by lane 0 when blk > 0), read by
 // the caller before this row writes out[i] (the last lane), so the boundary
@@ -226,7 +249,6 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
     const int sng = ic & NTMPGAP;
     const int srow = t.rowoff[sng];
     const int svext = (i > 1 && (ip & gap) && !(ic & gap)) ? sgop + sgext : sgext;
-    const bool even = (i & 1) == 0 && lenj >= 2;
     // left neighbour: previous row's last column of lane - 1 (lane 0: the
     // block boundary of row i - 1) and, for EH, the current row's
     int4 dg;
@@ -240,6 +262,7 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
         if (blk > 0) lb = lbv;
         dprev = lb;
     }
+    even_row_last_column(NOBT_LANE_ARGS, i);
     int nEV[K], nEB[K], nCB[K];
     int dEH = dg.x, dEV = dg.y, dEB = dg.z, dCB = dg.w;
 #pragma unroll
@@ -247,14 +270,12 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
         const int j = c0 + q;
         const int c = jc[q];
         const int jng = c & NTMPGAP;
-        const bool lastc = even && j == lenj;
-        const int uEV = lastc ? HIGH : pEV[q], uCB = lastc ? HIGH : pCB[q];
         if (j == 0) {
             nEV[q] = pEV[q] + svext;
             nEB[q] = HIGH;
             nCB[q] = HIGH;
         } else {
-            nEV[q] = tmin(uEV + svext, uCB + sgop + sgext);
+            nEV[q] = tmin(pEV[q] + svext, pCB[q] + sgop + sgext);
             const bool flag = (TMPGAP & ic) && (TMPGAP & c);
             const bool flag2 = !(TMPGAP & ip) && !((jpgap >> q) & 1);
             const int d = flag ? 0 : HIGH;
@@ -281,7 +302,7 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
     for (int q = 0; q < K; q++) {
         const int j = c0 + q;
         const MinPlus g = j == 0 ? MinPlus{BIG, HIGH}
-                                 : MinPlus{shx[q], tmin(cprev + gop[q] + jgr[q], BIG)};
+                                 : MinPlus{shx[q], tmin(cprev + gj[q], BIG)};
         f = compose(f, g);
         cprev = nCB[q];
     }
@@ -293,7 +314,7 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
 #pragma unroll
     for (int q = 0; q < K; q++) {
         const int j = c0 + q;
-        x = j == 0 ? HIGH : tmin(x + shx[q], cprev + gop[q] + jgr[q]);
+        x = j == 0 ? HIGH : tmin(x + shx[q], cprev + gj[q]);
         pEH[q] = x;
         pEV[q] = nEV[q];
         pEB[q] = nEB[q];
@@ -305,6 +326,118 @@ __device__ __forceinline__ void nobt_block_row(NOBT_LANE_PARAMS, const Tables& t
     for (int q = 0; q < K; q++)
         if (lane == last_lane && q == last_q)
             out[i] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
+}
+
+// Composition without the BIG clamps, for rows whose values all stay below
+// BIG: a "no path" term then only grows by the row's costs (far from 2^31),
+// and apply() gives what the clamped maps give.
+__device__ __forceinline__ MinPlus compose_nc(MinPlus f, MinPlus g)
+{
+    return MinPlus{f.s + g.s, __viaddmin_s32(f.t, g.s, g.t)};
+}
+__device__ __forceinline__ MinPlus warp_scan_nc(MinPlus f, int lane)
+{
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int ps = __shfl_up_sync(FULL, f.s, d);
+        const int pt = __shfl_up_sync(FULL, f.t, d);
+        if (lane >= d) f = compose_nc(MinPlus{ps, pt}, f);
+    }
+    return f;
+}
+
+// Row i of the block when the row's base carries neither gap bit and the
+// gap opening is not negative (the usual DNA row). Then the row's gap
+// opening is go, the EB path from EB / CB is closed (+ HIGH), the diagonal
+// gap-opening term is go, and CB's four terms share the substitution cost:
+//   CB = min(min(CB', EV', EB' + go) + c(i, j), EH' + c(i, j) + go [j gapped])
+// with tab[ic][jc] = {c(i, j), c(i, j) + (go if column j's base has the gap
+// bit)}. Same values as nobt_block_row while every value is below BIG.
+template <int K>
+__device__ __forceinline__ void nobt_block_row_plain(NOBT_LANE_PARAMS, const Tables& t,
+                                                     const int2* tab, int ic, int i, int blk,
+                                                     int lane, int4 lbv, int4* out)
+{
+    const int gap = t.gap, go = t.go;
+    const int ip = ic_last;
+    ic_last = ic;
+    const int sgext = tcost(t, ic, gap);
+    const int svext = (i > 1 && (ip & gap)) ? go + sgext : sgext;
+    const int sgoe = go + sgext;
+    const int2* tr = tab + ic * 32;
+    int4 dg;
+    dg.x = __shfl_up_sync(FULL, pEH[K - 1], 1);
+    dg.y = __shfl_up_sync(FULL, pEV[K - 1], 1);
+    dg.z = __shfl_up_sync(FULL, pEB[K - 1], 1);
+    dg.w = __shfl_up_sync(FULL, pCB[K - 1], 1);
+    int4 lb = make_int4(HIGH, HIGH, HIGH, HIGH);
+    if (lane == 0) {
+        dg = dprev;
+        if (blk > 0) lb = lbv;
+        dprev = lb;
+    }
+    even_row_last_column(NOBT_LANE_ARGS, i);
+    const bool z0 = c0 == 0;  // this lane holds column 0
+    int nEV[K], nEB[K], nCB[K];
+    int dEH = dg.x, dEV = dg.y, dEB = dg.z, dCB = dg.w;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const int2 cc = tr[jc[q]];
+        nEV[q] = __viaddmin_s32(pEV[q], svext, pCB[q] + sgoe);
+        nEB[q] = tmin(dEB, dCB) + HIGH;
+        nCB[q] = __viaddmin_s32(__vimin3_s32(dCB, dEV, dEB + go), cc.x, dEH + cc.y);
+        dEH = pEH[q];
+        dEV = pEV[q];
+        dEB = pEB[q];
+        dCB = pCB[q];
+    }
+    if (z0) {
+        nEV[0] = pEV[0] + svext;
+        nEB[0] = HIGH;
+        nCB[0] = HIGH;
+    }
+    const int cbl = __shfl_up_sync(FULL, nCB[K - 1], 1);
+    const int cin = lane == 0 ? lb.w : cbl;
+    int cprev = cin;
+    MinPlus f = z0 ? MinPlus{BIG, HIGH} : MinPlus{shx[0], cprev + gj[0]};
+    cprev = nCB[0];
+#pragma unroll
+    for (int q = 1; q < K; q++) {
+        f = compose_nc(f, MinPlus{shx[q], cprev + gj[q]});
+        cprev = nCB[q];
+    }
+    const MinPlus pre = warp_scan_nc(f, lane);
+    const MinPlus ex{__shfl_up_sync(FULL, pre.s, 1), __shfl_up_sync(FULL, pre.t, 1)};
+    const int lbx = __shfl_sync(FULL, lb.x, 0);
+    int x = lane == 0 ? lbx : __viaddmin_s32(lbx, ex.s, ex.t);
+    cprev = cin;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        x = __viaddmin_s32(x, shx[q], cprev + gj[q]);
+        if (q == 0 && z0) x = HIGH;
+        pEH[q] = x;
+        pEV[q] = nEV[q];
+        pEB[q] = nEB[q];
+        pCB[q] = nCB[q];
+        cprev = nCB[q];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < K; q++)
+        if (lane == last_lane && q == last_q)
+            out[i] = make_int4(pEH[q], pEV[q], pEB[q], pCB[q]);
+}
+
+// Row i of the block, by its kind (tab null: every row the general way).
+template <int K>
+__device__ __forceinline__ void nobt_row(NOBT_LANE_PARAMS, const Tables& t, const int2* tab,
+                                         int ic, int i, int lenj, int blk, int lane, int4 lbv,
+                                         int4* out)
+{
+    if (tab && !(ic & (TMPGAP | t.gap)))
+        nobt_block_row_plain<K>(NOBT_LANE_ARGS, t, tab, ic, i, blk, lane, lbv, out);
+    else
+        nobt_block_row<K>(NOBT_LANE_ARGS, t, ic, i, lenj, blk, lane, lbv, out);
 }
 
 // min of the four states of the block's last column (valid in every lane)
@@ -326,8 +459,9 @@ __device__ __forceinline__ int nobt_block_result(NOBT_LANE_PARAMS, int lane)
 // waits for its boundary word to come back from L2. A group's prefetch reads
 // rows this block has not yet rewritten.
 template <int K>
-__device__ __forceinline__ int nobt_warp(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
-                         int4* bnd, int lane, int4* pfb, uint8_t* pfs)
+__device__ __forceinline__ int nobt_warp(const Tables& t, const int2* tab, const uint8_t* si, int li,
+                                         const uint8_t* sj, int lj, int4* bnd, int lane,
+                                         int4* pfb, uint8_t* pfs)
 {
     const int leni = li - 1, lenj = lj - 1;
     const int nblk = (lenj + 1 + 32 * K - 1) / (32 * K);
@@ -353,8 +487,7 @@ __device__ __forceinline__ int nobt_warp(const Tables& t, const uint8_t* si, int
             }
             const int n = tmin(32, leni - i0 + 1);
             for (int q = 0; q < n; q++)
-                nobt_block_row<K>(NOBT_LANE_ARGS, t, pfs[q], i0 + q, lenj, blk, lane, pfb[q],
-                                  bnd);
+                nobt_row<K>(NOBT_LANE_ARGS, t, tab, pfs[q], i0 + q, lenj, blk, lane, pfb[q], bnd);
         }
         __syncwarp();
         if (blk == nblk - 1) result = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
@@ -377,8 +510,9 @@ __device__ __forceinline__ void cta_barrier() { asm volatile("barrier.sync 0;" :
 // column rows - NW + 1 barriers after it was written, so with li >= NW
 // every read sees the previous block's row and no later one.
 template <int K, int NW, bool RING = false>
-__device__ __forceinline__ int nobt_coop(const Tables& t, const uint8_t* si, int li, const uint8_t* sj, int lj,
-                         int4* cols, int col_stride, int warp, int lane, int* sres)
+__device__ __forceinline__ int nobt_coop(const Tables& t, const int2* tab, const uint8_t* si, int li,
+                                         const uint8_t* sj, int lj, int4* cols, int col_stride,
+                                         int warp, int lane, int* sres)
 {
     const int leni = li - 1, lenj = lj - 1;
     const int nblk = (lenj + 1 + 32 * K - 1) / (32 * K);
@@ -397,9 +531,8 @@ __device__ __forceinline__ int nobt_coop(const Tables& t, const uint8_t* si, int
         cta_barrier();
         it++;
         for (int i = 1; i <= leni; i++) {
-            nobt_block_row<K>(NOBT_LANE_ARGS, t, si[i], i, lenj, blk, lane,
-                              (lane == 0 && blk > 0) ? left[i] : make_int4(HIGH, HIGH, HIGH, HIGH),
-                              out);
+            nobt_row<K>(NOBT_LANE_ARGS, t, tab, si[i], i, lenj, blk, lane,
+                        (lane == 0 && blk > 0) ? left[i] : make_int4(HIGH, HIGH, HIGH, HIGH), out);
             if (blk == nblk - 1 && i == leni) {
                 const int r = nobt_block_result<K>(NOBT_LANE_ARGS, lane);
                 if (lane == 0) *sres = r;
@@ -421,6 +554,20 @@ __device__ __forceinline__ void load_tables_smem(Tables& st, const Tables* g)
     for (int k = threadIdx.x; k < (int)(sizeof(Tables) / 4); k += blockDim.x)
         reinterpret_cast<int*>(&st)[k] = reinterpret_cast<const int*>(g)[k];
     __syncthreads();
+}
+
+// The plain rows' table (nobt_block_row_plain): tab[a * 32 + b] = {c(a, b &
+// 15), c(a, b & 15) + (go if b has bits above the base's)} for row bases
+// a < 16; null when go < 0 (every row then takes the general way).
+__device__ __forceinline__ const int2* build_row_table(int2* tab, const Tables& st)
+{
+    for (int k = threadIdx.x; k < 16 * 32; k += blockDim.x) {
+        const int a = k >> 5, b = k & 31;
+        const int v = st.csw[st.rowoff[a] + (b & NTMPGAP)];
+        tab[k] = make_int2(v, v + ((b & NTMPGAP) == b ? 0 : st.go));
+    }
+    __syncthreads();
+    return st.go >= 0 ? tab : nullptr;
 }
 
 // Pair k's screening, as DOS.distance / cost_affine_3 need it (warp-uniform).
@@ -468,16 +615,34 @@ __device__ NobtPair nobt_screen(const NobtArgs& A, const Tables& st, int k, int 
     return q;
 }
 
+// Sum of la * lb over the batch into *A.total.
+__global__ void nobt_total_kernel(NobtArgs A)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long c = k < A.npairs ? (unsigned long long)A.lena[k] * A.lenb[k] : 0ull;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(FULL, c, d);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(const_cast<unsigned long long*>(A.total), c);
+}
+
 // The first position of the order in [ncoop, npairs) whose pair has fewer
-// than long_cells cells (the order is by la * lb, largest first), minus ncoop.
+// cells than the CTA threshold (the order is by la * lb, largest first),
+// minus ncoop. A pair above the batch's cells per launched warp would, on
+// one warp, outlast the others' share of the batch.
 __device__ int nobt_count_long(const NobtArgs& A)
 {
     if (!A.order || A.long_cells <= 0) return 0;
+    long long thr = A.long_cells;
+    if (A.total) {
+        const long long per_warp =
+            (long long)(*A.total / ((unsigned long long)gridDim.x * NOBT_WARPS));
+        thr = per_warp > thr ? per_warp : thr;
+    }
     int lo = A.ncoop, hi = A.npairs;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         const int k = A.order[mid];
-        if ((long long)A.lena[k] * A.lenb[k] >= A.long_cells) lo = mid + 1;
+        if ((long long)A.lena[k] * A.lenb[k] >= thr) lo = mid + 1;
         else hi = mid;
     }
     return lo - A.ncoop;
@@ -494,8 +659,10 @@ __global__ void __launch_bounds__(32 * NOBT_WARPS, 3) nobt_kernel(NobtArgs A)
     __shared__ int4 pfb[NOBT_WARPS][32];
     __shared__ uint8_t pfs[NOBT_WARPS][32];
     __shared__ int s_item, s_nlong, sres;
+    __shared__ int2 tabs[16 * 32];
     if (threadIdx.x == 0) s_nlong = nobt_count_long(A);
     load_tables_smem(st, A.tables);
+    const int2* tab = build_row_table(tabs, st);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int4* cols = A.bnd + (long long)blockIdx.x * NOBT_WARPS * A.bnd_stride;
     int4* bnd = cols + (long long)warp * A.bnd_stride;
@@ -508,14 +675,14 @@ __global__ void __launch_bounds__(32 * NOBT_WARPS, 3) nobt_kernel(NobtArgs A)
         if (item < nlong) {
             NobtPair q = nobt_screen(A, st, A.order[A.ncoop + item], lane);
             if (q.run && q.lj > 2 && q.li >= NOBT_WARPS) {
-                q.cost = nobt_coop<NOBT_K, NOBT_WARPS, true>(st, q.si, q.li, q.sj, q.lj, cols,
+                q.cost = nobt_coop<NOBT_K, NOBT_WARPS, true>(st, tab, q.si, q.li, q.sj, q.lj, cols,
                                                               A.bnd_stride, warp, lane, &sres);
             } else if (q.run && warp == 0) {
                 if (q.lj <= 2) {
                     if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
                     q.cost = __shfl_sync(FULL, q.cost, 0);
                 } else {
-                    q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, bnd, lane, pfb[0],
+                    q.cost = nobt_warp<NOBT_K>(st, tab, q.si, q.li, q.sj, q.lj, bnd, lane, pfb[0],
                                                pfs[0]);
                 }
             }
@@ -535,7 +702,7 @@ __global__ void __launch_bounds__(32 * NOBT_WARPS, 3) nobt_kernel(NobtArgs A)
                 if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
                 q.cost = __shfl_sync(FULL, q.cost, 0);
             } else {
-                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, bnd, lane, pfb[warp],
+                q.cost = nobt_warp<NOBT_K>(st, tab, q.si, q.li, q.sj, q.lj, bnd, lane, pfb[warp],
                                            pfs[warp]);
             }
         }
@@ -554,7 +721,9 @@ __global__ void __launch_bounds__(32 * COOP_WARPS) nobt_coop_kernel(NobtArgs A)
     __shared__ int sw, sres;
     __shared__ int4 pfb[32];
     __shared__ uint8_t pfs[32];
+    __shared__ int2 tabs[16 * 32];
     load_tables_smem(st, A.tables);
+    const int2* tab = build_row_table(tabs, st);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int4* cols = A.coop_cols + (long long)blockIdx.x * A.coop_stride;
     for (;;) {
@@ -567,14 +736,14 @@ __global__ void __launch_bounds__(32 * COOP_WARPS) nobt_coop_kernel(NobtArgs A)
         const int nblk = (q.lj + 32 * NOBT_K - 1) / (32 * NOBT_K);
         if (q.run && q.lj > 2 && q.li >= COOP_WARPS &&
             (long long)nblk * A.bnd_stride <= A.coop_stride) {
-            q.cost = nobt_coop<NOBT_K, COOP_WARPS>(st, q.si, q.li, q.sj, q.lj, cols,
+            q.cost = nobt_coop<NOBT_K, COOP_WARPS>(st, tab, q.si, q.li, q.sj, q.lj, cols,
                                                     A.bnd_stride, warp, lane, &sres);
         } else if (q.run && warp == 0) {  // short or narrow pairs: warp 0 alone
             if (q.lj <= 2) {
                 if (lane == 0) q.cost = nobt_tiny(st, q.si, q.li, q.sj, q.lj);
                 q.cost = __shfl_sync(FULL, q.cost, 0);
             } else {
-                q.cost = nobt_warp<NOBT_K>(st, q.si, q.li, q.sj, q.lj, cols, lane, pfb, pfs);
+                q.cost = nobt_warp<NOBT_K>(st, tab, q.si, q.li, q.sj, q.lj, cols, lane, pfb, pfs);
             }
         }
         if (threadIdx.x == 0) {
@@ -600,7 +769,10 @@ int nobt_coop_columns(int maxlen) { return (maxlen + 32 * NOBT_K - 1) / (32 * NO
 void launch_nobt(const NobtArgs& a, int grid, int coop_grid, cudaStream_t s)
 {
     if (a.ncoop > 0) nobt_coop_kernel<<<coop_grid, 32 * COOP_WARPS, 0, s>>>(a);
-    if (a.ncoop < a.npairs) nobt_kernel<<<grid, 32 * NOBT_WARPS, 0, s>>>(a);
+    if (a.ncoop < a.npairs) {
+        if (a.total) nobt_total_kernel<<<(a.npairs + 255) / 256, 256, 0, s>>>(a);
+        nobt_kernel<<<grid, 32 * NOBT_WARPS, 0, s>>>(a);
+    }
 }
 
 }  // namespace pa

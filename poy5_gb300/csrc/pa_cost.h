@@ -24,8 +24,9 @@ struct NobtArgs {
     int* next_coop;           // before the launch
     int ncoop;                // the first ncoop pairs of the order go one per CTA
                               // (nobt_coop_kernel); the rest to nobt_kernel, which
-    long long long_cells;     // gives its leading pairs of >= long_cells cells a
-                              // CTA each (0: none)
+                              // gives a CTA each to its leading pairs of at least
+    long long long_cells;     // max(long_cells, *total / warps launched) cells
+    const unsigned long long* total;  // cells of all pairs (null: long_cells alone)
     int4* bnd;                // per warp: block boundary column, bnd_stride rows
     int bnd_stride;           // >= the shorter length of every pair
     int4* coop_cols;          // per CTA of the cooperative kernel: one column per
@@ -34,13 +35,14 @@ struct NobtArgs {
     int* status;              // 0 ok, -4 empty, -6 too long, -7 bad state
 };
 
-// nobt_kernel: pairs of at least this many cells run one per CTA
-constexpr long long NOBT_LONG_CELLS = 1LL << 22;
+// nobt_kernel: no pair below this many cells runs one per CTA
+constexpr long long NOBT_LONG_CELLS = 1LL << 16;
 
 int nobt_warps_per_cta();
 int nobt_blocks_per_sm();
 // column blocks of a pair whose longer sequence has maxlen positions
 int nobt_coop_columns(int maxlen);
+// The cost-only launches; a.total (when set) is zero before them.
 void launch_nobt(const NobtArgs& a, int grid, int coop_grid, cudaStream_t s);
 
 }  // namespace pa
