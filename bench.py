@@ -65,6 +65,8 @@ def parse_args(argv=None):
                     help="arrival window of each serving rate")
     ap.add_argument("--serve-slots", type=int, default=2, help="server execution slots")
     ap.add_argument("--serve-batch", type=int, default=8192, help="server pairs per batch")
+    ap.add_argument("--percall-seconds", type=float, default=3.0,
+                    help="timed seconds of each per-call workload (--leg percall)")
     ap.add_argument("--newkk-arena-mb", type=int, default=0,
                     help="bound the Newkk direction arena (MB; 0: library default)")
     ap.add_argument("--mem-gb", type=float, default=0.0,
@@ -406,7 +408,7 @@ def run_percall(local: int, seconds: float = 3.0) -> dict:
     out = {}
     for w in (wl.affine_pairs(n_pairs=4096), wl.plain_pairs()):
         cm = pg.CostMatrix.of_transformations_and_gaps(ctx, w.subs, w.indel, w.gap_open)
-        plain_per_call(ctx, cm, w, seconds=0.3)  # warm-up
+        plain_per_call(ctx, cm, w, seconds=min(0.3, seconds))  # warm-up
         r = plain_per_call(ctx, cm, w, seconds=seconds)
         out[w.name] = {"alignments_per_s": round(r["alignments_per_s"], 1),
                        "gcups": round(r["gcups"], 3), "pairs": r["pairs"]}
@@ -992,7 +994,7 @@ def main(argv=None):
         elif args.leg == "plain":
             out = run_plain(local)
         elif args.leg == "percall":
-            out = run_percall(local)
+            out = run_percall(local, args.percall_seconds)
         elif args.leg == "downpass":
             out = run_downpass(local)
         elif args.leg == "long":
