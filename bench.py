@@ -863,7 +863,29 @@ def run_serving(local: int, seconds: float = 1.0, nslots: int = 2,
     med = sweep(MEDIAN, rates)
     store.close()
     return {"workload": "serving_requests_poisson_1-64pairs_lognormal1000", **cfg,
-            "distance": dist, "median": med}
+            "distance": dist, "median": med, "cpu_baseline": serving_cpu(w)}
+
+
+def serving_cpu(w, target_s: float = 5.0) -> dict:
+    """DOS.median of the serving pool's pairs on all host cores (the host
+    implementation; a pilot of 64 pairs sizes a sample of about target_s)."""
+    host_oracle()
+    import oracle_lib
+    orc = oracle_lib.Oracle("port")
+    ocm = orc.cm(subs=w.subs, indel=w.indel, gap_open=w.gap_open)
+    pairs = w.pairs
+    t0 = time.perf_counter()
+    orc.median_batch(ocm, [a for a, _ in pairs[:64]], [b for _, b in pairs[:64]], True)
+    pilot = time.perf_counter() - t0
+    n = int(min(len(pairs), max(64, 64 * target_s / max(pilot, 1e-6))))
+    sub = pairs[:n]
+    t0 = time.perf_counter()
+    orc.median_batch(ocm, [a for a, _ in sub], [b for _, b in sub], True)
+    dt = time.perf_counter() - t0
+    cells = sum(len(a) * len(b) for a, b in sub)
+    return {"alignments_per_s": round(n / dt, 1), "gcups": round(cells / dt / 1e9, 4),
+            "kind": "port", "cores": os.cpu_count(), "cpu_model": host_cpu(),
+            "sample": f"first {n} pairs of the serving pool, DOS.median ({dt:.1f} s)"}
 
 
 def _reduce(x: float, world: int, op: str) -> float:

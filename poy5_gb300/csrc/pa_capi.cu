@@ -124,9 +124,9 @@ int run_batch(poyalgn_ctx* c, const poyalgn_cm* cm, int affine, int npairs,
         if (npairs <= SPEC_FULL_PAIRS * c->nsm) spec_S = c->spec_passes;
         else if (npairs <= SPEC_MAX_PAIRS * c->nsm) spec_S = std::max(1, c->spec_passes - 2);
     }
-    // the row tile has the lower latency per pass, the lane pipeline the
-    // higher throughput: small batches take the row tile (unless their
-    // passes run speculatively on the lane pipeline)
+    // small batches take the row tile unless their passes run speculatively
+    // on the lane pipeline (one long pair: the row tile's per-row scans cost
+    // more per pass than a lane pipeline's anti-diagonal steps)
     const int row_tile = affine && !spec_S &&
                          (c->row_tile_mode == 1 ||
                           (c->row_tile_mode == 2 && npairs <= ROW_TILE_MAX_PAIRS * c->nsm));

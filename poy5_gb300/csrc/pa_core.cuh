@@ -1617,6 +1617,45 @@ struct AffDmRow {
     }
 };
 
+// Row-tile codes through a window of whole rows that one warp walks
+// together (every lane the same path): rows [ilo, itop] of the region (row
+// i at i * S, contiguous), refilled by all lanes at once with 16-byte loads
+// whenever the walk leaves them. A traceback only moves up or left, so a
+// refill takes the current row and the `rows` - 1 above it. Needs a 16-byte
+// aligned region of at least (i + 1) S bytes for every row i read.
+struct alignas(16) Word16 {
+    uint32_t v[4];
+};
+constexpr int RW_BYTES = 8192;  // row window of one warp
+struct AffDmRowWindow {
+    const uint8_t* dm;
+    Word16* win;     // rows * S bytes (shared memory on the device)
+    int S, newk, rows;
+    int lane, nl;    // this lane, and the lanes that refill together
+    int ilo = 1, itop = 0;  // empty
+
+    PA_HDM void refill(int i)
+    {
+#if defined(__CUDA_ARCH__)
+        __syncwarp();  // every lane is done with the old window
+#endif
+        itop = i;
+        ilo = i - rows + 1 > 0 ? i - rows + 1 : 0;
+        const Word16* src = reinterpret_cast<const Word16*>(dm + (long long)ilo * S);
+        const int n16 = (itop - ilo + 1) * (S >> 4);
+        for (int e = lane; e < n16; e += nl) win[e] = src[e];
+#if defined(__CUDA_ARCH__)
+        __syncwarp();
+#endif
+    }
+    PA_HDM int operator()(int i, int j)
+    {
+        if (i < ilo || i > itop) refill(i);
+        const uint8_t* w8 = reinterpret_cast<const uint8_t*>(win);
+        return lean_flags(w8[(i - ilo) * S + (j - i + newk)]);
+    }
+};
+
 // algn_calculate_from_2_aligned (src/algn.c:3003-3089), bitset alphabet:
 // the cost of an aligned pair under table `cost` (a functor of two
 // states), one gap opening per gap block of either sequence.

@@ -1467,9 +1467,9 @@ __global__ void deferred_traceback_kernel(BatchArgs A, int skip_win)
     __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
-    // lean lane-pipeline fills when deferred_traceback_win_kernel takes them
-    if (skip_win && A.affine && (A.lastcls[k] & (LASTCLS_LEAN | LASTCLS_ROW)) == LASTCLS_LEAN)
-        return;
+    // lean fills when deferred_traceback_win_kernel (lane pipeline) and
+    // deferred_traceback_row_kernel (row tile) take them
+    if (skip_win && A.affine && (A.lastcls[k] & LASTCLS_LEAN)) return;
     const int la = A.lena[k], lb = A.lenb[k];
     const int swaped = la <= lb ? 0 : 1;
     const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
@@ -1712,6 +1712,37 @@ __global__ void __launch_bounds__(32 * LWARP_WARPS)
     if (lane == 0) finish_pair(A, k, A.cost[k], r);
 }
 
+// The same for row-tile fills (lean affine, small batches): one warp per
+// pair through a window of whole rows (AffDmRowWindow, RW_BYTES per warp).
+constexpr int RWARP_WARPS = 4;
+__global__ void __launch_bounds__(32 * RWARP_WARPS) deferred_traceback_row_kernel(BatchArgs A)
+{
+    __shared__ Tables t;
+    __shared__ Word16 win[RWARP_WARPS][RW_BYTES / 16];
+    load_tables(t, A.tables);
+    __syncthreads();
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = blockIdx.x * RWARP_WARPS + wib;
+    // warp-uniform exits
+    if (k >= A.npairs || A.dm_off[k] < 0 || A.status[k] != 0) return;
+    if ((A.lastcls[k] & (LASTCLS_LEAN | LASTCLS_ROW)) != (LASTCLS_LEAN | LASTCLS_ROW)) return;
+    const int la = A.lena[k], lb = A.lenb[k];
+    const int swaped = la <= lb ? 0 : 1;
+    const uint8_t* x = A.seqs + (swaped ? A.offb[k] : A.offa[k]);
+    const uint8_t* y = A.seqs + (swaped ? A.offa[k] : A.offb[k]);
+    const int m = swaped ? lb : la, n = swaped ? la : lb;
+    const int tie = A.swap_override ? A.swap_override[k] : swaped;
+    const int cls = A.lastcls[k] & LASTCLS_MASK;
+    // the final pass's band: T doubled once per pass after the first
+    const PairPlan pl = plan_affine(t, la, lb);
+    const long long T = (long long)pl.T0 << tmax(A.passes[k] - 1, 0);
+    const AffBand b = aff_band(m, n, band_p((int)T, m, n));
+    const int S = 32 * rk_k_for(ladder_cap(A.lad, cls));
+    AffDmRowWindow rd{A.dm_arena + A.dm_off[k], win[wib], S, b.newk, RW_BYTES / S, lane, 32};
+    const PairRes r = aff_traceback_dm(rd, t, x, m, y, n, tie, pair_out(A, k));
+    if (lane == 0) finish_pair(A, k, A.cost[k], r);
+}
+
 }  // namespace
 
 int launch_deferred_traceback(const BatchArgs& a, bool warp_per_pair, cudaStream_t s)
@@ -1725,8 +1756,14 @@ int launch_deferred_traceback(const BatchArgs& a, bool warp_per_pair, cudaStream
     deferred_traceback_win_kernel<<<(a.npairs + LWARP_WARPS - 1) / LWARP_WARPS,
                                     32 * LWARP_WARPS, 0, s>>>(a);
     if (!a.affine) return 1;
+    int n = 2;
+    if (a.row_tile) {
+        deferred_traceback_row_kernel<<<(a.npairs + RWARP_WARPS - 1) / RWARP_WARPS,
+                                        32 * RWARP_WARPS, 0, s>>>(a);
+        n++;
+    }
     deferred_traceback_kernel<<<(a.npairs + threads - 1) / threads, threads, 0, s>>>(a, 1);
-    return 2;
+    return n;
 }
 
 namespace {

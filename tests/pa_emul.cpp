@@ -454,6 +454,11 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
             AffDmLeanWindow<false> rd{LinDmWindow<false>{dm8.data(), win.data(), PR, PR / 4, 0, 1}};
             r = aff_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
         }
+    } else if (lean_last && rk && E.window_all) {  // as the deferred row-tile traceback
+        const int S = 32 * rk;
+        std::vector<Word16> win(RW_BYTES / 16);
+        AffDmRowWindow rd{dm8.data(), win.data(), S, rk_newk, RW_BYTES / S, 0, 1};
+        r = aff_traceback_dm(rd, t, x, m, y, n, pl.swaped, o);
     } else {
         r = (lean_last && rk) ? aff_traceback_rowtile(dm8.data(), 32 * rk, rk_newk, t, x, m, y, n,
                                                       pl.swaped, o)

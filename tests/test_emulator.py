@@ -197,7 +197,8 @@ def test_window_traceback_lean_affine(emul, oracle, row_tile):
     """Lean affine tracebacks (gap-free pairs on the lane pipeline, one byte
     per cell) through the same window as the deferred lean traceback runs
     them, on every affine class including the R = 3 ones, whose P R is not
-    a power of two; row-tile fills keep their own layout."""
+    a power of two; row-tile fills through the window of whole rows the
+    deferred row-tile traceback uses (AffDmRowWindow)."""
     emul.pa_emul_set_window.argtypes = [_P, C.c_int]
     for name in ("golden_affine", "golden_affine_pairs"):
         g = golden_lib.load(name)

@@ -43,11 +43,14 @@ def test_every_candidate_ladder_gives_the_same_results(workload):
 
 @pytest.mark.parametrize("mode", [0, 1])
 def test_lean_paths_match_oracle(oracle, mode):
-    """Gap-free affine pairs on the lane pipeline (0) and on the row tile (1)."""
+    """Gap-free affine pairs on the lane pipeline (0) and on the row tile (1),
+    sequential passes (a speculative batch keeps the lane pipeline), the
+    tracebacks deferred: through the row window for row-tile fills."""
     import poy5_gb300 as pg
     from cases import random_pairs
     ctx = pg.Context(0)
     ctx.set_row_tile(mode)
+    ctx.set_speculation(0)
     w = wl.affine_pairs(n_pairs=160, seed=wl.SEED_BASE + 60)
     rng = np.random.default_rng(61)
     pairs = w.pairs + [(a, b) for a, b in random_pairs(rng, 200, maxlen=700, kinds=1)]
