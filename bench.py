@@ -356,12 +356,30 @@ def run_gpu(args):
         full = schedule.linear_full_plane(pk.lena, pk.lenb, [gaps(a) for a, _ in w.pairs],
                                           [gaps(b) for _, b in w.pairs])
     mnz = cm.tables()["min_non0_cost"]
-    computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, w.affine, full).sum())
+    computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, w.affine, full,
+                                           skipped_passes(w, pk, mnz, full)).sum())
     lib.poyalgn_batch_graph_free(graph)
     return dict(w=w, model=model, n=n, ms=ms, cells=cells, computed=computed, prof=prof,
                 clocks=clk, e2e=e2e, launches=launches_per_step, passes=passes,
                 world=world, rank=rank, pk=pk, plain=plain, tuned=tuned, peak=peak,
                 parity=parity)
+
+
+def skipped_passes(w, pk, mnz: int, full) -> np.ndarray:
+    """Per pair, the leading doubling passes the library counts as run
+    without filling them: linear pairs off the full plane, and affine pairs
+    on the lean cell (no gap state in either sequence, every state far below
+    HIGH: n (largest gap-free cost + gap opening + 1) + gap opening < HIGH / 4
+    for the subs / indel matrix)."""
+    from poy5_gb300 import schedule
+    s = schedule.unstoppable_passes(pk.lena, pk.lenb, mnz, w.affine)
+    if not w.affine:
+        return np.where(np.asarray(full, bool), 0, s)
+    mc = max(w.subs, w.indel)
+    n = np.maximum(pk.lena, pk.lenb).astype(np.int64)
+    gapfree = np.array([not (np.any(a[1:] & 16) or np.any(b[1:] & 16)) for a, b in w.pairs])
+    lean = gapfree & (n * (mc + w.gap_open + 1) + w.gap_open < 1000000 // 4)
+    return np.where(lean, s, 0)
 
 
 def batch_parity(w, pk, ints, bufs) -> dict:
@@ -574,7 +592,8 @@ def run_long(local: int, cpu_pairs: int = 1, parity_pairs: int = 4, n_pairs: int
     full = schedule.linear_full_plane(pk.lena, pk.lenb, [gaps(a) for a, _ in w.pairs],
                                       [gaps(b) for _, b in w.pairs])
     mnz = cm.tables()["min_non0_cost"]
-    computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, False, full).sum())
+    computed = int(schedule.cells_computed(pk.lena, pk.lenb, passes, mnz, False, full,
+                                           skipped_passes(w, pk, mnz, full)).sum())
     # full-length parity: the longest pairs (both sequences past 40 kb)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib

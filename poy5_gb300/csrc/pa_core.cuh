@@ -1374,6 +1374,32 @@ PA_HD bool aff_done(int T, int m, int n, int gapnum)
 PA_HD bool lin_covers(int T, int m, int n) { return (2 * T - (n - m)) / 2 - n + 1 >= 0; }
 PA_HD bool aff_covers(int T, int m, int n) { return (2 * T - (n - m)) / 2 - (n - 1) + 1 >= 0; }
 
+// Leading passes of the doubling that cannot end it. Every path from (0, 0)
+// to (m - 1, n - 1) takes n - m more horizontal steps than vertical ones,
+// so the gap count a pass reports is at least n - m: the linear walk counts
+// one path's insertions and deletions (backtrace_2d_gaps, src/algn.c:978-1005),
+// and the affine counts are, per direction, the largest over the tied
+// predecessors of path counts that start from row 0 / column 0
+// (algn_fill_gapnum, src/algn.c:126-176). The gap test (gapnum + 1 < p
+// linear, gapnum < p affine, p = (T - (n - m)) / 2) then needs
+// T >= 3 (n - m) + 4 (linear) or 3 (n - m) + 2 (affine); a pass below that
+// which does not cover the plane only fails its test. Such passes leave
+// nothing a later pass reads in the linear model or on the lean affine
+// cell (whose row-0 value is a function of the pass index), so those pairs
+// start at T0 << s with s passes counted as run. At most maxp.
+PA_HD int unstoppable_passes(int T0, int m, int n, bool affine, int maxp)
+{
+    const long long thr = 3LL * (n - m) + (affine ? 2 : 4);
+    long long T = T0;
+    int s = 0;
+    while (s < maxp && T > 0 && T < thr &&
+           !(affine ? aff_covers((int)T, m, n) : lin_covers((int)T, m, n))) {
+        T *= 2;
+        s++;
+    }
+    return s;
+}
+
 // ---------------------------------------------------------------------------
 // Tracebacks and medians. Outputs are written back to front so that each
 // sequence ends at index cap-1 of its buffer, as seq_prepend leaves them.

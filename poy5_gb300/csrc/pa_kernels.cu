@@ -1241,18 +1241,30 @@ __global__ void prep_kernel(BatchArgs A)
         return pick_class(A.lad, lin_wu(lin_band(pl.m, pl.n, pl.full,
                                                  pl.full ? 0 : band_p(T, pl.m, pl.n))), pl.n);
     };
-    const int c = class_of(pl.T0);
+    // the doubling's first passes that cannot end it (unstoppable_passes)
+    // are counted as run: linear pairs and lean affine ones, whose later
+    // passes read nothing an earlier pass leaves but the row-0 value
+    int s = 0;
+    if ((lean || (!A.affine && !pl.full)) && pl.T0 > 0) {
+        s = unstoppable_passes(pl.T0, pl.m, pl.n, A.affine != 0, MAX_PASSES - 1);
+        A.passes[k] = s;
+        if (s > 0 && lean && pl.m - 1 >= 2 &&
+            tmin(pl.m - 1, aff_band(pl.m, pl.n, band_p(pl.T0 << (s - 1), pl.m, pl.n)).newk) >= 2)
+            A.shadowEH0[k] = HIGH;
+    }
+    const int c = class_of(pl.T0 << s);
     if (c < 0) {
         A.status[k] = -5;
         return;
     }
     if (A.spec_S > 0 && (lean || !A.affine) && pl.T0 > 0) {
-        // queue the first passes at once (the doubling's bands, up to the
-        // one that covers the plane), each as its own item
+        // queue the next passes at once (the doubling's bands, up to the
+        // one that covers the plane), each as its own item; pass s first
         const int S = (!A.affine && pl.full) ? 1 : A.spec_S;
-        int T = pl.T0, nq = 0;
+        int T = pl.T0 << s, nq = 0;
         bool wide = false;
         for (;;) {
+            if (s + nq >= SPEC_STRIDE) break;  // spec_res holds passes 0 .. SPEC_STRIDE - 1
             const int cj = class_of(T);
             if (cj < 0) {
                 nq |= SPEC_NOCLASS;
@@ -1284,7 +1296,7 @@ __global__ void prep_kernel(BatchArgs A)
         A.spec_n[k] = -1;
         return;
     }
-    push_item(A, 2 * c + (lean ? 1 : 0), k, pl.T0);
+    push_item(A, 2 * c + (lean ? 1 : 0), k, pl.T0 << s);
 }
 
 // The sequential doubling resumed at pass j (band T) on the second sweep.
@@ -1332,9 +1344,12 @@ __global__ void spec_resolve_kernel(BatchArgs A)
         spec_resume(A, k, m, n, 0, T, lean);
         return;
     }
+    // passes j0 .. j0 + nq - 1 were queued (prep counted the j0 before them as run)
+    const int j0 = A.passes[k];
     const int nq = A.spec_n[k] & ~SPEC_NOCLASS;
     const bool full = !A.affine && (A.pfull[k] & 1);
-    for (int j = 0; j < nq; j++, T *= 2) {
+    T <<= j0;
+    for (int j = j0; j < j0 + nq; j++, T *= 2) {
         const int4 r = A.spec_res[(long long)k * SPEC_STRIDE + j];
         if (r.w != 1) {  // a queued pass did not run
             A.status[k] = -9;
@@ -1362,9 +1377,9 @@ __global__ void spec_resolve_kernel(BatchArgs A)
         // the gap count of the last pass predicts the final one: the first
         // whose p exceeds it by more than one (or that covers the plane);
         // every pass up to it runs at once in the second sweep
-        const int G = A.spec_res[(long long)k * SPEC_STRIDE + nq - 1].y;
+        const int G = A.spec_res[(long long)k * SPEC_STRIDE + j0 + nq - 1].y;
         int last = -1;
-        for (int j = nq; j < SPEC_STRIDE; j++, T *= 2) {
+        for (int j = j0 + nq; j < SPEC_STRIDE; j++, T *= 2) {
             const int c = pick_class(A.lad, lin_wu(lin_band(m, n, 0, band_p(T, m, n))), n);
             if (c < 0) break;
             push_item(A, 2 * c, k, T);
@@ -1372,13 +1387,13 @@ __global__ void spec_resolve_kernel(BatchArgs A)
             if (band_p(T, m, n) > G + 1 || lin_covers(T, m, n)) break;
         }
         if (last >= 0) {
-            A.spec_p2[k] = make_int2(nq, last);
+            A.spec_p2[k] = make_int2(j0 + nq, last);
             A.spec_Tstar[k] = A.spec_T0[k] << last;
             return;
         }
-        T = A.spec_T0[k] << nq;
+        T = A.spec_T0[k] << (j0 + nq);
     }
-    spec_resume(A, k, m, n, nq, T, lean);
+    spec_resume(A, k, m, n, j0 + nq, T, lean);
 }
 
 // One thread per pair still open after the first resolve, when the second

@@ -41,8 +41,34 @@ def band_cells(m, n, newk, affine: bool) -> np.ndarray:
     return e_sum - s_sum + m1
 
 
-def cells_computed(la, lb, passes, mnz: int, affine: bool, full=None) -> np.ndarray:
-    """Cells filled over all doubling iterations of each pair."""
+def unstoppable_passes(la, lb, mnz: int, affine: bool) -> np.ndarray:
+    """Leading doubling iterations that cannot end the doubling: a pass's gap
+    count is at least n - m, so its test needs T >= 3 (n - m) + 4 (linear)
+    or + 2 (affine) unless the band covers the plane. The library counts
+    these as run without filling them (linear pairs off the full plane and
+    gap-free affine pairs on the lean cell)."""
+    la = np.asarray(la, np.int64)
+    lb = np.asarray(lb, np.int64)
+    m = np.minimum(la, lb)
+    n = np.maximum(la, lb)
+    d = n - m
+    T = (d + 1) * mnz
+    thr = 3 * d + (2 if affine else 4)
+    s = np.zeros(len(m), np.int64)
+    for it in range(39):
+        cov = ((2 * T - d) // 2 - (n - 1 if affine else n) + 1) >= 0
+        step = (s == it) & (T > 0) & (T < thr) & ~cov
+        if not step.any():
+            break
+        s[step] += 1
+        T = np.where(step, 2 * T, T)
+    return s
+
+
+def cells_computed(la, lb, passes, mnz: int, affine: bool, full=None,
+                   skipped=None) -> np.ndarray:
+    """Cells filled over all doubling iterations of each pair (`skipped`:
+    per pair, leading iterations counted in `passes` but not filled)."""
     la = np.asarray(la, np.int64)
     lb = np.asarray(lb, np.int64)
     passes = np.asarray(passes, np.int64)
@@ -54,11 +80,12 @@ def cells_computed(la, lb, passes, mnz: int, affine: bool, full=None) -> np.ndar
         total[full] = (m[full] - 1) * n[full]
     else:
         full = np.zeros(len(m), bool)
+    skipped = np.zeros(len(m), np.int64) if skipped is None else np.asarray(skipped, np.int64)
     T = (n - m + 1) * mnz
     for it in range(int(passes.max()) if len(passes) else 0):
-        live = (passes > it) & ~full
-        if not live.any():
+        if not ((passes > it) & ~full).any():
             break
+        live = (passes > it) & ~full & (it >= skipped)
         p = (T - (n - m)) // 2
         kmax = (m - 2) if affine else (m - 1)
         newk = np.minimum(p, kmax)

@@ -286,6 +286,8 @@ struct Emul {
     Ladder lad[2] = {default_ladder(0), default_ladder(1)};
     int row_tile = 1;  // lean bands up to 512 wide on the row tile (0: lane pipeline)
     int window_all = 0;  // every linear traceback through the shared-memory window
+    int skip = 1;        // start after the passes that cannot end the doubling, as prep does
+    mutable std::vector<int> rec;  // affine passes run: T, gap count (pa_emul_aff_passes)
 };
 
 // The band doubling of plan pl (x = rows, y = columns), as the class
@@ -301,6 +303,11 @@ int lin_fill_doubling(const Emul& E, const PairPlan& pl, const uint8_t* x, const
     R = 1;
     *passes = 0;
     *last_class = -1;
+    if (E.skip && !pl.full) {
+        const int s = unstoppable_passes(T, m, n, false, 39);
+        T <<= s;
+        *passes = s;
+    }
     for (;;) {
         bd = lin_band(m, n, pl.full, pl.full ? 0 : band_p(T, m, n));
         int c = pick_class(E.lad[0], lin_wu(bd), n);
@@ -385,6 +392,13 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
     *last_class = -1;
     const bool lean = gapfree && aff_lean_ok(t, tmax(la, lb));
     int rk = 0, rk_newk = 0;
+    if (E.skip && lean) {  // as prep: the row-0 value of the first pass run
+        const int s = unstoppable_passes(T, m, n, true, 39);
+        if (s > 0 && m - 1 >= 2 && tmin(m - 1, aff_band(m, n, band_p(T << (s - 1), m, n)).newk) >= 2)
+            shadowEH0 = HIGH;
+        T <<= s;
+        *passes = s;
+    }
     for (;;) {
         AffBand bd = aff_band(m, n, band_p(T, m, n));
         const bool rt = lean && E.row_tile;
@@ -439,6 +453,8 @@ int run_affine(const Emul& E, const uint8_t* a, int la, const uint8_t* b, int lb
             }
             if (tmin(m - 1, bd.newk) >= 2) shadowEH0 = HIGH;
         }
+        E.rec.push_back(T);
+        E.rec.push_back(g);
         if (aff_done(T, m, n, g)) break;
         T *= 2;
     }
@@ -550,6 +566,15 @@ void pa_emul_set_row_tile(void* e, int mode) { ((Emul*)e)->row_tile = mode ? 1 :
 // linear pipelines of a warp or more).
 void pa_emul_set_window(void* e, int all) { ((Emul*)e)->window_all = all ? 1 : 0; }
 
+// 0: run every pass of the doubling from T0 (the reference's schedule)
+void pa_emul_set_skip(void* e, int on) { ((Emul*)e)->skip = on ? 1 : 0; }
+
+// unstoppable_passes (pa_core.cuh) for the host accounting's test
+int pa_emul_unstoppable(int T0, int m, int n, int affine)
+{
+    return unstoppable_passes(T0, m, n, affine != 0, 39);
+}
+
 // Copies out the product's host tables for comparison with the oracle.
 int pa_emul_tables(void* h, int* cost, uint8_t* median, int* worst, int* tail,
                    int* prepend, int* info)
@@ -581,6 +606,28 @@ int pa_emul_median(void* h, int affine, const uint8_t* a, int la,
     if (affine)
         return run_affine(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
     return run_linear(E, a, la, b, lb, cost, ea, eb, med, mwg, cap, res, passes, last_class);
+}
+
+// The affine doubling of one pair (DOS.median) pass by pass: T and the gap
+// count of every pass run, at most maxp; returns the number of passes run
+// (or a negative status).
+int pa_emul_aff_passes(void* h, const uint8_t* a, int la, const uint8_t* b, int lb, int* Ts,
+                       int* gaps, int maxp)
+{
+    const Emul& E = *(Emul*)h;
+    const int cap = la + lb + 2;
+    std::vector<uint8_t> ea(cap), eb(cap), med(cap), mwg(cap);
+    int cost = 0, res[4], passes = 0, lc = 0;
+    E.rec.clear();
+    const int rc = run_affine(E, a, la, b, lb, &cost, ea.data(), eb.data(), med.data(),
+                              mwg.data(), cap, res, &passes, &lc);
+    if (rc < 0 && rc != -4) return rc;
+    const int np = (int)E.rec.size() / 2;
+    for (int j = 0; j < np && j < maxp; j++) {
+        Ts[j] = E.rec[2 * j];
+        gaps[j] = E.rec[2 * j + 1];
+    }
+    return np;
 }
 
 // verify_aligned / median_no_gaps / worst_aligned (pa_core.cuh) on an
@@ -676,10 +723,14 @@ int pa_emul_lin_passes(void* h, const uint8_t* a, int la, const uint8_t* b, int 
         const int P = E.lad[0].P[c], R = E.lad[0].R[c];
         dm.assign((size_t)(m + n + 1) * P * R, 0);
         int cost = 0, g = 0;
-        switch (R) {
-            case 2: lin_pass<2>(bd, P, t, x, y, dm.data(), &cost, &g); break;
-            case 4: lin_pass<4>(bd, P, t, x, y, dm.data(), &cost, &g); break;
-            default: lin_pass<8>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+        if (m == 1) {  // no rows: row 0 is the whole alignment (as the class kernels)
+            g = n - 1;
+        } else {
+            switch (R) {
+                case 2: lin_pass<2>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+                case 4: lin_pass<4>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+                default: lin_pass<8>(bd, P, t, x, y, dm.data(), &cost, &g); break;
+            }
         }
         if (np < maxp) {
             Ts[np] = T;

@@ -225,3 +225,101 @@ def test_window_traceback_lean_affine(emul, oracle, row_tile):
         assert np.array_equal(med, r.median) and np.array_equal(mwg, r.medianwg)
     if row_tile == 0:
         assert {1, 3, 5} & classes and len(classes) >= 5, classes  # R = 3 classes walked
+
+
+def _pass_cases(rng):
+    from cases import edge_pairs, mutate, rseq
+    pairs = edge_pairs() + random_pairs(rng, 300, maxlen=700)
+    for _ in range(120):  # unequal lengths, gapped states, tiny sequences
+        la = int(rng.integers(1, 400))
+        a = rseq(rng, la, amb=0.05, gapp=float(rng.choice([0.0, 0.1])))
+        b = mutate(rng, a, 0.2, float(rng.choice([0.0, 0.05, 0.2])))
+        if rng.random() < 0.3:
+            b = np.concatenate([b, rseq(rng, int(rng.integers(1, 300)))[1:]])
+        pairs.append((a, b) if rng.random() < 0.5 else (b, a))
+    for name in ("golden_linear", "golden_affine", "golden_affine_pairs"):
+        if name in golden_lib.NAMES:
+            pairs += list(golden_lib.load(name).pairs)
+    return pairs
+
+
+@pytest.mark.parametrize("affine", [False, True])
+def test_every_pass_reports_at_least_the_length_difference(emul, affine):
+    """The bound the kernels use to skip the doubling's first passes
+    (unstoppable_passes): every pass's gap count is at least n - m, so a
+    pass with T below 3 (n - m) + 4 (linear) / + 2 (affine) cannot stop."""
+    emul.pa_emul_set_skip.argtypes = [_P, C.c_int]
+    f = emul.pa_emul_aff_passes if affine else emul.pa_emul_lin_passes
+    tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
+    e = Emu(emul, tcm, go)
+    emul.pa_emul_set_skip(e.h, 0)
+    rng = np.random.default_rng(900 + affine)
+    Ts, gaps, cls = (np.zeros(64, np.int32) for _ in range(3))
+    checked = 0
+    for a, b in _pass_cases(rng):
+        a = np.ascontiguousarray(a, np.uint8)
+        b = np.ascontiguousarray(b, np.uint8)
+        if affine:
+            np_ = f(e.h, _ptr(a), len(a), _ptr(b), len(b), _ptr(Ts), _ptr(gaps), 64)
+        else:
+            np_ = f(e.h, _ptr(a), len(a), _ptr(b), len(b), _ptr(Ts), _ptr(gaps), _ptr(cls), 64)
+        d = abs(len(a) - len(b))
+        for j in range(max(np_, 0)):
+            assert gaps[j] >= d, (len(a), len(b), j, int(Ts[j]), int(gaps[j]))
+            checked += 1
+    assert checked > 1000
+
+
+@pytest.mark.parametrize("affine", [False, True])
+def test_skipped_passes_change_nothing(emul, affine):
+    """Starting after the unstoppable passes gives every output of the full
+    doubling, and the same pass count."""
+    emul.pa_emul_set_skip.argtypes = [_P, C.c_int]
+    tcm, go = (AFF_TCM, 3) if affine else (STD_TCM, 0)
+    full, skip = Emu(emul, tcm, go), Emu(emul, tcm, go)
+    emul.pa_emul_set_skip(full.h, 0)
+    emul.pa_emul_set_skip(skip.h, 1)
+    rng = np.random.default_rng(910 + affine)
+    skipped = 0
+    for a, b in _pass_cases(rng):
+        try:
+            r0 = _median_passes(emul, full, a, b)
+        except AssertionError:
+            continue
+        r1 = _median_passes(emul, skip, a, b)
+        assert r0[0] == r1[0] and r0[2] == r1[2] and r0[-1] == r1[-1], (len(a), len(b))
+        for x, y in zip(r0[1], r1[1]):
+            assert np.array_equal(x, y), (len(a), len(b))
+        skipped += 1
+    assert skipped > 300
+
+
+def _median_passes(lib, e, a, b):
+    a = np.ascontiguousarray(a, np.uint8)
+    b = np.ascontiguousarray(b, np.uint8)
+    cap = len(a) + len(b) + 2
+    bufs = [np.zeros(cap, np.uint8) for _ in range(4)]
+    res = np.zeros(4, np.int32)
+    cost, ps, lc = C.c_int(), C.c_int(), C.c_int()
+    rc = lib.pa_emul_median(e.h, int(e.affine), _ptr(a), len(a), _ptr(b), len(b),
+                            C.byref(cost), *(_ptr(x) for x in bufs), cap, _ptr(res),
+                            C.byref(ps), C.byref(lc))
+    assert rc == 0, rc
+    return (cost.value, bufs, tuple(res), ps.value)
+
+
+def test_host_skip_accounting_matches_kernels(emul):
+    """schedule.unstoppable_passes (GCUPS accounting) is the kernels' rule."""
+    from poy5_gb300 import schedule
+    rng = np.random.default_rng(920)
+    la = rng.integers(1, 5000, 4000)
+    lb = np.where(rng.random(4000) < 0.5, la + rng.integers(-30, 30, 4000),
+                  rng.integers(1, 5000, 4000)).clip(1, None)
+    for affine in (False, True):
+        for mnz in (1, 2, 3):
+            got = schedule.unstoppable_passes(la, lb, mnz, affine)
+            m, n = np.minimum(la, lb), np.maximum(la, lb)
+            want = [emul.pa_emul_unstoppable(int((b - a + 1) * mnz), int(a), int(b), int(affine))
+                    for a, b in zip(m, n)]
+            assert np.array_equal(got, want), (affine, mnz)
+            assert got.max() <= 2

@@ -125,3 +125,20 @@ def test_schedule_cells_match_oracle(oracle):
         got = schedule.cells_computed(la, lb, np.array(its), 1, affine, full)
         ok = [a > 1 or affine is False for a in np.minimum(la, lb)]
         assert np.array_equal(got[ok], np.array(want)[ok])
+
+
+def test_schedule_skipped_passes_accounting():
+    """cells_computed with skipped leading passes: the full schedule's cells
+    minus those of the skipped passes (every pair skipping some)."""
+    from poy5_gb300 import schedule
+    rng = np.random.default_rng(5)
+    la = rng.integers(2, 3000, 500)
+    lb = (la + rng.integers(0, 40, 500)).astype(np.int64)
+    for affine in (False, True):
+        s = schedule.unstoppable_passes(la, lb, 1, affine)
+        assert s.min() >= 1
+        passes = s + rng.integers(1, 4, 500)
+        full = schedule.cells_computed(la, lb, passes, 1, affine)
+        head = schedule.cells_computed(la, lb, s, 1, affine)
+        got = schedule.cells_computed(la, lb, passes, 1, affine, skipped=s)
+        assert np.array_equal(got, full - head)
