@@ -323,6 +323,23 @@ __device__ __forceinline__ void spec_traced(const BatchArgs& A, const Item& w, i
     A.spec_res[si].z |= SPEC_TRACED | ((-r.status & 0xFF) << 16);
 }
 
+// Items at least half as long (m + n) as the longest item queued in this
+// class run one pass per class launch: after a failed pass whose next band
+// still fits here (or a narrower class), such an item moves on to the next
+// class, as long as that one has single-warp pipelines. A pass runs the
+// same band on any class it fits, so only the launch that runs it changes:
+// no pipeline runs several passes of a long pair back to back while the
+// rest of the GPU waits at the end of the launch. 0x7fffffff: never (no
+// length-sorted queue, row tile, or no such next class).
+__device__ __forceinline__ int promote_len(const BatchArgs& A, int q, int cls)
+{
+    if (!A.qsorted || A.row_tile || cls + 1 >= NCLASS || A.lad.P[cls + 1] > 32 ||
+        A.qcount[q] == 0)
+        return 0x7fffffff;
+    const int k = A.qsorted[(long long)q * A.qcap].x;  // longest first
+    return (A.lena[k] + A.lenb[k] + 1) / 2;
+}
+
 // ---------------------------------------------------------------------------
 // linear
 
@@ -445,10 +462,13 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
     int cost = 0, sj = 0;
     long long off = -2;  // arena region of the item: not taken yet
     uint8_t* dm = slot_dm;
-    // the item's band for its next pass: stays here, moves up the ladder, or fails
-    auto keep = [&]() {
+    const int plen = promote_len(A, q, cls);
+    // the item's band for its next pass: stays here, moves up the ladder, or
+    // fails (after a pass, a long item moves up whenever it fits)
+    auto keep = [&](bool after) {
         const LinBand b = lin_band(w.m, w.n, w.full, w.full ? 0 : band_p(w.T, w.m, w.n));
-        const int c = pick_class(A.lad, lin_wu(b), w.n);
+        int c = pick_class(A.lad, lin_wu(b), w.n);
+        if (after && c >= 0 && c <= cls && w.m + w.n >= plen) c = cls + 1;
         if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
             if (p.gl == 0) {
                 if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
@@ -470,7 +490,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                     live = true;
                     off = -2;
                     if (spec) sj = spec_pass(A, w);
-                    keep();
+                    keep(false);
                 }
             }
         }
@@ -521,7 +541,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? lin_narrow_minb(R
                     finished = true;
                 } else {
                     w.T *= 2;
-                    keep();
+                    keep(true);
                 }
             }
         }
@@ -759,11 +779,14 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
         off = -2;
         if (spec) sj = spec_pass(A, w);
     };
-    // the item's band for its next pass: stays here, moves up the ladder, or fails
-    auto keep = [&]() {
+    const int plen = promote_len(A, q, cls);
+    // the item's band for its next pass: stays here, moves up the ladder, or
+    // fails (after a pass, a long item moves up whenever it fits)
+    auto keep = [&](bool after) {
         const AffBand b = aff_band(w.m, w.n, band_p(w.T, w.m, w.n));
-        const int c = (FAST && A.row_tile) ? pick_class_lean(A.lad, aff_wu(b), w.n)
-                                           : pick_class(A.lad, aff_wu(b), w.n);
+        int c = (FAST && A.row_tile) ? pick_class_lean(A.lad, aff_wu(b), w.n)
+                                     : pick_class(A.lad, aff_wu(b), w.n);
+        if (after && c >= 0 && c <= cls && w.m + w.n >= plen) c = cls + 1;
         if (c > cls || c < 0 || w.npass >= MAX_PASSES) {
             if (p.gl == 0) {
                 if (c > cls && w.npass < MAX_PASSES) push_item(A, 2 * c + VARIANT, w.k, w.T);
@@ -782,7 +805,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
                     drained = true;
                 } else {
                     admit(it);
-                    keep();
+                    keep(false);
                 }
             }
         }
@@ -835,7 +858,7 @@ __global__ void __launch_bounds__(NARROW ? 128 : 512, NARROW ? aff_narrow_minb(R
                     finished = true;
                 } else {
                     w.T *= 2;
-                    keep();
+                    keep(true);
                 }
             }
         }
