@@ -335,13 +335,28 @@ PA_HD int trivial_cost(const Tables& t, const uint8_t* s1, int l1, const uint8_t
 // one is not rerun: it would repeat it. Returns the cost; k receives the
 // last pass's half-width.
 template <class FILL>
-PA_HD int drive(const Tables& t, int l1, int l2, FILL& fill, int& k, int& npass, int& status)
+PA_HD int drive(const Tables& t, int l1, int l2, FILL& fill, int& k, int& npass, int& status,
+                bool skip = true)
 {
     const int d = l2 - l1;
     long long T = (long long)(d + 1) * t.mnz;
     int prevk = -1, cost = 0;
     uint32_t g = 0;
     npass = 0;
+    // Passes that cannot end the loop are counted as run without a fill (skip;
+    // off only in tests, to check the bound on every pass): the
+    // gap counters are maxima over tied predecessors of path counts, so the
+    // last cell's larger one is at least d, and p <= d cannot exceed it. A
+    // skipped pass has k = p below lenX - 1 (k rises, every one would fill),
+    // no cover, and the fill of each pass is a function of its k alone.
+    while (skip && npass < MAX_PASSES - 1 && T > 0) {
+        const int p = (int)((T - d) / 2);
+        const long long newp = (T * 2 - d) / 2;
+        if (p >= l1 - 1 || T >= 3LL * d + 2 || newp - l2 + 1 >= 0) break;
+        prevk = p;
+        npass++;
+        T *= 2;
+    }
     for (;;) {
         const int p = (int)((T - d) / 2);
         k = p < l1 - 1 ? p : l1 - 1;

@@ -666,9 +666,12 @@ int pa_emul_newkk_median(void* h, const uint8_t* a, int la, const uint8_t* b, in
     } else {
         auto fill = [&](int kp, int& c, uint32_t& g) -> bool {
             c = nk_fill(E, t, s1, l1, s2, l2, kp, go, g);
+            Em.rec.push_back(kp);
+            Em.rec.push_back(tmax((int)(g & 0xffff), (int)(g >> 16)));
             return true;
         };
-        *cost = nk::drive(t, l1, l2, fill, kk, npass, status);
+        Em.rec.clear();
+        *cost = nk::drive(t, l1, l2, fill, kk, npass, status, Em.skip != 0);
     }
     *passes = npass;
     if (status) return status;
@@ -679,6 +682,27 @@ int pa_emul_newkk_median(void* h, const uint8_t* a, int la, const uint8_t* b, in
     res[2] = r.wlen;
     res[3] = r.maxcost;
     return r.status;
+}
+
+// The newkk pass loop of one pair: k and the larger gap counter of every
+// fill run (at most maxp), the pass count in *npass; returns the fills run
+// or a negative status.
+int pa_emul_newkk_passes(void* h, const uint8_t* a, int la, const uint8_t* b, int lb, int* ks,
+                         int* gns, int maxp, int* npass)
+{
+    const Emul& Em = *(Emul*)h;
+    const int cap = la + lb + 2;
+    std::vector<uint8_t> ea(cap), eb(cap), med(cap), mwg(cap);
+    int cost = 0, res[4];
+    const int rc = pa_emul_newkk_median(h, a, la, b, lb, &cost, ea.data(), eb.data(),
+                                        med.data(), mwg.data(), res, npass);
+    if (rc < 0 && rc != -4) return rc;
+    const int nf = (int)Em.rec.size() / 2;
+    for (int j = 0; j < nf && j < maxp; j++) {
+        ks[j] = Em.rec[2 * j];
+        gns[j] = Em.rec[2 * j + 1];
+    }
+    return nf;
 }
 
 // algn_CAML_simple_2 (caller's deltawh, s1 down the rows) followed by

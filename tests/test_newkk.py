@@ -273,3 +273,52 @@ def test_gpu_newkk_distance(ctx, oracle):
             continue
         s1, s2 = (a, b) if len(a) <= len(b) else (b, a)
         assert got[k] == oracle.newkk_align(ocm, s1, s2, 0)[0], k
+
+
+@pytest.mark.parametrize("model", [(1, 1, 3), (2, 1, 1), (3, 2, 5)])
+def test_replay_newkk_passes_bound_and_skip(nk_emul, model):
+    """Every fill of the newkk pass loop reports a larger gap counter of at
+    least lenY - lenX (the bound behind the passes drive() counts as run
+    without a fill), and skipping them gives the same outputs and pass
+    count as running them."""
+    import ctypes as C
+    subs, indel, go = model
+    tcm = [[0 if r == c else (indel if 4 in (r, c) else subs) for c in range(5)]
+           for r in range(5)]
+    lib = nk_emul
+    lib.pa_emul_set_skip.argtypes = [C.c_void_p, C.c_int]
+    full, skip = _emul_handle(lib, tcm, go), _emul_handle(lib, tcm, go)
+    lib.pa_emul_set_skip(full, 0)
+    lib.pa_emul_set_skip(skip, 1)
+    rng = np.random.default_rng(30 + go)
+    pairs = random_pairs(rng, 120, maxlen=400)
+    for L in (33, 65, 130, 257):
+        a = np.array([16] + list(rng.choice([1, 2, 4, 8], L - 1)), np.uint8)
+        for extra in (0, 3, 40, 300):
+            b = np.array([16] + list(rng.choice([1, 2, 4, 8], L - 1 + extra)), np.uint8)
+            pairs += [(a, b), (b, a)]
+    ks, gns = np.zeros(64, np.int32), np.zeros(64, np.int32)
+    p = lambda x: x.ctypes.data_as(C.c_void_p)
+    checked = 0
+    for a, b in pairs:
+        a = np.ascontiguousarray(a, np.uint8)
+        b = np.ascontiguousarray(b, np.uint8)
+        n0, n1 = C.c_int(), C.c_int()
+        nf = lib.pa_emul_newkk_passes(full, p(a), len(a), p(b), len(b), p(ks), p(gns), 64,
+                                      C.byref(n0))
+        if nf < 0:
+            continue
+        d = abs(len(a) - len(b))
+        for j in range(nf):
+            assert gns[j] >= d, (len(a), len(b), j, int(ks[j]), int(gns[j]))
+            checked += 1
+        lib.pa_emul_newkk_passes(skip, p(a), len(a), p(b), len(b), p(ks), p(gns), 64,
+                                 C.byref(n1))
+        assert n0.value == n1.value, (len(a), len(b))
+        r0, r1 = _emul_newkk(lib, full, a, b), _emul_newkk(lib, skip, a, b)
+        assert r0[0] == r1[0] and r0[1] == r1[1] and r0[-1] == r1[-1]
+        for x, y in zip(r0[2:6], r1[2:6]):
+            assert np.array_equal(x, y)
+    lib.pa_emul_free(full)
+    lib.pa_emul_free(skip)
+    assert checked > 200
