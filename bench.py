@@ -263,7 +263,7 @@ def run_gpu(args):
     tuned = None
     if not args.no_autotune:
         from poy5_gb300 import tune
-        tuned = tune.autotune(ctx, cm, pk, reps=1)
+        tuned = tune.autotune(ctx, cm, pk, reps=3)
     # the whole batch captured once as a CUDA graph and replayed per step
     graph = C.c_void_p()
     _lib.check(lib.poyalgn_batch_graph_create(
