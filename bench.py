@@ -37,9 +37,10 @@ METRIC = ("GCUPS & alignments/s batched+served vs plain per-pair kernel, 1 GB300
 OPS_PER_CELL = {"affine": 51, "linear": 8}   # int32 ops per DP cell
 DM_BYTES = {"affine": 1, "linear": 1}        # direction bytes written per cell (lean affine: 1)
 # DRAM bytes (read + write) the class kernels and the deferred traceback moved
-# per computed cell in one ncu capture of the 8,192-pair affine batch (4.80 GB
-# for 3.12 G cells); the traffic grows with the computed cells, so it scales
-# to the full batch.
+# per computed cell in one ncu capture of the 8,192-pair affine batch (4.03 GB
+# for 2.62 G cells with the doubling's unstoppable passes skipped; 4.80 GB for
+# 3.12 G cells before); the traffic grows with the computed cells, so it
+# scales to the full batch.
 DRAM_BYTES_PER_CELL = {"affine": 1.54}
 
 
