@@ -333,13 +333,16 @@ def run_gpu(args):
         e2e_step()
         barrier()
         t0 = time.perf_counter()
+        e2e_each = []
         for _ in range(args.steps):
+            t1 = time.perf_counter()
             e2e_step()
+            e2e_each.append(round((time.perf_counter() - t1) * 1e3, 2))
         e2e_s = (time.perf_counter() - t0) / args.steps
         barrier()
         h2d = int(pk.seqs.nbytes + pk.offa.nbytes * 3 + pk.lena.nbytes * 2)
         d2h = int(7 * 4 * n + 4 * pk.out_bytes)
-        e2e = {"seconds": e2e_s, "h2d": h2d, "d2h": d2h}
+        e2e = {"seconds": e2e_s, "h2d": h2d, "d2h": d2h, "step_ms": e2e_each}
 
     # every pair of the timed batch against the oracle (untimed; rank 0)
     parity = None
@@ -1039,7 +1042,7 @@ def gpu_line(args, r) -> dict:
         e_s = reduce_max(e["seconds"], world)
         line["e2e"] = {"value": round(cells / e_s / 1e9, 3), "unit": "GCUPS",
                        "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
-                       "alignments_per_s": round(pairs / e_s, 1)}
+                       "alignments_per_s": round(pairs / e_s, 1), "step_ms": e["step_ms"]}
     return line
 
 
