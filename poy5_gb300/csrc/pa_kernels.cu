@@ -325,9 +325,9 @@ __device__ __forceinline__ void spec_traced(const BatchArgs& A, const Item& w, i
 
 // Items at least a third as long (m + n) as the longest item queued in this
 // class run one pass per class launch (on the 65,536-pair batch: a third
-// 83.0 ms, a half 83.7, two thirds 86.7, never 90.4): after a failed pass whose next band
-// still fits here (or a narrower class), such an item moves on to the next
-// class, as long as that one has single-warp pipelines. A pass runs the
+// 83.0 ms, a half 83.7, two thirds 86.7, never 90.4): after a failed pass
+// whose next band still fits here (or a narrower class), such an item moves
+// on to the next class, as long as that one has single-warp pipelines. A pass runs the
 // same band on any class it fits, so only the launch that runs it changes:
 // no pipeline runs several passes of a long pair back to back while the
 // rest of the GPU waits at the end of the launch. 0x7fffffff: never (no
