@@ -714,6 +714,49 @@ int poyalgn_num_classes(void);
 int poyalgn_int32_peak(int device, int kind, int iters, double *inst_per_s,
                        float *ms, int64_t *thread_inst);
 
+/*
+ * ---- Three-sequence alignment ------------------------------------------
+ *
+ * poyalgn_powell_3d replaces the external `powell_3d` of Sequence.Align
+ * (src/sequence.ml:1309-1310, "powell_3D_align_bc" / "powell_3D_align",
+ * src/ukkCommon.c:109-150), which align_3_powell (src/sequence.ml:1312-1321)
+ * and so readjust_3d (:1373) call: Powell's optimal alignment of three
+ * sequences under linear or affine gap costs, recovered by Ukkonen
+ * check-pointing (src/ukk.checkp.c).
+ *
+ * a, b, c are POY sequences with their leading gap (la, lb, lc >= 1 bytes);
+ * each later position is read as the lowest of A, C, G, T it holds (a
+ * position with none: POYALGN_EPAIR / POYALGN_PAIR_BAD_STATE, where POY
+ * fails with "This is impossible!"). mm, go, ge are the mismatch, gap
+ * opening and gap extension costs as align_3_powell_inter passes them
+ * (src/sequence.ml:1323-1337); mm >= 1, go >= 0, ge >= 1. ra, rb, rc
+ * receive the three aligned sequences, leading gap included, written back
+ * to front so that they end at ra + cap (POY's seq_prepend into sequences
+ * of capacity la + lb + lc: cap >= la + lb + lc); *rlen is their length and
+ * *cost the alignment cost (the external's return value). Sequences longer
+ * than 32,768 positions: POYALGN_PAIR_TOO_LONG.
+ *
+ * poyalgn_powell_3d_batch runs many triples at once: triple k's sequences
+ * are seqs + off[3k + j], len[3k + j] bytes (j = 0, 1, 2 for a, b, c), and
+ * its aligned sequences end at ra/rb/rc + out_off[k] + len[3k] + len[3k+1] +
+ * len[3k+2]; rlen, cost and status have one entry per triple. Host pointers;
+ * returns POYALGN_EPAIR when any status is not POYALGN_PAIR_OK.
+ *
+ * poyalgn_powell_3d_stats reports the summed kernel time and the number of
+ * launch rounds of the last batch; poyalgn_powell_3d_set_budget caps the
+ * device memory the triples' workspaces take at once (0: half the free
+ * memory, at most 64 GB).
+ */
+int poyalgn_powell_3d(poyalgn_ctx *ctx, const uint8_t *a, int la, const uint8_t *b, int lb,
+                      const uint8_t *c, int lc, int mm, int go, int ge, uint8_t *ra,
+                      uint8_t *rb, uint8_t *rc, int cap, int32_t *rlen, int32_t *cost);
+int poyalgn_powell_3d_batch(poyalgn_ctx *ctx, int ntriples, const uint8_t *seqs,
+                            const int64_t *off, const int32_t *len, int mm, int go, int ge,
+                            const int64_t *out_off, uint8_t *ra, uint8_t *rb, uint8_t *rc,
+                            int32_t *rlen, int32_t *cost, int32_t *status);
+int poyalgn_powell_3d_stats(poyalgn_ctx *ctx, float *kernel_ms, int32_t *rounds);
+int poyalgn_powell_3d_set_budget(poyalgn_ctx *ctx, int64_t work_bytes);
+
 #ifdef __cplusplus
 }
 #endif

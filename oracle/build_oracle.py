@@ -39,7 +39,7 @@ def _stale(out, srcs):
 
 def build_port(force: bool = False) -> str:
     out = os.path.join(HERE, "libpoyoracle.so")
-    srcs = [os.path.join(HERE, f) for f in ("poy_oracle.c", "poy_tables.c")]
+    srcs = [os.path.join(HERE, f) for f in ("poy_oracle.c", "poy_tables.c", "poy_ukk3.c")]
     hdrs = [os.path.join(HERE, f) for f in ("poy_oracle.h", "poy_tables.h")]
     if force or _stale(out, srcs + hdrs):
         _run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp",
@@ -55,9 +55,11 @@ def build_ref(ref_src: str = DEFAULT_REF_SRC, force: bool = False):
     os.makedirs(outdir, exist_ok=True)
     # newkkonen.c (Algn_Newkk) and its queue; algn.c and newkkonen.c both
     # define the tentative global `backtrace_mode`, hence -fcommon.
+    # ukkCommon.c + ukk.checkp.c: Powell's three-sequence alignment
     srcs = [os.path.join(ref_src, f) for f in ("algn.c", "avl.c", "zarr.c",
                                                "newkkonen.c",
-                                               "queue_with_linkedlist.c")]
+                                               "queue_with_linkedlist.c",
+                                               "ukkCommon.c", "ukk.checkp.c")]
     mine = [os.path.join(HERE, f) for f in ("ref_harness.c", "poy_tables.c")]
     built = []
     for name, extra in (("libpoyref.so", []),
@@ -65,7 +67,11 @@ def build_ref(ref_src: str = DEFAULT_REF_SRC, force: bool = False):
         out = os.path.join(outdir, name)
         if force or _stale(out, mine + [os.path.join(HERE, "shim", "caml",
                                                       "poy_caml_shim.h")]):
+            # -Bsymbolic: the reference's own functions bind inside the
+            # library (glibc exports a legacy `step` that ukk.checkp.c's
+            # calls would otherwise reach when the library is dlopen'ed)
             _run(["gcc", "-O2", "-fgnu89-inline", "-fcommon", "-fPIC", "-shared", "-w",
+                  "-Wl,-Bsymbolic",
                   *extra, "-I", os.path.join(HERE, "shim"), "-I", ref_src,
                   "-I", HERE, "-o", out, *srcs, *mine])
         built.append(out)

@@ -63,4 +63,20 @@ int orc_newkk_median(void *cm, const uint8_t *a, int la, const uint8_t *b,
                      uint8_t *anc, int *anclen, uint8_t *mwg, int *mwglen,
                      int *maxcost);
 
+/* Sequence.Align.align_3_powell -> powell_3D_align (src/ukkCommon.c:109):
+ * three POY sequences with their leading gap; ra/rb/rc hold la + lb + lc
+ * bytes and receive the aligned sequences front to back (leading gap
+ * first), *rlen bytes each. Returns -2 where the reference fails ("This is
+ * impossible!": a position without A, C, G or T). */
+int orc_powell_3d(const uint8_t *a, int la, const uint8_t *b, int lb, const uint8_t *c,
+                  int lc, int mm, int go, int ge, uint8_t *ra, uint8_t *rb, uint8_t *rc,
+                  int *rlen, int *cost);
+
+/* orc_powell_3d over many triples, OpenMP over triples; outputs laid out as
+ * poyalgn_powell_3d_batch lays them out. Returns the count of failures. */
+int orc_powell_3d_batch(int n, const uint8_t *seqs, const int64_t *off, const int32_t *len,
+                        int mm, int go, int ge, const int64_t *out_off, uint8_t *ra,
+                        uint8_t *rb, uint8_t *rc, int32_t *rlen, int32_t *cost,
+                        int32_t *status, int nthreads);
+
 #endif

@@ -629,3 +629,38 @@ int ref_verify_and_nogap(void *cm, const uint8_t *a, const uint8_t *b, int len,
     freeblk(vm);
     return rc;
 }
+
+/* powell_3D_align (src/ukkCommon.c:109-145), as Sequence.Align.align_3_powell
+ * (src/sequence.ml:1312-1321) calls it: three POY sequences with their
+ * leading gap, result sequences of capacity la + lb + lc. The reference keeps
+ * its state in globals, so calls must not overlap. */
+value powell_3D_align(value, value, value, value, value, value, value, value, value);
+
+int ref_powell_3d(const uint8_t *a, int la, const uint8_t *b, int lb,
+                  const uint8_t *c, int lc, int mm, int go, int ge,
+                  uint8_t *ra, uint8_t *rb, uint8_t *rc_, int *rlen, int *cost)
+{
+    jmp_buf jb;
+    ref_jmp = &jb;
+    int cap = la + lb + lc;
+    value va = mkseq(la, a, la), vb = mkseq(lb, b, lb), vc = mkseq(lc, c, lc);
+    value wa = mkseq(cap, NULL, 0), wb = mkseq(cap, NULL, 0), wc = mkseq(cap, NULL, 0);
+    int rc = 0;
+    if (setjmp(jb)) {
+        rc = -1;
+    } else {
+        *cost = Int_val(powell_3D_align(va, vb, vc, wa, wb, wc, Val_int(mm),
+                                        Val_int(go), Val_int(ge)));
+        *rlen = getseq(wa, ra, cap);
+        getseq(wb, rb, cap);
+        getseq(wc, rc_, cap);
+    }
+    ref_jmp = NULL;
+    freeblk(va);
+    freeblk(vb);
+    freeblk(vc);
+    freeblk(wa);
+    freeblk(wb);
+    freeblk(wc);
+    return rc;
+}

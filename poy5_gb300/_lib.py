@@ -59,6 +59,10 @@ _SIGS = {
     "poyalgn_newkk_algn_affine": (_I, [_P, _P, _P, _I, _P, _I, _I, _P]),
     "poyalgn_newkk_backtrace_affine": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _I, _P, _I]),
     "poyalgn_newkk_get_k": (_I, [_P, _P]),
+    "poyalgn_powell_3d": (_I, [_P, _P, _I, _P, _I, _P, _I, _I, _I, _I, _P, _P, _P, _I, _P, _P]),
+    "poyalgn_powell_3d_batch": (_I, [_P, _I, _P, _P, _P, _I, _I, _I] + [_P] * 7),
+    "poyalgn_powell_3d_stats": (_I, [_P, _P, _P]),
+    "poyalgn_powell_3d_set_budget": (_I, [_P, _I64]),
     "poyalgn_newkk_set_arena_words": (_I, [_P, _I64]),
     "poyalgn_median_batch_device": (_I, [_P, _P, _I, _I, _I64] + [_P] * 18),
     "poyalgn_median_batch_device_noalloc": (_I, [_P, _I, _I, _I64] + [_P] * 18),

@@ -18,9 +18,9 @@ BUILD_DIR = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 UNITS = ["pa_kernels.cu", "pa_cost.cu", "pa_capi.cu", "pa_driver.cu", "pa_server.cu",
-         "pa_newkk.cu", "pa_peak.cu", "pa_tables.cpp"]
+         "pa_newkk.cu", "pa_peak.cu", "pa_ukk3.cu", "pa_tables.cpp"]
 HEADERS = ["pa_core.cuh", "pa_kernels.h", "pa_tables.h", "pa_runtime.h", "pa_cost.h",
-           "pa_newkk.cuh"]
+           "pa_newkk.cuh", "pa_ukk3.cuh"]
 
 
 def _deps():

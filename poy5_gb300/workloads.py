@@ -225,3 +225,37 @@ def yule_tree(n_taxa: int = 256, root_len: int = 1500, mean_branch: float = 0.05
     visit(0)
     return TreeWorkload(f"yule_tree_{n_taxa}_root{root_len}", leaves,
                         np.array(left, np.int32), np.array(right, np.int32), 1, 2, 0)
+
+
+@dataclass
+class TripleWorkload:
+    name: str
+    triples: list        # [(s1, s2, p)] bitset sequences with leading gap
+    mm: int
+    go: int
+    ge: int
+
+
+def readjust_triples(n_triples: int = 2048, seed: int = SEED_BASE + 6, lo: int = 100,
+                     hi: int = 300, sub_rate: float = 0.03,
+                     indel_rate: float = 0.005) -> TripleWorkload:
+    """Three-sequence readjustment inputs (Sequence.Align.readjust_3d: two
+    children and a parent): a uniform ancestor of length U[lo, hi] and three
+    descendants, each with `sub_rate` substitutions and indel events at
+    `indel_rate` per site (geometric lengths, mean 2), 1% of positions an
+    IUPAC ambiguity; costs as align_3_powell_inter takes them from POY's
+    default linear matrix (mismatch 1, gap opening 0, gap 2)."""
+    rng = np.random.default_rng(seed)
+    triples = []
+    for _ in range(n_triples):
+        anc = random_bases(rng, int(rng.integers(lo, hi + 1)))
+        t = []
+        for _ in range(3):
+            s = mutate(rng, anc, sub_rate, indel_rate, 2.0)
+            if len(s) == 0:
+                s = random_bases(rng, 1)
+            amb = rng.random(len(s)) < 0.01
+            s[amb] = AMBIG[rng.integers(0, len(AMBIG), int(amb.sum()))]
+            t.append(with_gap(s))
+        triples.append(tuple(t))
+    return TripleWorkload(f"readjust_triples_{n_triples}x{lo}-{hi}_linear", triples, 1, 0, 2)

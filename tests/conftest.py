@@ -28,7 +28,8 @@ def build_emulator() -> str:
     """Host replay of the kernels' lane pipeline (test-only library)."""
     csrc = os.path.join(ROOT, "poy5_gb300", "csrc")
     srcs = [os.path.join(ROOT, "tests", "pa_emul.cpp"), os.path.join(csrc, "pa_tables.cpp")]
-    deps = srcs + [os.path.join(csrc, f) for f in ("pa_core.cuh", "pa_tables.h", "pa_newkk.cuh")]
+    deps = srcs + [os.path.join(csrc, f) for f in ("pa_core.cuh", "pa_tables.h", "pa_newkk.cuh",
+                                                    "pa_ukk3.cuh")]
     if (not os.path.exists(EMUL_SO) or
             any(os.path.getmtime(d) > os.path.getmtime(EMUL_SO) for d in deps)):
         os.makedirs(os.path.dirname(EMUL_SO), exist_ok=True)

@@ -3,13 +3,15 @@
 Run here, where the POY sources exist (``python oracle/build_oracle.py`` first
 builds ``oracle/_ref/libpoyref.so``):
 
-    python tests/golden/make_golden.py [--only newkk]
+    python tests/golden/make_golden.py [--only newkk|powell3d]
 
 Each fixture holds the inputs of a set of pairs and what the reference's
 SeqCS.DOS.median sequence of C calls returned for them (cost, aligned pair,
 median, median with gaps, worst cost), plus the reference's cost tables.
 ``golden_newkk`` holds DOS.median with use_ukk (affine): the pair aligned by
 src/newkkonen.c, then ancestor_2 / median_2_with_gaps / max_cost_2.
+``golden_powell3d`` holds powell_3D_align (src/ukkCommon.c, src/ukk.checkp.c)
+on triples: the cost and the three aligned sequences.
 The GPU tests compare against these files directly, so parity is pinned to
 the reference itself and not only to the C restatement.
 """
@@ -65,10 +67,71 @@ def make_newkk(ref):
     make("golden_newkk", ref, AFF_TCM, 3, pairs, newkk=True)
 
 
+def powell_cases(rng, n_random=60):
+    """Triples for the three-sequence alignment fixture: edge cases under
+    three cost models, random triples of 0-80 positions at several
+    divergences and cost models, and readjust-shaped triples."""
+    G = 16
+    edge = [([G], [G], [G]), ([G, 1], [G], [G]), ([G], [G, 1, 2], [G, 4]),
+            ([G, 1, 2, 4], [G, 1, 2, 4], [G, 1, 2, 4]), ([G, 1, 2, 4], [G, 1, 2, 4], [G, 1, 2, 8]),
+            ([G, 1], [G, 2], [G, 4]), ([G, 1, 1, 1, 1], [G, 2, 2, 2, 2], [G, 4, 4, 4, 4]),
+            ([G, 3, 5, 15], [G, 1, 4, 8], [G, 2, 4, 8]), ([G, 1, 2, 4, 8], [G], [G, 1, 2, 4, 8])]
+    cases = [(t, c) for t in edge for c in ((1, 0, 2), (1, 3, 1), (2, 1, 1))]
+
+    def mut(s, div):
+        out = []
+        for x in s:
+            r = rng.random()
+            if r < div / 4:
+                continue
+            if r < div / 2:
+                out.append(int(rng.choice([1, 2, 4, 8])))
+            out.append(x if rng.random() > div else int(rng.choice([1, 2, 4, 8])))
+        return out
+
+    for _ in range(n_random):
+        L = int(rng.integers(0, 80))
+        div = float(rng.choice([0.02, 0.1, 0.3, 0.6]))
+        base = rng.choice([1, 2, 4, 8], L).tolist()
+        t = []
+        for _ in range(3):
+            s = [G] + mut(base, div)
+            for i in range(1, len(s)):
+                if rng.random() < 0.05:
+                    s[i] |= int(rng.choice([1, 2, 4, 8, 16]))
+            t.append(s)
+        c = (int(rng.choice([1, 2, 3])), int(rng.choice([0, 0, 1, 2, 3])),
+             int(rng.choice([1, 2, 3])))
+        cases.append((tuple(t), c))
+    from poy5_gb300 import workloads as wl
+    w = wl.readjust_triples(n_triples=8)
+    cases += [(t, (w.mm, w.go, w.ge)) for t in w.triples]
+    return cases
+
+
+def make_powell3d(ref):
+    """golden_powell3d: powell_3D_align (src/ukkCommon.c:109) on triples,
+    the cost and the three aligned sequences the reference returned."""
+    rng = np.random.default_rng(31337)
+    cases = powell_cases(rng)
+    res = [ref.powell_3d(*t, *c) for t, c in cases]
+    fields = {}
+    for j, key in enumerate(("a", "b", "c")):
+        fields[key], fields[key + "_off"] = pack([np.asarray(t[j], np.uint8) for t, _ in cases])
+        fields["r" + key], fields["r" + key + "_off"] = pack([r[1 + j] for r in res])
+    np.savez_compressed(os.path.join(HERE, "golden_powell3d.npz"),
+                        costs=np.array([c for _, c in cases], np.int32),
+                        cost=np.array([r[0] for r in res], np.int32), **fields)
+    print("golden_powell3d", len(cases), "triples")
+
+
 def main():
     ref = Oracle("ref")
     if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "newkk":
         make_newkk(ref)
+        return
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "powell3d":
+        make_powell3d(ref)
         return
     rng = np.random.default_rng(777)
     lin = edge_pairs() + random_pairs(rng, 120, maxlen=400)
@@ -82,6 +145,7 @@ def main():
     w2 = wl.affine_pairs(n_pairs=24)
     make("golden_affine_pairs", ref, AFF_TCM, 3, w2.pairs)
     make_newkk(ref)
+    make_powell3d(ref)
 
 
 if __name__ == "__main__":

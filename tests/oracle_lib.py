@@ -222,6 +222,40 @@ class Oracle:
         return (cost.value, r1[:n.value].copy(), r2[:n.value].copy(), it.value,
                 cells.value)
 
+    def powell_3d(self, a, b, c, mm: int, go: int, ge: int):
+        """powell_3D_align on three POY sequences (leading gap included):
+        (cost, aligned a, aligned b, aligned c), each front to back with the
+        leading gap. The reference build keeps its state in globals, so its
+        calls must not overlap."""
+        a, b, c = (np.ascontiguousarray(x, np.uint8) for x in (a, b, c))
+        cap = len(a) + len(b) + len(c)
+        ra, rb, rc = (np.zeros(cap, np.uint8) for _ in range(3))
+        n, cost = _I(), _I()
+        r = self._f("powell_3d")(_ptr(a), len(a), _ptr(b), len(b), _ptr(c), len(c),
+                                 mm, go, ge, _ptr(ra), _ptr(rb), _ptr(rc),
+                                 C.byref(n), C.byref(cost))
+        if r:
+            raise OracleError(self.error() if self.kind != "port" else f"powell_3d: {r}")
+        k = n.value
+        return cost.value, ra[:k].copy(), rb[:k].copy(), rc[:k].copy()
+
+    def powell_3d_batch(self, seqs, off, lens, out_off, mm, go, ge, nthreads: int = 0):
+        """orc_powell_3d_batch (the port only): arrays laid out as
+        poyalgn_powell_3d_batch takes them; returns dict of cost, rlen,
+        status, ra, rb, rc."""
+        n = len(out_off)
+        cap = np.asarray(lens, np.int64).reshape(-1, 3).sum(axis=1) if n else np.zeros(0)
+        tot = int((np.asarray(out_off) + cap).max()) if n else 1
+        ra, rb, rc = (np.zeros(tot, np.uint8) for _ in range(3))
+        rlen, cost, status = (np.zeros(max(n, 1), np.int32) for _ in range(3))
+        seqs, off, lens, out_off = (np.ascontiguousarray(a, dt) for a, dt in
+                                    ((seqs, np.uint8), (off, np.int64), (lens, np.int32),
+                                     (out_off, np.int64)))
+        self.lib.orc_powell_3d_batch(n, _ptr(seqs), _ptr(off), _ptr(lens), mm, go, ge,
+                                     _ptr(out_off), _ptr(ra), _ptr(rb), _ptr(rc), _ptr(rlen),
+                                     _ptr(cost), _ptr(status), nthreads or (os.cpu_count() or 1))
+        return dict(cost=cost[:n], rlen=rlen[:n], status=status[:n], ra=ra, rb=rb, rc=rc)
+
     def median_batch(self, cm, seqs_a, seqs_b, affine: bool, nthreads: int = 0):
         """DOS.median over many pairs on the host cores (OpenMP)."""
         la = np.array([len(s) for s in seqs_a], np.int32)

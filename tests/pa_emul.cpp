@@ -776,3 +776,33 @@ int pa_emul_pair_bounds(int la, int lb, int max_pair_len, long long out_off,
 }
 
 }  // extern "C"
+
+// ---- three-sequence alignment (pa_ukk3.cuh), one triple on the host -------
+
+#include "pa_ukk3.cuh"
+
+extern "C" int pa_emul_powell_3d(const uint8_t* a, int la, const uint8_t* b, int lb,
+                                 const uint8_t* c, int lc, int mm, int go, int ge, int D,
+                                 uint8_t* ra, uint8_t* rb, uint8_t* rc, int cap, int* rlen,
+                                 int* cost, long long* steps)
+{
+    u3::Model m;
+    u3::model_init(m, mm, go, ge);
+    const u3::Layout L = u3::layout(m, la - 1, lb - 1, lc - 1, D);
+    std::vector<unsigned char> mem((size_t)L.bytes, 0);
+    const u3::Work w = u3::work_at(mem.data(), L);
+    u3::Machine mc(m, w, a, la - 1, b, lb - 1, c, lc - 1);
+    int n = 0;
+    const int d = mc.run(ra + cap, rb + cap, rc + cap, cap, &n);
+    *rlen = n;
+    *cost = d;
+    *steps = mc.steps;
+    return mc.status;
+}
+
+extern "C" long long pa_emul_powell_3d_bytes(int la, int lb, int lc, int mm, int go, int ge, int D)
+{
+    u3::Model m;
+    u3::model_init(m, mm, go, ge);
+    return u3::layout(m, la - 1, lb - 1, lc - 1, D).bytes;
+}
