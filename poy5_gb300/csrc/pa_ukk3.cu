@@ -1,16 +1,16 @@
 // Three-sequence alignment on the GPU: Sequence.Align.align_3_powell ->
 // powell_3D_align (src/ukkCommon.c:109-145, src/ukk.checkp.c), many triples
-// per launch, one thread per triple replaying the reference recursion
+// per launch, one warp per triple replaying the reference recursion
 // (pa_ukk3.cuh).
 //
 // C ABI (include/poyalgn.h): poyalgn_powell_3d (the per-call external
 // `powell_3d`, src/sequence.ml:1309-1310) and poyalgn_powell_3d_batch.
 //
 // The replay is a chain of dependent loads and stores into the triple's own
-// workspace, so a thread is bound by memory latency, not by issue: the
-// driver keeps as many triples resident as the workspace budget allows and
-// spreads them over the warps (one triple per warp while there are fewer
-// triples than warp slots, so that no two replays diverge inside a warp).
+// workspace, so it is bound by memory latency, not by issue: a whole warp
+// runs each triple, its lanes loading a frame's candidate cells in one round
+// (pa_ukk3.cuh), and the driver keeps as many triples resident as the
+// workspace budget allows.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,6 +24,7 @@ namespace pa {
 namespace {
 
 constexpr int U3_BLOCK = 128;
+static_assert(u3::RING == 32, "one ring tag per lane is cleared at launch");
 
 struct U3Args {
     const uint8_t* seqs;
@@ -34,7 +35,6 @@ struct U3Args {
     const long long* wofs;  // per list entry: its workspace offset
     const int* win;         // per list entry: window half-width
     int nlist;
-    int spread;             // threads per triple; the first of each group runs it
     unsigned char* work;
     uint8_t *ra, *rb, *rc;
     int *rlen, *cost, *status;
@@ -44,16 +44,22 @@ struct U3Args {
 __global__ void __launch_bounds__(U3_BLOCK) powell_kernel(const U3Args A)
 {
     __shared__ u3::Model sm;
+    // each warp's stack top: frames popped from here do not wait on memory
+    __shared__ u3::Frame ring[U3_BLOCK / 32][u3::RING];
+    __shared__ int ring_tag[U3_BLOCK / 32][u3::RING];
     if (threadIdx.x == 0) sm = A.model;
+    ring_tag[threadIdx.x >> 5][threadIdx.x & 31] = -1;
     __syncthreads();
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g % A.spread) return;
-    const long long i = g / A.spread;
+    // one warp per triple: every lane holds the same machine state and the
+    // lanes load a frame's candidate cells together
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= A.nlist) return;
     const int k = A.list[i];
     const int la = A.len[3 * k] - 1, lb = A.len[3 * k + 1] - 1, lc = A.len[3 * k + 2] - 1;
     const u3::Layout L = u3::layout(sm, la, lb, lc, A.win[i]);
-    const u3::Work w = u3::work_at(A.work + A.wofs[i], L);
+    u3::Work w = u3::work_at(A.work + A.wofs[i], L);
+    w.ring = ring[threadIdx.x >> 5];
+    w.ring_tag = ring_tag[threadIdx.x >> 5];
     const int cap = la + lb + lc + 3;
     const long long end = A.out_off[k] + cap;
     u3::Machine mc(sm, w, A.seqs + A.off[3 * k], la, A.seqs + A.off[3 * k + 1], lb,
@@ -219,17 +225,11 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
             A.wofs = d_wofs;
             A.win = d_win;
             A.nlist = (int)nl;
-            // one triple per warp while the warps are not all taken, then
-            // more per warp (resident threads: SMs x 2048)
-            const long long slots = (long long)c->nsm * 2048;
-            int spread = 32;
-            while (spread > 1 && (long long)nl * spread > slots) spread >>= 1;
-            A.spread = spread;
             A.work = as<unsigned char>(c->u3_work);
             A.ra = B, A.rb = B + ot, A.rc = B + 2 * ot;
             A.rlen = d_rlen, A.cost = d_cost, A.status = d_st;
             A.model = model;
-            const long long threads = (long long)nl * spread;
+            const long long threads = (long long)nl * 32;
             const unsigned blocks = (unsigned)((threads + U3_BLOCK - 1) / U3_BLOCK);
             CU(cudaEventRecord(e0, st));
             powell_kernel<<<blocks, U3_BLOCK, 0, st>>>(A);

@@ -1,6 +1,6 @@
 // Powell's three-sequence alignment (POY's Sequence.Align.align_3_powell ->
 // powell_3D_align, src/ukkCommon.c:109-145, src/ukk.checkp.c) as a resumable
-// machine that one GPU thread runs per triple.
+// machine that one GPU warp runs per triple.
 //
 // The reference recursion is a memoised Ukkonen search over diagonals
 // (ab = i - j, ac = i - k), edit cost d and 16 column states, with a
@@ -19,8 +19,8 @@
 // finalCost / ge the first pass and every later pass stay inside. The host
 // picks D per triple; a cell outside the window, a stack overflow or a step
 // budget running out ends the triple with a status the host retries with a
-// wider window. Layout per triple: U cells [2*maxstep][wab][wac][16] of 16
-// bytes, check-point distances [maxstep][wab][wac][16], the frame stack and
+// wider window. Layout per triple: U cells [wab][wac][2*maxstep][16] of 16
+// bytes, check-point distances [wab][wac][maxstep][16], the frame stack and
 // the pass stack.
 #pragma once
 
@@ -110,7 +110,7 @@ struct Cell {
 
 struct Frame {
     int ab, ac, d;
-    int meta;   // to | phase << 5 | k << 8 | (fst + 1) << 13
+    int meta;   // to | phase << 5 | k << 8 | sub << 13 | (fst + 1) << 14
     int best, fabac, fcs, ext;
 };
 
@@ -118,11 +118,15 @@ struct Pass {
     int sab, sac, scost, sst, sdist, fab, fac, fcost, fst, fdist;
 };
 
+constexpr int RING = 32;  // frames of the stack top kept on chip
+
 struct Work {
     Cell* U;
     int* CP;
     Frame* st;
     Pass* sub;
+    Frame* ring;     // RING frames: slot j % RING holds frame j while ring_tag says so
+    int* ring_tag;
     int st_cap;
     int ab_lo, ac_lo, wab, wac;
     long long step_cap;
@@ -167,6 +171,8 @@ PA_HDM Work work_at(unsigned char* base, const Layout& L)
     w.CP = (int*)(base + L.cp_off);
     w.st = (Frame*)(base + L.st_off);
     w.sub = (Pass*)(base + L.sub_off);
+    w.ring = nullptr;
+    w.ring_tag = nullptr;
     w.st_cap = L.st_cap;
     w.ab_lo = L.ab_lo, w.ac_lo = L.ac_lo, w.wab = L.wab, w.wac = L.wac;
     w.step_cap = L.step_cap;
@@ -215,7 +221,49 @@ PA_HD int char_cost(int a, int b, int c)
     return 2;
 }
 
-enum Phase { PH_START = 0, PH_FS1 = 1, PH_FS2 = 2, PH_DM1 = 3, PH_EXT = 4 };
+enum Phase { PH_FS = 0, PH_X = 1 };
+
+// A frame's candidate cells, one per lane, loaded in one round: the tag is
+// the memo value when the slot holds this cost, TAG_MISS when it must be
+// computed, TAG_WINDOW when it lies outside the window and -INF outside the
+// matrix; abac / cs are the slot's `from` record. Lanes take them from each
+// other by index (a shuffle on the GPU; arrays when the machine runs on the
+// host).
+constexpr int TAG_MISS = -0x7fffffff;
+constexpr int TAG_WINDOW = -0x7ffffffe;
+
+struct Snap {
+#if defined(__CUDA_ARCH__)
+    int tag, abac, cs;
+#else
+    int tag[32], abac[32], cs[32];
+#endif
+};
+
+PA_HD int tag_of(const Snap& S, int k)
+{
+#if defined(__CUDA_ARCH__)
+    return __shfl_sync(0xffffffffu, S.tag, k);
+#else
+    return S.tag[k];
+#endif
+}
+PA_HD int abac_of(const Snap& S, int k)
+{
+#if defined(__CUDA_ARCH__)
+    return __shfl_sync(0xffffffffu, S.abac, k);
+#else
+    return S.abac[k];
+#endif
+}
+PA_HD int cs_of(const Snap& S, int k)
+{
+#if defined(__CUDA_ARCH__)
+    return __shfl_sync(0xffffffffu, S.cs, k);
+#else
+    return S.cs[k];
+#endif
+}
 
 // One triple's replay. Sequences are POY sequences with the leading gap;
 // output is written back to front so that it ends at out_end (the
@@ -248,18 +296,20 @@ struct Machine {
     {
         return ab >= w.ab_lo && ab < w.ab_lo + w.wab && ac >= w.ac_lo && ac < w.ac_lo + w.wac;
     }
-    PA_HDM long long slot(int ab, int ac, int plane, int s) const
+    // the planes of a diagonal pair are adjacent, so the cells a frame reads
+    // (two diagonals, a few costs, 16 states) lie within a few kilobytes
+    PA_HDM long long slot(int ab, int ac, int plane, int planes, int s) const
     {
-        return (((long long)plane * w.wab + (ab - w.ab_lo)) * w.wac + (ac - w.ac_lo)) * NS + s;
+        return ((((long long)(ab - w.ab_lo)) * w.wac + (ac - w.ac_lo)) * planes + plane) * NS + s;
     }
     // U slot: caller has checked the window
     PA_HDM Cell* U(int ab, int ac, int d, int s) const
     {
-        return w.U + slot(ab, ac, d % (2 * m.maxstep), s);
+        return w.U + slot(ab, ac, d % (2 * m.maxstep), 2 * m.maxstep, s);
     }
     PA_HDM int* CP(int ab, int ac, int d, int s) const
     {
-        return w.CP + slot(ab, ac, d % m.maxstep, s);
+        return w.CP + slot(ab, ac, d % m.maxstep, m.maxstep, s);
     }
 
     PA_HDM bool within(int ab, int ac, int d) const
@@ -280,7 +330,282 @@ struct Machine {
         if (status == OK) status = s;
     }
 
-    // Ukk(ab, ac, d, s) (src/ukk.checkp.c:576-604) with the stack
+    // one candidate: classify and load the slot
+    PA_HDM void load(int ab, int ac, int d, int s, int& tag, int& abac, int& cs) const
+    {
+        abac = 0, cs = 0;
+        if (!within(ab, ac, d)) {
+            tag = -INF;
+            return;
+        }
+        if (!in_window(ab, ac)) {
+            tag = TAG_WINDOW;
+            return;
+        }
+        const Cell* c = U(ab, ac, d, s);
+#if defined(__CUDA_ARCH__)
+        const int4 v = *reinterpret_cast<const int4*>(c);
+        tag = v.y == d + off ? v.x : TAG_MISS;
+        abac = v.z, cs = v.w;
+#else
+        tag = c->stamp == d + off ? c->dist : TAG_MISS;
+        abac = c->abac, cs = c->cs;
+#endif
+    }
+
+    // the predecessors on the neighbour diagonal: lanes 0-15 the cost of
+    // state k's transition (k = lane), lanes 16-31 that cost less a mismatch
+    PA_HDM void lane_fs(int l, const Frame& F, int to, int ab1, int ac1, int& tag, int& abac,
+                        int& cs) const
+    {
+        const int k = l & 15;
+        if (l >= 16 && !m.second[to]) {
+            tag = -INF, abac = 0, cs = 0;
+            return;
+        }
+        const int cost = F.d - m.trans[k][to] - m.cont[to] - (l >= 16 ? m.mm : 0);
+        load(ab1, ac1, cost, k, tag, abac, cs);
+    }
+    // lane 0: the same state one cost lower; lanes 1-15 (state 0 only): the
+    // other states at this cost
+    PA_HDM void lane_x(int l, const Frame& F, int to, int& tag, int& abac, int& cs) const
+    {
+        if (l == 0)
+            load(F.ab, F.ac, F.d - 1, to, tag, abac, cs);
+        else if (to == 0 && l < NS)
+            load(F.ab, F.ac, F.d, l, tag, abac, cs);
+        else
+            tag = -INF, abac = 0, cs = 0;
+    }
+    // both rounds of a frame in one go (the predecessor round only while
+    // the frame is still in it): the two loads of a lane overlap
+    PA_HDM void snap(Snap& Sf, Snap& Sx, const Frame& F, int to, int ph, int ab1, int ac1) const
+    {
+#if defined(__CUDA_ARCH__)
+        const int l = (int)(threadIdx.x & 31);
+        if (ph == PH_FS) lane_fs(l, F, to, ab1, ac1, Sf.tag, Sf.abac, Sf.cs);
+        lane_x(l, F, to, Sx.tag, Sx.abac, Sx.cs);
+#else
+        for (int l = 0; l < 32; l++) {
+            if (ph == PH_FS) lane_fs(l, F, to, ab1, ac1, Sf.tag[l], Sf.abac[l], Sf.cs[l]);
+            lane_x(l, F, to, Sx.tag[l], Sx.abac[l], Sx.cs[l]);
+        }
+#endif
+    }
+
+    PA_HDM void push(int& sp, const Frame& F) const
+    {
+        w.st[sp] = F;
+        if (w.ring) {
+            w.ring[sp % RING] = F;
+            w.ring_tag[sp % RING] = sp;
+        }
+        sp++;
+    }
+    PA_HDM void pop(int& sp, Frame& F) const
+    {
+        --sp;
+        if (w.ring && w.ring_tag[sp % RING] == sp)
+            F = w.ring[sp % RING];
+        else
+            F = w.st[sp];
+    }
+
+    PA_HDM void start(Frame& F, int ab, int ac, int d, int to) const
+    {
+        F.ab = ab, F.ac = ac, F.d = d;
+        F.best = -INF;
+        F.ext = -INF;
+        if (d >= cp_cost && d < cp_cost + m.maxstep) {
+            F.fabac = pack_abac(ab, ac);
+            F.fcs = d * 32 + to;
+        } else {
+            F.fabac = 0;
+            F.fcs = -32;
+        }
+        const int nb = m.neigh[to];
+        const int da = nb & 1, db = (nb >> 1) & 1, dc = (nb >> 2) & 1;
+        const int ab1 = ab - da + db, ac1 = ac - da + dc;
+        const bool diag = ab1 >= -endB && ab1 <= endA && ac1 >= -endC && ac1 <= endA;
+        F.meta = to | ((diag ? PH_FS : PH_X) << 5);
+    }
+
+    // ---- a phase's candidates, evaluated one per lane ----------------------
+
+    struct LaneRes {
+        int code;  // 0 value (or none), 1 call the first candidate, 2 the second, 3 window
+        int key;   // (dist + KEY_OFF) << 5 | (31 - k) for a value, 0 for none
+        int abac, cs;
+    };
+    static constexpr int KEY_OFF = 8192;
+
+    // predecessor k (src/ukk.checkp.c:644-691) from its two slots: the
+    // transition cost (t1) and, for the states that try it, that cost less a
+    // mismatch (t2). Candidates before k0 were taken already; at k0 with sub0
+    // the first slot was, too.
+    PA_HDM LaneRes fs_lane(int k, int k0, int sub0, const Frame& F, int to, int ab1, int ac1,
+                           bool copy, int t1, int abac1, int cs1, int t2, int abac2,
+                           int cs2) const
+    {
+        LaneRes r{0, 0, F.fabac, F.fcs};
+        if (k < k0 || k >= NS) return r;
+        const int nb = m.neigh[to];
+        const int da = nb & 1, db = (nb >> 1) & 1, dc = (nb >> 2) & 1;
+        const int cost = F.d - m.trans[k][to] - m.cont[to];
+        if (!(k == k0 && sub0)) {
+            if (t1 == TAG_MISS) return r.code = 1, r;
+            if (t1 == TAG_WINDOW) return r.code = 3, r;
+            if (ok_index(t1, da, endA) && ok_index(t1 - ab1, db, endB) &&
+                ok_index(t1 - ac1, dc, endC) &&
+                char_cost(da ? a_at(t1) : 16, db ? b_at(t1 - ab1) : 16,
+                          dc ? c_at(t1 - ac1) : 16) == 1) {
+                r.key = ((t1 + da + KEY_OFF) << 5) | (31 - k);
+                if (complete)
+                    r.abac = pack_abac(ab1, ac1), r.cs = cost * 32 + k;
+                else if (copy)
+                    r.abac = abac1, r.cs = cs1;
+                return r;
+            }
+            if (!m.second[to]) return r;
+        }
+        if (t2 == TAG_MISS) return r.code = 2, r;
+        if (t2 == TAG_WINDOW) return r.code = 3, r;
+        if (ok_index(t2, da, endA) && ok_index(t2 - ab1, db, endB) &&
+            ok_index(t2 - ac1, dc, endC)) {
+            r.key = ((t2 + da + KEY_OFF) << 5) | (31 - k);
+            if (complete)
+                r.abac = pack_abac(ab1, ac1), r.cs = (cost - m.mm) * 32 + k;
+            else if (copy)
+                r.abac = abac2, r.cs = cs2;
+        }
+        return r;
+    }
+
+    // state l at this cost (src/ukk.checkp.c:722-735), from k0 on
+    PA_HDM LaneRes x_lane(int l, int k0, int to, int t) const
+    {
+        LaneRes r{0, 0, 0, 0};
+        if (to != 0 || l < k0 || l >= NS) return r;
+        if (t == TAG_MISS) return r.code = 1, r;
+        if (t == TAG_WINDOW) return r.code = 3, r;
+        r.key = ((t + KEY_OFF) << 5) | (31 - l);
+        return r;
+    }
+
+    // position p continues the run of matches on diagonal (ab, ac)
+    PA_HDM bool run_at(int p, int ab, int ac) const
+    {
+        return ok_index(p, 1, endA) && ok_index(p - ab, 1, endB) && ok_index(p - ac, 1, endC) &&
+               a_at(p) == b_at(p - ab) && a_at(p) == c_at(p - ac);
+    }
+
+    // the first lane asking for a call (32 if none), and the largest key of
+    // the lanes before it (earliest lane among equals)
+    struct Reduced {
+        int first, key, abac, cs, code;
+    };
+
+#if defined(__CUDA_ARCH__)
+    PA_HDM Reduced reduce(const LaneRes& r) const
+    {
+        const unsigned full = 0xffffffffu;
+        const int l = (int)(threadIdx.x & 31);
+        const unsigned stop = __ballot_sync(full, r.code != 0);
+        const int first = stop ? __ffs(stop) - 1 : 32;
+        const int key = __reduce_max_sync(full, l < first ? r.key : 0);
+        const int bl = key ? 31 - (key & 31) : 0;
+        Reduced out;
+        out.first = first;
+        out.key = key;
+        out.abac = __shfl_sync(full, r.abac, bl);
+        out.cs = __shfl_sync(full, r.cs, bl);
+        out.code = __shfl_sync(full, r.code, first & 31);
+        return out;
+    }
+#else
+    PA_HDM Reduced reduce(const LaneRes* r) const
+    {
+        Reduced out{32, 0, 0, 0, 0};
+        for (int l = 0; l < 32; l++)
+            if (r[l].code) {
+                out.first = l;
+                break;
+            }
+        for (int l = 0; l < out.first; l++)
+            if (r[l].key > out.key) out.key = r[l].key;
+        const int bl = out.key ? 31 - (out.key & 31) : 0;
+        out.abac = r[bl].abac, out.cs = r[bl].cs;
+        out.code = r[out.first & 31].code;
+        return out;
+    }
+#endif
+
+    PA_HDM Reduced walk_fs(const Snap& S, int k0, int sub0, const Frame& F, int to, int ab1,
+                           int ac1, bool copy) const
+    {
+#if defined(__CUDA_ARCH__)
+        const unsigned full = 0xffffffffu;
+        const int l = (int)(threadIdx.x & 31);
+        const int t2 = __shfl_down_sync(full, S.tag, 16);
+        const int a2 = __shfl_down_sync(full, S.abac, 16);
+        const int c2 = __shfl_down_sync(full, S.cs, 16);
+        const LaneRes r = fs_lane(l < 16 ? l : NS, k0, sub0, F, to, ab1, ac1, copy, S.tag,
+                                  S.abac, S.cs, t2, a2, c2);
+        return reduce(r);
+#else
+        LaneRes r[32];
+        for (int l = 0; l < 32; l++)
+            r[l] = l < 16 ? fs_lane(l, k0, sub0, F, to, ab1, ac1, copy, S.tag[l], S.abac[l],
+                                    S.cs[l], S.tag[l + 16], S.abac[l + 16], S.cs[l + 16])
+                          : fs_lane(NS, k0, sub0, F, to, ab1, ac1, copy, 0, 0, 0, 0, 0, 0);
+        return reduce(r);
+#endif
+    }
+
+    PA_HDM Reduced walk_x(const Snap& S, int k0, int to) const
+    {
+#if defined(__CUDA_ARCH__)
+        return reduce(x_lane((int)(threadIdx.x & 31), k0, to, S.tag));
+#else
+        LaneRes r[32];
+        for (int l = 0; l < 32; l++) r[l] = x_lane(l, k0, to, S.tag[l]);
+        return reduce(r);
+#endif
+    }
+
+    // the end of the run of matches from `dist`, 32 positions a round
+    PA_HDM int run_end(int dist, int ab, int ac) const
+    {
+        for (;;) {
+#if defined(__CUDA_ARCH__)
+            const unsigned mis =
+                __ballot_sync(0xffffffffu, !run_at(dist + (int)(threadIdx.x & 31), ab, ac));
+#else
+            unsigned mis = 0;
+            for (int l = 0; l < 32; l++)
+                if (!run_at(dist + l, ab, ac)) mis |= 1u << l;
+#endif
+            if (mis) {
+#if defined(__CUDA_ARCH__)
+                return dist + __ffs(mis) - 1;
+#else
+                int l = 0;
+                while (!(mis >> l & 1u)) l++;
+                return dist + l;
+#endif
+            }
+            dist += 32;
+        }
+    }
+
+    // Ukk(ab, ac, d, s) (src/ukk.checkp.c:576-782), the whole warp running
+    // one triple: the frame on top of the stack lives in registers, its
+    // candidate cells are read in one round and evaluated one per lane, and
+    // ballots and a max-reduction give what the reference's loops over them
+    // give (the first candidate to compute, and the first strict maximum of
+    // the ones before it). A round is read again after every callee returns,
+    // since the callee may have written any slot; between reads nothing is
+    // written, so each value is the one the reference reads at that point.
     PA_HDM int ukk(int ab0, int ac0, int d0, int s0)
     {
         if (!within(ab0, ac0, d0)) return -INF;
@@ -293,186 +618,144 @@ struct Machine {
             if (c->stamp == d0 + off) return c->dist;
         }
         int sp = 0;
-        Frame* st = w.st;
-        st[sp++] = Frame{ab0, ac0, d0, s0 | (PH_START << 5), 0, 0, 0, 0};
-        int r = 0;
-        while (sp > 0) {
+        Frame F;
+        start(F, ab0, ac0, d0, s0);
+        Snap Sf, Sx;
+        bool fresh = false;
+        for (;;) {
             if (++steps > w.step_cap) {
                 fail(ERR_STEPS);
                 return -INF;
             }
-            Frame& f = st[sp - 1];
-            const int to = f.meta & 31;
-            const int ph = (f.meta >> 5) & 7;
-            int k = (f.meta >> 8) & 31;
+            const int to = F.meta & 31;
+            int ph = (F.meta >> 5) & 1;
+            int k = (F.meta >> 8) & 31;
+            int sub = (F.meta >> 13) & 1;
+            int fst = ((F.meta >> 14) & 31) - 1;
             const int nb = m.neigh[to];
             const int da = nb & 1, db = (nb >> 1) & 1, dc = (nb >> 2) & 1;
-            const int ab1 = f.ab - da + db, ac1 = f.ac - da + dc;
-            const bool copy = f.d >= cp_cost + m.maxstep;
-            // the callee of the next step: (cab, cac, cd, cs) with return phase nph
-            int cab = 0, cac = 0, cd = 0, cst = 0, nph = -1;
+            const int ab1 = F.ab - da + db, ac1 = F.ac - da + dc;
+            const bool copy = F.d >= cp_cost + m.maxstep;
+            if (!fresh) snap(Sf, Sx, F, to, ph, ab1, ac1);
+            fresh = true;
+            int cab = 0, cac = 0, cd = 0, cst = 0;
+            bool call = false;
+            if (ph == PH_FS) {
+                const Reduced R = walk_fs(Sf, k, sub, F, to, ab1, ac1, copy);
+                if (R.key) {
+                    const int dist = (R.key >> 5) - KEY_OFF;
+                    if (F.best < dist) {
+                        F.best = dist;
+                        F.fabac = R.abac;
+                        F.fcs = R.cs;
+                    }
+                }
+                if (R.first < NS) {
+                    if (R.code == 3) {
+                        fail(ERR_WINDOW);
+                        return -INF;
+                    }
+                    k = R.first;
+                    sub = R.code == 2;
+                    call = true, cab = ab1, cac = ac1, cst = k;
+                    cd = F.d - m.trans[k][to] - m.cont[to] - (sub ? m.mm : 0);
+                } else {
+                    // nothing was written since the round was read: the
+                    // second round of the same read is current
+                    ph = PH_X, k = 0, sub = 0;
+                }
+            }
             bool finish = false;
-            switch (ph) {
-            case PH_START: {
-                f.best = -INF;
-                if (f.d >= cp_cost && f.d < cp_cost + m.maxstep) {
-                    f.fabac = pack_abac(f.ab, f.ac);
-                    f.fcs = f.d * 32 + to;
-                } else {
-                    f.fabac = 0;
-                    f.fcs = -32;
-                }
-                if (ab1 >= -endB && ab1 <= endA && ac1 >= -endC && ac1 <= endA) {
-                    k = 0;
-                    cab = ab1, cac = ac1, cd = f.d - m.trans[0][to] - m.cont[to], cst = 0;
-                    nph = PH_FS1;
-                } else {
-                    cab = f.ab, cac = f.ac, cd = f.d - 1, cst = to, nph = PH_DM1;
-                }
-                break;
-            }
-            case PH_FS1:
-            case PH_FS2: {
-                const int cost = f.d - m.trans[k][to] - m.cont[to];
-                const int a = r;
-                int dist = -INF, fcost = 0;
-                bool tried = true;
-                if (ph == PH_FS1) {
-                    if (ok_index(a, da, endA) && ok_index(a - ab1, db, endB) &&
-                        ok_index(a - ac1, dc, endC) &&
-                        char_cost(da ? a_at(a) : 16, db ? b_at(a - ab1) : 16,
-                                  dc ? c_at(a - ac1) : 16) == 1) {
-                        fcost = cost, dist = a + da;
-                    } else if (m.second[to]) {
-                        // try the mismatch predecessor next
-                        cab = ab1, cac = ac1, cd = cost - m.mm, cst = k, nph = PH_FS2;
-                        tried = false;
-                    }
-                } else if (ok_index(a, da, endA) && ok_index(a - ab1, db, endB) &&
-                           ok_index(a - ac1, dc, endC)) {
-                    fcost = cost - m.mm, dist = a + da;
-                }
-                if (!tried) break;
-                if (f.best < dist) {
-                    f.best = dist;
-                    if (complete) {
-                        f.fabac = pack_abac(ab1, ac1);
-                        f.fcs = fcost * 32 + k;
-                    } else if (copy) {
-                        const Cell* c = U(ab1, ac1, fcost, k);
-                        f.fabac = c->abac;
-                        f.fcs = c->cs;
-                    }
-                }
-                if (++k < NS) {
-                    cab = ab1, cac = ac1, cd = f.d - m.trans[k][to] - m.cont[to], cst = k;
-                    nph = PH_FS1;
-                } else {
-                    cab = f.ab, cac = f.ac, cd = f.d - 1, cst = to, nph = PH_DM1;
-                }
-                break;
-            }
-            case PH_DM1: {
-                const int dist = r;
-                if (ok_index(dist, 0, endA) && ok_index(dist - f.ab, 0, endB) &&
-                    ok_index(dist - f.ac, 0, endC) && f.best < dist) {
-                    f.best = dist;
-                    if (complete) {
-                        f.fabac = pack_abac(f.ab, f.ac);
-                        f.fcs = (f.d - 1) * 32 + to;
-                    } else if (copy) {
-                        const Cell* c = U(f.ab, f.ac, f.d - 1, to);
-                        f.fabac = c->abac;
-                        f.fcs = c->cs;
-                    }
-                }
-                if (to == 0) {
-                    // furthest over the states at this cost, state 0 being
-                    // the value just found (src/ukk.checkp.c:722-735)
-                    if (f.best > -INF) {
-                        f.ext = f.best;
-                        f.meta = (f.meta & ~(31 << 13)) | (1 << 13);
+            if (!call) {
+                if (k == 0) {
+                    // the same state one cost lower (src/ukk.checkp.c:694-711)
+                    const int t = tag_of(Sx, 0);
+                    if (t == TAG_MISS) {
+                        call = true, cab = F.ab, cac = F.ac, cd = F.d - 1, cst = to;
+                    } else if (t == TAG_WINDOW) {
+                        fail(ERR_WINDOW);
+                        return -INF;
                     } else {
-                        f.ext = -INF;
-                        f.meta &= ~(31 << 13);
-                    }
-                    k = 1;
-                    cab = f.ab, cac = f.ac, cd = f.d, cst = 1, nph = PH_EXT;
-                } else {
-                    finish = true;
-                }
-                break;
-            }
-            case PH_EXT: {
-                if (r > f.ext) {
-                    f.ext = r;
-                    f.meta = (f.meta & ~(31 << 13)) | ((k + 1) << 13);
-                }
-                if (++k < NS) {
-                    cab = f.ab, cac = f.ac, cd = f.d, cst = k, nph = PH_EXT;
-                } else {
-                    int dist = f.ext;
-                    const int fst = ((f.meta >> 13) & 31) - 1;
-                    while (ok_index(dist, 1, endA) && ok_index(dist - f.ab, 1, endB) &&
-                           ok_index(dist - f.ac, 1, endC) && a_at(dist) == b_at(dist - f.ab) &&
-                           a_at(dist) == c_at(dist - f.ac))
-                        dist++;
-                    if (dist > f.best) {
-                        f.best = dist;
-                        if (fst != 0) {
+                        if (ok_index(t, 0, endA) && ok_index(t - F.ab, 0, endB) &&
+                            ok_index(t - F.ac, 0, endC) && F.best < t) {
+                            F.best = t;
                             if (complete) {
-                                f.fabac = pack_abac(f.ab, f.ac);
-                                f.fcs = f.d * 32 + fst;
+                                F.fabac = pack_abac(F.ab, F.ac);
+                                F.fcs = (F.d - 1) * 32 + to;
                             } else if (copy) {
-                                const Cell* c = U(f.ab, f.ac, f.d, fst);
-                                f.fabac = c->abac;
-                                f.fcs = c->cs;
+                                F.fabac = abac_of(Sx, 0);
+                                F.fcs = cs_of(Sx, 0);
                             }
                         }
+                        if (to != 0) {
+                            finish = true;
+                        } else {
+                            F.ext = F.best > -INF ? F.best : -INF;
+                            fst = F.best > -INF ? 0 : -1;
+                            k = 1;
+                        }
                     }
-                    finish = true;
                 }
-                break;
-            }
-            default:
-                fail(ERR_STEPS);
-                return -INF;
+                if (!call && !finish) {
+                    // the other states at this cost, then the run of matches
+                    // (src/ukk.checkp.c:712-759)
+                    const Reduced R = walk_x(Sx, k, to);
+                    if (R.key) {
+                        const int t = (R.key >> 5) - KEY_OFF;
+                        if (t > F.ext) {
+                            F.ext = t;
+                            fst = 31 - (R.key & 31);
+                        }
+                    }
+                    if (R.first < NS) {
+                        if (R.code == 3) {
+                            fail(ERR_WINDOW);
+                            return -INF;
+                        }
+                        k = R.first;
+                        call = true, cab = F.ab, cac = F.ac, cd = F.d, cst = k;
+                    } else {
+                        const int dist = run_end(F.ext, F.ab, F.ac);
+                        if (dist > F.best) {
+                            F.best = dist;
+                            if (fst != 0) {
+                                if (complete) {
+                                    F.fabac = pack_abac(F.ab, F.ac);
+                                    F.fcs = F.d * 32 + fst;
+                                } else if (copy) {
+                                    F.fabac = abac_of(Sx, fst);
+                                    F.fcs = cs_of(Sx, fst);
+                                }
+                            }
+                        }
+                        finish = true;
+                    }
+                }
             }
             if (finish) {
-                Cell* c = U(f.ab, f.ac, f.d, to);
-                c->dist = f.best;
-                c->stamp = f.d + off;
-                c->abac = f.fabac;
-                c->cs = f.fcs;
-                if (f.d >= cp_cost && f.d < cp_cost + m.maxstep) *CP(f.ab, f.ac, f.d, to) = f.best;
-                if (f.best > furthest) furthest = f.best;
-                r = f.best;
-                sp--;
+                Cell* c = U(F.ab, F.ac, F.d, to);
+                c->dist = F.best;
+                c->stamp = F.d + off;
+                c->abac = F.fabac;
+                c->cs = F.fcs;
+                if (F.d >= cp_cost && F.d < cp_cost + m.maxstep) *CP(F.ab, F.ac, F.d, to) = F.best;
+                if (F.best > furthest) furthest = F.best;
+                if (sp == 0) return F.best;
+                pop(sp, F);
+                fresh = false;
                 continue;
             }
-            if (status != OK) return -INF;
-            f.meta = (f.meta & ~((7 << 5) | (31 << 8))) | (nph << 5) | (k << 8);
-            // the call: resolved here when outside the matrix or memoised
-            if (!within(cab, cac, cd)) {
-                r = -INF;
-                continue;
-            }
-            if (!in_window(cab, cac)) {
-                fail(ERR_WINDOW);
-                return -INF;
-            }
-            const Cell* c = U(cab, cac, cd, cst);
-            if (c->stamp == cd + off) {
-                r = c->dist;
-                continue;
-            }
+            // the callee was a miss in the current round, so it lies in the
+            // matrix and the window
+            F.meta = to | (ph << 5) | (k << 8) | (sub << 13) | ((fst + 1) << 14);
             if (sp >= w.st_cap) {
                 fail(ERR_STACK);
                 return -INF;
             }
-            st[sp++] = Frame{cab, cac, cd, cst | (PH_START << 5), 0, 0, 0, 0};
+            push(sp, F);
+            start(F, cab, cac, cd, cst);
+            fresh = false;
         }
-        return r;
     }
 
     // furthest distance (or its state) at (ab, ac, d) over the states

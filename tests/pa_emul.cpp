@@ -790,7 +790,11 @@ extern "C" int pa_emul_powell_3d(const uint8_t* a, int la, const uint8_t* b, int
     u3::model_init(m, mm, go, ge);
     const u3::Layout L = u3::layout(m, la - 1, lb - 1, lc - 1, D);
     std::vector<unsigned char> mem((size_t)L.bytes, 0);
-    const u3::Work w = u3::work_at(mem.data(), L);
+    u3::Work w = u3::work_at(mem.data(), L);
+    std::vector<u3::Frame> ring(u3::RING);
+    std::vector<int> ring_tag(u3::RING, -1);
+    w.ring = ring.data();
+    w.ring_tag = ring_tag.data();
     u3::Machine mc(m, w, a, la - 1, b, lb - 1, c, lc - 1);
     int n = 0;
     const int d = mc.run(ra + cap, rb + cap, rc + cap, cap, &n);
