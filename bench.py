@@ -74,7 +74,7 @@ def parse_args(argv=None):
                     help="cap each context's direction slabs and traceback arena (GB; 0: "
                          "library defaults), e.g. to keep a profiled case small")
     ap.add_argument("--leg", choices=["main", "peak", "plain", "percall", "downpass", "long",
-                                      "serving", "distance", "newkk"],
+                                      "serving", "distance", "newkk", "powell3d"],
                     default="main", help="run one measurement alone and print its object")
     return ap.parse_args(argv)
 
@@ -769,6 +769,58 @@ def run_distance(local: int, n_pairs: int = 8192, reps: int = 3) -> dict:
             "alignments_per_s": round(pk.npairs / ms * 1e3, 1)}
 
 
+def run_powell3d(local: int, n_triples: int = 8192, reps: int = 2, cpu_triples: int = 1024) -> dict:
+    """Three-sequence alignment (Sequence.Align.align_3_powell ->
+    powell_3D_align) on readjust-shaped triples: the host-pointer batch API
+    end to end (inputs and outputs through host memory) and its summed kernel
+    time; the oracle port on all host cores on the first `cpu_triples`
+    triples beside it, with every output of those triples compared."""
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    from poy5_gb300.three_d import pack_triples
+    w = wl.readjust_triples(n_triples=n_triples)
+    ctx = pg.Context(local)
+    pg.powell_3d_batch(ctx, w.triples, w.mm, w.go, w.ge)  # warm-up
+    walls, kms = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        res = pg.powell_3d_batch(ctx, w.triples, w.mm, w.go, w.ge)
+        walls.append(time.perf_counter() - t0)
+        kms.append(res.kernel_ms)
+    wall = float(np.median(walls))
+    kms_ = float(np.median(kms))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    orc = oracle_lib.Oracle("port")
+    sub = w.triples[:cpu_triples]
+    seqs, off, lens, out_off, cap = pack_triples(sub)
+    threads = os.cpu_count() or 1
+    c0 = time.perf_counter()
+    ref = orc.powell_3d_batch(seqs, off, lens, out_off, w.mm, w.go, w.ge, nthreads=threads)
+    cpu_s = time.perf_counter() - c0
+    # parity on the sample: costs, lengths and the three aligned sequences
+    bad = int((ref["status"] != 0).sum()) + int((res.status[:len(sub)] != 0).sum())
+    bad += int((ref["cost"] != res.cost[:len(sub)]).sum())
+    for k in range(len(sub)):
+        n = int(ref["rlen"][k])
+        e_ref = int(out_off[k] + cap[k])
+        got = res.aligned(k)
+        if n != int(res.rlen[k]) or any(not np.array_equal(ref[x][e_ref - n:e_ref], g)
+                                        for x, g in zip(("ra", "rb", "rc"), got)):
+            bad += 1
+    nt = len(w.triples)
+    return {"workload": w.name, "triples": nt, "status_ok": int((res.status == 0).sum()),
+            "e2e_ms": round(wall * 1e3, 1), "kernel_ms": round(kms_, 1),
+            "launch_rounds": res.rounds,
+            "triples_per_s": round(nt / wall, 1),
+            "triples_per_s_kernel": round(nt / (kms_ / 1e3), 1),
+            "cost_sum": int(res.cost.sum()),
+            "parity": {"against": "oracle port", "triples": len(sub), "mismatches": bad},
+            "cpu_baseline": {"triples_per_s": round(len(sub) / cpu_s, 1), "kind": "port",
+                             "cores": threads, "cpu_model": host_cpu(),
+                             "sample": f"first {len(sub)} triples of {w.name} ({cpu_s:.1f} s)"}}
+
+
 def run_newkk(local: int, n_pairs: int = 65536, reps: int = 2, cpu_s: float = 8.0,
               arena_mb: int = 0) -> dict:
     """DOS.median with use_ukk (Algn_Newkk, src/newkkonen.c) on the affine
@@ -1070,6 +1122,8 @@ def main(argv=None):
             out = run_serving(local, args.serve_seconds, args.serve_slots, args.serve_batch)
         elif args.leg == "newkk":
             out = run_newkk(local, args.pairs or 65536, arena_mb=args.newkk_arena_mb)
+        elif args.leg == "powell3d":
+            out = run_powell3d(local, args.pairs or 8192)
         else:
             out = run_distance(local, args.pairs or 8192)
         print(json.dumps({"leg": args.leg, **out}))
@@ -1121,6 +1175,10 @@ def main(argv=None):
                 line["newkk"] = {"error": f"{type(e).__name__}: {e}"[:300]}
             line["serving"] = run_serving(local, args.serve_seconds, args.serve_slots,
                                           args.serve_batch)
+            try:
+                line["powell3d"] = run_powell3d(local)
+            except Exception as e:  # keep the headline line if this leg fails
+                line["powell3d"] = {"error": f"{type(e).__name__}: {e}"[:300]}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

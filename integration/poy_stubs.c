@@ -4,7 +4,8 @@
  *
  * A POY maintainer compiles this file against POY's own headers (seq.h,
  * cm.h and the OCaml runtime headers), links it in place of the
- * definitions in src/algn.c / src/seq.c / src/newkkonen.c that it replaces,
+ * definitions in src/algn.c / src/seq.c / src/newkkonen.c / src/ukkCommon.c
+ * that it replaces,
  * and links -lpoyalgn. No OCaml changes: every symbol keeps the name and
  * argument list of the external it replaces (file:line in the POY 5.1.1
  * source tree beside each one), including the bytecode twins (_bc) of the
@@ -435,4 +436,44 @@ value newkkonen_CAML_get_k(value m)
     int32_t k = 0;
     if (poyalgn_newkk_get_k(ctx(), &k) != 0) failwith((char *)poyalgn_last_error());
     CAMLreturn(Val_int(k));
+}
+
+/* ---- three-sequence alignment ------------------------------------------ */
+
+/* powell_3D_align (src/ukkCommon.c:109), the external `powell_3d` of
+ * Sequence.Align (src/sequence.ml:1309): the aligned sequences are
+ * prepended into ra, rb, rc (created by align_3_powell with capacity
+ * la + lb + lc) and the alignment cost returned. */
+value powell_3D_align(value sa, value sb, value sc, value ra, value rb, value rc, value mm,
+                      value go, value ge)
+{
+    CAMLparam5(sa, sb, sc, mm, go);
+    CAMLxparam4(ge, ra, rb, rc);
+    seqt a, b, c, wa, wb, wc;
+    int32_t len = 0, cost = 0;
+    Seq_custom_val(a, sa);
+    Seq_custom_val(b, sb);
+    Seq_custom_val(c, sc);
+    Seq_custom_val(wa, ra);
+    Seq_custom_val(wb, rb);
+    Seq_custom_val(wc, rc);
+    const int cap = a->len + b->len + c->len;
+    unsigned char *buf = alloc_or_fail((size_t)cap * 3, NULL);
+    if (poyalgn_powell_3d(ctx(), a->begin, a->len, b->begin, b->len, c->begin, c->len,
+                          Int_val(mm), Int_val(go), Int_val(ge), buf, buf + cap, buf + 2 * cap,
+                          cap, &len, &cost) != 0)
+        fail_free(buf, NULL);
+    fill_seq(wa, buf, cap, len);
+    fill_seq(wb, buf + cap, cap, len);
+    fill_seq(wc, buf + 2 * cap, cap, len);
+    free(buf);
+    CAMLreturn(Val_int(cost));
+}
+
+/* powell_3D_align_bc (src/ukkCommon.c:147) */
+value powell_3D_align_bc(value *argv, int argn)
+{
+    (void)argn;
+    return powell_3D_align(argv[0], argv[1], argv[2], argv[3], argv[4], argv[5], argv[6],
+                           argv[7], argv[8]);
 }

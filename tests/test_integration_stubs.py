@@ -16,8 +16,8 @@ from build_oracle import DEFAULT_REF_SRC  # noqa: E402
 STUBS = os.path.join(ROOT, "integration", "poy_stubs.c")
 LIBDIR = os.path.join(ROOT, "poy5_gb300")
 
-# every external of the path (src/algn.c, src/seq.c, src/newkkonen.c) the
-# stub library replaces, bytecode twins included
+# every external of the path (src/algn.c, src/seq.c, src/newkkonen.c,
+# src/ukkCommon.c) the stub library replaces, bytecode twins included
 EXTERNALS = [
     "algn_CAML_simple_2", "algn_CAML_backtrace_2d", "algn_CAML_backtrace_2d_bc",
     "algn_CAML_align_2d", "algn_CAML_align_2d_bc", "algn_CAML_limit_2",
@@ -27,7 +27,7 @@ EXTERNALS = [
     "algn_CAML_worst_2", "algn_CAML_verify_2", "seq_CAML_median_2_no_gaps",
     "seq_CAML_median_2_with_gaps", "newkkonen_CAML_algn_affine",
     "newkkonen_CAML_backtrace_affine", "newkkonen_CAML_backtrace_affine_bc",
-    "newkkonen_CAML_get_k",
+    "newkkonen_CAML_get_k", "powell_3D_align", "powell_3D_align_bc",
 ]
 
 needs_poy = pytest.mark.skipif(not os.path.isfile(os.path.join(DEFAULT_REF_SRC, "seq.h")),
