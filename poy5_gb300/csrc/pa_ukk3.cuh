@@ -112,6 +112,10 @@ struct Frame {
     int ab, ac, d;
     int meta;   // to | phase << 5 | k << 8 | sub << 13 | (fst + 1) << 14
     int best, fabac, fcs, ext;
+    // fixed for the frame's life: the window index of its diagonal pair and
+    // of the neighbour pair (-1 outside the window), both pairs' cost bound
+    // from the pass start (withinMatrix), and the plane of d
+    int diag0, diag1, ch0, ch1, pd;
 };
 
 struct Pass {
@@ -312,17 +316,28 @@ struct Machine {
         return w.CP + slot(ab, ac, d % m.maxstep, m.maxstep, s);
     }
 
-    PA_HDM bool within(int ab, int ac, int d) const
+    // withinMatrix's lower bound on the cost of reaching (ab, ac) from the
+    // pass's start (src/ukk.checkp.c:543-573)
+    PA_HDM int cheapest(int ab, int ac) const
     {
-        if (d < 0) return false;
         int g = iabs3(sab - ab), h = iabs3(sac - ac), k = iabs3((sac - sab) - (ac - ab));
         // g, h = the two smallest
         if (h < g) { const int t = g; g = h; h = t; }
         if (k < h) h = k;
         if (h < g) { const int t = g; g = h; h = t; }
-        const int cheapest = sst == 0 ? (g ? m.go + g * m.ge : 0) + (h ? m.go + h * m.ge : 0)
-                                      : g * m.ge + h * m.ge;
-        return cheapest + scost <= d;
+        return sst == 0 ? (g ? m.go + g * m.ge : 0) + (h ? m.go + h * m.ge : 0)
+                        : g * m.ge + h * m.ge;
+    }
+    PA_HDM bool within(int ab, int ac, int d) const
+    {
+        return d >= 0 && cheapest(ab, ac) + scost <= d;
+    }
+    PA_HDM int diag_of(int ab, int ac) const { return (ab - w.ab_lo) * w.wac + (ac - w.ac_lo); }
+    // the plane of cost d - x from the plane of d (0 <= x < 2 maxstep)
+    PA_HDM int plane_back(int pd, int x) const
+    {
+        const int p = pd - x;
+        return p < 0 ? p + 2 * m.maxstep : p;
     }
 
     PA_HDM void fail(int s)
@@ -330,19 +345,21 @@ struct Machine {
         if (status == OK) status = s;
     }
 
-    // one candidate: classify and load the slot
-    PA_HDM void load(int ab, int ac, int d, int s, int& tag, int& abac, int& cs) const
+    // one candidate on a diagonal pair of the frame (its window index diag,
+    // -1 outside, and its cost bound ch): classify and load the slot of
+    // cost d, plane pl, state s
+    PA_HDM void load(int diag, int ch, int d, int pl, int s, int& tag, int& abac, int& cs) const
     {
         abac = 0, cs = 0;
-        if (!within(ab, ac, d)) {
+        if (d < 0 || ch + scost > d) {
             tag = -INF;
             return;
         }
-        if (!in_window(ab, ac)) {
+        if (diag < 0) {
             tag = TAG_WINDOW;
             return;
         }
-        const Cell* c = U(ab, ac, d, s);
+        const Cell* c = w.U + ((long long)diag * (2 * m.maxstep) + pl) * NS + s;
 #if defined(__CUDA_ARCH__)
         const int4 v = *reinterpret_cast<const int4*>(c);
         tag = v.y == d + off ? v.x : TAG_MISS;
@@ -363,17 +380,17 @@ struct Machine {
             tag = -INF, abac = 0, cs = 0;
             return;
         }
-        const int cost = F.d - m.trans[k][to] - m.cont[to] - (l >= 16 ? m.mm : 0);
-        load(ab1, ac1, cost, k, tag, abac, cs);
+        const int x = m.trans[k][to] + m.cont[to] + (l >= 16 ? m.mm : 0);
+        load(F.diag1, F.ch1, F.d - x, plane_back(F.pd, x), k, tag, abac, cs);
     }
     // lane 0: the same state one cost lower; lanes 1-15 (state 0 only): the
     // other states at this cost
     PA_HDM void lane_x(int l, const Frame& F, int to, int& tag, int& abac, int& cs) const
     {
         if (l == 0)
-            load(F.ab, F.ac, F.d - 1, to, tag, abac, cs);
+            load(F.diag0, F.ch0, F.d - 1, plane_back(F.pd, 1), to, tag, abac, cs);
         else if (to == 0 && l < NS)
-            load(F.ab, F.ac, F.d, l, tag, abac, cs);
+            load(F.diag0, F.ch0, F.d, F.pd, l, tag, abac, cs);
         else
             tag = -INF, abac = 0, cs = 0;
     }
@@ -411,9 +428,12 @@ struct Machine {
             F = w.st[sp];
     }
 
-    PA_HDM void start(Frame& F, int ab, int ac, int d, int to) const
+    // a frame for (ab, ac, d, to) on diagonal pair diag0 (cost bound ch0),
+    // d in plane pd
+    PA_HDM void start(Frame& F, int ab, int ac, int d, int to, int diag0, int ch0, int pd) const
     {
         F.ab = ab, F.ac = ac, F.d = d;
+        F.diag0 = diag0, F.ch0 = ch0, F.pd = pd;
         F.best = -INF;
         F.ext = -INF;
         if (d >= cp_cost && d < cp_cost + m.maxstep) {
@@ -427,6 +447,12 @@ struct Machine {
         const int da = nb & 1, db = (nb >> 1) & 1, dc = (nb >> 2) & 1;
         const int ab1 = ab - da + db, ac1 = ac - da + dc;
         const bool diag = ab1 >= -endB && ab1 <= endA && ac1 >= -endC && ac1 <= endA;
+        if (diag) {
+            F.ch1 = cheapest(ab1, ac1);
+            F.diag1 = in_window(ab1, ac1) ? diag_of(ab1, ac1) : -1;
+        } else {
+            F.ch1 = 0, F.diag1 = -1;
+        }
         F.meta = to | ((diag ? PH_FS : PH_X) << 5);
     }
 
@@ -619,7 +645,7 @@ struct Machine {
         }
         int sp = 0;
         Frame F;
-        start(F, ab0, ac0, d0, s0);
+        start(F, ab0, ac0, d0, s0, diag_of(ab0, ac0), cheapest(ab0, ac0), d0 % (2 * m.maxstep));
         Snap Sf, Sx;
         bool fresh = false;
         for (;;) {
@@ -638,7 +664,7 @@ struct Machine {
             const bool copy = F.d >= cp_cost + m.maxstep;
             if (!fresh) snap(Sf, Sx, F, to, ph, ab1, ac1);
             fresh = true;
-            int cab = 0, cac = 0, cd = 0, cst = 0;
+            int cab = 0, cac = 0, cd = 0, cst = 0, cdiag = 0, cch = 0, cpl = 0;
             bool call = false;
             if (ph == PH_FS) {
                 const Reduced R = walk_fs(Sf, k, sub, F, to, ab1, ac1, copy);
@@ -657,8 +683,9 @@ struct Machine {
                     }
                     k = R.first;
                     sub = R.code == 2;
-                    call = true, cab = ab1, cac = ac1, cst = k;
-                    cd = F.d - m.trans[k][to] - m.cont[to] - (sub ? m.mm : 0);
+                    const int x = m.trans[k][to] + m.cont[to] + (sub ? m.mm : 0);
+                    call = true, cab = ab1, cac = ac1, cst = k, cd = F.d - x;
+                    cdiag = F.diag1, cch = F.ch1, cpl = plane_back(F.pd, x);
                 } else {
                     // nothing was written since the round was read: the
                     // second round of the same read is current
@@ -672,6 +699,7 @@ struct Machine {
                     const int t = tag_of(Sx, 0);
                     if (t == TAG_MISS) {
                         call = true, cab = F.ab, cac = F.ac, cd = F.d - 1, cst = to;
+                        cdiag = F.diag0, cch = F.ch0, cpl = plane_back(F.pd, 1);
                     } else if (t == TAG_WINDOW) {
                         fail(ERR_WINDOW);
                         return -INF;
@@ -714,6 +742,7 @@ struct Machine {
                         }
                         k = R.first;
                         call = true, cab = F.ab, cac = F.ac, cd = F.d, cst = k;
+                        cdiag = F.diag0, cch = F.ch0, cpl = F.pd;
                     } else {
                         const int dist = run_end(F.ext, F.ab, F.ac);
                         if (dist > F.best) {
@@ -733,12 +762,15 @@ struct Machine {
                 }
             }
             if (finish) {
-                Cell* c = U(F.ab, F.ac, F.d, to);
+                Cell* c = w.U + ((long long)F.diag0 * (2 * m.maxstep) + F.pd) * NS + to;
                 c->dist = F.best;
                 c->stamp = F.d + off;
                 c->abac = F.fabac;
                 c->cs = F.fcs;
-                if (F.d >= cp_cost && F.d < cp_cost + m.maxstep) *CP(F.ab, F.ac, F.d, to) = F.best;
+                if (F.d >= cp_cost && F.d < cp_cost + m.maxstep) {
+                    const int cpl_ = F.pd >= m.maxstep ? F.pd - m.maxstep : F.pd;
+                    w.CP[((long long)F.diag0 * m.maxstep + cpl_) * NS + to] = F.best;
+                }
                 if (F.best > furthest) furthest = F.best;
                 if (sp == 0) return F.best;
                 pop(sp, F);
@@ -753,7 +785,7 @@ struct Machine {
                 return -INF;
             }
             push(sp, F);
-            start(F, cab, cac, cd, cst);
+            start(F, cab, cac, cd, cst, cdiag, cch, cpl);
             fresh = false;
         }
     }
