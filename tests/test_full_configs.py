@@ -5,7 +5,9 @@ ambiguity codes, subs 1 / indel 2) and the affine pair workload (65,536
 pairs, lognormal lengths with median 800, gap opening 3, extension 1,
 subs 1) at their full sizes: cost, worst cost, aligned pair, median and
 median with gaps of each pair, byte for byte, against the oracle's C
-restatement run over the same pairs on all host cores.
+restatement run over the same pairs on all host cores. The three-sequence
+workload (8,192 readjust triples) likewise: cost, length and the three
+aligned sequences of every triple.
 """
 import os
 
@@ -31,3 +33,27 @@ def test_full_workload_matches_oracle(ctx, oracle, name):
     ints = [res.cost, res.maxcost, res.alen, res.mlen, res.wlen, res.status]
     par = compare_batch(ref, ints, [res.ea, res.eb, res.med, res.mwg], pk.out_off, pk.cap)
     assert par["mismatches"] == 0, par
+
+
+def test_full_readjust_triples_match_oracle(ctx, oracle):
+    """Every one of the 8,192 three-sequence alignments the bench times
+    (readjust_triples_8192x100-300_linear): cost, length and the three
+    aligned sequences against the oracle restatement on all host cores."""
+    import numpy as np
+    import poy5_gb300 as pg
+    from poy5_gb300.three_d import pack_triples
+    w = wl.readjust_triples(n_triples=8192)
+    res = pg.powell_3d_batch(ctx, w.triples, w.mm, w.go, w.ge)
+    seqs, off, lens, out_off, cap = pack_triples(w.triples)
+    ref = oracle.powell_3d_batch(seqs, off, lens, out_off, w.mm, w.go, w.ge,
+                                 nthreads=os.cpu_count() or 1)
+    assert (ref["status"] == 0).all() and (res.status == 0).all()
+    assert np.array_equal(ref["cost"], res.cost)
+    assert np.array_equal(ref["rlen"], res.rlen)
+    # the bytes each triple's alignment occupies: the rlen bytes that end at
+    # its slot's end (the rest of a slot is never written)
+    n = res.rlen.astype(np.int64)
+    end = out_off + cap
+    idx = np.repeat(end - n, n) + (np.arange(int(n.sum())) - np.repeat(np.cumsum(n) - n, n))
+    for name, got in (("ra", res.ra), ("rb", res.rb), ("rc", res.rc)):
+        assert np.array_equal(ref[name][idx], got[idx]), name
