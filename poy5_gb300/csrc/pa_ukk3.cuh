@@ -54,7 +54,7 @@ struct Model {
     int mm, go, ge, maxstep;
     int8_t neigh[NS], second[NS];
     int16_t cont[NS];
-    int16_t trans[NS][NS];
+    int16_t trans[NS][NS];  // [to][from]: a row per target state, read one entry per lane
 };
 
 PA_HDM void model_init(Model& m, int mm, int go, int ge)
@@ -95,7 +95,7 @@ PA_HDM void model_init(Model& m, int mm, int go, int ge)
                 const int to = digit(code[t], i);
                 if (to != 0 && to != digit(code[f], i)) c += go;
             }
-            m.trans[f][t] = (int16_t)c;
+            m.trans[t][f] = (int16_t)c;
             const int step = c + m.cont[t] + mm * (count(code[t], 0) - 1);
             mx = step > mx ? step : mx;
         }
@@ -380,7 +380,7 @@ struct Machine {
             tag = -INF, abac = 0, cs = 0;
             return;
         }
-        const int x = m.trans[k][to] + m.cont[to] + (l >= 16 ? m.mm : 0);
+        const int x = m.trans[to][k] + m.cont[to] + (l >= 16 ? m.mm : 0);
         load(F.diag1, F.ch1, F.d - x, plane_back(F.pd, x), k, tag, abac, cs);
     }
     // lane 0: the same state one cost lower; lanes 1-15 (state 0 only): the
@@ -477,7 +477,7 @@ struct Machine {
         if (k < k0 || k >= NS) return r;
         const int nb = m.neigh[to];
         const int da = nb & 1, db = (nb >> 1) & 1, dc = (nb >> 2) & 1;
-        const int cost = F.d - m.trans[k][to] - m.cont[to];
+        const int cost = F.d - m.trans[to][k] - m.cont[to];
         if (!(k == k0 && sub0)) {
             if (t1 == TAG_MISS) return r.code = 1, r;
             if (t1 == TAG_WINDOW) return r.code = 3, r;
@@ -525,49 +525,69 @@ struct Machine {
                a_at(p) == b_at(p - ab) && a_at(p) == c_at(p - ac);
     }
 
-    // the first lane asking for a call (32 if none), and the largest key of
-    // the lanes before it (earliest lane among equals)
-    struct Reduced {
-        int first, key, abac, cs, code;
-    };
-
+    // the lanes' results of a round (each lane its own on the GPU)
+    struct Lanes {
 #if defined(__CUDA_ARCH__)
-    PA_HDM Reduced reduce(const LaneRes& r) const
+        LaneRes r;
+#else
+        LaneRes r[32];
+#endif
+    };
+    // one lane's result, read by every lane (a warp-uniform index)
+    PA_HDM int lane_abac(const Lanes& L, int k) const
     {
+#if defined(__CUDA_ARCH__)
+        return __shfl_sync(0xffffffffu, L.r.abac, k);
+#else
+        return L.r[k].abac;
+#endif
+    }
+    PA_HDM int lane_cs(const Lanes& L, int k) const
+    {
+#if defined(__CUDA_ARCH__)
+        return __shfl_sync(0xffffffffu, L.r.cs, k);
+#else
+        return L.r[k].cs;
+#endif
+    }
+    PA_HDM int lane_code(const Lanes& L, int k) const
+    {
+#if defined(__CUDA_ARCH__)
+        return __shfl_sync(0xffffffffu, L.r.code, k);
+#else
+        return L.r[k].code;
+#endif
+    }
+
+    // the first lane asking for a call (32 if none), and the largest key of
+    // the lanes before it (earliest lane among equals; 0 if none)
+    struct Reduced {
+        int first, key;
+    };
+    PA_HDM Reduced reduce(const Lanes& L) const
+    {
+        Reduced out;
+#if defined(__CUDA_ARCH__)
         const unsigned full = 0xffffffffu;
         const int l = (int)(threadIdx.x & 31);
-        const unsigned stop = __ballot_sync(full, r.code != 0);
-        const int first = stop ? __ffs(stop) - 1 : 32;
-        const int key = __reduce_max_sync(full, l < first ? r.key : 0);
-        const int bl = key ? 31 - (key & 31) : 0;
-        Reduced out;
-        out.first = first;
-        out.key = key;
-        out.abac = __shfl_sync(full, r.abac, bl);
-        out.cs = __shfl_sync(full, r.cs, bl);
-        out.code = __shfl_sync(full, r.code, first & 31);
-        return out;
-    }
+        const unsigned stop = __ballot_sync(full, L.r.code != 0);
+        out.first = stop ? __ffs(stop) - 1 : 32;
+        out.key = __reduce_max_sync(full, l < out.first ? L.r.key : 0);
 #else
-    PA_HDM Reduced reduce(const LaneRes* r) const
-    {
-        Reduced out{32, 0, 0, 0, 0};
+        out.first = 32, out.key = 0;
         for (int l = 0; l < 32; l++)
-            if (r[l].code) {
+            if (L.r[l].code) {
                 out.first = l;
                 break;
             }
         for (int l = 0; l < out.first; l++)
-            if (r[l].key > out.key) out.key = r[l].key;
-        const int bl = out.key ? 31 - (out.key & 31) : 0;
-        out.abac = r[bl].abac, out.cs = r[bl].cs;
-        out.code = r[out.first & 31].code;
+            if (L.r[l].key > out.key) out.key = L.r[l].key;
+#endif
         return out;
     }
-#endif
 
     PA_HDM Reduced walk_fs(const Snap& S, int k0, int sub0, const Frame& F, int to, int ab1,
-                           int ac1, bool copy) const
+                           int ac1, bool copy, Lanes& L) const
     {
 #if defined(__CUDA_ARCH__)
         const unsigned full = 0xffffffffu;
@@ -575,28 +595,25 @@ struct Machine {
         const int t2 = __shfl_down_sync(full, S.tag, 16);
         const int a2 = __shfl_down_sync(full, S.abac, 16);
         const int c2 = __shfl_down_sync(full, S.cs, 16);
-        const LaneRes r = fs_lane(l < 16 ? l : NS, k0, sub0, F, to, ab1, ac1, copy, S.tag,
-                                  S.abac, S.cs, t2, a2, c2);
-        return reduce(r);
+        L.r = fs_lane(l < 16 ? l : NS, k0, sub0, F, to, ab1, ac1, copy, S.tag, S.abac, S.cs, t2,
+                      a2, c2);
 #else
-        LaneRes r[32];
         for (int l = 0; l < 32; l++)
-            r[l] = l < 16 ? fs_lane(l, k0, sub0, F, to, ab1, ac1, copy, S.tag[l], S.abac[l],
-                                    S.cs[l], S.tag[l + 16], S.abac[l + 16], S.cs[l + 16])
-                          : fs_lane(NS, k0, sub0, F, to, ab1, ac1, copy, 0, 0, 0, 0, 0, 0);
-        return reduce(r);
+            L.r[l] = l < 16 ? fs_lane(l, k0, sub0, F, to, ab1, ac1, copy, S.tag[l], S.abac[l],
+                                      S.cs[l], S.tag[l + 16], S.abac[l + 16], S.cs[l + 16])
+                            : fs_lane(NS, k0, sub0, F, to, ab1, ac1, copy, 0, 0, 0, 0, 0, 0);
 #endif
+        return reduce(L);
     }
 
-    PA_HDM Reduced walk_x(const Snap& S, int k0, int to) const
+    PA_HDM Reduced walk_x(const Snap& S, int k0, int to, Lanes& L) const
     {
 #if defined(__CUDA_ARCH__)
-        return reduce(x_lane((int)(threadIdx.x & 31), k0, to, S.tag));
+        L.r = x_lane((int)(threadIdx.x & 31), k0, to, S.tag);
 #else
-        LaneRes r[32];
-        for (int l = 0; l < 32; l++) r[l] = x_lane(l, k0, to, S.tag[l]);
-        return reduce(r);
+        for (int l = 0; l < 32; l++) L.r[l] = x_lane(l, k0, to, S.tag[l]);
 #endif
+        return reduce(L);
     }
 
     // the end of the run of matches from `dist`, 32 positions a round
@@ -666,24 +683,27 @@ struct Machine {
             fresh = true;
             int cab = 0, cac = 0, cd = 0, cst = 0, cdiag = 0, cch = 0, cpl = 0;
             bool call = false;
+            Lanes L;
             if (ph == PH_FS) {
-                const Reduced R = walk_fs(Sf, k, sub, F, to, ab1, ac1, copy);
+                const Reduced R = walk_fs(Sf, k, sub, F, to, ab1, ac1, copy, L);
                 if (R.key) {
                     const int dist = (R.key >> 5) - KEY_OFF;
                     if (F.best < dist) {
+                        const int bl = 31 - (R.key & 31);
                         F.best = dist;
-                        F.fabac = R.abac;
-                        F.fcs = R.cs;
+                        F.fabac = lane_abac(L, bl);
+                        F.fcs = lane_cs(L, bl);
                     }
                 }
                 if (R.first < NS) {
-                    if (R.code == 3) {
+                    const int code = lane_code(L, R.first);
+                    if (code == 3) {
                         fail(ERR_WINDOW);
                         return -INF;
                     }
                     k = R.first;
-                    sub = R.code == 2;
-                    const int x = m.trans[k][to] + m.cont[to] + (sub ? m.mm : 0);
+                    sub = code == 2;
+                    const int x = m.trans[to][k] + m.cont[to] + (sub ? m.mm : 0);
                     call = true, cab = ab1, cac = ac1, cst = k, cd = F.d - x;
                     cdiag = F.diag1, cch = F.ch1, cpl = plane_back(F.pd, x);
                 } else {
@@ -727,7 +747,7 @@ struct Machine {
                 if (!call && !finish) {
                     // the other states at this cost, then the run of matches
                     // (src/ukk.checkp.c:712-759)
-                    const Reduced R = walk_x(Sx, k, to);
+                    const Reduced R = walk_x(Sx, k, to, L);
                     if (R.key) {
                         const int t = (R.key >> 5) - KEY_OFF;
                         if (t > F.ext) {
@@ -736,7 +756,7 @@ struct Machine {
                         }
                     }
                     if (R.first < NS) {
-                        if (R.code == 3) {
+                        if (lane_code(L, R.first) == 3) {
                             fail(ERR_WINDOW);
                             return -INF;
                         }
