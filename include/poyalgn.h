@@ -745,7 +745,7 @@ int poyalgn_int32_peak(int device, int kind, int iters, double *inst_per_s,
  * poyalgn_powell_3d_stats reports the summed kernel time and the number of
  * launch rounds of the last batch; poyalgn_powell_3d_set_budget caps the
  * device memory the triples' workspaces take at once (0: half the free
- * memory, at most 64 GB).
+ * memory, at most 192 GB).
  */
 int poyalgn_powell_3d(poyalgn_ctx *ctx, const uint8_t *a, int la, const uint8_t *b, int lb,
                       const uint8_t *c, int lc, int mm, int go, int ge, uint8_t *ra,

@@ -107,7 +107,7 @@ struct poyalgn_ctx {
     const poyalgn_cm* nk_cm = nullptr;
     std::vector<uint8_t> nk_s1, nk_s2, nk_r1, nk_r2;
     // three-sequence alignment (pa_ukk3.cu): triple workspaces and metadata,
-    // the workspace budget (0: half the free memory, at most 64 GB), and the
+    // the workspace budget (0: half the free memory, at most 192 GB), and the
     // kernel time and launch rounds of the last batch
     pa::DevBuf u3_work, u3_meta;
     long long u3_budget = 0;

@@ -171,12 +171,14 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
         CU(cudaMemcpyAsync(d_off, off, ni * 24, cudaMemcpyHostToDevice, st));
         CU(cudaMemcpyAsync(d_len, len, ni * 12, cudaMemcpyHostToDevice, st));
         CU(cudaMemcpyAsync(d_oo, out_off, ni * 8, cudaMemcpyHostToDevice, st));
-        // workspace budget: the caller's, else half the free memory (at most 64 GB)
+        // workspace budget: the caller's, else half the free memory (at most
+        // 192 GB). A launch lasts as long as its slowest triple, so a batch
+        // that fits one round finishes in about that triple's time.
         long long budget = c->u3_budget;
         if (budget <= 0) {
             size_t fr = 0, tot = 0;
             CU(cudaMemGetInfo(&fr, &tot));
-            budget = std::min<long long>((long long)(fr / 2), 64LL << 30);
+            budget = std::min<long long>((long long)(fr / 2), 192LL << 30);
         }
         cudaEvent_t e0, e1;
         CU(cudaEventCreate(&e0));
