@@ -729,12 +729,14 @@ int poyalgn_int32_peak(int device, int kind, int iters, double *inst_per_s,
  * position with none: POYALGN_EPAIR / POYALGN_PAIR_BAD_STATE, where POY
  * fails with "This is impossible!"). mm, go, ge are the mismatch, gap
  * opening and gap extension costs as align_3_powell_inter passes them
- * (src/sequence.ml:1323-1337); mm >= 1, go >= 0, ge >= 1. ra, rb, rc
+ * (src/sequence.ml:1323-1337); 1 <= mm, ge <= 10,000 and 0 <= go <= 10,000
+ * (else POYALGN_EINVAL). ra, rb, rc
  * receive the three aligned sequences, leading gap included, written back
  * to front so that they end at ra + cap (POY's seq_prepend into sequences
  * of capacity la + lb + lc: cap >= la + lb + lc); *rlen is their length and
  * *cost the alignment cost (the external's return value). Sequences longer
- * than 32,768 positions: POYALGN_PAIR_TOO_LONG.
+ * than 32,768 positions, or a triple whose cost bound (the largest single
+ * column cost times la + lb + lc - 2) passes 2^26: POYALGN_PAIR_TOO_LONG.
  *
  * poyalgn_powell_3d_batch runs many triples at once: triple k's sequences
  * are seqs + off[3k + j], len[3k + j] bytes (j = 0, 1, 2 for a, b, c), and

@@ -99,8 +99,10 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
 {
     c->u3_ms = 0.f;
     if (n <= 0) return 0;
-    if (mm < 1 || go < 0 || ge < 1)
-        return set_err(POYALGN_EINVAL, "powell_3d: costs must be mm >= 1, go >= 0, ge >= 1");
+    if (mm < 1 || go < 0 || ge < 1 || mm > u3::MAXCOST || go > u3::MAXCOST || ge > u3::MAXCOST)
+        return set_err(POYALGN_EINVAL,
+                       "powell_3d: costs must be 1 <= mm, ge <= %d and 0 <= go <= %d",
+                       u3::MAXCOST, u3::MAXCOST);
     u3::Model model;
     u3::model_init(model, mm, go, ge);
     long long seq_bytes = 0, out_total = 0;
@@ -115,7 +117,8 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
             status[k] = POYALGN_PAIR_EMPTY;
             continue;
         }
-        if (l[0] - 1 > u3::MAXLEN || l[1] - 1 > u3::MAXLEN || l[2] - 1 > u3::MAXLEN) {
+        if (l[0] - 1 > u3::MAXLEN || l[1] - 1 > u3::MAXLEN || l[2] - 1 > u3::MAXLEN ||
+            u3::cost_bound(model.maxstep, l[0] - 1, l[1] - 1, l[2] - 1) > u3::MAX_COST_BOUND) {
             status[k] = POYALGN_PAIR_TOO_LONG;
             continue;
         }

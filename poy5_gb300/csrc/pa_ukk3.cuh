@@ -35,6 +35,16 @@ constexpr int INF = 5000;      // INFINITY = MAXINT / 2 with MAXINT 10000
 constexpr int NS = 16;         // states with a match and at most one insert
 constexpr int SUB_CAP = 96;    // pending check-point passes
 constexpr int MAXLEN = 32767;  // diagonals packed as int16 in `from`
+constexpr int MAXCOST = 10000;  // mm, go, ge: the state tables hold int16
+// bound on a triple's alignment cost, maxstep (la + lb + lc + 1): costs are
+// packed as cost * 32 + state in an int, and the frame stack holds twice it
+constexpr long long MAX_COST_BOUND = 1LL << 26;
+
+// the cost bound of a triple (la, lb, lc without the leading gap)
+PA_HDM long long cost_bound(int maxstep, int la, int lb, int lc)
+{
+    return (long long)maxstep * ((long long)la + lb + lc + 1);
+}
 
 enum Status : int {
     OK = 0,
@@ -153,7 +163,7 @@ PA_HDM Layout layout(const Model& m, int la, int lb, int lc, int D)
     L.ac_lo = -(D < lc ? D : lc);
     L.wab = (D < la ? D : la) - L.ab_lo + 1;
     L.wac = (D < la ? D : la) - L.ac_lo + 1;
-    const long long ub = (long long)m.maxstep * (la + lb + lc + 1);
+    const long long ub = cost_bound(m.maxstep, la, lb, lc);  // <= MAX_COST_BOUND (host check)
     L.st_cap = (int)(2 * ub + 8);
     const long long cells = (long long)L.wab * L.wac * NS;
     auto up16 = [](long long v) { return (v + 15) & ~15LL; };
@@ -897,7 +907,7 @@ struct Machine {
         const int fab = la - lb, fac = la - lc;
         bool cp_on_dist = true;
         // no alignment costs more than maxstep per column
-        const long long ub = (long long)m.maxstep * (la + lb + lc + 1);
+        const long long ub = cost_bound(m.maxstep, la, lb, lc);
         int d = -1;
         do {
             d++;

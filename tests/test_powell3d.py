@@ -267,4 +267,11 @@ def test_gpu_per_triple_errors(ctx):
     with pytest.raises(_lib.PoyAlgnError):
         pg.powell_3d_batch(ctx, [good], 0, 0, 2)     # mismatch cost 0
     with pytest.raises(_lib.PoyAlgnError):
+        pg.powell_3d_batch(ctx, [good], 1, 20000, 2)  # past the state tables' range
+    # a cost bound past 2^26 (large gap costs on long sequences) is refused per
+    # triple before any launch
+    G_ = [G] + [1] * 30000
+    big = pg.powell_3d_batch(ctx, [(G_, G_, G_), good], 1, 9000, 9000, raise_on_error=False)
+    assert list(big.status) == [-6, 0]
+    with pytest.raises(_lib.PoyAlgnError):
         pg.powell_3d_batch(ctx, [bad_base], 1, 0, 2)
