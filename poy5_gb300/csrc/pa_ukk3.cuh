@@ -55,7 +55,24 @@ enum Status : int {
     ERR_LEN = 5,     // a sequence longer than MAXLEN or shorter than 1
     ERR_STAMP = 6,   // cost offsets past int32
     ERR_OUT = 7,     // output longer than its capacity
+    ERR_TIME = 8,    // the triple ran past TIME_LIMIT_NS (not retried)
 };
+
+// wall-clock bound of one triple's replay on the GPU: far above any triple
+// of the workloads (about 2 s at most), it keeps a replay that went wrong
+// from holding the device
+constexpr unsigned long long TIME_LIMIT_NS = 120ull * 1000000000ull;
+
+PA_HD unsigned long long now_ns()
+{
+#if defined(__CUDA_ARCH__)
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+#else
+    return 0;  // the host replay has no time bound
+#endif
+}
 
 // Column-state model (src/ukkCommon.c:244-338): neighbour step bits, the cost
 // of continuing a state, whether a second (mismatch) predecessor is tried,
@@ -291,6 +308,7 @@ struct Machine {
     int off, final_cost, furthest, cp_cost, complete;
     int sab, sac, scost, sst, endA, endB, endC;
     long long steps;
+    unsigned long long t0;  // start of the replay (GPU global timer)
     int status;
     int n;  // columns emitted
 
@@ -300,6 +318,7 @@ struct Machine {
           furthest(-1), cp_cost(INF), complete(0), sab(0), sac(0), scost(0), sst(0), endA(la_),
           endB(lb_), endC(lc_), steps(0), status(OK), n(0)
     {
+        t0 = now_ns();
     }
 
     PA_HDM int a_at(int i) const { return base_at(A, i); }
@@ -678,6 +697,10 @@ struct Machine {
         for (;;) {
             if (++steps > w.step_cap) {
                 fail(ERR_STEPS);
+                return -INF;
+            }
+            if ((steps & 4095) == 0 && now_ns() - t0 > TIME_LIMIT_NS) {
+                fail(ERR_TIME);
                 return -INF;
             }
             const int to = F.meta & 31;
