@@ -71,11 +71,15 @@ __global__ void __launch_bounds__(U3_BLOCK) powell_kernel(const U3Args A)
     A.rlen[k] = n;
 }
 
-void destroy_events(cudaEvent_t a, cudaEvent_t b)
-{
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-}
+// the two timing events of a batch, destroyed on every return path
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~EventPair()
+    {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
 
 int status_code(int s)
 {
@@ -183,9 +187,10 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
             CU(cudaMemGetInfo(&fr, &tot));
             budget = std::min<long long>((long long)(fr / 2), 192LL << 30);
         }
-        cudaEvent_t e0, e1;
-        CU(cudaEventCreate(&e0));
-        CU(cudaEventCreate(&e1));
+        EventPair ev;
+        CU(cudaEventCreate(&ev.a));
+        CU(cudaEventCreate(&ev.b));
+        cudaEvent_t e0 = ev.a, e1 = ev.b;
         std::vector<int> list, hst((size_t)n);
         std::vector<long long> wofs;
         std::vector<int> lwin;
@@ -212,10 +217,7 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
                     rest.push_back(k);
                 }
             }
-            if ((rc_ = reserve(c->u3_work, (size_t)used))) {
-                destroy_events(e0, e1);
-                return rc_;
-            }
+            if ((rc_ = reserve(c->u3_work, (size_t)used))) return rc_;
             const size_t nl = list.size();
             CU(cudaMemcpyAsync(d_list, list.data(), nl * 4, cudaMemcpyHostToDevice, st));
             CU(cudaMemcpyAsync(d_wofs, wofs.data(), nl * 8, cudaMemcpyHostToDevice, st));
@@ -261,7 +263,6 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
             }
             pending.swap(rest);
         }
-        destroy_events(e0, e1);
         c->u3_ms = ms_total;
         c->u3_rounds = rounds;
         CU(cudaMemcpyAsync(rlen, d_rlen, ni * 4, cudaMemcpyDeviceToHost, st));

@@ -89,7 +89,11 @@ def pack_triples(triples):
 
 def powell_3d_batch(ctx: Context, triples, mm: int, go: int, ge: int,
                     budget_bytes: int | None = None, raise_on_error: bool = True) -> Powell3DBatch:
-    """align_3_powell on many triples at once (poyalgn_powell_3d_batch)."""
+    """align_3_powell on many triples at once (poyalgn_powell_3d_batch).
+
+    budget_bytes, when given, caps the device memory the triples' workspaces
+    take at once for this and every later batch on ctx (0 restores the
+    default: half the free memory, at most 192 GB)."""
     lib = _lib.load()
     if budget_bytes is not None:
         check(lib.poyalgn_powell_3d_set_budget(ctx.handle, int(budget_bytes)))
