@@ -808,8 +808,21 @@ def run_powell3d(local: int, n_triples: int = 8192, reps: int = 2, cpu_triples: 
         if n != int(res.rlen[k]) or any(not np.array_equal(ref[x][e_ref - n:e_ref], g)
                                         for x, g in zip(("ra", "rb", "rc"), got)):
             bad += 1
+    # the per-call drop-in (one powell_3d call per triple, what unmodified POY
+    # issues) on the first 16 triples, and one host thread on the same ones
+    few = w.triples[:16]
+    t0 = time.perf_counter()
+    for tr in few:
+        pg.align_3_powell(ctx, *tr, w.mm, w.go, w.ge)
+    call_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for tr in few:
+        orc.powell_3d(*tr, w.mm, w.go, w.ge)
+    one_s = time.perf_counter() - t0
     nt = len(w.triples)
     return {"workload": w.name, "triples": nt, "status_ok": int((res.status == 0).sum()),
+            "per_call": {"calls": len(few), "ms_per_call": round(call_s / len(few) * 1e3, 2),
+                         "host_one_thread_ms_per_call": round(one_s / len(few) * 1e3, 2)},
             "e2e_ms": round(wall * 1e3, 1), "kernel_ms": round(kms_, 1),
             "launch_rounds": res.rounds,
             "triples_per_s": round(nt / wall, 1),
