@@ -142,6 +142,10 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
         }
         out_total = std::max<long long>(out_total, out_off[k] + l[0] + l[1] + l[2]);
         win[k] = u3::first_window(l[0] - 1, l[1] - 1, l[2] - 1);
+        if (!u3::window_fits(model, l[0] - 1, l[1] - 1, l[2] - 1, win[k])) {
+            status[k] = POYALGN_PAIR_TOO_LONG;
+            continue;
+        }
         pending.push_back(k);
     }
     if (pending.empty()) goto done;
@@ -254,8 +258,14 @@ int run_powell(poyalgn_ctx* c, int n, const uint8_t* seqs, const int64_t* off,
                     const int full = u3::full_window(len[3 * k] - 1, len[3 * k + 1] - 1,
                                                      len[3 * k + 2] - 1);
                     if (win[k] < full) {
-                        win[k] = std::min(2 * win[k], full);
-                        rest.push_back(k);
+                        const int wider = std::min(2 * win[k], full);
+                        if (u3::window_fits(model, len[3 * k] - 1, len[3 * k + 1] - 1,
+                                            len[3 * k + 2] - 1, wider)) {
+                            win[k] = wider;
+                            rest.push_back(k);
+                            continue;
+                        }
+                        status[k] = POYALGN_PAIR_TOO_LONG;
                         continue;
                     }
                 }

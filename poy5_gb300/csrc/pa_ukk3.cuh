@@ -195,6 +195,13 @@ PA_HDM Layout layout(const Model& m, int la, int lb, int lc, int D)
     return L;
 }
 
+// a window whose diagonal pairs are indexed in an int (diag_of)
+PA_HDM bool window_fits(const Model& m, int la, int lb, int lc, int D)
+{
+    const Layout L = layout(m, la, lb, lc, D);
+    return (long long)L.wab * L.wac < (1LL << 31);
+}
+
 PA_HDM Work work_at(unsigned char* base, const Layout& L)
 {
     Work w;
