@@ -509,37 +509,35 @@ struct Machine {
                            bool copy, int t1, int abac1, int cs1, int t2, int abac2,
                            int cs2) const
     {
-        LaneRes r{0, 0, F.fabac, F.fcs};
-        if (k < k0 || k >= NS) return r;
+        // written with predicates rather than early returns: the lanes of a
+        // warp take different outcomes, and one straight path keeps them
+        // together
+        const bool live = k >= k0 && k < NS;
+        const int kk = live ? k : 0;
         const int nb = m.neigh[to];
         const int da = nb & 1, db = (nb >> 1) & 1, dc = (nb >> 2) & 1;
-        const int cost = F.d - m.trans[to][k] - m.cont[to];
-        if (!(k == k0 && sub0)) {
-            if (t1 == TAG_MISS) return r.code = 1, r;
-            if (t1 == TAG_WINDOW) return r.code = 3, r;
-            if (ok_index(t1, da, endA) && ok_index(t1 - ab1, db, endB) &&
-                ok_index(t1 - ac1, dc, endC) &&
-                char_cost(da ? a_at(t1) : 16, db ? b_at(t1 - ab1) : 16,
-                          dc ? c_at(t1 - ac1) : 16) == 1) {
-                r.key = ((t1 + da + KEY_OFF) << 5) | (31 - k);
-                if (complete)
-                    r.abac = pack_abac(ab1, ac1), r.cs = cost * 32 + k;
-                else if (copy)
-                    r.abac = abac1, r.cs = cs1;
-                return r;
-            }
-            if (!m.second[to]) return r;
-        }
-        if (t2 == TAG_MISS) return r.code = 2, r;
-        if (t2 == TAG_WINDOW) return r.code = 3, r;
-        if (ok_index(t2, da, endA) && ok_index(t2 - ab1, db, endB) &&
-            ok_index(t2 - ac1, dc, endC)) {
-            r.key = ((t2 + da + KEY_OFF) << 5) | (31 - k);
-            if (complete)
-                r.abac = pack_abac(ab1, ac1), r.cs = (cost - m.mm) * 32 + k;
-            else if (copy)
-                r.abac = abac2, r.cs = cs2;
-        }
+        const int cost = F.d - m.trans[to][kk] - m.cont[to];
+        const bool first = live && !(k == k0 && sub0);  // the first slot is still to judge
+        const bool miss1 = first && t1 == TAG_MISS;
+        const bool win1 = first && t1 == TAG_WINDOW;
+        bool ok1 = first && !miss1 && !win1 && ok_index(t1, da, endA) &&
+                   ok_index(t1 - ab1, db, endB) && ok_index(t1 - ac1, dc, endC);
+        if (ok1)
+            ok1 = char_cost(da ? a_at(t1) : 16, db ? b_at(t1 - ab1) : 16,
+                            dc ? c_at(t1 - ac1) : 16) == 1;
+        // the second slot: when the first failed on a state that tries it, or
+        // when the first was taken already
+        const bool second = live && !miss1 && !win1 && !ok1 && (!first || m.second[to]);
+        const bool miss2 = second && t2 == TAG_MISS;
+        const bool win2 = second && t2 == TAG_WINDOW;
+        const bool ok2 = second && !miss2 && !win2 && ok_index(t2, da, endA) &&
+                         ok_index(t2 - ab1, db, endB) && ok_index(t2 - ac1, dc, endC);
+        LaneRes r;
+        r.code = miss1 ? 1 : (win1 || win2) ? 3 : miss2 ? 2 : 0;
+        const int t = ok1 ? t1 : t2;
+        r.key = (ok1 || ok2) ? (((t + da + KEY_OFF) << 5) | (31 - kk)) : 0;
+        r.abac = complete ? pack_abac(ab1, ac1) : copy ? (ok1 ? abac1 : abac2) : F.fabac;
+        r.cs = complete ? (cost - (ok1 ? 0 : m.mm)) * 32 + kk : copy ? (ok1 ? cs1 : cs2) : F.fcs;
         return r;
     }
 
