@@ -275,3 +275,24 @@ def test_gpu_per_triple_errors(ctx):
     assert list(big.status) == [-6, 0]
     with pytest.raises(_lib.PoyAlgnError):
         pg.powell_3d_batch(ctx, [bad_base], 1, 0, 2)
+
+
+@pytest.mark.gpu
+def test_gpu_readjust_workload_affine_costs_match_oracle(ctx, oracle):
+    """The readjust triples under affine costs (mismatch 1, opening 3,
+    extension 1): 16 cost planes and wider windows than the linear model."""
+    import poy5_gb300 as pg
+    from poy5_gb300 import workloads as wl
+    from poy5_gb300.three_d import pack_triples
+    w = wl.readjust_triples(n_triples=128, lo=80, hi=200)
+    mm, go, ge = 1, 3, 1
+    res = pg.powell_3d_batch(ctx, w.triples, mm, go, ge)
+    seqs, off, lens, out_off, cap = pack_triples(w.triples)
+    ref = oracle.powell_3d_batch(seqs, off, lens, out_off, mm, go, ge)
+    assert (ref["status"] == 0).all() and (res.status == 0).all()
+    assert np.array_equal(ref["cost"], res.cost)
+    assert np.array_equal(ref["rlen"], res.rlen)
+    for k in range(len(w.triples)):
+        e, n = int(out_off[k] + cap[k]), int(res.rlen[k])
+        for name, got in (("ra", res.ra), ("rb", res.rb), ("rc", res.rc)):
+            assert np.array_equal(ref[name][e - n:e], got[e - n:e]), (name, k)
