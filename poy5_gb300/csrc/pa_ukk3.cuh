@@ -10,7 +10,9 @@
 // from slots without a stamp check. So the machine replays the recursion call
 // for call: an explicit stack of frames stands in for Ukk / calcUkk
 // (src/ukk.checkp.c:576-782) and a second stack for the check-point passes
-// (src/ukk.checkp.c:214-365), both in the triple's own workspace.
+// (src/ukk.checkp.c:214-365), both in the triple's own workspace. Every lane
+// of the warp holds the same machine state; the lanes read a frame's
+// candidate cells together and judge one each.
 //
 // Storage: a window of diagonals |ab|, |ac| <= D (clipped to the sequences)
 // holds every cell a call can touch: a pass starting at cost c0 on diagonal
@@ -19,7 +21,8 @@
 // finalCost / ge the first pass and every later pass stay inside. The host
 // picks D per triple; a cell outside the window, a stack overflow or a step
 // budget running out ends the triple with a status the host retries with a
-// wider window. Layout per triple: U cells [wab][wac][2*maxstep][16] of 16
+// wider window; a replay that passes TIME_LIMIT_NS of wall clock ends with a
+// status of its own. Layout per triple: U cells [wab][wac][2*maxstep][16] of 16
 // bytes, check-point distances [wab][wac][maxstep][16], the frame stack and
 // the pass stack.
 #pragma once
